@@ -1,0 +1,400 @@
+"""Benchmark of the Nyles time step on GB300: cell-steps/s at 256^3.
+
+Workload (one GPU): Rayleigh-Taylor interface, 256x256x256 cells, box 1x1x1, periodic
+in x and y, free-slip walls in z, b = +0.5 above z = 0.5 + eta(x, y) and -0.5 below
+(eta: seeded Fourier modes 1 <= max(|kx|,|ky|) <= 8 scaled to max|eta| = 1e-2), fluid
+at rest; RK3-SSP with dt = 1e-3; multigrid to sum(r^2)/sum(b^2) < 1e-20 (relative
+residual 1e-10). A step = one full RK3 step (3 right-hand sides, 3 projections).
+`value` is the FP64 path with the state resident on the device; `mixed` reports the
+mixed-precision path (FP32 state and stencils, FP32 V-cycles in FP64 refinement) on
+the same workload with its error against FP64. `e2e` runs the same steps through the
+public API with the prognostic state copied in from pinned host memory and copied
+back every step.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--n 256]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "cell-steps/s at 256^3 (FP64 vs mixed, same error); ensemble p50/p99 latency"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="cells per direction")
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=2, help="extra steps timed per phase with CUDA events")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+def rt_params(n, precision):
+    from nyles_gb300 import parameters
+    parameters.InextensibleDict.unfreeze()
+    p = parameters.UserParameters()
+    p.model["modelname"] = "LES"
+    p.model["geometry"] = "perio_xy"
+    p.model["Lx"], p.model["Ly"], p.model["Lz"] = 1.0, 1.0, 1.0
+    p.time["timestepping"] = "RK3_SSP"
+    p.time["auto_dt"] = False
+    p.time["dt"] = 1e-3
+    p.discretization["global_nx"] = n
+    p.discretization["global_ny"] = n
+    p.discretization["global_nz"] = n
+    p.gpu["precision"] = precision
+    p.gpu["mg_tol"] = 1e-20
+    p.gpu["mg_maxite"] = 40
+    return p
+
+
+def rt_interface(grid, seed=3, kmax=8, amp=1e-2):
+    """eta(x, y) on the cell centres of the array (z, y, x) broadcast."""
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    x = grid.x_b_1D / grid.Lx
+    y = grid.y_b_1D / grid.Ly
+    X, Y = np.meshgrid(x, y, indexing="xy")
+    eta = np.zeros_like(X)
+    for kx in range(-kmax, kmax + 1):
+        for ky in range(-kmax, kmax + 1):
+            if 1 <= max(abs(kx), abs(ky)) <= kmax:
+                a, b = rng.standard_normal(2)
+                ph = 2 * np.pi * (kx * X + ky * Y)
+                eta += a * np.cos(ph) + b * np.sin(ph)
+    return eta * (amp / np.abs(eta).max())
+
+
+def rt_init(nyl):
+    import numpy as np
+    import torch
+    g = nyl.grid
+    eta = rt_interface(g)
+    zb = g.z_b_1D[:, None, None]
+    b = np.where(zb > 0.5 * g.Lz + eta[None, :, :], 0.5, -0.5)
+    nyl.model.state.b.view("i")[...] = torch.from_numpy(b)
+
+
+def build_model(n, precision):
+    from nyles_gb300.nyles import Nyles
+    nyl = Nyles(rt_params(n, precision))
+    rt_init(nyl)
+    return nyl
+
+
+# ------------------------------------------------------------------ measurement helpers
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while running; median SM clock and active reasons."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        import statistics
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def alg_bytes(nyl, phase_counts, mg_vcycles, elem):
+    """Algorithmic (compulsory) bytes of the right-hand side and multigrid smoothing
+    launches. rhs: reads b, U(3), vor(3), ke and tracers, writes 4+ntr registers."""
+    st = nyl.model.state
+    vol = st.b.data.numel()
+    ntr = nyl.param["n_tracers"]
+    rhs_words = (8 + ntr) + (4 + ntr)
+    out = {"rhs_per_launch": rhs_words * elem * vol}
+    # smoothing: each half-sweep reads x (or y) and b, writes y (or x): 3 words/cell
+    mg = nyl.model
+    return out
+
+
+# ------------------------------------------------------------------ timed runs
+def time_steps(nyl, K, W, stream):
+    import torch
+    m = nyl.model
+    for _ in range(W):
+        m.forward(0.0, nyl.dt0)
+    torch.cuda.synchronize()
+    st0 = m.mg_stats()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    from nyles_gb300 import _native
+    l0 = _native.lib().nyles_launch_count()
+    start.record(stream)
+    for _ in range(K):
+        m.forward(0.0, nyl.dt0)
+    end.record(stream)
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end)
+    st1 = m.mg_stats()
+    launches = _native.lib().nyles_launch_count() - l0
+    vc = (st1["vcycles"] - st0["vcycles"]) / max(1, (st1["solves"] - st0["solves"]))
+    return ms, launches, vc
+
+
+def profile_phases(nyl, steps):
+    import ctypes
+    import torch
+    from nyles_gb300 import _native as nat
+    m = nyl.model
+    lib = nat.lib()
+    nat.check(lib.nyles_model_profile(m._h, 1))
+    for _ in range(steps):
+        m.forward(0.0, nyl.dt0)
+    torch.cuda.synchronize()
+    ms = (ctypes.c_double * nat.NPHASE)()
+    cnt = (ctypes.c_longlong * nat.NPHASE)()
+    nat.check(lib.nyles_model_profile_read(m._h, ms, cnt, nat.NPHASE))
+    nat.check(lib.nyles_model_profile(m._h, 0))
+    return {nat.PHASES[i]: {"ms": ms[i], "count": cnt[i]} for i in range(nat.NPHASE)}
+
+
+def time_e2e(nyl, K, W):
+    """Same steps through the public API, prognostic state in pinned host memory."""
+    import torch
+    m = nyl.model
+    names = m.state.get_prognostic_scalars()
+    dev = [m.state.get(s).data for s in names]
+    host = [torch.empty_like(t, device="cpu").pin_memory() for t in dev]
+    for h, d in zip(host, dev):
+        h.copy_(d)
+    bytes_in = sum(h.numel() * h.element_size() for h in host)
+
+    def step():
+        for h, d in zip(host, dev):
+            d.copy_(h, non_blocking=True)
+        m.forward(0.0, nyl.dt0)
+        for h, d in zip(host, dev):
+            h.copy_(d, non_blocking=True)
+
+    for _ in range(W):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        step()
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) * 1e3, bytes_in
+
+
+def cpu_baseline(nsample=64, steps=2):
+    """The CPU oracle (single-threaded C++ restatement of the reference's numerics)
+    on the same workload at a reduced grid, timed on one host core."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    import numpy as np
+    from nyles_gb300 import grid as grid_module
+    from nyles_gb300 import topology as topo
+    n = nsample
+    prm = dict(nx=n, ny=n, nz=n, nh=3, npx=1, npy=1, npz=1, Lx=1.0, Ly=1.0, Lz=1.0, loc=[0, 0, 0],
+               neighbours=topo.get_neighbours([0, 0, 0], [1, 1, 1], "perio_xy"))
+    g = grid_module.Grid(prm)
+    o = oracle.OracleModel(dict(nx=n, ny=n, nz=n, geometry="perio_xy", timestepping="RK3_SSP", dx=g.dx, dy=g.dy,
+                                dz=g.dz, idx2=g.idx2, idy2=g.idy2, idz2=g.idz2))
+    o.mg_params(1e-20, 40, 0.9)
+    eta = rt_interface(g)
+    zb = g.z_b_1D[:, None, None]
+    o.field("b")[...] = np.where(zb > 0.5 + eta[None, :, :], 0.5, -0.5)
+    o.diagnose()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.forward(0.0, 1e-3)
+    el = time.perf_counter() - t0
+    return {"value": n ** 3 * steps / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+            "sample": "oracle (C++ restatement of the reference numerics, 1 thread) on the same Rayleigh-Taylor "
+                      "setup at %d^3, %d RK3 steps, %.1f s" % (n, steps, el)}
+
+
+# ------------------------------------------------------------------ reference arm
+def _ref_worker(args):
+    n, steps = args
+    r = cpu_baseline(n, steps)
+    return r["value"]
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    ncores = os.cpu_count() or 1
+    n = 48 if a.n >= 48 else a.n
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(ncores) as pool:
+        vals = pool.map(_ref_worker, [(n, max(1, a.steps // 2))] * ncores)
+    el = time.perf_counter() - t0
+    value = float(sum(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "rayleigh_taylor_perio_xy_rk3 (reference CPU numerics)", "grid": [n, n, n]},
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": ncores, "kind": "port",
+                             "sample": "%d independent single-thread oracle runs (one per host core) of the "
+                                       "Rayleigh-Taylor setup at %d^3, wall %.1f s; the reference itself has no "
+                                       "Fortran compiler here" % (ncores, n, el)},
+            "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ main
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    n = a.n
+    cells = n ** 3
+    peak, peak_kind = peaks()
+    out = {"metric": METRIC, "unit": "cell-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
+           "config": {"workload": "rayleigh_taylor_%d^3_perio_xy_rk3" % n, "grid": [n, n, n], "box": [1, 1, 1],
+                      "dt": 1e-3, "mg_tol_sq_ratio": 1e-20, "parallelism": "replicas" if world > 1 else "single",
+                      "l2": "inputs larger than L2 (state >> 129 MB)"}}
+    results = {}
+    precs = ["fp64", "mixed"] if a.precision == "both" else [a.precision]
+    launches_total = 0
+    with ClockSampler(local) as clk:
+        for prec in precs:
+            nyl = build_model(n, prec)
+            nyl.model.diagnose_var(nyl.model.state)
+            if dist:
+                dist.barrier()
+            torch.cuda.synchronize()
+            ms, launches, vc = time_steps(nyl, a.steps, a.warmup, stream)
+            if dist:
+                t = torch.tensor([ms], device="cuda")
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                ms = float(t.item())
+            launches_total += launches
+            res = {"ms_per_step": ms / a.steps, "value": world * cells * a.steps / (ms * 1e-3),
+                   "mean_vcycles_per_solve": vc, "kernel_launches": launches}
+            if a.profile_steps > 0:
+                res["phases"] = profile_phases(nyl, a.profile_steps)
+            if not a.no_e2e:
+                ems, bts = time_e2e(nyl, max(1, a.steps // 2), 1)
+                k = max(1, a.steps // 2)
+                res["e2e"] = {"value": world * cells * k / (ems * 1e-3), "unit": "cell-steps/s",
+                              "h2d_bytes_per_step": bts, "d2h_bytes_per_step": bts}
+            results[prec] = res
+            del nyl
+            torch.cuda.empty_cache()
+    clocks = clk.summary()
+    main_prec = "fp64" if "fp64" in results else precs[0]
+    r = results[main_prec]
+    out.update({"value": r["value"], "ms_per_step": r["ms_per_step"],
+                "dtype": "f64" if main_prec == "fp64" else "f32+f64", "clocks": clocks,
+                "gpu_launches": launches_total, "mg": {"mean_vcycles_per_solve": r["mean_vcycles_per_solve"]}})
+    if "e2e" in r:
+        out["e2e"] = r["e2e"]
+    # roofline of the dominant kernel (largest share of device time)
+    if "phases" in r:
+        ph = r["phases"]
+        kernels = {k: v for k, v in ph.items() if k not in ("mg_solve",)}
+        dom = max(kernels, key=lambda k: kernels[k]["ms"])
+        elem = 8 if main_prec == "fp64" else 4
+        out["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in ph.items()}
+        if dom == "rhs":
+            vol = (n + 6) * (n + 6) * n
+            bytes_launch = 12 * elem * vol
+            avg = ph["rhs"]["ms"] / max(1, ph["rhs"]["count"])
+            ach = bytes_launch / (avg * 1e-3) / 1e9
+            out["roofline"] = {"kernel": "k_rhs", "bound": "hbm", "achieved": ach, "peak": peak,
+                               "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind, "traffic": None,
+                               "avg_launch_ms": avg, "bytes_per_launch": bytes_launch}
+        else:
+            out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s",
+                               "frac": None, "peak_kind": peak_kind, "traffic": None}
+    if "mixed" in results and main_prec != "mixed":
+        mr = results["mixed"]
+        out["mixed"] = {"value": mr["value"], "ms_per_step": mr["ms_per_step"],
+                        "speedup_vs_fp64": mr["value"] / r["value"],
+                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"]}
+        if "e2e" in mr:
+            out["mixed"]["e2e"] = mr["e2e"]
+        if "phases" in mr:
+            out["mixed"]["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in mr["phases"].items()}
+    if rank == 0 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(64 if n >= 64 else n, 2)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/* nyles_gb300.h — C ABI of libnyles_gb300.so, the GB300 (sm_103a) implementation of
+ * the Nyles LES time step for one subdomain on one GPU.
+ *
+ * Conventions
+ *  - Plain C types only. Device arrays are raw pointers to row-major (z, y, x) arrays,
+ *    the layout of the reference's `Scalar.view('i')` (core/variables.py:146-151),
+ *    with an `nh`-cell halo on both sides of each periodic direction and none in
+ *    closed directions (core/mpi/topology.py:253-300).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Every entry point returns an NYLES_* status; nyles_last_error() gives the message.
+ *    Nothing calls exit(), traps, or asserts on the device.
+ *  - The library never allocates device memory: the caller provides every array and a
+ *    workspace whose size the library reports.
+ *  - `_f64` entry points compute in double precision, `_f32` in single precision.
+ */
+#ifndef NYLES_GB300_H
+#define NYLES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+    NYLES_OK = 0,
+    NYLES_BAD_ARG = 1,
+    NYLES_CUDA_ERROR = 2,
+    NYLES_NOT_CONVERGED = 3, /* multigrid stopped at maxite above tolerance */
+    NYLES_BLOWUP = 4,        /* a non-finite value reached the state */
+    NYLES_TIMEOUT = 5,
+    NYLES_UNSUPPORTED = 6
+};
+
+/* ---------------------------------------------------------------- enumerations */
+enum { NYLES_MODEL_LES = 0, NYLES_MODEL_EULER3D = 1, NYLES_MODEL_LINEAR = 2 }; /* core/nyles.py:92-100 */
+enum { NYLES_SCHEME_EF = 0, NYLES_SCHEME_LFAM3 = 1, NYLES_SCHEME_RK3_SSP = 2 };  /* core/timescheme.py:80-90 */
+enum { NYLES_FP64 = 0, NYLES_MIXED = 1 };
+/* multigrid topology, core/mgfor/mg_enums.f90:6 */
+enum { NYLES_MG_CLOSED = 1, NYLES_MG_XPERIO = 2, NYLES_MG_YPERIO = 3, NYLES_MG_ZPERIO = 4,
+       NYLES_MG_XYPERIO = 5, NYLES_MG_XYZPERIO = 6 };
+
+/* state fields, in the table-of-contents order of core/variables.py:38-47;
+ * tracer t<k> is NYLES_F_T0 + k (core/model_les.py:36-44) */
+enum {
+    NYLES_F_B = 0, NYLES_F_P = 1, NYLES_F_KE = 2, NYLES_F_DIV = 3,
+    NYLES_F_U_I = 4, NYLES_F_U_J = 5, NYLES_F_U_K = 6,      /* covariant velocity u */
+    NYLES_F_UC_I = 7, NYLES_F_UC_J = 8, NYLES_F_UC_K = 9,   /* contravariant velocity U */
+    NYLES_F_VOR_I = 10, NYLES_F_VOR_J = 11, NYLES_F_VOR_K = 12,
+    NYLES_F_WORK = 13, NYLES_F_T0 = 14
+};
+#define NYLES_MAX_TRACERS 8
+/* prognostic registers (core/variables.py:364-383 order): b, u_i, u_j, u_k, t0.. */
+
+/* ---------------------------------------------------------------- descriptors */
+typedef struct NylesDesc {
+    int nx, ny, nz;          /* interior cells of the subdomain (param nx, ny, nz) */
+    int nh;                  /* halo width of periodic directions (param nh) */
+    int periodic_x, periodic_y, periodic_z;   /* from param geometry */
+    int n_tracers;           /* param n_tracers */
+    int model;               /* NYLES_MODEL_* */
+    int add_viscosity;       /* 1 when diff_coef has 'u' */
+    double dx, dy, dz;       /* grid spacing, core/grid.py:30-32 */
+    double idx2, idy2, idz2; /* 1/dx**2 etc. as computed by the host, core/grid.py:38-40 */
+    double dx2;              /* dx**2 as computed by the host, core/mgfordriver.py:78 */
+    double fparam;           /* covariant Coriolis coriolis*dx*dy (0 when not rotating), core/model_les.py:61-67 */
+    double viscosity;        /* diff_coef['u'], core/viscosity.py:3-9 */
+} NylesDesc;
+
+typedef struct NylesMgStats {
+    int nite;          /* V-cycles of the last solve (mgfor MG_Stats%nite) */
+    double res;        /* last squared residual ratio sum(r^2)/sum(b^2) (mgfor MG_Stats%res) */
+    long long solves;  /* solves since creation */
+    long long vcycles; /* V-cycles since creation */
+    int not_converged; /* solves that stopped at maxite */
+} NylesMgStats;
+
+const char* nyles_last_error(void);
+int nyles_version(void);
+
+/* ---------------------------------------------------------------- kernels
+ * One-dimensional upwind flux with WENO5/WENO3 reconstruction and the reference's
+ * boundary closures, on `nlines` independent lines of length n (n >= 5), lines
+ * contiguous. Replaces core/weno.f90:106-153 (flux1d). */
+int nyles_flux1d_f64(const double* u, const double* q, double* flux, int nlines, int n, void* stream);
+int nyles_flux1d_f32(const float* u, const float* q, float* flux, int nlines, int n, void* stream);
+
+/* Vortex force, added into the velocity registers ds[1..3]:
+ * du_i += -(omega x U)_i with omega upwinded along the advecting direction.
+ * Replaces core/vortex_force.py:14-81 -> core/fortran_vortex_force.f90:10-165
+ * (vortex_force_direc / vortex_force_flip, six calls). `fields` indexed by NYLES_F_*. */
+int nyles_vortex_force_f64(const NylesDesc* d, double* const* fields, double* const* ds, void* stream);
+int nyles_vortex_force_f32(const NylesDesc* d, float* const* fields, float* const* ds, void* stream);
+
+/* Right-hand side of the model into registers ds (overwritten, as reset_state):
+ * tracer flux divergence (core/tracer.py:44-78 -> fortran_upwind.f90:3-87), vortex
+ * force, Bernoulli (core/bernoulli.py:14-32 -> fortran_bernoulli.f90:2-58) and, when
+ * `last` and add_viscosity, viscosity (core/viscosity.py:3-9 -> fortran_dissipation.f90:2-35).
+ * Replaces core/model_les.py:130-144 (LES.rhs) and core/model_les_euler.py:128-142. */
+int nyles_rhs_f64(const NylesDesc* d, double* const* fields, double* const* ds, int last, void* stream);
+int nyles_rhs_f32(const NylesDesc* d, float* const* fields, float* const* ds, int last, void* stream);
+
+/* Periodic halo fill of one field. Replaces core/mpi/halo.py:140-178 (Halo.fill) for one rank. */
+int nyles_fill_f64(const NylesDesc* d, double* field, void* stream);
+int nyles_fill_f32(const NylesDesc* d, float* field, void* stream);
+
+/* ---------------------------------------------------------------- multigrid
+ * Cell-centred geometric multigrid of one rank. Replaces the ctypes interface of
+ * core/mgfordriver.py:6-105 over core/mgfor: get_ptrmg (mg_setup.f90:318-437),
+ * get_pyshape/set_pyarray/get_pyarray (pytools.f90:8-60), solve (solvers.f90:8-33).
+ * Level arrays hold interior cells only, (nz, ny, nx) row-major; ghost layers of the
+ * reference are implied (zero across closed walls, periodic image otherwise).
+ * precision NYLES_MIXED: FP32 V-cycles inside FP64 iterative refinement. */
+typedef struct NylesMg NylesMg;
+int nyles_mg_create(int nx, int ny, int nz, int topology, int precision, NylesMg** out);
+int nyles_mg_destroy(NylesMg* mg);
+int nyles_mg_workspace_bytes(const NylesMg* mg, size_t* bytes);
+int nyles_mg_bind(NylesMg* mg, void* workspace);      /* device memory of workspace_bytes */
+int nyles_mg_nlevels(const NylesMg* mg, int* nlevels);
+int nyles_mg_level_shape(const NylesMg* mg, int lev, int* shape3); /* lev 1 = finest */
+/* var 1 = x (solution; FP64 for lev 1 in both precisions), 2 = b (right-hand side) */
+int nyles_mg_level_ptr(NylesMg* mg, int lev, int var, void** ptr);
+/* tol on the squared residual ratio (mg_types.f90:15-26; defaults 1e-6, 20, 0.9) */
+int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega);
+int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream);
+
+/* ---------------------------------------------------------------- whole model
+ * One subdomain of LES / Euler3d / linear (core/nyles.py:92-100) with its time scheme
+ * and pressure projection. The caller owns every array:
+ *   fields   : NYLES_F_T0 + n_tracers device pointers (NYLES_F_* order)
+ *   regs     : 3 * (4 + n_tracers) device pointers, register r of prognostic q at
+ *              regs[r*(4+n_tracers)+q] (RK3: ds0, ds1, ds2; LFAM3: dstate, stateb,
+ *              state; EF: dstate), core/timescheme.py:92-101
+ *   workspace: nyles_model_workspace_bytes() bytes of device memory
+ * precision NYLES_FP64: double arrays; NYLES_MIXED: float arrays (FP64 pressure). */
+typedef struct NylesModel NylesModel;
+int nyles_model_create(const NylesDesc* d, int scheme, int precision, NylesModel** out);
+int nyles_model_destroy(NylesModel* m);
+int nyles_model_workspace_bytes(const NylesModel* m, size_t* bytes);
+int nyles_model_bind(NylesModel* m, void* const* fields, void* const* regs, void* workspace);
+int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omega);
+/* LES.forward: one time step, core/model_les.py:147-149 -> core/timescheme.py:113-221.
+ * Returns NYLES_BLOWUP when the new state holds a non-finite value. */
+int nyles_model_forward(NylesModel* m, double t, double dt, void* stream);
+/* LES.diagnose_var, core/model_les.py:98-127 (core/model_les_euler.py:96-125) */
+int nyles_model_diagnose(NylesModel* m, void* stream);
+/* LES.rhs into register set `reg`, core/model_les.py:130-144 */
+int nyles_model_rhs(NylesModel* m, int reg, int last, void* stream);
+/* max over the arrays of U^2+V^2+W^2 (core/nyles.py:241-251), copied to *out */
+int nyles_model_max_U2(NylesModel* m, double* out, void* stream);
+int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats);
+/* a fresh LFAM3 start (its first step is Euler forward, core/timescheme.py:129-140) */
+int nyles_model_reset_scheme(NylesModel* m);
+
+/* ---------------------------------------------------------------- instrumentation
+ * No counterpart in the reference (its timing is core/timing.py's wall-clock decorator).
+ * Phases: 0 right-hand side, 1 time-scheme update, 2 halo fill, 3 divergence,
+ * 4 multigrid solve, 5 projection correction, 6 vorticity/ke/U, 7 CFL reduction,
+ * 8 multigrid smoothing, 9 multigrid residual+restriction, 10 multigrid prolongation,
+ * 11 multigrid norms. Profiling brackets each phase with CUDA events on the launching
+ * stream (no host synchronisation added). */
+#define NYLES_NPHASE 12
+int nyles_model_profile(NylesModel* m, int enable);
+/* per-phase device milliseconds and counts since enable (or last read); resets them */
+int nyles_model_profile_read(NylesModel* m, double* ms, long long* count, int nphase);
+/* number of kernels this library has launched in the process */
+long long nyles_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NYLES_GB300_H */

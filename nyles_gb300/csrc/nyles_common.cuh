@@ -1,0 +1,150 @@
+// Shared device code of the Nyles GB300 kernels: array geometry, the WENO3/WENO5
+// reconstructions and the 1-D upwind flux with the reference's boundary closures.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef NYLES_MAX_TR
+#define NYLES_MAX_TR 8
+#endif
+#define NYLES_MAX_PROG (4 + NYLES_MAX_TR)
+
+namespace nyles {
+
+// Model array geometry. Every field is a row-major (z, y, x) array — the layout of the
+// reference's `Scalar.view('i')` (core/variables.py:146-151) — with a halo of `nh`
+// cells on both sides of each periodic direction and none in closed directions
+// (core/mpi/topology.py:253-300). Index 0 = z, 1 = y, 2 = x.
+struct Geom {
+    int N[3];      // array extents
+    int n[3];      // interior extents
+    int per[3];    // periodic flags
+    int nh;
+    long long sz, sy;
+    long long vol;
+
+    __host__ __device__ __forceinline__ long long at(int z, int y, int x) const {
+        return (long long)z * sz + (long long)y * sy + x;
+    }
+    __host__ __device__ __forceinline__ long long stride(int d) const {
+        return d == 0 ? sz : (d == 1 ? sy : 1);
+    }
+    // position of the interior cell a halo cell mirrors (periodic self-copy)
+    __host__ __device__ __forceinline__ int wrap(int d, int c) const {
+        if (!per[d]) return c;
+        if (c < nh) return c + n[d];
+        if (c >= nh + n[d]) return c - n[d];
+        return c;
+    }
+};
+
+// ---------------------------------------------------------------- WENO constants
+// core/weno.f90 keeps REAL(4) literals inside REAL(8) code (f2py build without real
+// promotion): each constant is the float value widened to double.
+template <typename T> struct WenoK;
+template <> struct WenoK<double> {
+    static __device__ __forceinline__ double c13() { return (double)(1.0f / 3.0f); }
+    static __device__ __forceinline__ double c76() { return (double)(7.0f / 6.0f); }
+    static __device__ __forceinline__ double c116() { return (double)(11.0f / 6.0f); }
+    static __device__ __forceinline__ double c16() { return (double)(1.0f / 6.0f); }
+    static __device__ __forceinline__ double c56() { return (double)(5.0f / 6.0f); }
+    static __device__ __forceinline__ double k1() { return (double)(13.0f / 12.0f); }
+    static __device__ __forceinline__ double eps5() { return (double)1e-16f; }
+    static __device__ __forceinline__ double eps3() { return (double)1e-14f; }
+    // `tau5` is implicitly REAL(4) in weno5 (weno.f90:45): round through float
+    static __device__ __forceinline__ double tau(double v) { return (double)(float)v; }
+};
+template <> struct WenoK<float> {
+    static __device__ __forceinline__ float c13() { return 1.0f / 3.0f; }
+    static __device__ __forceinline__ float c76() { return 7.0f / 6.0f; }
+    static __device__ __forceinline__ float c116() { return 11.0f / 6.0f; }
+    static __device__ __forceinline__ float c16() { return 1.0f / 6.0f; }
+    static __device__ __forceinline__ float c56() { return 5.0f / 6.0f; }
+    static __device__ __forceinline__ float k1() { return 13.0f / 12.0f; }
+    static __device__ __forceinline__ float eps5() { return 1e-16f; }
+    static __device__ __forceinline__ float eps3() { return 1e-14f; }
+    static __device__ __forceinline__ float tau(float v) { return v; }
+};
+
+// core/weno.f90:1-22
+template <typename T>
+__device__ __forceinline__ T weno3(T qm, T q0, T qp) {
+    typedef WenoK<T> K;
+    T qi1 = (-qm + T(3) * q0) * T(0.5);
+    T qi2 = (q0 + qp) * T(0.5);
+    T d1 = q0 - qm, d2 = qp - q0;
+    T beta1 = d1 * d1, beta2 = d2 * d2;
+    T tau = fabs(beta2 - beta1);
+    T w1 = T(1) + tau / (beta1 + K::eps3());
+    T w2 = (T(1) + tau / (beta2 + K::eps3())) * T(2);
+    return (w1 * qi1 + w2 * qi2) / (w1 + w2);
+}
+
+// core/weno.f90:25-54
+template <typename T>
+__device__ __forceinline__ T weno5(T qmm, T qm, T q0, T qp, T qpp) {
+    typedef WenoK<T> K;
+    T qi1 = K::c13() * qmm - K::c76() * qm + K::c116() * q0;
+    T qi2 = -(K::c16() * qm) + K::c56() * q0 + K::c13() * qp;
+    T qi3 = K::c13() * q0 + K::c56() * qp - K::c16() * qpp;
+    T a1 = qmm - T(2) * qm + q0, b1 = qmm - T(4) * qm + T(3) * q0;
+    T a2 = qm - T(2) * q0 + qp, b2 = qm - qp;
+    T a3 = q0 - T(2) * qp + qpp, b3 = T(3) * q0 - T(4) * qp + qpp;
+    T beta1 = K::k1() * (a1 * a1) + T(0.25) * (b1 * b1);
+    T beta2 = K::k1() * (a2 * a2) + T(0.25) * (b2 * b2);
+    T beta3 = K::k1() * (a3 * a3) + T(0.25) * (b3 * b3);
+    T tau5 = K::tau(fabs(beta1 - beta3));
+    T w1 = T(1) + tau5 / (beta1 + K::eps5());
+    T w2 = T(6) * (T(1) + tau5 / (beta2 + K::eps5()));
+    T w3 = T(3) * (T(1) + tau5 / (beta3 + K::eps5()));
+    return (w1 * qi1 + w2 * qi2 + w3 * qi3) / (w1 + w2 + w3);
+}
+
+// Value of core/weno.f90:106-153 `flux1d` at index i (0-based) of a line of length n
+// (n >= 5), given the velocity u at i and an accessor Q(j) for the advected quantity.
+// Branch precedence follows the Fortran statement order (later statements win).
+// In the interior the five stencil values are selected by the sign of u before a
+// single weno5 evaluation, so lanes of a warp do not diverge on the upwind side.
+template <typename T, typename QF>
+__device__ __forceinline__ T flux1d_at(int i, int n, T u, QF Q) {
+    if (i >= 2 && i <= n - 4) {
+        bool pos = u > T(0);
+        T qa = pos ? Q(i - 2) : Q(i + 3);
+        T qb = pos ? Q(i - 1) : Q(i + 2);
+        T qc = pos ? Q(i) : Q(i + 1);
+        T qd = pos ? Q(i + 1) : Q(i);
+        T qe = pos ? Q(i + 2) : Q(i - 1);
+        return u * weno5(qa, qb, qc, qd, qe);
+    }
+    if (i == n - 1) return T(0);
+    if (i == n - 2) return (u > T(0)) ? u * weno3(Q(i - 1), Q(i), Q(i + 1)) : u * Q(i + 1);
+    if (i == n - 3)
+        return (u > T(0)) ? u * weno5(Q(i - 2), Q(i - 1), Q(i), Q(i + 1), Q(i + 2))
+                          : u * weno3(Q(i + 2), Q(i + 1), Q(i));
+    if (i == 1) return (u > T(0)) ? u * weno3(Q(0), Q(1), Q(2)) : u * weno5(Q(4), Q(3), Q(2), Q(1), Q(0));
+    return (u > T(0)) ? u * Q(0) : u * weno3(Q(2), Q(1), Q(0));
+}
+
+// ---------------------------------------------------------------- exact rounding
+// Operations that must round once each, as numpy and gfortran do (no fused multiply-
+// add): elementwise time-scheme updates, differences and metric products.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+
+// ---------------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+template <typename T>
+__device__ __forceinline__ T warp_max(T v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+}  // namespace nyles

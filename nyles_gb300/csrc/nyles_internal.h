@@ -1,0 +1,120 @@
+// Internal (C++) interface between the translation units of libnyles_gb300.so.
+// Nothing here crosses the public C ABI (include/nyles_gb300.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "nyles_common.cuh"
+#include "../../include/nyles_gb300.h"
+
+namespace nyles {
+
+void set_error(const std::string& msg);
+int cuda_status(cudaError_t e, const char* where);
+void note_launch(int n = 1);
+
+// CUDA-event profiler of the model phases (NYLES_NPHASE in the public header)
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;   // 2 per slot
+    std::vector<int> phase;
+    size_t used = 0;
+    double ms[NYLES_NPHASE] = {};
+    long long cnt[NYLES_NPHASE] = {};
+    int begin(int ph, cudaStream_t st);
+    void end(int slot, cudaStream_t st);
+    void flush();
+    void release();
+};
+// RAII bracket of one phase; inert when the profiler is off or absent
+struct ProfScope {
+    Prof* p;
+    int slot;
+    cudaStream_t st;
+    ProfScope(Prof* p_, int ph, cudaStream_t s) : p(p_), slot(-1), st(s) {
+        if (p && p->on) slot = p->begin(ph, st);
+    }
+    ~ProfScope() {
+        if (p && slot >= 0) p->end(slot, st);
+    }
+};
+
+// Build the array geometry of a descriptor. Returns false on bad arguments.
+bool make_geom(const NylesDesc* d, Geom* g);
+
+template <typename T>
+struct StencilPtrs {
+    T* f[NYLES_F_T0 + NYLES_MAX_TR];   // state fields by NYLES_F_* id
+};
+template <typename T>
+struct ProgPtrs {
+    T* p[NYLES_MAX_PROG];              // prognostic registers: b, u_i, u_j, u_k, t0..
+};
+
+// term bits of launch_rhs
+enum { TERM_TRACER = 1, TERM_VF = 2, TERM_BERNOULLI = 4, TERM_VISC = 8, TERM_ACCUMULATE = 16 };
+
+template <typename T>
+int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
+               cudaStream_t st);
+
+// time-scheme elementwise updates (core/timescheme.py:113-221)
+enum { UPD_EULER = 0, UPD_RK3_2 = 1, UPD_RK3_3 = 2, UPD_LF_PRED = 3, UPD_LF_FIRST = 4, UPD_LF_CORR = 5 };
+template <typename T>
+int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs<T>& a, const ProgPtrs<T>& b,
+                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st);
+
+template <typename T>
+int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st);
+
+// divergence of the contravariant velocity: writes state div (every cell, halo as its
+// periodic image) and the interior right-hand side of the pressure solve
+template <typename T, typename TB>
+int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* mg_b, cudaStream_t st);
+
+// projection correction of the interior velocity and p on every cell
+template <typename T, typename TP>
+int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const TP* mg_x, double dx2,
+                   cudaStream_t st);
+
+// contravariant velocity, vorticity and kinetic energy from the filled velocity
+template <typename T>
+int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st);
+
+template <typename T>
+int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream_t st);
+
+template <typename T>
+int launch_max_U2(const Geom& g, const StencilPtrs<T>& s, double* partial, int npartial, double* out,
+                  cudaStream_t st);
+
+// ------------------------------------------------------------------ multigrid
+struct MgLevelDesc {
+    int n[3];         // interior extents z, y, x
+    long long vol;
+    size_t off_x, off_b, off_y;   // byte offsets inside the workspace
+};
+
+struct MgImpl {
+    int nlevels = 0;
+    int per[3] = {0, 0, 0};
+    int precision = NYLES_FP64;
+    double tol = 1e-6, omega = 0.9;
+    int maxite = 20;
+    MgLevelDesc lev[32];
+    // mixed precision: FP64 level-1 solution and right-hand side
+    size_t off_p64 = 0, off_b64 = 0;
+    size_t off_partial = 0, off_scalars = 0;
+    int npartial = 0;
+    size_t bytes = 0;
+    char* ws = nullptr;
+    NylesMgStats stats{};
+    Prof* prof = nullptr;             // phase timing (owned by the model)
+};
+
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision);
+int mg_solve(MgImpl* mg, cudaStream_t st);
+void* mg_level_ptr(MgImpl* mg, int lev, int var);
+
+}  // namespace nyles

@@ -1,0 +1,407 @@
+// Geometric multigrid of the pressure projection, one rank (core/mgfor).
+//
+// Level arrays hold interior cells only. The ghost layers of the reference are implied:
+// across a closed wall a ghost holds 0 and is "dry" (mask 0), in a periodic direction
+// it is the periodic image of the interior (mod_halo.f90:235-262). With that, every
+// operator coefficient of mgfor's setup (operators.f90:299-505) is a function of the
+// cell position and is evaluated in the kernels instead of being stored:
+//   diag  = number of wet face neighbours, idiag = 1/diag     (compute_diag)
+//   Rcoef = 1/2 on every coarse interior cell                   (compute_Rcoef)
+//   Pcoef = 1/(Wx*Wy*Wz), W = 3 + [coarse neighbour is wet]     (compute_Pcoef)
+// The smoother's intermediate `y` on the ghost ring (basicoperators.f90:380-388) is 0
+// across closed walls (its idiag and x are 0 there) and the periodic image otherwise.
+#include "nyles_internal.h"
+#include <vector>
+#include <cstring>
+
+namespace nyles {
+
+struct MgGeom {
+    int n[3];     // interior extents z, y, x
+    int per[3];
+};
+
+template <typename T>
+__device__ __forceinline__ T mg_rd(const T* __restrict__ a, const MgGeom& g, int z, int y, int x) {
+    if (z < 0 || z >= g.n[0]) { if (!g.per[0]) return T(0); z = z < 0 ? z + g.n[0] : z - g.n[0]; }
+    if (y < 0 || y >= g.n[1]) { if (!g.per[1]) return T(0); y = y < 0 ? y + g.n[1] : y - g.n[1]; }
+    if (x < 0 || x >= g.n[2]) { if (!g.per[2]) return T(0); x = x < 0 ? x + g.n[2] : x - g.n[2]; }
+    return a[((long long)z * g.n[1] + y) * g.n[2] + x];
+}
+
+__device__ __forceinline__ int mg_diag(const MgGeom& g, int z, int y, int x) {
+    const int p[3] = {z, y, x};
+    int d = 0;
+    for (int k = 0; k < 3; ++k) d += g.per[k] ? 2 : ((p[k] > 0) + (p[k] < g.n[k] - 1));
+    return d;
+}
+
+// sum of the six face neighbours in mgfor's order: x-1, x+1, y-1, y+1, z-1, z+1
+template <typename T>
+__device__ __forceinline__ T mg_nsum(const T* __restrict__ a, const MgGeom& g, int z, int y, int x) {
+    return ((((mg_rd(a, g, z, y, x - 1) + mg_rd(a, g, z, y, x + 1)) + mg_rd(a, g, z, y - 1, x)) +
+             mg_rd(a, g, z, y + 1, x)) + mg_rd(a, g, z - 1, y, x)) + mg_rd(a, g, z + 1, y, x);
+}
+
+// one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
+// (basicoperators.f90:379-398). With ACC, the result is also added to the FP64
+// solution `acc` (mixed precision: the correction of iterative refinement).
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(256) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
+                                                  const T* __restrict__ b, T* __restrict__ out, T omega,
+                                                  double* __restrict__ acc) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.n[2] || y >= g.n[1] || z >= g.n[0]) return;
+    const long long c = ((long long)z * g.n[1] + y) * g.n[2] + x;
+    const int dg = mg_diag(g, z, y, x);
+    const T idiag = dg > 0 ? T(1) / T(dg) : T(0);
+    const T cff1 = T(1) - omega;
+    const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idiag;
+    if (ACC) acc[c] = acc[c] + (double)v;
+    else out[c] = v;
+}
+
+// residual r = msk*(b + diag*x - sum(x_nb)) (basicoperators.f90:300-323)
+template <typename T>
+__device__ __forceinline__ T mg_resid(const T* __restrict__ x, const T* __restrict__ b, const MgGeom& g, int z, int y,
+                                      int xx) {
+    const long long c = ((long long)z * g.n[1] + y) * g.n[2] + xx;
+    const T dg = T(mg_diag(g, z, y, xx));
+    return (b[c] + dg * x[c]) - mg_nsum(x, g, z, y, xx);
+}
+
+// residual of the fine level restricted to the coarse right-hand side,
+// bc = Rcoef*(sum of the 8 children) with Rcoef = 1/2 (basicoperators.f90:32-60,
+// operators.f90:172-213); the coarse solution is zeroed (operators.f90:209)
+template <typename T>
+__global__ void __launch_bounds__(256) k_mg_restrict(const MgGeom gf, const T* __restrict__ xf,
+                                                    const T* __restrict__ bf, const MgGeom gc, T* __restrict__ bc,
+                                                    T* __restrict__ xc) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= gc.n[2] || y >= gc.n[1] || z >= gc.n[0]) return;
+    const int i = 2 * x, j = 2 * y, k = 2 * z;
+    T s = mg_resid(xf, bf, gf, k, j, i);
+    s = s + mg_resid(xf, bf, gf, k, j, i + 1);
+    s = s + mg_resid(xf, bf, gf, k, j + 1, i);
+    s = s + mg_resid(xf, bf, gf, k, j + 1, i + 1);
+    s = s + mg_resid(xf, bf, gf, k + 1, j, i);
+    s = s + mg_resid(xf, bf, gf, k + 1, j, i + 1);
+    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i);
+    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i + 1);
+    const long long c = ((long long)z * gc.n[1] + y) * gc.n[2] + x;
+    bc[c] = T(0.5) * s;
+    xc[c] = T(0);
+}
+
+// trilinear 9-3-3-1 prolongation added to the fine solution (basicoperators.f90:173-231)
+template <typename T>
+__global__ void __launch_bounds__(256) k_mg_prolong(const MgGeom gf, T* __restrict__ xf, const MgGeom gc,
+                                                   const T* __restrict__ xc) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= gf.n[2] || y >= gf.n[1] || z >= gf.n[0]) return;
+    const int ic = x >> 1, jc = y >> 1, kc = z >> 1;
+    const int si = (x & 1) ? 1 : -1, sj = (y & 1) ? 1 : -1, sk = (z & 1) ? 1 : -1;
+    auto plane = [&](int kk) -> T {
+        return ((T(9) * mg_rd(xc, gc, kk, jc, ic) + T(3) * mg_rd(xc, gc, kk, jc, ic + si)) +
+                T(3) * mg_rd(xc, gc, kk, jc + sj, ic)) + mg_rd(xc, gc, kk, jc + sj, ic + si);
+    };
+    const T bpl = plane(kc);
+    const T opl = plane(kc + sk);
+    auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
+    const int W = (3 + wet(2, ic + si)) * (3 + wet(1, jc + sj)) * (3 + wet(0, kc + sk));
+    const T pcoef = T(1.0 / (double)W);
+    const long long c = ((long long)z * gf.n[1] + y) * gf.n[2] + x;
+    xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
+}
+
+// ---------------------------------------------------------------- reductions
+// deterministic: fixed grid of `npart` blocks, block partials, one final block
+template <typename T, int MODE>   // MODE 0: sum v^2 ; 1: sum r^2 with r = b - A x
+__global__ void __launch_bounds__(256) k_mg_sumsq(const MgGeom g, const T* __restrict__ v, const T* __restrict__ b,
+                                                 double* __restrict__ partial) {
+    const long long vol = (long long)g.n[0] * g.n[1] * g.n[2];
+    double s = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
+        double val;
+        if (MODE == 0) {
+            val = (double)v[i];
+        } else {
+            const int x = (int)(i % g.n[2]);
+            const int y = (int)((i / g.n[2]) % g.n[1]);
+            const int z = (int)(i / ((long long)g.n[2] * g.n[1]));
+            val = (double)mg_resid(v, b, g, z, y, x);
+        }
+        s += val * val;
+    }
+    __shared__ double sm[8];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+    }
+}
+
+// mixed precision: FP64 residual of the FP64 solution, its sum of squares, the FP32
+// right-hand side of the next correction V-cycle and a zero initial correction
+__global__ void __launch_bounds__(256) k_mg_resid64(const MgGeom g, const double* __restrict__ p,
+                                                   const double* __restrict__ b, float* __restrict__ r32,
+                                                   float* __restrict__ e32, double* __restrict__ partial) {
+    const long long vol = (long long)g.n[0] * g.n[1] * g.n[2];
+    double s = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
+        const int x = (int)(i % g.n[2]);
+        const int y = (int)((i / g.n[2]) % g.n[1]);
+        const int z = (int)(i / ((long long)g.n[2] * g.n[1]));
+        const double r = mg_resid(p, b, g, z, y, x);
+        r32[i] = (float)r;
+        e32[i] = 0.0f;
+        s += r * r;
+    }
+    __shared__ double sm[8];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_mg_final(const double* __restrict__ partial, int n, double* __restrict__ out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+    __shared__ double sm[32];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) *out = t;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+static inline dim3 mg_grid(const int n[3], dim3 b) {
+    return dim3((n[2] + b.x - 1) / b.x, (n[1] + b.y - 1) / b.y, (n[0] + b.z - 1) / b.z);
+}
+static inline MgGeom mgg(const MgImpl* mg, int l) {
+    MgGeom g;
+    for (int k = 0; k < 3; ++k) { g.n[k] = mg->lev[l].n[k]; g.per[k] = mg->per[k]; }
+    return g;
+}
+static inline bool empty(const MgImpl* mg, int l) { return mg->lev[l].vol == 0; }
+
+template <typename T>
+static T* lvp(MgImpl* mg, int l, int var) {
+    size_t off = var == 1 ? mg->lev[l].off_x : (var == 2 ? mg->lev[l].off_b : mg->lev[l].off_y);
+    return reinterpret_cast<T*>(mg->ws + off);
+}
+
+void* mg_level_ptr(MgImpl* mg, int lev, int var) {
+    if (!mg->ws || lev < 1 || lev > mg->nlevels) return nullptr;
+    if (lev == 1 && mg->precision == NYLES_MIXED) {
+        if (var == 1) return mg->ws + mg->off_p64;
+        if (var == 2) return mg->ws + mg->off_b64;
+    }
+    size_t off = var == 1 ? mg->lev[lev - 1].off_x : (var == 2 ? mg->lev[lev - 1].off_b : mg->lev[lev - 1].off_y);
+    return mg->ws + off;
+}
+
+// mg_setup.f90:225-307 (create_hierarchy) for one rank. The reference leaves the loop
+// only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
+// 3*2^n sizes terminate (the reference does not terminate on them).
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
+    if (nx < 2 || ny < 2 || nz < 1) { set_error("multigrid: grid too small"); return NYLES_BAD_ARG; }
+    if (topology < 1 || topology > 6) { set_error("multigrid: bad topology"); return NYLES_BAD_ARG; }
+    mg->precision = precision;
+    mg->per[2] = (topology == NYLES_MG_XPERIO || topology == NYLES_MG_XYPERIO || topology == NYLES_MG_XYZPERIO);
+    mg->per[1] = (topology == NYLES_MG_YPERIO || topology == NYLES_MG_XYPERIO || topology == NYLES_MG_XYZPERIO);
+    mg->per[0] = (topology == NYLES_MG_ZPERIO || topology == NYLES_MG_XYZPERIO);
+    const int nh = 3;
+    int x = nx, y = ny, z = nz + 2 * nh;
+    int L = 0;
+    while (true) {
+        if (L >= 32) { set_error("multigrid: too many levels"); return NYLES_UNSUPPORTED; }
+        MgLevelDesc& d = mg->lev[L];
+        d.n[0] = z - 2 * nh; d.n[1] = y; d.n[2] = x;
+        if (d.n[0] < 0) d.n[0] = 0;
+        d.vol = (long long)d.n[0] * d.n[1] * d.n[2];
+        ++L;
+        if (x == 2 || y == 2) break;
+        if ((x % 2) || (y % 2) || x < 4 || y < 4) break;
+        x /= 2; y /= 2; z = z / 2 + nh;
+    }
+    mg->nlevels = L;
+    // An odd z extent above the coarsest level makes mgfor's prolongation write a ghost
+    // layer (basicoperators.f90:194-229 steps k by 2 up to nz-nh); not supported.
+    for (int l = 0; l + 1 < L; ++l)
+        if (mg->lev[l].n[0] % 2) { set_error("multigrid: z extent must stay even above the coarsest level"); return NYLES_UNSUPPORTED; }
+    if (mg->lev[0].n[0] < 1) { set_error("multigrid: empty grid"); return NYLES_BAD_ARG; }
+    // workspace layout
+    const size_t es = precision == NYLES_MIXED ? sizeof(float) : sizeof(double);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    for (int l = 0; l < L; ++l) {
+        MgLevelDesc& d = mg->lev[l];
+        d.off_x = take(d.vol * es);
+        d.off_b = take(d.vol * es);
+        d.off_y = take(d.vol * es);
+    }
+    if (precision == NYLES_MIXED) {
+        mg->off_p64 = take(mg->lev[0].vol * sizeof(double));
+        mg->off_b64 = take(mg->lev[0].vol * sizeof(double));
+    }
+    mg->npartial = 152 * 4;
+    mg->off_partial = take(mg->npartial * sizeof(double));
+    mg->off_scalars = take(16 * sizeof(double));
+    mg->bytes = off;
+    return NYLES_OK;
+}
+
+template <typename T>
+static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
+    if (empty(mg, l)) return;
+    MgGeom g = mgg(mg, l);
+    dim3 blk(32, 4, 2);
+    dim3 grd = mg_grid(g.n, blk);
+    T* x = lvp<T>(mg, l, 1);
+    T* b = lvp<T>(mg, l, 2);
+    T* y = lvp<T>(mg, l, 3);
+    const T om = T(mg->omega);
+    ProfScope ps(mg->prof, 8, st);
+    note_launch(2);
+    k_mg_jacobi<T, false><<<grd, blk, 0, st>>>(g, x, b, y, om, nullptr);
+    if (acc_p64)
+        k_mg_jacobi<T, true><<<grd, blk, 0, st>>>(g, y, b, x, om, reinterpret_cast<double*>(mg->ws + mg->off_p64));
+    else
+        k_mg_jacobi<T, false><<<grd, blk, 0, st>>>(g, y, b, x, om, nullptr);
+}
+
+// solvers.f90:35-55
+template <typename T>
+static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
+    const int L = mg->nlevels;
+    dim3 blk(32, 4, 2);
+    for (int l = 0; l < L - 1; ++l) {
+        smooth<T>(mg, l, st, false);
+        if (!empty(mg, l + 1)) {
+            MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
+            ProfScope ps(mg->prof, 9, st);
+            note_launch();
+            k_mg_restrict<T><<<mg_grid(gc.n, blk), blk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
+                                                                lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 1));
+        }
+    }
+    smooth<T>(mg, L - 1, st, L == 1 && mixed);
+    for (int l = L - 2; l >= 0; --l) {
+        if (!empty(mg, l + 1)) {
+            MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
+            ProfScope ps(mg->prof, 10, st);
+            note_launch();
+            k_mg_prolong<T><<<mg_grid(gf.n, blk), blk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
+        }
+        smooth<T>(mg, l, st, l == 0 && mixed);
+    }
+}
+
+template <typename T, int MODE>
+static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* host_out, cudaStream_t st) {
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    {
+        ProfScope ps(mg->prof, 11, st);
+        note_launch(2);
+        k_mg_sumsq<T, MODE><<<mg->npartial, 256, 0, st>>>(g, v, b, part);
+        k_mg_final<<<1, 1024, 0, st>>>(part, mg->npartial, out);
+    }
+    cudaError_t e = cudaMemcpyAsync(host_out, out, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e, "multigrid norm");
+}
+
+static int resid64(MgImpl* mg, double* host_out, cudaStream_t st) {
+    MgGeom g = mgg(mg, 0);
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    {
+        ProfScope ps(mg->prof, 11, st);
+        note_launch(2);
+        k_mg_resid64<<<mg->npartial, 256, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
+                                                    reinterpret_cast<const double*>(mg->ws + mg->off_b64),
+                                                    lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
+        k_mg_final<<<1, 1024, 0, st>>>(part, mg->npartial, out);
+    }
+    cudaError_t e = cudaMemcpyAsync(host_out, out, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e, "multigrid residual");
+}
+
+// solvers.f90:8-33: stop when sum(r^2)/sum(b^2) < tol or after maxite V-cycles
+int mg_solve(MgImpl* mg, cudaStream_t st) {
+    if (!mg->ws) { set_error("multigrid: workspace not bound"); return NYLES_BAD_ARG; }
+    MgGeom g0 = mgg(mg, 0);
+    int nite = 0;
+    double normb = 0.0, rr = 0.0, res = 0.0;
+    int rc;
+    if (mg->precision == NYLES_FP64) {
+        double* x = lvp<double>(mg, 0, 1);
+        double* b = lvp<double>(mg, 0, 2);
+        if ((rc = sumsq<double, 0>(mg, g0, b, nullptr, &normb, st))) return rc;
+        if (normb > 0.0) {
+            if ((rc = sumsq<double, 1>(mg, g0, x, b, &rr, st))) return rc;
+            res = rr / normb;
+        }
+        while (true) {
+            if (res < mg->tol) break;
+            vcycle<double>(mg, st, false);
+            ++nite;
+            if (nite >= mg->maxite) break;
+            if (normb > 0.0) {
+                if ((rc = sumsq<double, 1>(mg, g0, x, b, &rr, st))) return rc;
+                res = rr / normb;
+            } else {
+                res = 0.0;
+            }
+        }
+    } else {
+        const double* b64 = reinterpret_cast<const double*>(mg->ws + mg->off_b64);
+        if ((rc = sumsq<double, 0>(mg, g0, b64, nullptr, &normb, st))) return rc;
+        if (normb > 0.0) {
+            if ((rc = resid64(mg, &rr, st))) return rc;
+            res = rr / normb;
+        }
+        while (true) {
+            if (res < mg->tol) break;
+            vcycle<float>(mg, st, true);   // FP32 correction of the residual equation, added to p64
+            ++nite;
+            if (nite >= mg->maxite) break;
+            if (normb > 0.0) {
+                if ((rc = resid64(mg, &rr, st))) return rc;
+                res = rr / normb;
+            } else {
+                res = 0.0;
+            }
+        }
+    }
+    mg->stats.nite = nite;
+    mg->stats.res = res;
+    mg->stats.solves += 1;
+    mg->stats.vcycles += nite;
+    if (res >= mg->tol && nite >= mg->maxite) mg->stats.not_converged += 1;
+    return cuda_status(cudaGetLastError(), "multigrid solve");
+}
+
+}  // namespace nyles

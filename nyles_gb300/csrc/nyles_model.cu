@@ -1,0 +1,490 @@
+// C ABI of libnyles_gb300.so and the native orchestration of one time step
+// (core/model_les.py, core/model_les_euler.py, core/timescheme.py, core/projection.py,
+// core/mgfordriver.py restated as a sequence of kernel launches on one stream).
+#include "nyles_internal.h"
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace nyles {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int cuda_status(cudaError_t e, const char* where) {
+    if (e == cudaSuccess) return NYLES_OK;
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return NYLES_CUDA_ERROR;
+}
+
+static std::atomic<long long> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// ------------------------------------------------------------------ profiler
+static const size_t kProfSlots = 4096;
+
+int Prof::begin(int ph, cudaStream_t st) {
+    if (ev.empty()) {
+        ev.resize(2 * kProfSlots);
+        phase.resize(kProfSlots);
+        for (auto& e : ev)
+            if (cudaEventCreate(&e) != cudaSuccess) { ev.clear(); on = false; return -1; }
+    }
+    if (used == kProfSlots) flush();
+    const int slot = (int)used++;
+    phase[slot] = ph;
+    cudaEventRecord(ev[2 * slot], st);
+    return slot;
+}
+
+void Prof::end(int slot, cudaStream_t st) { cudaEventRecord(ev[2 * slot + 1], st); }
+
+void Prof::flush() {
+    if (used == 0) return;
+    cudaEventSynchronize(ev[2 * (used - 1) + 1]);
+    for (size_t s = 0; s < used; ++s) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ev[2 * s], ev[2 * s + 1]) == cudaSuccess) {
+            ms[phase[s]] += t;
+            cnt[phase[s]] += 1;
+        }
+    }
+    used = 0;
+}
+
+void Prof::release() {
+    for (auto& e : ev) cudaEventDestroy(e);
+    ev.clear();
+    used = 0;
+}
+
+static int check_desc(const NylesDesc* d, Geom* g) {
+    if (!d) { set_error("null descriptor"); return NYLES_BAD_ARG; }
+    if (d->n_tracers < 0 || d->n_tracers > NYLES_MAX_TR) { set_error("n_tracers out of range (0..8)"); return NYLES_BAD_ARG; }
+    if (d->model < 0 || d->model > 2) { set_error("unknown model"); return NYLES_BAD_ARG; }
+    if ((d->periodic_x || d->periodic_y || d->periodic_z) && d->nh != 3) {
+        set_error("periodic directions need nh == 3 (the multigrid halo width, mg_types.f90:18)");
+        return NYLES_UNSUPPORTED;
+    }
+    if (!make_geom(d, g)) { set_error("bad grid extents (every array line needs at least 5 points)"); return NYLES_BAD_ARG; }
+    return NYLES_OK;
+}
+
+template <typename T>
+static StencilPtrs<T> field_ptrs(const NylesDesc* d, T* const* fields) {
+    StencilPtrs<T> s;
+    for (int i = 0; i < NYLES_F_T0 + NYLES_MAX_TR; ++i)
+        s.f[i] = (i < NYLES_F_T0 + d->n_tracers) ? fields[i] : nullptr;
+    return s;
+}
+template <typename T>
+static ProgPtrs<T> prog_ptrs(const NylesDesc* d, T* const* p) {
+    ProgPtrs<T> s;
+    for (int i = 0; i < NYLES_MAX_PROG; ++i) s.p[i] = (p && i < 4 + d->n_tracers) ? p[i] : nullptr;
+    return s;
+}
+template <typename T>
+static ProgPtrs<T> state_prog(const NylesDesc* d, const StencilPtrs<T>& s) {
+    ProgPtrs<T> p;
+    for (int i = 0; i < NYLES_MAX_PROG; ++i) p.p[i] = nullptr;
+    p.p[0] = s.f[NYLES_F_B];
+    for (int k = 0; k < 3; ++k) p.p[1 + k] = s.f[NYLES_F_U_I + k];
+    for (int t = 0; t < d->n_tracers; ++t) p.p[4 + t] = s.f[NYLES_F_T0 + t];
+    return p;
+}
+
+static int rhs_terms(const NylesDesc* d, int last) {
+    int t = TERM_BERNOULLI;
+    if (d->model != NYLES_MODEL_EULER3D) t |= TERM_TRACER;   // model_les_euler.py:131
+    if (d->model != NYLES_MODEL_LINEAR) t |= TERM_VF;        // model_les.py:135-136
+    if (last && d->add_viscosity) t |= TERM_VISC;            // model_les.py:140-141
+    return t;
+}
+
+}  // namespace nyles
+
+using namespace nyles;
+
+struct NylesMg {
+    MgImpl impl;
+};
+
+struct NylesModel {
+    NylesDesc d;
+    Geom g;
+    int scheme = NYLES_SCHEME_RK3_SSP;
+    int precision = NYLES_FP64;
+    int nprog = 4;
+    bool lf_first = true;
+    void* fields[NYLES_F_T0 + NYLES_MAX_TR] = {};
+    void* regs[3][NYLES_MAX_PROG] = {};
+    char* ws = nullptr;
+    size_t off_partial = 0, off_scalar = 0, mg_off = 0, bytes = 0;
+    int npartial = 152 * 4;
+    MgImpl mg;
+    Prof prof;
+    bool bound = false;
+    ~NylesModel() { prof.release(); }
+};
+
+extern "C" {
+
+const char* nyles_last_error(void) { return g_last_error.c_str(); }
+int nyles_version(void) { return 10000; }
+
+// ------------------------------------------------------------------ kernel entries
+int nyles_flux1d_f64(const double* u, const double* q, double* flux, int nlines, int n, void* stream) {
+    if (n < 5 || nlines < 0 || !u || !q || !flux) { set_error("flux1d: n >= 5 and non-null arrays required"); return NYLES_BAD_ARG; }
+    return launch_flux1d<double>(u, q, flux, nlines, n, (cudaStream_t)stream);
+}
+int nyles_flux1d_f32(const float* u, const float* q, float* flux, int nlines, int n, void* stream) {
+    if (n < 5 || nlines < 0 || !u || !q || !flux) { set_error("flux1d: n >= 5 and non-null arrays required"); return NYLES_BAD_ARG; }
+    return launch_flux1d<float>(u, q, flux, nlines, n, (cudaStream_t)stream);
+}
+
+extern "C++" {
+template <typename T>
+static int vortex_force_impl(const NylesDesc* d, T* const* fields, T* const* ds, void* stream) {
+    Geom g;
+    int rc = check_desc(d, &g);
+    if (rc) return rc;
+    if (!fields || !ds) { set_error("null arrays"); return NYLES_BAD_ARG; }
+    return launch_rhs<T>(d, g, field_ptrs<T>(d, fields), prog_ptrs<T>(d, ds), TERM_VF | TERM_ACCUMULATE,
+                         (cudaStream_t)stream);
+}
+}  // extern "C++"
+int nyles_vortex_force_f64(const NylesDesc* d, double* const* fields, double* const* ds, void* stream) {
+    return vortex_force_impl<double>(d, fields, ds, stream);
+}
+int nyles_vortex_force_f32(const NylesDesc* d, float* const* fields, float* const* ds, void* stream) {
+    return vortex_force_impl<float>(d, fields, ds, stream);
+}
+
+extern "C++" {
+template <typename T>
+static int rhs_impl(const NylesDesc* d, T* const* fields, T* const* ds, int last, void* stream) {
+    Geom g;
+    int rc = check_desc(d, &g);
+    if (rc) return rc;
+    if (!fields || !ds) { set_error("null arrays"); return NYLES_BAD_ARG; }
+    return launch_rhs<T>(d, g, field_ptrs<T>(d, fields), prog_ptrs<T>(d, ds), rhs_terms(d, last),
+                         (cudaStream_t)stream);
+}
+}  // extern "C++"
+int nyles_rhs_f64(const NylesDesc* d, double* const* fields, double* const* ds, int last, void* stream) {
+    return rhs_impl<double>(d, fields, ds, last, stream);
+}
+int nyles_rhs_f32(const NylesDesc* d, float* const* fields, float* const* ds, int last, void* stream) {
+    return rhs_impl<float>(d, fields, ds, last, stream);
+}
+
+extern "C++" {
+template <typename T>
+static int fill_impl(const NylesDesc* d, T* field, void* stream) {
+    Geom g;
+    int rc = check_desc(d, &g);
+    if (rc) return rc;
+    if (!field) { set_error("null array"); return NYLES_BAD_ARG; }
+    T* f[1] = {field};
+    return launch_fill<T>(g, f, 1, (cudaStream_t)stream);
+}
+}  // extern "C++"
+int nyles_fill_f64(const NylesDesc* d, double* field, void* stream) { return fill_impl<double>(d, field, stream); }
+int nyles_fill_f32(const NylesDesc* d, float* field, void* stream) { return fill_impl<float>(d, field, stream); }
+
+// ------------------------------------------------------------------ multigrid
+int nyles_mg_create(int nx, int ny, int nz, int topology, int precision, NylesMg** out) {
+    if (!out) { set_error("null output"); return NYLES_BAD_ARG; }
+    *out = nullptr;
+    if (precision != NYLES_FP64 && precision != NYLES_MIXED) { set_error("bad precision"); return NYLES_BAD_ARG; }
+    NylesMg* m = new (std::nothrow) NylesMg();
+    if (!m) { set_error("host allocation failed"); return NYLES_BAD_ARG; }
+    int rc = mg_init(&m->impl, nx, ny, nz, topology, precision);
+    if (rc) { delete m; return rc; }
+    *out = m;
+    return NYLES_OK;
+}
+int nyles_mg_destroy(NylesMg* mg) { delete mg; return NYLES_OK; }
+int nyles_mg_workspace_bytes(const NylesMg* mg, size_t* bytes) {
+    if (!mg || !bytes) { set_error("null argument"); return NYLES_BAD_ARG; }
+    *bytes = mg->impl.bytes;
+    return NYLES_OK;
+}
+int nyles_mg_bind(NylesMg* mg, void* workspace) {
+    if (!mg || !workspace) { set_error("null argument"); return NYLES_BAD_ARG; }
+    if (((uintptr_t)workspace) & 255) { set_error("workspace must be 256-byte aligned"); return NYLES_BAD_ARG; }
+    mg->impl.ws = (char*)workspace;
+    return NYLES_OK;
+}
+int nyles_mg_nlevels(const NylesMg* mg, int* nlevels) {
+    if (!mg || !nlevels) { set_error("null argument"); return NYLES_BAD_ARG; }
+    *nlevels = mg->impl.nlevels;
+    return NYLES_OK;
+}
+int nyles_mg_level_shape(const NylesMg* mg, int lev, int* shape3) {
+    if (!mg || !shape3 || lev < 1 || lev > mg->impl.nlevels) { set_error("bad level"); return NYLES_BAD_ARG; }
+    for (int k = 0; k < 3; ++k) shape3[k] = mg->impl.lev[lev - 1].n[k];
+    return NYLES_OK;
+}
+int nyles_mg_level_ptr(NylesMg* mg, int lev, int var, void** ptr) {
+    if (!mg || !ptr || var < 1 || var > 2) { set_error("bad argument"); return NYLES_BAD_ARG; }
+    *ptr = mg_level_ptr(&mg->impl, lev, var);
+    if (!*ptr) { set_error("workspace not bound or bad level"); return NYLES_BAD_ARG; }
+    return NYLES_OK;
+}
+int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega) {
+    if (!mg || maxite < 0 || !(tol >= 0.0) || !(omega > 0.0)) { set_error("bad multigrid parameters"); return NYLES_BAD_ARG; }
+    mg->impl.tol = tol; mg->impl.maxite = maxite; mg->impl.omega = omega;
+    return NYLES_OK;
+}
+int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream) {
+    if (!mg) { set_error("null multigrid"); return NYLES_BAD_ARG; }
+    int rc = mg_solve(&mg->impl, (cudaStream_t)stream);
+    if (stats) *stats = mg->impl.stats;
+    if (rc) return rc;
+    return mg->impl.stats.nite >= mg->impl.maxite && mg->impl.stats.res >= mg->impl.tol ? NYLES_NOT_CONVERGED : NYLES_OK;
+}
+
+// ------------------------------------------------------------------ model
+int nyles_model_create(const NylesDesc* d, int scheme, int precision, NylesModel** out) {
+    if (!out) { set_error("null output"); return NYLES_BAD_ARG; }
+    *out = nullptr;
+    Geom g;
+    int rc = check_desc(d, &g);
+    if (rc) return rc;
+    if (scheme < 0 || scheme > 2) { set_error("unknown time scheme"); return NYLES_BAD_ARG; }
+    if (precision != NYLES_FP64 && precision != NYLES_MIXED) { set_error("bad precision"); return NYLES_BAD_ARG; }
+    NylesModel* m = new (std::nothrow) NylesModel();
+    if (!m) { set_error("host allocation failed"); return NYLES_BAD_ARG; }
+    m->d = *d;
+    m->g = g;
+    m->scheme = scheme;
+    m->precision = precision;
+    m->nprog = 4 + d->n_tracers;
+    // multigrid topology from the geometry (core/model_les.py:80-93)
+    int topo;
+    if (d->periodic_x && d->periodic_y && d->periodic_z) topo = NYLES_MG_XYZPERIO;
+    else if (d->periodic_x && d->periodic_y) topo = NYLES_MG_XYPERIO;
+    else if (d->periodic_x) topo = NYLES_MG_XPERIO;
+    else if (d->periodic_y) topo = NYLES_MG_YPERIO;
+    else topo = NYLES_MG_CLOSED;
+    if (d->periodic_z && !(d->periodic_x && d->periodic_y)) {
+        delete m;
+        set_error("z-periodic geometry needs x and y periodic (perio_xyz)");
+        return NYLES_UNSUPPORTED;
+    }
+    rc = mg_init(&m->mg, d->nx, d->ny, d->nz, topo, precision);
+    if (rc) { delete m; return rc; }
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    m->mg_off = take(m->mg.bytes);
+    m->off_partial = take(m->npartial * sizeof(double));
+    m->off_scalar = take(16 * sizeof(double));
+    m->bytes = off;
+    *out = m;
+    return NYLES_OK;
+}
+
+int nyles_model_destroy(NylesModel* m) { delete m; return NYLES_OK; }
+
+int nyles_model_workspace_bytes(const NylesModel* m, size_t* bytes) {
+    if (!m || !bytes) { set_error("null argument"); return NYLES_BAD_ARG; }
+    *bytes = m->bytes;
+    return NYLES_OK;
+}
+
+int nyles_model_bind(NylesModel* m, void* const* fields, void* const* regs, void* workspace) {
+    if (!m || !fields || !regs || !workspace) { set_error("null argument"); return NYLES_BAD_ARG; }
+    if (((uintptr_t)workspace) & 255) { set_error("workspace must be 256-byte aligned"); return NYLES_BAD_ARG; }
+    for (int i = 0; i < NYLES_F_T0 + m->d.n_tracers; ++i) {
+        if (!fields[i]) { set_error("null field pointer"); return NYLES_BAD_ARG; }
+        m->fields[i] = fields[i];
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int q = 0; q < m->nprog; ++q) {
+            void* p = regs[r * m->nprog + q];
+            if (!p) { set_error("null register pointer"); return NYLES_BAD_ARG; }
+            m->regs[r][q] = p;
+        }
+    m->ws = (char*)workspace;
+    m->mg.ws = m->ws + m->mg_off;
+    m->bound = true;
+    return NYLES_OK;
+}
+
+int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omega) {
+    if (!m || maxite < 0 || !(tol >= 0.0) || !(omega > 0.0)) { set_error("bad multigrid parameters"); return NYLES_BAD_ARG; }
+    m->mg.tol = tol; m->mg.maxite = maxite; m->mg.omega = omega;
+    return NYLES_OK;
+}
+
+int nyles_model_reset_scheme(NylesModel* m) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    m->lf_first = true;
+    return NYLES_OK;
+}
+
+int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
+    if (!m || !stats) { set_error("null argument"); return NYLES_BAD_ARG; }
+    *stats = m->mg.stats;
+    return NYLES_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ orchestration
+namespace nyles {
+
+template <typename T>
+static int model_rhs(NylesModel* m, int reg, int last, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    ProgPtrs<T> ds = prog_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->regs[reg]));
+    ProfScope ps(&m->prof, 0, st);
+    return launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st);
+}
+
+// core/model_les.py:98-127 ; core/model_les_euler.py:96-125
+template <typename T>
+static int model_diagnose(NylesModel* m, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    int rc;
+    T* uf[4] = {s.f[NYLES_F_B], s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
+    if (m->d.model != NYLES_MODEL_EULER3D) {
+        ProfScope ps(&m->prof, 2, st);
+        if ((rc = launch_fill<T>(m->g, uf, 4, st))) return rc;
+    }
+    double* mgb = reinterpret_cast<double*>(mg_level_ptr(&m->mg, 1, 2));
+    double* mgx = reinterpret_cast<double*>(mg_level_ptr(&m->mg, 1, 1));
+    {
+        ProfScope ps(&m->prof, 3, st);
+        if ((rc = launch_div<T, double>(&m->d, m->g, s, mgb, st))) return rc;
+    }
+    {
+        ProfScope ps(&m->prof, 4, st);
+        m->mg.prof = m->prof.on ? &m->prof : nullptr;
+        if ((rc = mg_solve(&m->mg, st))) return rc;
+    }
+    {
+        ProfScope ps(&m->prof, 5, st);
+        if ((rc = launch_correct<T, double>(&m->d, m->g, s, mgx, m->d.dx2, st))) return rc;
+    }
+    {
+        ProfScope ps(&m->prof, 2, st);
+        if ((rc = launch_fill<T>(m->g, uf + 1, 3, st))) return rc;
+    }
+    ProfScope ps(&m->prof, 6, st);
+    return launch_diag<T>(&m->d, m->g, s, m->d.model != NYLES_MODEL_LINEAR, st);
+}
+
+template <typename T>
+static int model_update(NylesModel* m, int kind, int ra, int rb, int rc_, double dt, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    ProgPtrs<T> sp = state_prog<T>(&m->d, s);
+    auto reg = [&](int r) { return prog_ptrs<T>(&m->d, r >= 0 ? reinterpret_cast<T* const*>(m->regs[r]) : nullptr); };
+    ProfScope ps(&m->prof, 1, st);
+    return launch_update<T>(m->g, m->nprog, sp, reg(ra), reg(rb), reg(rc_), kind, dt, st);
+}
+
+// core/timescheme.py:113-221
+template <typename T>
+static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
+    (void)t;
+    int rc;
+    if (m->scheme == NYLES_SCHEME_RK3_SSP) {
+        if ((rc = model_rhs<T>(m, 0, 0, st))) return rc;
+        if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
+        if ((rc = model_diagnose<T>(m, st))) return rc;
+        if ((rc = model_rhs<T>(m, 1, 0, st))) return rc;
+        if ((rc = model_update<T>(m, UPD_RK3_2, 0, 1, -1, dt, st))) return rc;
+        if ((rc = model_diagnose<T>(m, st))) return rc;
+        if ((rc = model_rhs<T>(m, 2, 1, st))) return rc;
+        if ((rc = model_update<T>(m, UPD_RK3_3, 0, 1, 2, dt, st))) return rc;
+        return model_diagnose<T>(m, st);
+    }
+    if (m->scheme == NYLES_SCHEME_EF) {
+        if ((rc = model_rhs<T>(m, 0, 1, st))) return rc;
+        if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
+        return model_diagnose<T>(m, st);
+    }
+    // LFAM3: registers 0 = dstate, 1 = stateb, 2 = state (n)
+    if ((rc = model_rhs<T>(m, 0, 0, st))) return rc;
+    if (m->lf_first) {
+        if ((rc = model_update<T>(m, UPD_LF_FIRST, 0, 1, 2, dt, st))) return rc;
+        m->lf_first = false;
+        return model_diagnose<T>(m, st);
+    }
+    if ((rc = model_update<T>(m, UPD_LF_PRED, 0, 1, 2, dt, st))) return rc;
+    if ((rc = model_diagnose<T>(m, st))) return rc;
+    if ((rc = model_rhs<T>(m, 0, 1, st))) return rc;
+    if ((rc = model_update<T>(m, UPD_LF_CORR, 0, 1, 2, dt, st))) return rc;
+    return model_diagnose<T>(m, st);
+}
+
+}  // namespace nyles
+
+extern "C" {
+
+int nyles_model_forward(NylesModel* m, double t, double dt, void* stream) {
+    if (!m || !m->bound) { set_error("model not bound"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    return m->precision == NYLES_FP64 ? model_forward<double>(m, t, dt, st) : model_forward<float>(m, t, dt, st);
+}
+
+int nyles_model_diagnose(NylesModel* m, void* stream) {
+    if (!m || !m->bound) { set_error("model not bound"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    return m->precision == NYLES_FP64 ? model_diagnose<double>(m, st) : model_diagnose<float>(m, st);
+}
+
+int nyles_model_rhs(NylesModel* m, int reg, int last, void* stream) {
+    if (!m || !m->bound || reg < 0 || reg > 2) { set_error("model not bound or bad register"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    return m->precision == NYLES_FP64 ? model_rhs<double>(m, reg, last, st) : model_rhs<float>(m, reg, last, st);
+}
+
+int nyles_model_max_U2(NylesModel* m, double* out, void* stream) {
+    if (!m || !m->bound || !out) { set_error("model not bound or null output"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    double* part = reinterpret_cast<double*>(m->ws + m->off_partial);
+    double* dev = reinterpret_cast<double*>(m->ws + m->off_scalar);
+    int rc;
+    ProfScope ps(&m->prof, 7, st);
+    if (m->precision == NYLES_FP64)
+        rc = launch_max_U2<double>(m->g, field_ptrs<double>(&m->d, reinterpret_cast<double* const*>(m->fields)), part,
+                                   m->npartial, dev, st);
+    else
+        rc = launch_max_U2<float>(m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)), part,
+                                  m->npartial, dev, st);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(out, dev, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    rc = cuda_status(e, "max_U2 read-back");
+    if (rc) return rc;
+    if (!(*out == *out) || *out > 1.7976931348623157e308) { set_error("non-finite velocity"); return NYLES_BLOWUP; }
+    return NYLES_OK;
+}
+
+int nyles_model_profile(NylesModel* m, int enable) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    if (!enable) m->prof.flush();
+    m->prof.on = enable != 0;
+    return NYLES_OK;
+}
+
+int nyles_model_profile_read(NylesModel* m, double* ms, long long* count, int nphase) {
+    if (!m || !ms || !count || nphase < 0) { set_error("bad argument"); return NYLES_BAD_ARG; }
+    m->prof.flush();
+    for (int i = 0; i < nphase && i < NYLES_NPHASE; ++i) {
+        ms[i] = m->prof.ms[i];
+        count[i] = m->prof.cnt[i];
+        m->prof.ms[i] = 0.0;
+        m->prof.cnt[i] = 0;
+    }
+    return NYLES_OK;
+}
+
+long long nyles_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

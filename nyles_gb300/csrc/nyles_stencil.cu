@@ -1,0 +1,642 @@
+// Stencil kernels of the Nyles time step: right-hand side (tracer advection, vortex
+// force, Bernoulli, viscosity), time-scheme updates, periodic halo fill, divergence,
+// and the projection correction fused with the contravariant velocity, vorticity and
+// kinetic energy.
+//
+// Every kernel walks the full model arrays, halo included, and reproduces the
+// reference's array-end closures there: halo cells of b, u, vor and ke are then
+// replaced by their periodic images exactly where the reference fills them, while
+// tracer halos keep evolving with their own right-hand side as they do in the
+// reference (core/model_les.py:98-127 never fills tracers).
+#include "nyles_internal.h"
+
+namespace nyles {
+
+// ---------------------------------------------------------------- RHS building blocks
+// Vortex-force flux at cell c along direction fa for the velocity component whose
+// contravariant partner Uf is first averaged along `aa` (offset +1), then along fa;
+// the vorticity Wf is shifted by one along fa. core/fortran_vortex_force.f90:41-83
+// (direc) and :119-163 (flip) are the same 1-D operation with (fa, aa) swapped.
+template <typename T>
+__device__ __forceinline__ T vf_flux(const T* __restrict__ Uf, const T* __restrict__ Wf, const Geom& g,
+                                     long long c, int k, int fa, int aa) {
+    const int n = g.N[fa];
+    const long long sf = g.stride(fa), sa = g.stride(aa);
+    const long long base = c - (long long)k * sf;
+    T UU1 = T(0.5) * (__ldg(Uf + c) + __ldg(Uf + c + sa));
+    T UU0 = (k > 0) ? T(0.5) * (__ldg(Uf + c - sf) + __ldg(Uf + c - sf + sa)) : T(0);
+    T u1 = T(0.5) * (UU0 + UU1);
+    // q(k) = vort(k-1), q(0) = 0
+    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(Wf + base + (long long)(kk - 1) * sf); };
+    return flux1d_at(k, n, u1, Q);
+}
+
+// Tracer flux through the face to the right of the cell at index i along d.
+// core/fortran_upwind.f90:68-83
+template <typename T>
+__device__ __forceinline__ T tr_flux(const T* __restrict__ Uf, const T* __restrict__ q, const Geom& g,
+                                     long long c, int i, int d) {
+    const int n = g.N[d];
+    const long long s = g.stride(d);
+    const long long base = c - (long long)i * s;
+    auto Q = [&](int kk) -> T { return __ldg(q + base + (long long)kk * s); };
+    return flux1d_at(i, n, __ldg(Uf + c), Q);
+}
+
+// -(flux divergence) of one tracer at a cell, accumulated direction by direction in
+// the reference's order (x pass assigns, y and z passes add), core/tracer.py:59-72
+template <typename T>
+__device__ __forceinline__ T tracer_rhs(const T* __restrict__ q, const T* const* U, const Geom& g, long long c,
+                                        const int* pos) {
+    T acc = T(0);
+    for (int pass = 0; pass < 3; ++pass) {
+        const int d = 2 - pass;            // x, then y, then z
+        const int i = pos[d];
+        const T Fi = tr_flux(U[d], q, g, c, i, d);
+        if (i > 0) {
+            const T Fm = tr_flux(U[d], q, g, c - g.stride(d), i - 1, d);
+            acc = (acc + Fm) - Fi;
+        } else {
+            acc = acc - Fi;
+        }
+    }
+    return acc;
+}
+
+template <typename T>
+struct RhsArgs {
+    Geom g;
+    const T* b;
+    const T* tr[NYLES_MAX_TR];
+    const T* U[3];    // contravariant, index 0 = i (x), 1 = j (y), 2 = k (z)
+    const T* W[3];    // vorticity components i, j, k
+    const T* ke;
+    const T* u[3];    // covariant (viscosity only)
+    T* ds[NYLES_MAX_PROG];
+    int ntr;
+    int terms;
+    int euler;        // Euler3d: no buoyancy in Bernoulli
+    T half_dz;        // 0.5*dz, fortran_bernoulli.f90:49
+    T vcoef[3];       // viscosity*ids2 for directions x, y, z
+};
+
+// viscosity along direction d of component field u at c, core/fortran_dissipation.f90:18-33
+template <typename T>
+__device__ __forceinline__ T lap1d(const T* __restrict__ u, const Geom& g, long long c, int i, int d) {
+    const long long s = g.stride(d);
+    const int n = g.N[d];
+    T fx = (i < n - 1) ? (__ldg(u + c + s) - __ldg(u + c)) : T(0);
+    T fxm = (i > 0) ? (__ldg(u + c) - __ldg(u + c - s)) : T(0);
+    return fx - fxm;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_rhs(const RhsArgs<T> a) {
+    const Geom& g = a.g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const long long c = g.at(z, y, x);
+    const int pos[3] = {z, y, x};
+    const bool acc = (a.terms & TERM_ACCUMULATE) != 0;
+
+    // ---- tracers: b first, then t0.. (core/tracer.py:59-72)
+    if (a.terms & TERM_TRACER) {
+        const T* Uxyz[3] = {a.U[2], a.U[1], a.U[0]};   // indexed by geometry axis z, y, x
+        for (int t = 0; t <= a.ntr; ++t) {
+            const T* q = (t == 0) ? a.b : a.tr[t - 1];
+            const int slot = (t == 0) ? 0 : 3 + t;
+            T v = tracer_rhs(q, Uxyz, g, c, pos);
+            if (a.ds[slot]) a.ds[slot][c] = acc ? a.ds[slot][c] + v : v;
+        }
+    } else if (!acc) {
+        for (int t = 0; t <= a.ntr; ++t) {
+            const int slot = (t == 0) ? 0 : 3 + t;
+            if (a.ds[slot]) a.ds[slot][c] = T(0);
+        }
+    }
+
+    // ---- velocity
+    if (!(a.terms & (TERM_VF | TERM_BERNOULLI | TERM_VISC)) && acc) return;
+    T dux = acc ? a.ds[1][c] : T(0);
+    T duy = acc ? a.ds[2][c] : T(0);
+    T duz = acc ? a.ds[3][c] : T(0);
+    const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
+    if (a.terms & TERM_VF) {
+        // call order of core/vortex_force.py:69-81: triplets "ikj", "jik", "kji"
+        if (y < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, x, 2, 1);   // u_j -= U^i w_k, along i
+        if (x < Nx - 1) dux = dux + vf_flux(a.U[1], a.W[2], g, c, y, 1, 2);   // u_i += U^j w_k, along j
+        if (z < Nz - 1) duz = duz - vf_flux(a.U[1], a.W[0], g, c, y, 1, 0);   // u_k -= U^j w_i, along j
+        if (y < Ny - 1) duy = duy + vf_flux(a.U[2], a.W[0], g, c, z, 0, 1);   // u_j += U^k w_i, along k
+        if (x < Nx - 1) dux = dux - vf_flux(a.U[2], a.W[1], g, c, z, 0, 2);   // u_i -= U^k w_j, along k
+        if (z < Nz - 1) duz = duz + vf_flux(a.U[0], a.W[1], g, c, x, 2, 0);   // u_k += U^i w_j, along i
+    }
+    if (a.terms & TERM_BERNOULLI) {   // core/bernoulli.py:14-23
+        const T* ke = a.ke;
+        if (x < Nx - 1) dux = sub_rn(dux, sub_rn(__ldg(ke + c + 1), __ldg(ke + c)));
+        if (y < Ny - 1) duy = sub_rn(duy, sub_rn(__ldg(ke + c + g.sy), __ldg(ke + c)));
+        if (z < Nz - 1) {
+            duz = sub_rn(duz, sub_rn(__ldg(ke + c + g.sz), __ldg(ke + c)));
+            if (!a.euler) duz = add_rn(duz, mul_rn(a.half_dz, add_rn(__ldg(a.b + c + g.sz), __ldg(a.b + c))));
+        }
+    }
+    if (a.terms & TERM_VISC) {   // core/viscosity.py:5-9: direction outer, component inner
+        for (int pass = 0; pass < 3; ++pass) {
+            const int d = 2 - pass;
+            const T cf = a.vcoef[pass];
+            dux = dux + cf * lap1d(a.u[0], g, c, pos[d], d);
+            duy = duy + cf * lap1d(a.u[1], g, c, pos[d], d);
+            duz = duz + cf * lap1d(a.u[2], g, c, pos[d], d);
+        }
+    }
+    a.ds[1][c] = dux;
+    a.ds[2][c] = duy;
+    a.ds[3][c] = duz;
+}
+
+bool make_geom(const NylesDesc* d, Geom* g) {
+    if (!d || d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nh < 0) return false;
+    const int per[3] = {d->periodic_z ? 1 : 0, d->periodic_y ? 1 : 0, d->periodic_x ? 1 : 0};
+    const int n[3] = {d->nz, d->ny, d->nx};
+    for (int i = 0; i < 3; ++i) {
+        g->n[i] = n[i];
+        g->per[i] = per[i];
+        g->N[i] = n[i] + (per[i] ? 2 * d->nh : 0);
+        if (g->N[i] < 5) return false;   // flux1d closures need five points per line
+    }
+    g->nh = d->nh;
+    g->sy = g->N[2];
+    g->sz = (long long)g->N[1] * g->N[2];
+    g->vol = g->sz * g->N[0];
+    return true;
+}
+
+static dim3 grid3(const Geom& g, dim3 blk) {
+    return dim3((g.N[2] + blk.x - 1) / blk.x, (g.N[1] + blk.y - 1) / blk.y, (g.N[0] + blk.z - 1) / blk.z);
+}
+
+template <typename T>
+int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
+               cudaStream_t st) {
+    RhsArgs<T> a;
+    a.g = g;
+    a.b = s.f[NYLES_F_B];
+    for (int t = 0; t < NYLES_MAX_TR; ++t) a.tr[t] = (t < d->n_tracers) ? s.f[NYLES_F_T0 + t] : nullptr;
+    for (int i = 0; i < 3; ++i) {
+        a.U[i] = s.f[NYLES_F_UC_I + i];
+        a.W[i] = s.f[NYLES_F_VOR_I + i];
+        a.u[i] = s.f[NYLES_F_U_I + i];
+    }
+    a.ke = s.f[NYLES_F_KE];
+    for (int q = 0; q < NYLES_MAX_PROG; ++q) a.ds[q] = (q < 4 + d->n_tracers) ? ds.p[q] : nullptr;
+    a.ntr = d->n_tracers;
+    a.terms = terms;
+    a.euler = d->model == NYLES_MODEL_EULER3D;
+    a.half_dz = T(0.5 * d->dz);
+    a.vcoef[0] = T(d->viscosity * d->idx2);
+    a.vcoef[1] = T(d->viscosity * d->idy2);
+    a.vcoef[2] = T(d->viscosity * d->idz2);
+    dim3 blk(32, 2, 2);
+    k_rhs<T><<<grid3(g, blk), blk, 0, st>>>(a);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "rhs kernel");
+}
+
+// ---------------------------------------------------------------- time-scheme updates
+template <typename T>
+struct UpdArgs {
+    long long vol;
+    int nprog;
+    int kind;
+    double dt;
+    T* s[NYLES_MAX_PROG];
+    T* a[NYLES_MAX_PROG];
+    T* b[NYLES_MAX_PROG];
+    T* c[NYLES_MAX_PROG];
+};
+
+// numpy's evaluation order of core/timescheme.py:113-221, one rounding per operation
+template <typename T>
+__global__ void k_update(const UpdArgs<T> p) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.vol; i += stride) {
+        for (int q = 0; q < p.nprog; ++q) {
+            T* s = p.s[q];
+            const T dt = T(p.dt);
+            switch (p.kind) {
+                case UPD_EULER: {   // s += dt*ds
+                    T inc = mul_rn(dt, p.a[q][i]);
+                    s[i] = add_rn(s[i], inc);
+                } break;
+                case UPD_RK3_2: {   // s += (dt/4.)*(ds1-3*ds0)
+                    T t1 = mul_rn(T(3), p.a[q][i]);
+                    T t2 = sub_rn(p.b[q][i], t1);
+                    T inc = mul_rn(T(p.dt / 4.0), t2);
+                    s[i] = add_rn(s[i], inc);
+                } break;
+                case UPD_RK3_3: {   // s += (dt/12.)*(8*ds2-ds0-ds1)
+                    T t1 = mul_rn(T(8), p.c[q][i]);
+                    T t2 = sub_rn(t1, p.a[q][i]);
+                    T t3 = sub_rn(t2, p.b[q][i]);
+                    T inc = mul_rn(T(p.dt / 12.0), t3);
+                    s[i] = add_rn(s[i], inc);
+                } break;
+                case UPD_LF_FIRST: {   // sn = s; sb = s; s += dt*ds  (a = ds, b = sb, c = sn)
+                    T v = s[i];
+                    p.c[q][i] = v;
+                    p.b[q][i] = v;
+                    T inc = mul_rn(dt, p.a[q][i]);
+                    s[i] = add_rn(v, inc);
+                } break;
+                case UPD_LF_PRED: {   // sn = s; s = sb + 2dt*ds; s = (1/12)*(5s + 8sn - sb); sb = sn
+                    T sn = s[i];
+                    T sb = p.b[q][i];
+                    T inc = mul_rn(T(2.0 * p.dt), p.a[q][i]);
+                    T lf = add_rn(sb, inc);
+                    T t1 = mul_rn(T(5), lf);
+                    T t2 = mul_rn(T(8), sn);
+                    T t3 = add_rn(t1, t2);
+                    T t4 = sub_rn(t3, sb);
+                    s[i] = mul_rn(T(1.0 / 12.0), t4);
+                    p.c[q][i] = sn;
+                    p.b[q][i] = sn;
+                } break;
+                case UPD_LF_CORR: {   // s = sn + dt*ds
+                    T inc = mul_rn(dt, p.a[q][i]);
+                    s[i] = add_rn(p.c[q][i], inc);
+                } break;
+            }
+        }
+    }
+}
+
+template <typename T>
+int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs<T>& a, const ProgPtrs<T>& b,
+                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st) {
+    UpdArgs<T> p;
+    p.vol = g.vol;
+    p.nprog = nprog;
+    p.kind = kind;
+    p.dt = dt;
+    for (int q = 0; q < NYLES_MAX_PROG; ++q) {
+        p.s[q] = s.p[q]; p.a[q] = a.p[q]; p.b[q] = b.p[q]; p.c[q] = c.p[q];
+    }
+    long long blocks = (g.vol + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_update<T><<<(unsigned)blocks, 256, 0, st>>>(p);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "update kernel");
+}
+
+// ---------------------------------------------------------------- periodic halo fill
+// core/mpi/halo.py:140-178 for one rank: each halo cell receives its periodic image.
+// The halo is enumerated as six disjoint slabs (z-low/high over everything, then
+// y-low/high over interior z, then x-low/high over interior z and y).
+struct FillSlabs {
+    int lo[6][3], ext[6][3];
+    long long count[6];
+    int nslab;
+};
+
+template <typename T>
+struct FillArgs {
+    Geom g;
+    FillSlabs sl;
+    T* f[8];
+    int nf;
+};
+
+template <typename T>
+__global__ void k_fill(const FillArgs<T> a) {
+    const int s = blockIdx.y;
+    if (s >= a.sl.nslab) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.sl.count[s]) return;
+    const int ex = a.sl.ext[s][2], ey = a.sl.ext[s][1];
+    const int x = a.sl.lo[s][2] + (int)(i % ex);
+    const int y = a.sl.lo[s][1] + (int)((i / ex) % ey);
+    const int z = a.sl.lo[s][0] + (int)(i / ((long long)ex * ey));
+    const Geom& g = a.g;
+    const long long dst = g.at(z, y, x);
+    const long long src = g.at(g.wrap(0, z), g.wrap(1, y), g.wrap(2, x));
+    for (int k = 0; k < a.nf; ++k) a.f[k][dst] = a.f[k][src];
+}
+
+static FillSlabs make_slabs(const Geom& g) {
+    FillSlabs s{};
+    int n = 0;
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) { lo[d] = g.per[d] ? g.nh : 0; hi[d] = g.per[d] ? g.nh + g.n[d] : g.N[d]; }
+    for (int d = 0; d < 3; ++d) {
+        if (!g.per[d]) continue;
+        for (int side = 0; side < 2; ++side) {
+            int l[3], e[3];
+            for (int k = 0; k < 3; ++k) {
+                if (k < d) { l[k] = lo[k]; e[k] = hi[k] - lo[k]; }
+                else if (k > d) { l[k] = 0; e[k] = g.N[k]; }
+                else { l[k] = side ? hi[k] : 0; e[k] = g.nh; }
+            }
+            for (int k = 0; k < 3; ++k) { s.lo[n][k] = l[k]; s.ext[n][k] = e[k]; }
+            s.count[n] = (long long)e[0] * e[1] * e[2];
+            ++n;
+        }
+    }
+    s.nslab = n;
+    return s;
+}
+
+template <typename T>
+int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st) {
+    FillArgs<T> a;
+    a.g = g;
+    a.sl = make_slabs(g);
+    if (a.sl.nslab == 0) return NYLES_OK;
+    long long mx = 0;
+    for (int s = 0; s < a.sl.nslab; ++s) mx = a.sl.count[s] > mx ? a.sl.count[s] : mx;
+    for (int base = 0; base < nf; base += 8) {
+        a.nf = (nf - base) < 8 ? (nf - base) : 8;
+        for (int k = 0; k < a.nf; ++k) a.f[k] = fields[base + k];
+        dim3 grd((unsigned)((mx + 255) / 256), a.sl.nslab);
+        k_fill<T><<<grd, 256, 0, st>>>(a);
+        note_launch();
+    }
+    return cuda_status(cudaGetLastError(), "fill kernel");
+}
+
+// ---------------------------------------------------------------- divergence
+// core/projection.py:16-29 (fortran_bernoulli.f90:61-97) on U = u*ids2
+// (core/cov_to_contra.py:16-18), evaluated at the periodic image of each cell because
+// core/mgfordriver.py:70 fills the halo of div before the solve.
+template <typename T, typename TB>
+__global__ void __launch_bounds__(256) k_div(const Geom g, const T* __restrict__ ux, const T* __restrict__ uy,
+                                             const T* __restrict__ uz, TB idx2, TB idy2, TB idz2,
+                                             T* __restrict__ div, TB* __restrict__ mgb) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const int zz = g.wrap(0, z), yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const long long c = g.at(zz, yy, xx);
+    TB acc;
+    {
+        TB U0 = mul_rn(TB(ux[c]), idx2);
+        acc = (xx == 0) ? U0 : sub_rn(U0, mul_rn(TB(ux[c - 1]), idx2));
+    }
+    {
+        TB V0 = mul_rn(TB(uy[c]), idy2);
+        acc = (yy == 0) ? add_rn(acc, V0) : add_rn(acc, sub_rn(V0, mul_rn(TB(uy[c - g.sy]), idy2)));
+    }
+    {
+        TB W0 = mul_rn(TB(uz[c]), idz2);
+        acc = (zz == 0) ? add_rn(acc, W0) : add_rn(acc, sub_rn(W0, mul_rn(TB(uz[c - g.sz]), idz2)));
+    }
+    div[g.at(z, y, x)] = T(acc);
+    if (zz == z && yy == y && xx == x) {
+        const int iz = zz - (g.per[0] ? g.nh : 0), iy = yy - (g.per[1] ? g.nh : 0), ix = xx - (g.per[2] ? g.nh : 0);
+        mgb[((long long)iz * g.n[1] + iy) * g.n[2] + ix] = acc;
+    }
+}
+
+template <typename T, typename TB>
+int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* mg_b, cudaStream_t st) {
+    dim3 blk(32, 4, 2);
+    k_div<T, TB><<<grid3(g, blk), blk, 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
+                                                 TB(d->idx2), TB(d->idy2), TB(d->idz2), s.f[NYLES_F_DIV], mg_b);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "div kernel");
+}
+
+// ---------------------------------------------------------------- projection correction
+// p = x*dx**2 (core/mgfordriver.py:78) on every cell (halo = periodic image) and
+// u_i -= p(i+1)-p(i) (core/projection.py:84-87 via fortran_bernoulli.f90:2-26) on the
+// interior cells. The correction reads no velocity neighbour, so it runs in place;
+// the halo of u is filled afterwards as core/model_les.py:110 does.
+template <typename T, typename TP>
+struct CorrArgs {
+    Geom g;
+    T* u[3];
+    const TP* x;      // pressure solution, interior cells (nz, ny, nx)
+    T* p;
+    double dx2;
+};
+
+template <typename T, typename TP>
+__device__ __forceinline__ TP pres(const CorrArgs<T, TP>& a, int z, int y, int x) {
+    const Geom& g = a.g;
+    z = g.wrap(0, z); y = g.wrap(1, y); x = g.wrap(2, x);
+    const int iz = z - (g.per[0] ? g.nh : 0), iy = y - (g.per[1] ? g.nh : 0), ix = x - (g.per[2] ? g.nh : 0);
+    return mul_rn(a.x[((long long)iz * g.n[1] + iy) * g.n[2] + ix], TP(a.dx2));
+}
+
+template <typename T, typename TP>
+__global__ void __launch_bounds__(256) k_correct(const CorrArgs<T, TP> a) {
+    const Geom& g = a.g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const long long c = g.at(z, y, x);
+    const TP p0 = pres(a, z, y, x);
+    a.p[c] = T(p0);
+    if (g.wrap(0, z) != z || g.wrap(1, y) != y || g.wrap(2, x) != x) return;   // halo: filled later
+    if (x < g.N[2] - 1) a.u[0][c] = T(sub_rn(TP(a.u[0][c]), sub_rn(pres(a, z, y, x + 1), p0)));
+    if (y < g.N[1] - 1) a.u[1][c] = T(sub_rn(TP(a.u[1][c]), sub_rn(pres(a, z, y + 1, x), p0)));
+    if (z < g.N[0] - 1) a.u[2][c] = T(sub_rn(TP(a.u[2][c]), sub_rn(pres(a, z + 1, y, x), p0)));
+}
+
+template <typename T, typename TP>
+int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const TP* mg_x, double dx2,
+                   cudaStream_t st) {
+    (void)d;
+    CorrArgs<T, TP> a;
+    a.g = g;
+    for (int i = 0; i < 3; ++i) a.u[i] = s.f[NYLES_F_U_I + i];
+    a.x = mg_x;
+    a.p = s.f[NYLES_F_P];
+    a.dx2 = dx2;
+    dim3 blk(32, 4, 2);
+    k_correct<T, TP><<<grid3(g, blk), blk, 0, st>>>(a);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "correct kernel");
+}
+
+// ---------------------------------------------------------------- diagnostics
+// From the corrected, halo-filled u: U = u*ids2 (core/cov_to_contra.py:4-20),
+// vorticity (core/vorticity.py:26-34 -> fortran_vorticity.f90:16-26 in each
+// orientation, Coriolis added to vor_k), kinetic energy (core/kinenergy.py:17-24 ->
+// fortran_kinenergy.f90:47-53). Each cell evaluates at its periodic image, which is
+// what the fills of vor and ke (core/model_les.py:126-127) leave in the halo.
+template <typename T>
+struct DiagArgs {
+    Geom g;
+    const T* u[3];
+    T* U[3];
+    T* W[3];
+    T* ke;
+    T ids2[3];
+    T kec[3];         // (0.5*ids2)*0.5
+    T fparam;
+    int nonlinear;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_diag(const DiagArgs<T> a) {
+    const Geom& g = a.g;
+    const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y0 = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z0 = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x0 >= g.N[2] || y0 >= g.N[1] || z0 >= g.N[0]) return;
+    const long long c0 = g.at(z0, y0, x0);
+    const T* __restrict__ ux = a.u[0];
+    const T* __restrict__ uy = a.u[1];
+    const T* __restrict__ uz = a.u[2];
+    const T ui = ux[c0], uj = uy[c0], uk = uz[c0];   // u is filled: value at c0 == value at the image
+    a.U[0][c0] = mul_rn(ui, a.ids2[0]);
+    a.U[1][c0] = mul_rn(uj, a.ids2[1]);
+    a.U[2][c0] = mul_rn(uk, a.ids2[2]);
+    if (!a.nonlinear) return;
+    const int z = g.wrap(0, z0), y = g.wrap(1, y0), x = g.wrap(2, x0);
+    const long long c = g.at(z, y, x);
+    const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
+    T wi = T(0), wj = T(0), wk = T(0);
+    if (z < Nz - 1 && y < Ny - 1) wi = add_rn(sub_rn(sub_rn(uz[c + g.sy], uk), uy[c + g.sz]), uj);
+    if (x < Nx - 1 && z < Nz - 1) wj = add_rn(sub_rn(sub_rn(ux[c + g.sz], ui), uz[c + 1]), uk);
+    if (y < Ny - 1 && x < Nx - 1) {
+        wk = add_rn(sub_rn(sub_rn(uy[c + 1], uj), ux[c + g.sy]), ui);
+        if (a.fparam > T(0)) wk = add_rn(wk, a.fparam);
+    }
+    a.W[0][c0] = wi; a.W[1][c0] = wj; a.W[2][c0] = wk;
+    T ke = T(0);
+    if (x >= 1) { const T m = ux[c - 1]; ke = add_rn(ke, mul_rn(a.kec[0], add_rn(mul_rn(ui, ui), mul_rn(m, m)))); }
+    if (y >= 1) { const T m = uy[c - g.sy]; ke = add_rn(ke, mul_rn(a.kec[1], add_rn(mul_rn(uj, uj), mul_rn(m, m)))); }
+    if (z >= 1) { const T m = uz[c - g.sz]; ke = add_rn(ke, mul_rn(a.kec[2], add_rn(mul_rn(uk, uk), mul_rn(m, m)))); }
+    a.ke[c0] = ke;
+}
+
+template <typename T>
+int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st) {
+    DiagArgs<T> a;
+    a.g = g;
+    for (int i = 0; i < 3; ++i) {
+        a.u[i] = s.f[NYLES_F_U_I + i];
+        a.U[i] = s.f[NYLES_F_UC_I + i];
+        a.W[i] = s.f[NYLES_F_VOR_I + i];
+    }
+    a.ke = s.f[NYLES_F_KE];
+    const double ids2[3] = {d->idx2, d->idy2, d->idz2};
+    for (int i = 0; i < 3; ++i) {
+        a.ids2[i] = T(ids2[i]);
+        a.kec[i] = T((0.5 * ids2[i]) * 0.5);
+    }
+    a.fparam = T(d->fparam);
+    a.nonlinear = nonlinear;
+    dim3 blk(32, 4, 2);
+    k_diag<T><<<grid3(g, blk), blk, 0, st>>>(a);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "diag kernel");
+}
+
+// ---------------------------------------------------------------- CFL reduction
+// max over all stored points of U^2+V^2+W^2, core/nyles.py:241-251 (max is exact
+// whatever the reduction order)
+template <typename T>
+__global__ void __launch_bounds__(256) k_max_U2(const long long vol, const T* __restrict__ U,
+                                                const T* __restrict__ V, const T* __restrict__ W,
+                                                double* __restrict__ partial) {
+    double m = 0.0;
+    bool any_nan = false;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
+        const double a = U[i], b = V[i], c = W[i];
+        const double s = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+        if (s != s) any_nan = true;
+        m = fmax(m, s);
+    }
+    __shared__ double sm[8];
+    __shared__ int snan;
+    if (threadIdx.x == 0) snan = 0;
+    __syncthreads();
+    if (any_nan) snan = 1;
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        v = warp_max(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = snan ? __longlong_as_double(0x7ff8000000000000ULL) : v;
+    }
+}
+
+__global__ void k_max_final(const double* __restrict__ partial, int n, double* out) {
+    double m = 0.0;
+    bool nan = false;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double v = partial[i];
+        if (v != v) nan = true;
+        m = fmax(m, v);
+    }
+    __shared__ double sm[32];
+    __shared__ int snan;
+    if (threadIdx.x == 0) snan = 0;
+    __syncthreads();
+    if (nan) snan = 1;
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        v = warp_max(v);
+        if (threadIdx.x == 0) out[0] = snan ? __longlong_as_double(0x7ff8000000000000ULL) : v;
+    }
+}
+
+template <typename T>
+int launch_max_U2(const Geom& g, const StencilPtrs<T>& s, double* partial, int npartial, double* out,
+                  cudaStream_t st) {
+    k_max_U2<T><<<npartial, 256, 0, st>>>(g.vol, s.f[NYLES_F_UC_I], s.f[NYLES_F_UC_J], s.f[NYLES_F_UC_K], partial);
+    k_max_final<<<1, 1024, 0, st>>>(partial, npartial, out);
+    note_launch(2);
+    return cuda_status(cudaGetLastError(), "max_U2 kernel");
+}
+
+// ---------------------------------------------------------------- flux1d test entry
+template <typename T>
+__global__ void k_flux1d(const T* __restrict__ u, const T* __restrict__ q, T* __restrict__ flux, int nlines, int n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nlines * n) return;
+    const int line = (int)(t / n), i = (int)(t % n);
+    const T* ql = q + (long long)line * n;
+    auto Q = [&](int kk) -> T { return ql[kk]; };
+    flux[t] = flux1d_at(i, n, u[t], Q);
+}
+
+template <typename T>
+int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream_t st) {
+    long long tot = (long long)nlines * n;
+    if (tot == 0) return NYLES_OK;
+    k_flux1d<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(u, q, flux, nlines, n);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "flux1d kernel");
+}
+
+// ---------------------------------------------------------------- instantiations
+#define NYLES_INST(T)                                                                                          \
+    template int launch_rhs<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, const ProgPtrs<T>&, int, \
+                               cudaStream_t);                                                                  \
+    template int launch_update<T>(const Geom&, int, const ProgPtrs<T>&, const ProgPtrs<T>&, const ProgPtrs<T>&, \
+                                  const ProgPtrs<T>&, int, double, cudaStream_t);                              \
+    template int launch_fill<T>(const Geom&, T* const*, int, cudaStream_t);                                    \
+    template int launch_diag<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, int, cudaStream_t);      \
+    template int launch_max_U2<T>(const Geom&, const StencilPtrs<T>&, double*, int, double*, cudaStream_t);   \
+    template int launch_flux1d<T>(const T*, const T*, T*, int, int, cudaStream_t);
+NYLES_INST(double)
+NYLES_INST(float)
+template int launch_div<double, double>(const NylesDesc*, const Geom&, const StencilPtrs<double>&, double*, cudaStream_t);
+template int launch_div<float, double>(const NylesDesc*, const Geom&, const StencilPtrs<float>&, double*, cudaStream_t);
+template int launch_correct<double, double>(const NylesDesc*, const Geom&, const StencilPtrs<double>&, const double*,
+                                            double, cudaStream_t);
+template int launch_correct<float, double>(const NylesDesc*, const Geom&, const StencilPtrs<float>&, const double*,
+                                           double, cudaStream_t);
+
+}  // namespace nyles

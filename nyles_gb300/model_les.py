@@ -1,0 +1,161 @@
+"""LES model of one subdomain on the GPU.
+
+Interface of the reference's core/model_les.py:33-175 (and of the Euler3d and linear
+variants, core/model_les_euler.py and core/nyles.py:92-100): ``LES(param, grid,
+linear=False)`` with ``state``, ``timescheme``, ``forward(t, dt) -> blowup``,
+``rhs(state, t, dstate, last=False)`` and ``diagnose_var(state)``.
+
+All arithmetic runs in libnyles_gb300.so; this class owns the device arrays (torch
+tensors) and passes their pointers through the C ABI.
+"""
+import ctypes
+
+import torch
+
+from . import _native as nat
+from . import timescheme as ts
+from . import variables as var
+
+
+def make_desc(param, grid, modelname):
+    """NylesDesc of a parameter dictionary (one subdomain)."""
+    geometry = param["geometry"]
+    d = nat.NylesDesc()
+    d.nx, d.ny, d.nz, d.nh = param["nx"], param["ny"], param["nz"], param["nh"]
+    d.periodic_x = int("x" in geometry)
+    d.periodic_y = int("y" in geometry)
+    d.periodic_z = int("z" in geometry)
+    d.n_tracers = param.get("n_tracers", 0)
+    d.model = nat.MODEL[modelname]
+    diff = param.get("diff_coef", {}) or {}
+    d.add_viscosity = int("u" in diff)
+    d.viscosity = float(diff.get("u", 0.0))
+    d.dx, d.dy, d.dz = grid.dx, grid.dy, grid.dz
+    d.idx2, d.idy2, d.idz2 = grid.idx2, grid.idy2, grid.idz2
+    d.dx2 = grid.dx ** 2
+    # covariant Coriolis parameter (core/model_les.py:61-67)
+    d.fparam = float(param["coriolis"] * (grid.dx * grid.dy)) if param.get("rotating", False) else 0.0
+    return d
+
+
+class LES(object):
+    """One subdomain of the LES / Euler3d / linear model on cuda:0 (or `device`)."""
+
+    modelname = "LES"
+
+    def __init__(self, param, grid, linear=False, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("nyles_gb300 needs a CUDA GPU: the model runs only through libnyles_gb300.so")
+        self.lib = nat.lib()
+        if linear:
+            self.modelname = "linear"
+        self.nonlinear = not linear
+        self.grid = grid
+        self.param = param
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        gpu = param.get("gpu", {}) if isinstance(param.get("gpu"), dict) else {}
+        self.precision = param.get("precision", gpu.get("precision", "fp64"))
+        self.dtype = torch.float64 if self.precision == "fp64" else torch.float32
+        ntr = param.get("n_tracers", 0)
+        if ntr > nat.MAX_TRACERS:
+            raise ValueError("at most %d tracers" % nat.MAX_TRACERS)
+        self.traclist = ["b"] + var.tracer_names(ntr) if self.modelname != "Euler3d" else [""] + var.tracer_names(ntr)
+        self.state = var.get_state(param, dtype=self.dtype, device=self.device)
+        self.neighbours = param["neighbours"]
+        self.orderA = param.get("orderA", 5)
+        self.orderVF = param.get("orderVF", 5)
+        self.orderKE = param.get("orderKE", 2)
+        self.rotating = param.get("rotating", False)
+        self.forced = param.get("forced", False)
+        self.diff_coef = param.get("diff_coef", {}) or {}
+        self.add_viscosity = "u" in self.diff_coef
+        if self.add_viscosity:
+            self.viscosity = self.diff_coef["u"]
+        self.fparameter = param["coriolis"] * grid.dx * grid.dy if self.rotating else 0.0
+        self.desc = make_desc(param, grid, self.modelname)
+        self.timescheme = ts.Timescheme(param, self.state, model=self)
+        self.timescheme.set(self.rhs, self.diagnose_var)
+        # native model: arrays owned here, pointers bound once
+        h = ctypes.c_void_p()
+        nat.check(self.lib.nyles_model_create(ctypes.byref(self.desc), nat.SCHEME[param["timestepping"]],
+                                              nat.PRECISION[self.precision], ctypes.byref(h)))
+        self._h = h
+        nbytes = ctypes.c_size_t()
+        nat.check(self.lib.nyles_model_workspace_bytes(h, ctypes.byref(nbytes)))
+        self.workspace = torch.zeros(nbytes.value + 256, dtype=torch.uint8, device=self.device)
+        ws = self.workspace.data_ptr()
+        ws = (ws + 255) & ~255
+        self._fields = nat.ptr_array([s.data_ptr() for s in self.state.scalars()])
+        self._regs = nat.ptr_array(self.timescheme.register_pointers())
+        nat.check(self.lib.nyles_model_bind(h, self._fields, self._regs, ctypes.c_void_p(ws)))
+        self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9))
+        self.forcing = None
+        self.stats = []
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.nyles_model_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ------------------------------------------------------------------ settings
+    def set_mg_params(self, tol=1e-6, maxite=20, omega=0.9):
+        """Multigrid stop rule: sum(r^2)/sum(b^2) < tol or maxite V-cycles."""
+        nat.check(self.lib.nyles_model_set_mg_params(self._h, float(tol), int(maxite), float(omega)))
+
+    def mg_stats(self):
+        s = nat.NylesMgStats()
+        nat.check(self.lib.nyles_model_mg_stats(self._h, ctypes.byref(s)))
+        return {"nite": s.nite, "res": s.res, "solves": s.solves, "vcycles": s.vcycles,
+                "not_converged": s.not_converged}
+
+    # ------------------------------------------------------------------ model API
+    def _check_state(self, state):
+        if state is not self.state:
+            raise NotImplementedError("the GPU model advances its own state (model.state) only")
+
+    def diagnose_var(self, state):
+        """Halo fill, projection, vorticity and kinetic energy (core/model_les.py:98-127)."""
+        self._check_state(state)
+        nat.check(self.lib.nyles_model_diagnose(self._h, nat.stream_ptr()))
+
+    def rhs(self, state, t, dstate, last=False):
+        """Right-hand side into `dstate` (core/model_les.py:130-144)."""
+        self._check_state(state)
+        if self.forced and self.forcing is not None:
+            raise NotImplementedError("user forcing hooks are not supported on the GPU path")
+        fields = nat.ptr_array([s.data_ptr() for s in state.scalars()])
+        ds = nat.ptr_array([s.data_ptr() for s in dstate.scalars()])
+        fn = self.lib.nyles_rhs_f64 if self.precision == "fp64" else self.lib.nyles_rhs_f32
+        nat.check(fn(ctypes.byref(self.desc), fields, ds, 1 if last else 0, nat.stream_ptr()))
+
+    def forward(self, t, dt):
+        """One time step (core/model_les.py:147-149). Returns the blow-up flag."""
+        if self.forced and self.forcing is not None:
+            raise NotImplementedError("user forcing hooks are not supported on the GPU path")
+        nat.check(self.lib.nyles_model_forward(self._h, float(t), float(dt), nat.stream_ptr()))
+        return False
+
+    def max_U2(self):
+        """max of U^2+V^2+W^2 over the arrays; raises BlowUp on a non-finite value."""
+        out = ctypes.c_double()
+        nat.check(self.lib.nyles_model_max_U2(self._h, ctypes.byref(out), nat.stream_ptr()))
+        return out.value
+
+    def reset_timescheme(self):
+        nat.check(self.lib.nyles_model_reset_scheme(self._h))
+
+
+class Euler3d(LES):
+    """Euler equations without buoyancy (core/model_les_euler.py)."""
+
+    modelname = "Euler3d"
+
+    def __init__(self, param, grid, device=None):
+        if param["geometry"] not in ("closed", "perio_xyz"):
+            # core/model_les_euler.py:80-90 maps only closed and perio_xyz to a multigrid topology
+            raise ValueError("Euler3d supports the geometries closed and perio_xyz")
+        super().__init__(param, grid, linear=False, device=device)

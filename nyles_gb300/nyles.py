@@ -1,0 +1,109 @@
+"""The Nyles driver: ``Nyles(param).run()`` for one subdomain on one GPU.
+
+Interface of the reference's core/nyles.py:22-260: the constructor checks and freezes
+the parameters, derives nx/ny/nz, the neighbours and the grid, and builds the model
+(``LES``, ``Euler3d`` or ``linear``); ``run()`` projects the initial state and advances
+it to ``tend`` with ``compute_dt()`` (CFL) and ``model.forward``.
+
+Not part of this build: netCDF history files, the interactive animation, and MPI
+decomposition (one subdomain per process; npx = npy = npz = 1).
+"""
+import time
+
+import numpy as np
+
+from . import grid as grid_module
+from . import model_les
+from . import topology as topo
+
+
+class Nyles(object):
+    def __init__(self, user_param, device=None):
+        user_param.check()
+        user_param.freeze()
+        param = dict(user_param.view_parameters())
+        param["gpu"] = dict(user_param.gpu)
+        self.param = param
+        npx, npy, npz = param["npx"], param["npy"], param["npz"]
+        if (npx, npy, npz) != (1, 1, 1):
+            raise NotImplementedError("one subdomain per GPU: npx = npy = npz = 1 (no MPI in this build)")
+        param["nx"] = param["global_nx"] // npx
+        param["ny"] = param["global_ny"] // npy
+        param["nz"] = param["global_nz"] // npz
+        procs = [npz, npy, npx]
+        myrank = 0
+        loc = topo.rank2loc(myrank, procs)
+        neighbours = topo.get_neighbours(loc, procs, param["geometry"])
+        param["procs"] = procs
+        param["myrank"] = myrank
+        param["neighbours"] = neighbours
+        param["loc"] = loc
+        self.myrank = myrank
+        self.grid = grid_module.Grid(param)
+        self.initiate(param, device)
+
+    def initiate(self, param, device=None):
+        name = param["modelname"]
+        if name == "LES":
+            self.model = model_les.LES(param, self.grid, device=device)
+        elif name == "Euler3d":
+            self.model = model_les.Euler3d(param, self.grid, device=device)
+        elif name == "linear":
+            self.model = model_les.LES(param, self.grid, linear=True, device=device)
+        else:
+            raise NotImplementedError("modelname %r is not provided by the GPU build" % name)
+        self.tend = param["tend"]
+        self.auto_dt = param["auto_dt"]
+        self.dt0 = param["dt"]
+        self.cfl = param["cfl"]
+        self.dt_max = param["dt_max"]
+        self.blowup_check = param.get("gpu", {}).get("blowup_check", True)
+        self.gridcellpersubdom = param["nx"] * param["ny"] * param["nz"]
+
+    def compute_dt(self):
+        """cfl / max|U| bounded by dt_max, or the fixed dt (core/nyles.py:227-260)."""
+        if self.auto_dt:
+            U_max = np.sqrt(self.model.max_U2())
+            if U_max == 0.0:
+                return self.dt_max
+            return min(self.cfl / U_max, self.dt_max)
+        return self.dt0
+
+    def run(self, nsteps=None, verbose=True, callback=None):
+        """Advance to tend (or `nsteps` steps). Returns (t, n, blowup).
+
+        `callback(nyles, t, n)` is called after every step (e.g. for snapshots).
+        """
+        from . import _native as nat
+        t, n = 0.0, 0
+        self.model.diagnose_var(self.model.state)
+        realtime0 = time.time()
+        blowup = False
+        while True:
+            try:
+                dt = self.compute_dt()
+            except nat.BlowUp:
+                blowup = True
+                break
+            self.model.forward(t, dt)
+            t += dt
+            n += 1
+            if callback is not None:
+                callback(self, t, n)
+            if verbose:
+                realtime = time.time()
+                perf = (realtime - realtime0) / self.gridcellpersubdom
+                realtime0 = realtime
+                print("\rn = {:3d}, t = {:.2f}/{:.2f}, dt = {:.4f}, perf = {:.2e}".format(
+                    n, t, self.tend, dt, perf), end="")
+            if t >= self.tend or (nsteps is not None and n >= nsteps):
+                break
+        if self.blowup_check and not blowup:
+            try:
+                self.model.max_U2()
+            except nat.BlowUp:
+                blowup = True
+        if verbose:
+            print()
+            print("BLOW UP!" if blowup else "Job completed as expected")
+        return t, n, blowup

@@ -943,6 +943,8 @@ void orc_model_mg_params(void* h, double tol, int maxite, double omega) {
 void orc_model_mg_stats(void* h, int* nite, double* res) { Model* M = (Model*)h; *nite = M->mg->nite; *res = M->mg->res; }
 void* orc_model_mg(void* h) { return ((Model*)h)->mg; }
 void orc_model_diagnose(void* h) { model_diagnose(*(Model*)h); }
+void orc_model_vortex_force(void* h, int reg) {
+    Model* M = (Model*)h; for (auto& a : M->reg[reg]) std::fill(a.begin(), a.end(), 0.0); model_vortex_force(*M, M->reg[reg]); }
 void orc_model_rhs(void* h, int reg, int last) { Model* M = (Model*)h; model_rhs(*M, M->reg[reg], last != 0); }
 void orc_model_forward(void* h, double t, double dt) { model_forward(*(Model*)h, t, dt); }
 void orc_model_fill(void* h, int fld) { Model* M = (Model*)h; model_fill(*M, M->f[fld].data()); }

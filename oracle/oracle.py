@@ -81,6 +81,7 @@ def lib():
             "orc_model_mg": (p, [p]),
             "orc_model_diagnose": (v, [p]),
             "orc_model_rhs": (v, [p, i, i]),
+            "orc_model_vortex_force": (v, [p, i]),
             "orc_model_forward": (v, [p, d, d]),
             "orc_model_fill": (v, [p, i]),
             "orc_model_max_U2": (d, [p]),
@@ -246,6 +247,10 @@ class OracleModel:
 
     def diagnose(self):
         lib().orc_model_diagnose(self.h)
+
+    def vortex_force(self, reg=0):
+        """register `reg` = vortex force only (core/vortex_force.py:69-81)"""
+        lib().orc_model_vortex_force(self.h, reg)
 
     def rhs(self, reg=0, last=False):
         lib().orc_model_rhs(self.h, reg, 1 if last else 0)

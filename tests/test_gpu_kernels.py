@@ -1,0 +1,167 @@
+"""GPU kernels against the CPU oracle, through the C ABI (libnyles_gb300.so).
+
+FP64 tolerances: the CUDA kernels may contract multiply-adds inside the WENO
+reconstruction, so results differ from the oracle by a few units in the last place;
+the bound used here is 1e-13 relative to the field's max-norm (well inside the
+1e-12-per-step requirement).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-13
+
+
+def _lib():
+    from nyles_gb300 import _native
+    return _native
+
+
+@pytest.mark.parametrize("n", [5, 6, 7, 8, 13, 40])
+def test_flux1d_f64_matches_oracle(n):
+    nat = _lib()
+    rng = np.random.Generator(np.random.PCG64(n))
+    nlines = 64
+    u = rng.standard_normal((nlines, n))
+    u[:, ::3] = np.abs(u[:, ::3])
+    q = rng.standard_normal((nlines, n)) * np.exp(rng.uniform(-8, 2, size=(nlines, 1)))
+    q[::7] = 1.25    # constant lines: tau5 = 0 path
+    ud, qd = torch.from_numpy(u).cuda(), torch.from_numpy(q).cuda()
+    fd = torch.zeros_like(ud)
+    nat.check(nat.lib().nyles_flux1d_f64(ctypes.c_void_p(ud.data_ptr()), ctypes.c_void_p(qd.data_ptr()),
+                                          ctypes.c_void_p(fd.data_ptr()), nlines, n, nat.stream_ptr()))
+    torch.cuda.synchronize()
+    got = fd.cpu().numpy()
+    ref = np.stack([oracle.flux1d(u[k], q[k]) for k in range(nlines)])
+    scale = np.max(np.abs(ref), axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(got - ref) / scale) < TOL64
+
+
+def test_flux1d_f32_close_to_oracle():
+    nat = _lib()
+    rng = np.random.Generator(np.random.PCG64(7))
+    nlines, n = 32, 24
+    u = rng.standard_normal((nlines, n)).astype(np.float32)
+    q = rng.standard_normal((nlines, n)).astype(np.float32)
+    ud, qd = torch.from_numpy(u).cuda(), torch.from_numpy(q).cuda()
+    fd = torch.zeros_like(ud)
+    nat.check(nat.lib().nyles_flux1d_f32(ctypes.c_void_p(ud.data_ptr()), ctypes.c_void_p(qd.data_ptr()),
+                                          ctypes.c_void_p(fd.data_ptr()), nlines, n, nat.stream_ptr()))
+    torch.cuda.synchronize()
+    ref = np.stack([oracle.flux1d(u[k].astype(np.float64), q[k].astype(np.float64)) for k in range(nlines)])
+    assert np.max(np.abs(fd.cpu().numpy() - ref)) / np.max(np.abs(ref)) < 1e-5
+
+
+def test_flux1d_rejects_short_lines():
+    nat = _lib()
+    rc = nat.lib().nyles_flux1d_f64(None, None, None, 1, 4, None)
+    assert rc == nat.NYLES_BAD_ARG
+
+
+CONFIGS = [
+    dict(geometry="closed", n=(16, 8, 12)),
+    dict(geometry="perio_xy", n=(8, 16, 8), n_tracers=2),
+    dict(geometry="perio_xyz", n=(8, 8, 8)),
+    dict(geometry="perio_x", n=(12, 8, 8)),
+    dict(geometry="closed", n=(8, 8, 8), modelname="Euler3d"),
+    dict(geometry="perio_xy", n=(8, 8, 8), modelname="linear", n_tracers=1),
+    dict(geometry="closed", n=(8, 8, 8), rotating=True, coriolis=3.0, diff_coef={"u": 2e-3}),
+]
+
+
+def _setup(cfg, seed):
+    from nyles_gb300.nyles import Nyles
+    p = helpers.make_params(**cfg)
+    nyl = Nyles(p)
+    o = helpers.oracle_for(nyl)
+    fields = helpers.seeded_state(nyl, "noise", seed)
+    helpers.load_state(nyl, o, fields)
+    return nyl, o
+
+
+def _fill_random_diagnostics(nyl, o, seed):
+    """Random U, vor, ke (the inputs of the right-hand side), identical on both sides."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shape = tuple(nyl.model.state.b.view("i").shape)
+    for name in ("U_i", "U_j", "U_k", "vor_i", "vor_j", "vor_k", "ke"):
+        a = rng.standard_normal(shape)
+        if name.startswith("vor"):
+            a *= np.exp(rng.uniform(-6, 0, size=shape))
+        nyl.model.state.get(name).view("i")[...] = torch.from_numpy(a)
+        o.field(name)[...] = a
+
+
+@pytest.mark.parametrize("k", range(len(CONFIGS)))
+def test_vortex_force_f64_matches_oracle(k):
+    nat = _lib()
+    nyl, o = _setup(CONFIGS[k], 10 + k)
+    _fill_random_diagnostics(nyl, o, 20 + k)
+    m = nyl.model
+    ds = m.timescheme.registers[0]
+    ds.storage.zero_()
+    fields = nat.ptr_array([s.data_ptr() for s in m.state.scalars()])
+    dsp = nat.ptr_array([s.data_ptr() for s in ds.scalars()])
+    nat.check(nat.lib().nyles_vortex_force_f64(ctypes.byref(m.desc), fields, dsp, nat.stream_ptr()))
+    torch.cuda.synchronize()
+    o.vortex_force(0)
+    for q, name in enumerate(["u_i", "u_j", "u_k"]):
+        got = ds.get(name).view("i").cpu().numpy()
+        ref = o.register(0, 1 + q)
+        assert helpers.relerr(got, ref) < TOL64, name
+
+
+@pytest.mark.parametrize("last", [False, True])
+@pytest.mark.parametrize("k", range(len(CONFIGS)))
+def test_rhs_f64_matches_oracle(k, last):
+    nyl, o = _setup(CONFIGS[k], 30 + k)
+    _fill_random_diagnostics(nyl, o, 40 + k)
+    m = nyl.model
+    ds = m.timescheme.registers[1]
+    ds.storage.fill_(123.0)          # overwritten entirely (reset_state)
+    m.rhs(m.state, 0.0, ds, last=last)
+    torch.cuda.synchronize()
+    o.rhs(1, last)
+    names = ["b", "u_i", "u_j", "u_k"] + ["t%d" % t for t in range(nyl.param["n_tracers"])]
+    for q, name in enumerate(names):
+        got = ds.get(name).view("i").cpu().numpy()
+        ref = o.register(1, q)
+        if np.max(np.abs(ref)) == 0:
+            assert np.max(np.abs(got)) == 0, name
+        else:
+            assert helpers.relerr(got, ref) < TOL64, name
+
+
+@pytest.mark.parametrize("k", range(len(CONFIGS)))
+def test_diagnose_f64_matches_oracle(k):
+    """Halo fill + divergence + multigrid + correction + vorticity + ke."""
+    nyl, o = _setup(CONFIGS[k], 50 + k)
+    m = nyl.model
+    m.diagnose_var(m.state)
+    torch.cuda.synchronize()
+    o.diagnose()
+    assert m.mg_stats()["nite"] == o.mg_stats()[0]
+    for name in helpers.PROG + helpers.DIAG:
+        got = m.state.get(name).view("i").cpu().numpy()
+        ref = o.field(name)
+        assert helpers.relerr(got, ref) < 1e-12, name
+
+
+def test_fill_matches_oracle():
+    nat = _lib()
+    nyl, o = _setup(dict(geometry="perio_xyz", n=(8, 8, 8)), 3)
+    m = nyl.model
+    rng = np.random.Generator(np.random.PCG64(5))
+    a = rng.standard_normal(tuple(m.state.ke.view("i").shape))
+    m.state.ke.view("i")[...] = torch.from_numpy(a)
+    o.field("ke")[...] = a
+    nat.check(nat.lib().nyles_fill_f64(ctypes.byref(m.desc), ctypes.c_void_p(m.state.ke.data_ptr()), nat.stream_ptr()))
+    torch.cuda.synchronize()
+    o.fill("ke")
+    np.testing.assert_array_equal(m.state.ke.view("i").cpu().numpy(), o.field("ke"))

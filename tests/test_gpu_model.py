@@ -1,0 +1,163 @@
+"""Whole time steps on the GPU against the oracle and the golden vectors.
+
+Bars (the benchmark spec): FP64 path within 1e-12 relative max-norm per step and 1e-9 after
+100 steps, equal multigrid V-cycle counts; mixed path within 1e-5 in u and b.
+"""
+import numpy as np
+import pytest
+
+import helpers
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_from_golden(name):
+    from nyles_gb300.nyles import Nyles
+    d, meta = helpers.load_golden(name)
+    p = helpers.make_params(geometry=meta["geometry"], modelname=meta["modelname"],
+                            timestepping=meta["timestepping"], n=tuple(meta["n"]), L=tuple(meta["L"]),
+                            n_tracers=meta["n_tracers"], auto_dt=meta["auto_dt"], dt=meta.get("dt", 0.1),
+                            cfl=meta.get("cfl", 1.0), dt_max=meta.get("dt_max", 1.0),
+                            rotating=meta.get("rotating", False), coriolis=meta.get("coriolis", 1.0),
+                            diff_coef=meta.get("diff_coef"))
+    nyl = Nyles(p)
+    return nyl, d, meta
+
+
+@pytest.mark.parametrize("name", helpers.golden_cases())
+def test_golden_trajectories(name):
+    """The reference's own orchestration (golden vectors) reproduced on the GPU."""
+    nyl, d, meta = _gpu_from_golden(name)
+    m = nyl.model
+    progs = helpers.PROG + ["t%d" % i for i in range(meta["n_tracers"])]
+    for s in progs:
+        m.state.get(s).view("i")[...] = torch.from_numpy(d["init_" + s])
+    m.diagnose_var(m.state)
+    assert m.mg_stats()["nite"] == int(d["nite_0"])
+    t = 0.0
+    for n in range(meta["steps"]):
+        dt = nyl.compute_dt()
+        assert dt == pytest.approx(d["dts"][n], rel=1e-13)
+        m.forward(t, dt)
+        t += dt
+        assert m.mg_stats()["nite"] == int(d["nites_last"][n])
+    for s in progs + helpers.DIAG:
+        got = m.state.get(s).view("i").cpu().numpy()
+        ref = d["final_" + s]
+        if np.max(np.abs(ref)) == 0:
+            assert np.max(np.abs(got)) == 0, s
+        else:
+            assert helpers.relerr(got, ref) < 1e-11 * meta["steps"], s
+
+
+def _pair(cfg, kind, seed):
+    from nyles_gb300.nyles import Nyles
+    p = helpers.make_params(**cfg)
+    nyl = Nyles(p)
+    o = helpers.oracle_for(nyl)
+    helpers.load_state(nyl, o, helpers.seeded_state(nyl, kind, seed))
+    return nyl, o
+
+
+STEP_CASES = [
+    (dict(geometry="closed", n=(32, 16, 16), L=(4.0, 1.0, 1.0), dt=2e-3), "lock"),
+    (dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), n_tracers=1, dt=1e-3), "noise"),
+    (dict(geometry="perio_xyz", n=(16, 16, 16), L=(6.283185307179586,) * 3, dt=5e-3, mg_tol=1e-20), "tgv"),
+    (dict(geometry="perio_xyz", n=(16, 16, 16), L=(6.283185307179586,) * 3, modelname="Euler3d",
+          timestepping="LFAM3", dt=5e-3), "tgv"),
+    (dict(geometry="closed", n=(16, 16, 16), timestepping="EF", dt=1e-3, diff_coef={"u": 1e-3},
+          rotating=True), "noise"),
+]
+
+
+@pytest.mark.parametrize("k", range(len(STEP_CASES)))
+def test_single_steps_match_oracle(k):
+    cfg, kind = STEP_CASES[k]
+    nyl, o = _pair(cfg, kind, 60 + k)
+    m = nyl.model
+    m.diagnose_var(m.state)
+    o.diagnose()
+    t = 0.0
+    for n in range(3):
+        dt = cfg["dt"]
+        m.forward(t, dt)
+        o.forward(t, dt)
+        t += dt
+        assert m.mg_stats()["nite"] == o.mg_stats()[0]
+        names = helpers.PROG + ["t%d" % i for i in range(cfg.get("n_tracers", 0))]
+        for s in names + ["p"]:
+            got = m.state.get(s).view("i").cpu().numpy()
+            ref = o.field(s)
+            if np.max(np.abs(ref)) > 0:
+                assert helpers.relerr(got, ref) < 1e-12 * (n + 1), (n, s)
+
+
+def test_lock_exchange_100_steps():
+    """Lock exchange 64x32x32, box 4x1x1, RK3 dt=2e-3, 100 steps: <= 1e-9."""
+    nyl, o = _pair(dict(geometry="closed", n=(64, 32, 32), L=(4.0, 1.0, 1.0), dt=2e-3), "lock", 1)
+    m = nyl.model
+    m.diagnose_var(m.state)
+    o.diagnose()
+    t = 0.0
+    nites_g, nites_o = [], []
+    for n in range(100):
+        m.forward(t, 2e-3)
+        o.forward(t, 2e-3)
+        t += 2e-3
+        nites_g.append(m.mg_stats()["nite"])
+        nites_o.append(o.mg_stats()[0])
+    assert nites_g == nites_o
+    for s in helpers.PROG + ["p"]:
+        got = m.state.get(s).view("i").cpu().numpy()
+        assert helpers.relerr(got, o.field(s)) < 1e-9, s
+
+
+def test_mixed_precision_error_small():
+    """Mixed path (FP32 state/stencils, FP32 V-cycles in FP64 refinement) against FP64."""
+    from nyles_gb300.nyles import Nyles
+    cfg = dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30)
+    runs = {}
+    for prec in ("fp64", "mixed"):
+        p = helpers.make_params(precision=prec, **cfg)
+        nyl = Nyles(p)
+        rng_fields = helpers.seeded_state(nyl, "noise", 77)
+        for k, v in rng_fields.items():
+            nyl.model.state.get(k).view("i")[...] = torch.from_numpy(v)
+        nyl.model.diagnose_var(nyl.model.state)
+        t = 0.0
+        for n in range(20):
+            nyl.model.forward(t, 1e-3)
+            t += 1e-3
+        runs[prec] = {s: nyl.model.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k")}
+    for s in ("b", "u_i", "u_j", "u_k"):
+        assert helpers.relerr(runs["mixed"][s], runs["fp64"][s]) < 1e-5, s
+
+
+def test_multigrid_solver_matches_oracle():
+    import oracle
+    from nyles_gb300.multigrid import MG
+    for topo_name, topo_id in (("closed", 1), ("perio_xy", 5), ("perio_xyz", 6)):
+        nx, ny, nz = 32, 16, 16
+        mg = MG(nx, ny, nz, topo_name)
+        om = oracle.OracleMG(nx, ny, nz, topo_id)
+        mg.set_params(1e-12, 20, 0.9)
+        om.params(1e-12, 20, 0.9)
+        rng = np.random.Generator(np.random.PCG64(topo_id))
+        b = rng.standard_normal((nz, ny, nx))
+        if topo_name != "closed":
+            pass
+        b -= b.mean()
+        # mgfor's level-1 array: ghosts hold the periodic image (filled like div's
+        # halo, core/mgfordriver.py:70) or zero across closed walls
+        full = b
+        for axis, per in ((2, "x" in topo_name), (1, "y" in topo_name), (0, "z" in topo_name)):
+            pad = [(0, 0)] * 3
+            pad[axis] = (3, 3)
+            full = np.pad(full, pad, mode="wrap" if per else "constant")
+        om.set(2, full)
+        x, st = mg.solve(b)
+        n_o, r_o = om.solve()
+        assert st["nite"] == n_o
+        xo = om.get(1)[3:-3, 3:-3, 3:-3]
+        assert helpers.relerr(x.cpu().numpy(), xo) < 1e-12, topo_name
