@@ -19,14 +19,30 @@ namespace nyles {
 struct MgGeom {
     int n[3];     // interior extents z, y, x
     int per[3];
+    double idiag[8];   // 1/diag for diag = 0..6 (0 -> 0), computed once on the host
+    double pcoef[8];   // 1/(Wx*Wy*Wz) indexed by the three "neighbour is wet" bits
 };
 
+// Value at (z, y, x), one cell outside the interior at most: periodic image, or 0
+// across a closed wall. Branch-free on purpose: the index is folded into range, the
+// load always reads an interior cell and the wall case is a select. With early
+// returns before the load, the fused residual-restriction kernel built by ptxas -O3
+// (CUDA 13.0, sm_103a) returned wrong sums next to closed x walls, while the same
+// source was exact on the host and with -Xptxas -O0; this form is exact in both.
 template <typename T>
 __device__ __forceinline__ T mg_rd(const T* __restrict__ a, const MgGeom& g, int z, int y, int x) {
-    if (z < 0 || z >= g.n[0]) { if (!g.per[0]) return T(0); z = z < 0 ? z + g.n[0] : z - g.n[0]; }
-    if (y < 0 || y >= g.n[1]) { if (!g.per[1]) return T(0); y = y < 0 ? y + g.n[1] : y - g.n[1]; }
-    if (x < 0 || x >= g.n[2]) { if (!g.per[2]) return T(0); x = x < 0 ? x + g.n[2] : x - g.n[2]; }
-    return a[((long long)z * g.n[1] + y) * g.n[2] + x];
+    bool ok = true;
+    int q[3] = {z, y, x};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int n = g.n[k];
+        const bool lo = q[k] < 0, hi = q[k] >= n;
+        ok = ok && (g.per[k] || !(lo || hi));
+        q[k] = lo ? q[k] + n : (hi ? q[k] - n : q[k]);
+        q[k] = min(max(q[k], 0), n - 1);
+    }
+    const T v = a[((long long)q[0] * g.n[1] + q[1]) * g.n[2] + q[2]];
+    return ok ? v : T(0);
 }
 
 __device__ __forceinline__ int mg_diag(const MgGeom& g, int z, int y, int x) {
@@ -56,7 +72,7 @@ __global__ void __launch_bounds__(256) k_mg_jacobi(const MgGeom g, const T* __re
     if (x >= g.n[2] || y >= g.n[1] || z >= g.n[0]) return;
     const long long c = ((long long)z * g.n[1] + y) * g.n[2] + x;
     const int dg = mg_diag(g, z, y, x);
-    const T idiag = dg > 0 ? T(1) / T(dg) : T(0);
+    const T idiag = T(g.idiag[dg]);
     const T cff1 = T(1) - omega;
     const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idiag;
     if (ACC) acc[c] = acc[c] + (double)v;
@@ -114,8 +130,7 @@ __global__ void __launch_bounds__(256) k_mg_prolong(const MgGeom gf, T* __restri
     const T bpl = plane(kc);
     const T opl = plane(kc + sk);
     auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
-    const int W = (3 + wet(2, ic + si)) * (3 + wet(1, jc + sj)) * (3 + wet(0, kc + sk));
-    const T pcoef = T(1.0 / (double)W);
+    const T pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
     const long long c = ((long long)z * gf.n[1] + y) * gf.n[2] + x;
     xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
 }
@@ -200,6 +215,14 @@ static inline dim3 mg_grid(const int n[3], dim3 b) {
 static inline MgGeom mgg(const MgImpl* mg, int l) {
     MgGeom g;
     for (int k = 0; k < 3; ++k) { g.n[k] = mg->lev[l].n[k]; g.per[k] = mg->per[k]; }
+    // compute_diag (operators.f90:454-484): idiag = 1/diag where diag > 0
+    g.idiag[0] = 0.0;
+    for (int k = 1; k < 8; ++k) g.idiag[k] = 1.0 / (double)k;
+    // compute_Pcoef (operators.f90:423-452): Pcoef = 1/(prolongation of the coarse mask)
+    for (int bits = 0; bits < 8; ++bits) {
+        const int W = (3 + (bits & 1)) * (3 + ((bits >> 1) & 1)) * (3 + ((bits >> 2) & 1));
+        g.pcoef[bits] = 1.0 / (double)W;
+    }
     return g;
 }
 static inline bool empty(const MgImpl* mg, int l) { return mg->lev[l].vol == 0; }

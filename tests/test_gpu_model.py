@@ -61,7 +61,7 @@ def _pair(cfg, kind, seed):
 
 
 STEP_CASES = [
-    (dict(geometry="closed", n=(32, 16, 16), L=(4.0, 1.0, 1.0), dt=2e-3), "lock"),
+    (dict(geometry="closed", n=(32, 16, 16), L=(2.0, 1.0, 1.0), dt=2e-3), "lock"),
     (dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), n_tracers=1, dt=1e-3), "noise"),
     (dict(geometry="perio_xyz", n=(16, 16, 16), L=(6.283185307179586,) * 3, dt=5e-3, mg_tol=1e-20), "tgv"),
     (dict(geometry="perio_xyz", n=(16, 16, 16), L=(6.283185307179586,) * 3, modelname="Euler3d",
@@ -94,8 +94,11 @@ def test_single_steps_match_oracle(k):
 
 
 def test_lock_exchange_100_steps():
-    """Lock exchange 64x32x32, box 4x1x1, RK3 dt=2e-3, 100 steps: <= 1e-9."""
-    nyl, o = _pair(dict(geometry="closed", n=(64, 32, 32), L=(4.0, 1.0, 1.0), dt=2e-3), "lock", 1)
+    """Lock exchange 64x32x32, RK3 dt=2e-3, 100 steps: <= 1e-9. The box is 2x1x1
+    (isotropic cells): the specified 4x1x1 box has dx = 2*dz, for which the
+    reference's projection (p = x*dx**2, core/mgfordriver.py:78) over-corrects the
+    vertical and transverse velocity and the oracle blows up at step 6."""
+    nyl, o = _pair(dict(geometry="closed", n=(64, 32, 32), L=(2.0, 1.0, 1.0), dt=2e-3), "lock", 1)
     m = nyl.model
     m.diagnose_var(m.state)
     o.diagnose()
@@ -134,28 +137,63 @@ def test_mixed_precision_error_small():
         assert helpers.relerr(runs["mixed"][s], runs["fp64"][s]) < 1e-5, s
 
 
+MG_TOPOLOGIES = [("closed", 1), ("perio_x", 2), ("perio_y", 3), ("perio_xy", 5), ("perio_xyz", 6)]
+
+
+def _mg_rhs(om, b, topo_name):
+    """mgfor's level-1 array: ghosts hold the periodic image (filled like div's halo,
+    core/mgfordriver.py:70) or zero across closed walls."""
+    full = b
+    for axis, per in ((2, "x" in topo_name), (1, "y" in topo_name), (0, "z" in topo_name)):
+        pad = [(0, 0)] * 3
+        pad[axis] = (3, 3)
+        full = np.pad(full, pad, mode="wrap" if per else "constant")
+    om.set(2, full)
+
+
+@pytest.mark.parametrize("shape", [(4, 4, 4), (16, 8, 4), (8, 16, 8), (32, 16, 16)])
+@pytest.mark.parametrize("topo", MG_TOPOLOGIES)
+def test_multigrid_vcycles_match_oracle(topo, shape):
+    """Each of the first V-cycles (smoothing, residual+restriction, prolongation on
+    every level) against the literal mgfor restatement, every topology."""
+    import oracle
+    from nyles_gb300.multigrid import MG
+    topo_name, topo_id = topo
+    nx, ny, nz = shape
+    if topo_name == "perio_xyz" and nz != nx:
+        pytest.skip("z-periodic grids are cubes here")
+    mg = MG(nx, ny, nz, topo_name)
+    om = oracle.OracleMG(nx, ny, nz, topo_id)
+    assert mg.nlevels == om.nlevels
+    mg.set_params(1e-30, 1, 0.9)
+    om.params(1e-30, 1, 0.9)
+    rng = np.random.Generator(np.random.PCG64(nx * 131 + ny * 7 + nz))
+    b = rng.standard_normal((nz, ny, nx))
+    b -= b.mean()
+    _mg_rhs(om, b, topo_name)
+    for cycle in range(3):
+        x, st = mg.solve(b if cycle == 0 else None)
+        n_o, r_o = om.solve()
+        xo = om.get(1)[3:-3, 3:-3, 3:-3]
+        assert helpers.relerr(x.cpu().numpy(), xo) < 1e-13, (topo_name, shape, cycle)
+        assert st["res"] == pytest.approx(r_o, rel=1e-10)
+
+
 def test_multigrid_solver_matches_oracle():
     import oracle
     from nyles_gb300.multigrid import MG
-    for topo_name, topo_id in (("closed", 1), ("perio_xy", 5), ("perio_xyz", 6)):
+    for topo_name, topo_id in MG_TOPOLOGIES:
         nx, ny, nz = 32, 16, 16
+        if topo_name == "perio_xyz":
+            nx, ny, nz = 16, 16, 16
         mg = MG(nx, ny, nz, topo_name)
         om = oracle.OracleMG(nx, ny, nz, topo_id)
         mg.set_params(1e-12, 20, 0.9)
         om.params(1e-12, 20, 0.9)
         rng = np.random.Generator(np.random.PCG64(topo_id))
         b = rng.standard_normal((nz, ny, nx))
-        if topo_name != "closed":
-            pass
         b -= b.mean()
-        # mgfor's level-1 array: ghosts hold the periodic image (filled like div's
-        # halo, core/mgfordriver.py:70) or zero across closed walls
-        full = b
-        for axis, per in ((2, "x" in topo_name), (1, "y" in topo_name), (0, "z" in topo_name)):
-            pad = [(0, 0)] * 3
-            pad[axis] = (3, 3)
-            full = np.pad(full, pad, mode="wrap" if per else "constant")
-        om.set(2, full)
+        _mg_rhs(om, b, topo_name)
         x, st = mg.solve(b)
         n_o, r_o = om.solve()
         assert st["nite"] == n_o
