@@ -152,6 +152,28 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fp64_peak_tflops():
+    """Measured double-precision rate of this GPU: cuBLAS DGEMM (torch.mm float64),
+    best of 5, 2*n^3 flops. GB300's FP64 rate is a small fraction of its FP32 rate,
+    which bounds every FP64 stencil here before HBM bandwidth does."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.mm(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def peaks():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -160,16 +182,64 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def alg_bytes(nyl, phase_counts, mg_vcycles, elem):
-    """Algorithmic (compulsory) bytes of the right-hand side and multigrid smoothing
-    launches. rhs: reads b, U(3), vor(3), ke and tracers, writes 4+ntr registers."""
-    st = nyl.model.state
-    vol = st.b.data.numel()
-    ntr = nyl.param["n_tracers"]
-    rhs_words = (8 + ntr) + (4 + ntr)
-    out = {"rhs_per_launch": rhs_words * elem * vol}
-    # smoothing: each half-sweep reads x (or y) and b, writes y (or x): 3 words/cell
-    mg = nyl.model
+def mg_levels(n):
+    """Interior extents of the multigrid levels of an n^3 perio_xy grid (x, y halve
+    until 2; z interior halves alongside)."""
+    levels, x, z = [], n, n
+    while True:
+        levels.append((z, x, x))
+        if x == 2:
+            break
+        x //= 2
+        z //= 2
+    return levels
+
+
+# FP64 operations (DADD + DMUL + DFMA instructions, thread level) per cell of one
+# k_rhs_march<double, true, true> launch, counted by ncu on a 128^3 case
+# (profiles/k_rhs_march_fp64_128.md); None until measured.
+RHS_FP64_OPS_PER_CELL = None
+
+
+def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
+    """Algorithmic-bytes roofline of one kernel family from the CUDA-event phase times.
+
+    rhs       : one launch reads b, U(3), vor(3), ke and writes 4 registers: 12 words
+                per cell of the (n+6)^2 n array.
+    mg_smooth : each Jacobi half-sweep reads its input and b and writes its output:
+                3 words per level cell; per V-cycle 4 half-sweeps on every level but
+                the coarsest (2).
+    """
+    if ph.get(kernel, {}).get("count", 0) == 0:
+        return None
+    ms = ph[kernel]["ms"]
+    out = {"kernel": kernel, "bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": None}
+    if kernel == "rhs":
+        vol = (n + 6) * (n + 6) * n
+        launches = ph[kernel]["count"]
+        per_launch = 12 * elem * vol
+        avg = ms / launches
+        out.update({"kernel": "k_rhs_march", "bytes_per_launch": per_launch, "avg_launch_ms": avg,
+                    "achieved": per_launch / (avg * 1e-3) / 1e9})
+        if elem == 8 and fp64_peak:
+            ops = RHS_FP64_OPS_PER_CELL
+            out["fp64"] = {"peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM)",
+                           "achieved_tflops": (ops * vol / (avg * 1e-3) / 1e12) if ops else None,
+                           "ops_per_cell": ops}
+            if ops:
+                out["fp64"]["frac"] = out["fp64"]["achieved_tflops"] / fp64_peak
+    elif kernel == "mg_smooth":
+        lev = mg_levels(n)
+        per_vcycle = sum((4 if i < len(lev) - 1 else 2) * 3 * elem * (z * y * x) for i, (z, y, x) in enumerate(lev))
+        calls_per_vcycle = 2 * (len(lev) - 1) + 1
+        vcycles = ph[kernel]["count"] / calls_per_vcycle
+        total = per_vcycle * vcycles
+        out.update({"kernel": "k_mg_jacobi", "bytes_per_vcycle": per_vcycle, "vcycles": vcycles,
+                    "avg_launch_ms": ms / (2 * ph[kernel]["count"]), "achieved": total / (ms * 1e-3) / 1e9})
+    else:
+        out["achieved"] = None
+    if out.get("achieved") is not None:
+        out["frac"] = out["achieved"] / peak
     return out
 
 
@@ -319,6 +389,7 @@ def main():
     n = a.n
     cells = n ** 3
     peak, peak_kind = peaks()
+    fp64_peak = fp64_peak_tflops() if a.precision in ("fp64", "both") else None
     out = {"metric": METRIC, "unit": "cell-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
            "config": {"workload": "rayleigh_taylor_%d^3_perio_xy_rk3" % n, "grid": [n, n, n], "box": [1, 1, 1],
@@ -367,17 +438,9 @@ def main():
         dom = max(kernels, key=lambda k: kernels[k]["ms"])
         elem = 8 if main_prec == "fp64" else 4
         out["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in ph.items()}
-        if dom == "rhs":
-            vol = (n + 6) * (n + 6) * n
-            bytes_launch = 12 * elem * vol
-            avg = ph["rhs"]["ms"] / max(1, ph["rhs"]["count"])
-            ach = bytes_launch / (avg * 1e-3) / 1e9
-            out["roofline"] = {"kernel": "k_rhs", "bound": "hbm", "achieved": ach, "peak": peak,
-                               "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind, "traffic": None,
-                               "avg_launch_ms": avg, "bytes_per_launch": bytes_launch}
-        else:
-            out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s",
-                               "frac": None, "peak_kind": peak_kind, "traffic": None}
+        out["roofline"] = roofline(dom, ph, n, elem, peak, peak_kind, fp64_peak)
+        out["roofline_kernels"] = {k: roofline(k, ph, n, elem, peak, peak_kind, fp64_peak)
+                                   for k in ("rhs", "mg_smooth") if k != dom}
     if "mixed" in results and main_prec != "mixed":
         mr = results["mixed"]
         out["mixed"] = {"value": mr["value"], "ms_per_step": mr["ms_per_step"],
@@ -386,7 +449,10 @@ def main():
         if "e2e" in mr:
             out["mixed"]["e2e"] = mr["e2e"]
         if "phases" in mr:
-            out["mixed"]["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in mr["phases"].items()}
+            mph = mr["phases"]
+            out["mixed"]["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in mph.items()}
+            mdom = max((k for k in mph if k != "mg_solve"), key=lambda k: mph[k]["ms"])
+            out["mixed"]["roofline"] = roofline(mdom, mph, n, 4, peak, peak_kind, None)
     if rank == 0 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(64 if n >= 64 else n, 2)
     if dist:

@@ -100,6 +100,34 @@ __device__ __forceinline__ T weno5(T qmm, T qm, T q0, T qp, T qpp) {
     return (w1 * qi1 + w2 * qi2 + w3 * qi3) / (w1 + w2 + w3);
 }
 
+// Double precision: the same reconstruction with one division instead of four.
+// With d_k = beta_k + eps and e_k = d_k + tau5, the weights are w1 = e1/d1,
+// w2 = 6 e2/d2, w3 = 3 e3/d3; multiplying numerator and denominator of
+// sum(w_k qi_k)/sum(w_k) by d1 d2 d3 leaves positive terms only, so the result
+// differs from the four-division form by rounding alone. d_k >= 1e-16 keeps the
+// triple products far from underflow in double (not so in float, which keeps the
+// form above). FP64 division is a multi-instruction sequence on the FP64 pipe, the
+// scarce unit on GB300.
+template <>
+__device__ __forceinline__ double weno5<double>(double qmm, double qm, double q0, double qp, double qpp) {
+    typedef WenoK<double> K;
+    const double qi1 = K::c13() * qmm - K::c76() * qm + K::c116() * q0;
+    const double qi2 = -(K::c16() * qm) + K::c56() * q0 + K::c13() * qp;
+    const double qi3 = K::c13() * q0 + K::c56() * qp - K::c16() * qpp;
+    const double a1 = qmm - 2.0 * qm + q0, b1 = qmm - 4.0 * qm + 3.0 * q0;
+    const double a2 = qm - 2.0 * q0 + qp, b2 = qm - qp;
+    const double a3 = q0 - 2.0 * qp + qpp, b3 = 3.0 * q0 - 4.0 * qp + qpp;
+    const double beta1 = K::k1() * (a1 * a1) + 0.25 * (b1 * b1);
+    const double beta2 = K::k1() * (a2 * a2) + 0.25 * (b2 * b2);
+    const double beta3 = K::k1() * (a3 * a3) + 0.25 * (b3 * b3);
+    const double tau5 = K::tau(fabs(beta1 - beta3));
+    const double d1 = beta1 + K::eps5(), d2 = beta2 + K::eps5(), d3 = beta3 + K::eps5();
+    const double A = (d1 + tau5) * (d2 * d3);
+    const double B = 6.0 * (d2 + tau5) * (d1 * d3);
+    const double C = 3.0 * (d3 + tau5) * (d1 * d2);
+    return (A * qi1 + B * qi2 + C * qi3) / (A + B + C);
+}
+
 // Value of core/weno.f90:106-153 `flux1d` at index i (0-based) of a line of length n
 // (n >= 5), given the velocity u at i and an accessor Q(j) for the advected quantity.
 // Branch precedence follows the Fortran statement order (later statements win).

@@ -10,6 +10,11 @@
 //   Pcoef = 1/(Wx*Wy*Wz), W = 3 + [coarse neighbour is wet]     (compute_Pcoef)
 // The smoother's intermediate `y` on the ghost ring (basicoperators.f90:380-388) is 0
 // across closed walls (its idiag and x are 0 there) and the periodic image otherwise.
+//
+// Kernel layout: blocks of 32 x 8 threads over (x, y); each thread marches over a chunk
+// of z, keeping the z-1, z, z+1 values in registers. A block whose cells and stencil
+// neighbours all lie inside the level takes a fast path with direct strided loads;
+// only blocks touching the level's faces go through the ghost logic.
 #include "nyles_internal.h"
 #include <vector>
 #include <cstring>
@@ -17,11 +22,18 @@
 namespace nyles {
 
 struct MgGeom {
-    int n[3];     // interior extents z, y, x
+    int n[3];          // interior extents z, y, x
     int per[3];
     double idiag[8];   // 1/diag for diag = 0..6 (0 -> 0), computed once on the host
     double pcoef[8];   // 1/(Wx*Wy*Wz) indexed by the three "neighbour is wet" bits
 };
+
+constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
+constexpr int MG_RZC = 4;                          // restriction (coarse z per thread)
+
+__device__ __forceinline__ long long mg_at(const MgGeom& g, int z, int y, int x) {
+    return ((long long)z * g.n[1] + y) * g.n[2] + x;
+}
 
 // Value at (z, y, x), one cell outside the interior at most: periodic image, or 0
 // across a closed wall. Branch-free on purpose: the index is folded into range, the
@@ -46,9 +58,10 @@ __device__ __forceinline__ T mg_rd(const T* __restrict__ a, const MgGeom& g, int
 }
 
 __device__ __forceinline__ int mg_diag(const MgGeom& g, int z, int y, int x) {
-    const int p[3] = {z, y, x};
     int d = 0;
-    for (int k = 0; k < 3; ++k) d += g.per[k] ? 2 : ((p[k] > 0) + (p[k] < g.n[k] - 1));
+    d += g.per[0] ? 2 : ((z > 0) + (z < g.n[0] - 1));
+    d += g.per[1] ? 2 : ((y > 0) + (y < g.n[1] - 1));
+    d += g.per[2] ? 2 : ((x > 0) + (x < g.n[2] - 1));
     return d;
 }
 
@@ -59,139 +72,218 @@ __device__ __forceinline__ T mg_nsum(const T* __restrict__ a, const MgGeom& g, i
              mg_rd(a, g, z, y + 1, x)) + mg_rd(a, g, z - 1, y, x)) + mg_rd(a, g, z + 1, y, x);
 }
 
-// one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
-// (basicoperators.f90:379-398). With ACC, the result is also added to the FP64
-// solution `acc` (mixed precision: the correction of iterative refinement).
-template <typename T, bool ACC>
-__global__ void __launch_bounds__(256) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
-                                                  const T* __restrict__ b, T* __restrict__ out, T omega,
-                                                  double* __restrict__ acc) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= g.n[2] || y >= g.n[1] || z >= g.n[0]) return;
-    const long long c = ((long long)z * g.n[1] + y) * g.n[2] + x;
-    const int dg = mg_diag(g, z, y, x);
-    const T idiag = T(g.idiag[dg]);
-    const T cff1 = T(1) - omega;
-    const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idiag;
-    if (ACC) acc[c] = acc[c] + (double)v;
-    else out[c] = v;
-}
-
-// residual r = msk*(b + diag*x - sum(x_nb)) (basicoperators.f90:300-323)
+// residual r = msk*(b + diag*x - sum(x_nb)) (basicoperators.f90:300-323), ghost logic
 template <typename T>
 __device__ __forceinline__ T mg_resid(const T* __restrict__ x, const T* __restrict__ b, const MgGeom& g, int z, int y,
                                       int xx) {
-    const long long c = ((long long)z * g.n[1] + y) * g.n[2] + xx;
+    const long long c = mg_at(g, z, y, xx);
     const T dg = T(mg_diag(g, z, y, xx));
     return (b[c] + dg * x[c]) - mg_nsum(x, g, z, y, xx);
+}
+// same with every neighbour inside the level (diag = 6), direct loads
+template <typename T>
+__device__ __forceinline__ T mg_resid_in(const T* __restrict__ x, const T* __restrict__ b, long long c, long long sy,
+                                         long long sz) {
+    return (b[c] + T(6) * x[c]) - (((((x[c - 1] + x[c + 1]) + x[c - sy]) + x[c + sy]) + x[c - sz]) + x[c + sz]);
+}
+
+// this block's cells plus a margin of `r` cells lie inside the level in every direction
+__device__ __forceinline__ bool mg_block_inside(const MgGeom& g, int z0, int z1, int r) {
+    const int x0 = blockIdx.x * MG_BX, y0 = blockIdx.y * MG_BY;
+    const int x1 = min(x0 + MG_BX, g.n[2]) - 1, y1 = min(y0 + MG_BY, g.n[1]) - 1;
+    return x0 >= r && x1 <= g.n[2] - 1 - r && y0 >= r && y1 <= g.n[1] - 1 - r && z0 >= r && z1 <= g.n[0] - 1 - r &&
+           (x0 + MG_BX <= g.n[2]) && (y0 + MG_BY <= g.n[1]);
+}
+
+// one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
+// (basicoperators.f90:379-398). With ACC, the result is added to the FP64 solution
+// `acc` instead of being stored (mixed precision: the correction of iterative
+// refinement, fused into the last half-sweep of the V-cycle).
+template <typename T, bool ACC>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
+                                                            const T* __restrict__ b, T* __restrict__ out, T omega,
+                                                            double* __restrict__ acc) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_ZC;
+    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    const T cff1 = T(1) - omega;
+    if (mg_block_inside(g, z0, z1, 1)) {
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        const T idg = T(g.idiag[6]);
+        long long c = mg_at(g, z0, y, x);
+        T xm = in[c - sz], x0 = in[c];
+        for (int z = z0; z <= z1; ++z, c += sz) {
+            const T xp = in[c + sz];
+            const T s = ((((in[c - 1] + in[c + 1]) + in[c - sy]) + in[c + sy]) + xm) + xp;
+            const T v = cff1 * x0 + omega * (s - b[c]) * idg;
+            if (ACC) acc[c] = acc[c] + (double)v;
+            else out[c] = v;
+            xm = x0;
+            x0 = xp;
+        }
+        return;
+    }
+    if (x >= g.n[2] || y >= g.n[1]) return;
+    for (int z = z0; z <= z1; ++z) {
+        const long long c = mg_at(g, z, y, x);
+        const T idg = T(g.idiag[mg_diag(g, z, y, x)]);
+        const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
+        if (ACC) acc[c] = acc[c] + (double)v;
+        else out[c] = v;
+    }
 }
 
 // residual of the fine level restricted to the coarse right-hand side,
 // bc = Rcoef*(sum of the 8 children) with Rcoef = 1/2 (basicoperators.f90:32-60,
 // operators.f90:172-213); the coarse solution is zeroed (operators.f90:209)
 template <typename T>
-__global__ void __launch_bounds__(256) k_mg_restrict(const MgGeom gf, const T* __restrict__ xf,
-                                                    const T* __restrict__ bf, const MgGeom gc, T* __restrict__ bc,
-                                                    T* __restrict__ xc) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= gc.n[2] || y >= gc.n[1] || z >= gc.n[0]) return;
-    const int i = 2 * x, j = 2 * y, k = 2 * z;
-    T s = mg_resid(xf, bf, gf, k, j, i);
-    s = s + mg_resid(xf, bf, gf, k, j, i + 1);
-    s = s + mg_resid(xf, bf, gf, k, j + 1, i);
-    s = s + mg_resid(xf, bf, gf, k, j + 1, i + 1);
-    s = s + mg_resid(xf, bf, gf, k + 1, j, i);
-    s = s + mg_resid(xf, bf, gf, k + 1, j, i + 1);
-    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i);
-    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i + 1);
-    const long long c = ((long long)z * gc.n[1] + y) * gc.n[2] + x;
-    bc[c] = T(0.5) * s;
-    xc[c] = T(0);
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, const T* __restrict__ xf,
+                                                              const T* __restrict__ bf, const MgGeom gc,
+                                                              T* __restrict__ bc, T* __restrict__ xc) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_RZC;
+    const int z1 = min(z0 + MG_RZC, gc.n[0]) - 1;
+    if (x >= gc.n[2] || y >= gc.n[1]) return;
+    // fast path when every child and its face neighbours are inside the fine level
+    const int bx0 = blockIdx.x * MG_BX, by0 = blockIdx.y * MG_BY;
+    const bool inside = bx0 >= 1 && 2 * (bx0 + MG_BX) + 1 <= gf.n[2] - 1 && by0 >= 1 &&
+                        2 * (by0 + MG_BY) + 1 <= gf.n[1] - 1 && z0 >= 1 && 2 * z1 + 2 <= gf.n[0] - 1;
+    const long long sy = gf.n[2], sz = (long long)gf.n[1] * gf.n[2];
+    for (int z = z0; z <= z1; ++z) {
+        const int i = 2 * x, j = 2 * y, k = 2 * z;
+        T s;
+        if (inside) {
+            const long long c = mg_at(gf, k, j, i);
+            s = mg_resid_in(xf, bf, c, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + 1, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sy, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sy + 1, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sz, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sz + 1, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sz + sy, sy, sz);
+            s = s + mg_resid_in(xf, bf, c + sz + sy + 1, sy, sz);
+        } else {
+            s = mg_resid(xf, bf, gf, k, j, i);
+            s = s + mg_resid(xf, bf, gf, k, j, i + 1);
+            s = s + mg_resid(xf, bf, gf, k, j + 1, i);
+            s = s + mg_resid(xf, bf, gf, k, j + 1, i + 1);
+            s = s + mg_resid(xf, bf, gf, k + 1, j, i);
+            s = s + mg_resid(xf, bf, gf, k + 1, j, i + 1);
+            s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i);
+            s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i + 1);
+        }
+        const long long c = mg_at(gc, z, y, x);
+        bc[c] = T(0.5) * s;
+        xc[c] = T(0);
+    }
 }
 
 // trilinear 9-3-3-1 prolongation added to the fine solution (basicoperators.f90:173-231)
 template <typename T>
-__global__ void __launch_bounds__(256) k_mg_prolong(const MgGeom gf, T* __restrict__ xf, const MgGeom gc,
-                                                   const T* __restrict__ xc) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= gf.n[2] || y >= gf.n[1] || z >= gf.n[0]) return;
-    const int ic = x >> 1, jc = y >> 1, kc = z >> 1;
-    const int si = (x & 1) ? 1 : -1, sj = (y & 1) ? 1 : -1, sk = (z & 1) ? 1 : -1;
-    auto plane = [&](int kk) -> T {
-        return ((T(9) * mg_rd(xc, gc, kk, jc, ic) + T(3) * mg_rd(xc, gc, kk, jc, ic + si)) +
-                T(3) * mg_rd(xc, gc, kk, jc + sj, ic)) + mg_rd(xc, gc, kk, jc + sj, ic + si);
-    };
-    const T bpl = plane(kc);
-    const T opl = plane(kc + sk);
-    auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
-    const T pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
-    const long long c = ((long long)z * gf.n[1] + y) * gf.n[2] + x;
-    xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T* __restrict__ xf, const MgGeom gc,
+                                                             const T* __restrict__ xc) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_ZC;
+    const int z1 = min(z0 + MG_ZC, gf.n[0]) - 1;
+    if (x >= gf.n[2] || y >= gf.n[1]) return;
+    const int ic = x >> 1, jc = y >> 1;
+    const int si = (x & 1) ? 1 : -1, sj = (y & 1) ? 1 : -1;
+    // fast path: all coarse neighbours of the block inside the coarse level
+    const int bx0 = blockIdx.x * MG_BX, by0 = blockIdx.y * MG_BY;
+    const bool inside = (bx0 >> 1) >= 1 && ((bx0 + MG_BX - 1) >> 1) + 1 <= gc.n[2] - 1 && (by0 >> 1) >= 1 &&
+                        ((by0 + MG_BY - 1) >> 1) + 1 <= gc.n[1] - 1 && (z0 >> 1) >= 1 && (z1 >> 1) + 1 <= gc.n[0] - 1;
+    const long long csy = gc.n[2], csz = (long long)gc.n[1] * gc.n[2];
+    for (int z = z0; z <= z1; ++z) {
+        const int kc = z >> 1, sk = (z & 1) ? 1 : -1;
+        T bpl, opl, pcoef;
+        if (inside) {
+            const long long c0 = mg_at(gc, kc, jc, ic);
+            auto plane = [&](long long c) -> T {
+                return ((T(9) * xc[c] + T(3) * xc[c + si]) + T(3) * xc[c + sj * csy]) + xc[c + sj * csy + si];
+            };
+            bpl = plane(c0);
+            opl = plane(c0 + sk * csz);
+            pcoef = T(gf.pcoef[7]);
+        } else {
+            auto plane = [&](int kk) -> T {
+                return ((T(9) * mg_rd(xc, gc, kk, jc, ic) + T(3) * mg_rd(xc, gc, kk, jc, ic + si)) +
+                        T(3) * mg_rd(xc, gc, kk, jc + sj, ic)) + mg_rd(xc, gc, kk, jc + sj, ic + si);
+            };
+            bpl = plane(kc);
+            opl = plane(kc + sk);
+            auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
+            pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
+        }
+        const long long c = mg_at(gf, z, y, x);
+        xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
+    }
 }
 
 // ---------------------------------------------------------------- reductions
-// deterministic: fixed grid of `npart` blocks, block partials, one final block
-template <typename T, int MODE>   // MODE 0: sum v^2 ; 1: sum r^2 with r = b - A x
-__global__ void __launch_bounds__(256) k_mg_sumsq(const MgGeom g, const T* __restrict__ v, const T* __restrict__ b,
-                                                 double* __restrict__ partial) {
-    const long long vol = (long long)g.n[0] * g.n[1] * g.n[2];
-    double s = 0.0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
-        double val;
-        if (MODE == 0) {
-            val = (double)v[i];
-        } else {
-            const int x = (int)(i % g.n[2]);
-            const int y = (int)((i / g.n[2]) % g.n[1]);
-            const int z = (int)(i / ((long long)g.n[2] * g.n[1]));
-            val = (double)mg_resid(v, b, g, z, y, x);
-        }
-        s += val * val;
-    }
-    __shared__ double sm[8];
+// Deterministic sums: one partial per block of the (x, y, z-chunk) grid, then one
+// block adds the partials in a fixed order.
+__device__ __forceinline__ void block_partial(double s, double* __restrict__ partial) {
+    __shared__ double sm[MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
     s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    if ((tid & 31) == 0) sm[tid >> 5] = s;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+    if (tid < 32) {
+        double t = (tid < MG_BX * MG_BY / 32) ? sm[tid] : 0.0;
         t = warp_sum(t);
-        if (threadIdx.x == 0) partial[blockIdx.x] = t;
+        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
     }
+}
+
+// MODE 0: sum v^2 ; MODE 1: sum r^2 with r = b + diag*x - sum(x_nb)
+template <typename T, int MODE>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq(const MgGeom g, const T* __restrict__ v,
+                                                           const T* __restrict__ b, double* __restrict__ partial) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_ZC;
+    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    double s = 0.0;
+    if (MODE == 1 && mg_block_inside(g, z0, z1, 1)) {
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        for (int z = z0; z <= z1; ++z) {
+            const double r = (double)mg_resid_in(v, b, mg_at(g, z, y, x), sy, sz);
+            s += r * r;
+        }
+    } else if (x < g.n[2] && y < g.n[1]) {
+        for (int z = z0; z <= z1; ++z) {
+            const double r = MODE == 0 ? (double)v[mg_at(g, z, y, x)] : (double)mg_resid(v, b, g, z, y, x);
+            s += r * r;
+        }
+    }
+    block_partial(s, partial);
 }
 
 // mixed precision: FP64 residual of the FP64 solution, its sum of squares, the FP32
 // right-hand side of the next correction V-cycle and a zero initial correction
-__global__ void __launch_bounds__(256) k_mg_resid64(const MgGeom g, const double* __restrict__ p,
-                                                   const double* __restrict__ b, float* __restrict__ r32,
-                                                   float* __restrict__ e32, double* __restrict__ partial) {
-    const long long vol = (long long)g.n[0] * g.n[1] * g.n[2];
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid64(const MgGeom g, const double* __restrict__ p,
+                                                             const double* __restrict__ b, float* __restrict__ r32,
+                                                             float* __restrict__ e32, double* __restrict__ partial) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_ZC;
+    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
     double s = 0.0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
-        const int x = (int)(i % g.n[2]);
-        const int y = (int)((i / g.n[2]) % g.n[1]);
-        const int z = (int)(i / ((long long)g.n[2] * g.n[1]));
-        const double r = mg_resid(p, b, g, z, y, x);
-        r32[i] = (float)r;
-        e32[i] = 0.0f;
-        s += r * r;
+    const bool inside = mg_block_inside(g, z0, z1, 1);
+    if (inside || (x < g.n[2] && y < g.n[1])) {
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        for (int z = z0; z <= z1; ++z) {
+            const long long c = mg_at(g, z, y, x);
+            const double r = inside ? mg_resid_in(p, b, c, sy, sz) : mg_resid(p, b, g, z, y, x);
+            r32[c] = (float)r;
+            e32[c] = 0.0f;
+            s += r * r;
+        }
     }
-    __shared__ double sm[8];
-    s = warp_sum(s);
-    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double t = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
-        t = warp_sum(t);
-        if (threadIdx.x == 0) partial[blockIdx.x] = t;
-    }
+    block_partial(s, partial);
 }
 
 __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __restrict__ out) {
@@ -209,9 +301,11 @@ __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __
 }
 
 // ---------------------------------------------------------------- host side
-static inline dim3 mg_grid(const int n[3], dim3 b) {
-    return dim3((n[2] + b.x - 1) / b.x, (n[1] + b.y - 1) / b.y, (n[0] + b.z - 1) / b.z);
+static inline dim3 grid_zc(const int n[3], int zc) {
+    return dim3((n[2] + MG_BX - 1) / MG_BX, (n[1] + MG_BY - 1) / MG_BY, (n[0] + zc - 1) / zc);
 }
+static const dim3 kBlk(MG_BX, MG_BY, 1);
+
 static inline MgGeom mgg(const MgImpl* mg, int l) {
     MgGeom g;
     for (int k = 0; k < 3; ++k) { g.n[k] = mg->lev[l].n[k]; g.per[k] = mg->per[k]; }
@@ -287,7 +381,8 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         mg->off_p64 = take(mg->lev[0].vol * sizeof(double));
         mg->off_b64 = take(mg->lev[0].vol * sizeof(double));
     }
-    mg->npartial = 152 * 4;
+    const dim3 g0 = grid_zc(mg->lev[0].n, MG_ZC);
+    mg->npartial = (int)(g0.x * g0.y * g0.z);
     mg->off_partial = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
     mg->bytes = off;
@@ -298,34 +393,32 @@ template <typename T>
 static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
     if (empty(mg, l)) return;
     MgGeom g = mgg(mg, l);
-    dim3 blk(32, 4, 2);
-    dim3 grd = mg_grid(g.n, blk);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
     T* x = lvp<T>(mg, l, 1);
     T* b = lvp<T>(mg, l, 2);
     T* y = lvp<T>(mg, l, 3);
     const T om = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch(2);
-    k_mg_jacobi<T, false><<<grd, blk, 0, st>>>(g, x, b, y, om, nullptr);
+    k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr);
     if (acc_p64)
-        k_mg_jacobi<T, true><<<grd, blk, 0, st>>>(g, y, b, x, om, reinterpret_cast<double*>(mg->ws + mg->off_p64));
+        k_mg_jacobi<T, true><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<double*>(mg->ws + mg->off_p64));
     else
-        k_mg_jacobi<T, false><<<grd, blk, 0, st>>>(g, y, b, x, om, nullptr);
+        k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr);
 }
 
 // solvers.f90:35-55
 template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     const int L = mg->nlevels;
-    dim3 blk(32, 4, 2);
     for (int l = 0; l < L - 1; ++l) {
         smooth<T>(mg, l, st, false);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 9, st);
             note_launch();
-            k_mg_restrict<T><<<mg_grid(gc.n, blk), blk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
-                                                                lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 1));
+            k_mg_restrict<T><<<grid_zc(gc.n, MG_RZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
+                                                                    lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 1));
         }
     }
     smooth<T>(mg, L - 1, st, L == 1 && mixed);
@@ -334,42 +427,47 @@ static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 10, st);
             note_launch();
-            k_mg_prolong<T><<<mg_grid(gf.n, blk), blk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
+            k_mg_prolong<T><<<grid_zc(gf.n, MG_ZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
         }
         smooth<T>(mg, l, st, l == 0 && mixed);
     }
+}
+
+static int read_scalar(MgImpl* mg, double* host_out, cudaStream_t st) {
+    double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    cudaError_t e = cudaMemcpyAsync(host_out, out, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e, "multigrid norm");
 }
 
 template <typename T, int MODE>
 static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* host_out, cudaStream_t st) {
     double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
     double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
     {
         ProfScope ps(mg->prof, 11, st);
         note_launch(2);
-        k_mg_sumsq<T, MODE><<<mg->npartial, 256, 0, st>>>(g, v, b, part);
-        k_mg_final<<<1, 1024, 0, st>>>(part, mg->npartial, out);
+        k_mg_sumsq<T, MODE><<<grd, kBlk, 0, st>>>(g, v, b, part);
+        k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
     }
-    cudaError_t e = cudaMemcpyAsync(host_out, out, sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return cuda_status(e, "multigrid norm");
+    return read_scalar(mg, host_out, st);
 }
 
 static int resid64(MgImpl* mg, double* host_out, cudaStream_t st) {
     MgGeom g = mgg(mg, 0);
     double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
     double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
     {
         ProfScope ps(mg->prof, 11, st);
         note_launch(2);
-        k_mg_resid64<<<mg->npartial, 256, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
-                                                    reinterpret_cast<const double*>(mg->ws + mg->off_b64),
-                                                    lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
-        k_mg_final<<<1, 1024, 0, st>>>(part, mg->npartial, out);
+        k_mg_resid64<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
+                                           reinterpret_cast<const double*>(mg->ws + mg->off_b64),
+                                           lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
+        k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
     }
-    cudaError_t e = cudaMemcpyAsync(host_out, out, sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return cuda_status(e, "multigrid residual");
+    return read_scalar(mg, host_out, st);
 }
 
 // solvers.f90:8-33: stop when sum(r^2)/sum(b^2) < tol or after maxite V-cycles

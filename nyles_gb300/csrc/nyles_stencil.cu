@@ -155,6 +155,118 @@ __global__ void __launch_bounds__(128) k_rhs(const RhsArgs<T> a) {
     a.ds[3][c] = duz;
 }
 
+// ---------------------------------------------------------------- z-marching RHS
+// The full right-hand side with tracer face fluxes shared between the two cells of
+// each face: along x through a warp shuffle (one warp = one x row of 32 cells), along
+// y through shared memory, along z carried in a register while the thread marches up
+// its column chunk. One WENO5 per direction and tracer per cell instead of two; same
+// arithmetic and accumulation order as k_rhs.
+constexpr int RZ_BX = 32, RZ_BY = 8, RZ_ZC = 16;
+
+template <typename T>
+struct TracerMarch {
+    T fz_prev;
+    // -(flux divergence) at (z, ys, xs); all threads of the block must call it
+    __device__ __forceinline__ T step(const T* __restrict__ q, const T* const* U, const Geom& g, long long c, int z,
+                                      int ys, int xs, T (*sfy)[RZ_BX]) {
+        const int tx = threadIdx.x, ty = threadIdx.y;
+        const T fx = tr_flux(U[2], q, g, c, xs, 2);
+        T fxm = __shfl_up_sync(0xffffffffu, fx, 1);
+        if (tx == 0 && xs > 0) fxm = tr_flux(U[2], q, g, c - 1, xs - 1, 2);
+        T acc = (xs > 0) ? (T(0) + fxm) - fx : T(0) - fx;
+        const T fy = tr_flux(U[1], q, g, c, ys, 1);
+        sfy[ty][tx] = fy;
+        __syncthreads();
+        T fym = (ty > 0) ? sfy[ty - 1][tx] : T(0);
+        __syncthreads();
+        if (ty == 0 && ys > 0) fym = tr_flux(U[1], q, g, c - g.sy, ys - 1, 1);
+        acc = (ys > 0) ? (acc + fym) - fy : acc - fy;
+        const T fz = tr_flux(U[0], q, g, c, z, 0);
+        acc = (z > 0) ? (acc + fz_prev) - fz : acc - fz;
+        fz_prev = fz;
+        return acc;
+    }
+};
+
+// TR: buoyancy advection on; VF: vortex force on. ds[0..3] are written.
+template <typename T, bool TR, bool VF>
+__global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a) {
+    __shared__ T sfy[RZ_BY][RZ_BX];
+    const Geom& g = a.g;
+    const int x = blockIdx.x * RZ_BX + threadIdx.x;
+    const int y = blockIdx.y * RZ_BY + threadIdx.y;
+    const int z0 = blockIdx.z * RZ_ZC;
+    const int z1 = min(z0 + RZ_ZC, g.N[0]) - 1;
+    const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
+    const bool valid = x < Nx && y < Ny;
+    const int xs = min(x, Nx - 1), ys = min(y, Ny - 1);   // idle lanes shadow a real cell
+    const T* Uzyx[3] = {a.U[2], a.U[1], a.U[0]};
+    TracerMarch<T> tm;
+    tm.fz_prev = T(0);
+    if (TR && z0 > 0) tm.fz_prev = tr_flux(Uzyx[0], a.b, g, g.at(z0 - 1, ys, xs), z0 - 1, 0);
+    for (int z = z0; z <= z1; ++z) {
+        const long long c = g.at(z, ys, xs);
+        const int pos[3] = {z, ys, xs};
+        T db = T(0);
+        if (TR) db = tm.step(a.b, Uzyx, g, c, z, ys, xs, sfy);
+        T dux = T(0), duy = T(0), duz = T(0);
+        if (VF) {
+            if (ys < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, xs, 2, 1);
+            if (xs < Nx - 1) dux = dux + vf_flux(a.U[1], a.W[2], g, c, ys, 1, 2);
+            if (z < Nz - 1) duz = duz - vf_flux(a.U[1], a.W[0], g, c, ys, 1, 0);
+            if (ys < Ny - 1) duy = duy + vf_flux(a.U[2], a.W[0], g, c, z, 0, 1);
+            if (xs < Nx - 1) dux = dux - vf_flux(a.U[2], a.W[1], g, c, z, 0, 2);
+            if (z < Nz - 1) duz = duz + vf_flux(a.U[0], a.W[1], g, c, xs, 2, 0);
+        }
+        {
+            const T* ke = a.ke;
+            if (xs < Nx - 1) dux = sub_rn(dux, sub_rn(__ldg(ke + c + 1), __ldg(ke + c)));
+            if (ys < Ny - 1) duy = sub_rn(duy, sub_rn(__ldg(ke + c + g.sy), __ldg(ke + c)));
+            if (z < Nz - 1) {
+                duz = sub_rn(duz, sub_rn(__ldg(ke + c + g.sz), __ldg(ke + c)));
+                if (!a.euler) duz = add_rn(duz, mul_rn(a.half_dz, add_rn(__ldg(a.b + c + g.sz), __ldg(a.b + c))));
+            }
+        }
+        if (a.terms & TERM_VISC) {
+            for (int pass = 0; pass < 3; ++pass) {
+                const int d = 2 - pass;
+                const T cf = a.vcoef[pass];
+                dux = dux + cf * lap1d(a.u[0], g, c, pos[d], d);
+                duy = duy + cf * lap1d(a.u[1], g, c, pos[d], d);
+                duz = duz + cf * lap1d(a.u[2], g, c, pos[d], d);
+            }
+        }
+        if (valid) {
+            a.ds[0][c] = db;
+            a.ds[1][c] = dux;
+            a.ds[2][c] = duy;
+            a.ds[3][c] = duz;
+        }
+    }
+}
+
+// advection of one passive tracer (core/tracer.py:59-72) with the same flux sharing
+template <typename T>
+__global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, const T* __restrict__ Ux,
+                                                                const T* __restrict__ Uy, const T* __restrict__ Uz,
+                                                                const T* __restrict__ q, T* __restrict__ dq) {
+    __shared__ T sfy[RZ_BY][RZ_BX];
+    const int x = blockIdx.x * RZ_BX + threadIdx.x;
+    const int y = blockIdx.y * RZ_BY + threadIdx.y;
+    const int z0 = blockIdx.z * RZ_ZC;
+    const int z1 = min(z0 + RZ_ZC, g.N[0]) - 1;
+    const bool valid = x < g.N[2] && y < g.N[1];
+    const int xs = min(x, g.N[2] - 1), ys = min(y, g.N[1] - 1);
+    const T* U[3] = {Uz, Uy, Ux};
+    TracerMarch<T> tm;
+    tm.fz_prev = z0 > 0 ? tr_flux(U[0], q, g, g.at(z0 - 1, ys, xs), z0 - 1, 0) : T(0);
+    for (int z = z0; z <= z1; ++z) {
+        const long long c = g.at(z, ys, xs);
+        const T v = tm.step(q, U, g, c, z, ys, xs, sfy);
+        if (valid) dq[c] = v;
+    }
+}
+
 bool make_geom(const NylesDesc* d, Geom* g) {
     if (!d || d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nh < 0) return false;
     const int per[3] = {d->periodic_z ? 1 : 0, d->periodic_y ? 1 : 0, d->periodic_x ? 1 : 0};
@@ -197,9 +309,28 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     a.vcoef[0] = T(d->viscosity * d->idx2);
     a.vcoef[1] = T(d->viscosity * d->idy2);
     a.vcoef[2] = T(d->viscosity * d->idz2);
-    dim3 blk(32, 2, 2);
-    k_rhs<T><<<grid3(g, blk), blk, 0, st>>>(a);
+    if (terms & TERM_ACCUMULATE) {   // add into existing registers (vortex force alone)
+        dim3 blk(32, 2, 2);
+        k_rhs<T><<<grid3(g, blk), blk, 0, st>>>(a);
+        note_launch();
+        return cuda_status(cudaGetLastError(), "rhs kernel");
+    }
+    const dim3 blk(RZ_BX, RZ_BY, 1);
+    const dim3 grd((g.N[2] + RZ_BX - 1) / RZ_BX, (g.N[1] + RZ_BY - 1) / RZ_BY, (g.N[0] + RZ_ZC - 1) / RZ_ZC);
+    const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
+    if (tr && vf) k_rhs_march<T, true, true><<<grd, blk, 0, st>>>(a);
+    else if (tr) k_rhs_march<T, true, false><<<grd, blk, 0, st>>>(a);
+    else if (vf) k_rhs_march<T, false, true><<<grd, blk, 0, st>>>(a);
+    else k_rhs_march<T, false, false><<<grd, blk, 0, st>>>(a);
     note_launch();
+    for (int t = 0; t < d->n_tracers; ++t) {
+        if (tr) {
+            k_tracer_march<T><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.tr[t], a.ds[4 + t]);
+            note_launch();
+        } else {   // Euler3d: tracers are not advected, their tendency is zero (reset_state)
+            cudaMemsetAsync(a.ds[4 + t], 0, sizeof(T) * g.vol, st);
+        }
+    }
     return cuda_status(cudaGetLastError(), "rhs kernel");
 }
 

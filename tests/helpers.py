@@ -93,11 +93,31 @@ def load_state(nyl, o, fields):
         o.field(k)[...] = v
 
 
-def relerr(a, b):
+def relerr(a, b, scale=None):
+    """max|a-b| / max|b| (or / scale)."""
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
-    den = max(np.max(np.abs(b)), 1e-300)
+    den = max(np.max(np.abs(b)) if scale is None else scale, 1e-300)
     return float(np.max(np.abs(a - b)) / den)
+
+
+VECTORS = {"u": ("u_i", "u_j", "u_k"), "U": ("U_i", "U_j", "U_k"), "vor": ("vor_i", "vor_j", "vor_k")}
+
+
+def parity_errors(get_a, get_b, names):
+    """Relative max-norm error per variable. Scalars are normalised by their own
+    max-norm; components of a vector field (u, U, vor) by the max-norm of the whole
+    vector, so that a component that is only round-off noise (v in a 2-D flow) is
+    judged against the velocity scale, not against its own noise level."""
+    out = {}
+    scales = {}
+    for vec, comps in VECTORS.items():
+        if any(c in names for c in comps):
+            scales[vec] = max(float(np.max(np.abs(np.asarray(get_b(c), dtype=np.float64)))) for c in comps)
+    for n in names:
+        vec = next((v for v, comps in VECTORS.items() if n in comps), None)
+        out[n] = relerr(get_a(n), get_b(n), scales.get(vec))
+    return out
 
 
 def golden_cases():

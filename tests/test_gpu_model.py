@@ -42,13 +42,10 @@ def test_golden_trajectories(name):
         m.forward(t, dt)
         t += dt
         assert m.mg_stats()["nite"] == int(d["nites_last"][n])
-    for s in progs + helpers.DIAG:
-        got = m.state.get(s).view("i").cpu().numpy()
-        ref = d["final_" + s]
-        if np.max(np.abs(ref)) == 0:
-            assert np.max(np.abs(got)) == 0, s
-        else:
-            assert helpers.relerr(got, ref) < 1e-11 * meta["steps"], s
+    names = progs + helpers.DIAG
+    errs = helpers.parity_errors(lambda s: m.state.get(s).view("i").cpu().numpy(), lambda s: d["final_" + s], names)
+    for s in names:
+        assert errs[s] < 1e-11 * meta["steps"], (s, errs[s])
 
 
 def _pair(cfg, kind, seed):
@@ -85,12 +82,10 @@ def test_single_steps_match_oracle(k):
         o.forward(t, dt)
         t += dt
         assert m.mg_stats()["nite"] == o.mg_stats()[0]
-        names = helpers.PROG + ["t%d" % i for i in range(cfg.get("n_tracers", 0))]
-        for s in names + ["p"]:
-            got = m.state.get(s).view("i").cpu().numpy()
-            ref = o.field(s)
-            if np.max(np.abs(ref)) > 0:
-                assert helpers.relerr(got, ref) < 1e-12 * (n + 1), (n, s)
+        names = helpers.PROG + ["t%d" % i for i in range(cfg.get("n_tracers", 0))] + ["p"]
+        errs = helpers.parity_errors(lambda s: m.state.get(s).view("i").cpu().numpy(), o.field, names)
+        for s in names:
+            assert errs[s] < 1e-12 * (n + 1), (n, s, errs[s])
 
 
 def test_lock_exchange_100_steps():
@@ -111,9 +106,10 @@ def test_lock_exchange_100_steps():
         nites_g.append(m.mg_stats()["nite"])
         nites_o.append(o.mg_stats()[0])
     assert nites_g == nites_o
-    for s in helpers.PROG + ["p"]:
-        got = m.state.get(s).view("i").cpu().numpy()
-        assert helpers.relerr(got, o.field(s)) < 1e-9, s
+    names = helpers.PROG + ["p"]
+    errs = helpers.parity_errors(lambda s: m.state.get(s).view("i").cpu().numpy(), o.field, names)
+    for s in names:
+        assert errs[s] < 1e-9, (s, errs[s])
 
 
 def test_mixed_precision_error_small():
