@@ -195,10 +195,10 @@ def mg_levels(n):
     return levels
 
 
-# FP64 operations (DADD + DMUL + DFMA instructions, thread level) per cell of one
-# k_rhs_march<double, true, true> launch, counted by ncu on a 128^3 case
-# (profiles/k_rhs_march_fp64_128.md); None until measured.
-RHS_FP64_OPS_PER_CELL = None
+# FP64 flops (DADD + DMUL + 2 x DFMA thread instructions) per array cell of one
+# k_rhs_march<double, 1, 1> launch, counted by ncu on the 128^3 case of this workload
+# (profiles/k_rhs_march_fp64_rayleigh_taylor_128.md: 237 + 251 + 2 x 252).
+RHS_FP64_OPS_PER_CELL = 992
 
 
 def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
