@@ -167,6 +167,24 @@ int nyles_model_profile_read(NylesModel* m, double* ms, long long* count, int np
 /* number of kernels this library has launched in the process */
 long long nyles_launch_count(void);
 
+/* ---------------------------------------------------------------- allocation-free CFL reduction
+ * No counterpart in the reference. Same result as nyles_model_max_U2 (the maximum over
+ * n cells of U^2+V^2+W^2, core/nyles.py:241-251), written to *out, a device double,
+ * without a model, a workspace or any allocation. It is meant for callers that cannot
+ * allocate device memory: a host framework that owns every device allocation through a
+ * pre-sized pool, a time loop that must not allocate between steps, a caller reaching
+ * this library through a plain C or ctypes binding with no allocator of its own.
+ * The reduction's block partials live in a static device array of NYLES_STATIC_PARTIALS
+ * doubles (8 KiB, held by every GPU that loads the library until the process exits).
+ * n is limited to NYLES_STATIC_MAX_CELLS; larger n returns NYLES_BAD_ARG.
+ * The first call on a device looks up the array's device address (once per device, with
+ * that device current): make that first call before any stream capture. Calls share the
+ * array, so calls that overlap on the GPU (different streams or threads) race. */
+#define NYLES_STATIC_PARTIALS 1024
+#define NYLES_STATIC_MAX_CELLS (1LL << 28)
+int nyles_max_U2_static_f64(const double* U, const double* V, const double* W, long long n, double* out,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -95,6 +95,7 @@ SIGNATURES = {
     "nyles_model_profile": (_I, [_P, _I]),
     "nyles_model_profile_read": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _I]),
     "nyles_launch_count": (ctypes.c_longlong, []),
+    "nyles_max_U2_static_f64": (_I, [_P, _P, _P, ctypes.c_longlong, _P, _P]),
 }
 
 NPHASE = 12

@@ -9,6 +9,8 @@
 // tracer halos keep evolving with their own right-hand side as they do in the
 // reference (core/model_les.py:98-127 never fills tracers).
 #include "nyles_internal.h"
+#include <mutex>
+#include <string>
 
 namespace nyles {
 
@@ -770,4 +772,52 @@ template int launch_correct<double, double>(const NylesDesc*, const Geom&, const
 template int launch_correct<float, double>(const NylesDesc*, const Geom&, const StencilPtrs<float>&, const double*,
                                            double, cudaStream_t);
 
+// ---------------------------------------------------------------- allocation-free CFL reduction
+// The reduction's block partials live in this file-scope array instead of a caller
+// workspace. Every GPU that loads the library holds it (8 KiB) until the process exits.
+static __device__ __align__(256) double g_static_partials[NYLES_STATIC_PARTIALS];
+
+// Device address of g_static_partials, looked up once per device with that device
+// current. In host code the array's name is only a host-side stand-in; handing it to a
+// kernel would make the kernel touch the wrong memory, so only this address is used.
+static double* static_partials_for_current_device(int* status) {
+    static std::mutex mtx;
+    static double* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { *status = cuda_status(e, "cudaGetDevice"); return nullptr; }
+    if (dev < 0 || dev >= 64) { set_error("device ordinal above 63"); *status = NYLES_UNSUPPORTED; return nullptr; }
+    std::lock_guard<std::mutex> lock(mtx);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_partials);
+        if (e != cudaSuccess) { *status = cuda_status(e, "cudaGetSymbolAddress(g_static_partials)"); return nullptr; }
+        addr[dev] = static_cast<double*>(p);
+    }
+    *status = NYLES_OK;
+    return addr[dev];
+}
+
 }  // namespace nyles
+
+extern "C" int nyles_max_U2_static_f64(const double* U, const double* V, const double* W, long long n,
+                                       double* out, void* stream) {
+    using namespace nyles;
+    if (!U || !V || !W || !out || n <= 0) { set_error("max_U2_static: null array or empty size"); return NYLES_BAD_ARG; }
+    if (n > NYLES_STATIC_MAX_CELLS) {
+        set_error("max_U2_static: " + std::to_string(n) + " cells exceed the maximum of " +
+                  std::to_string((long long)NYLES_STATIC_MAX_CELLS) + " for the static scratch");
+        return NYLES_BAD_ARG;
+    }
+    int status = NYLES_OK;
+    double* partial = static_partials_for_current_device(&status);
+    if (!partial) return status;
+    // one block per 2^18 cells (at least one), at most NYLES_STATIC_PARTIALS blocks
+    long long blocks = (n + (1LL << 18) - 1) >> 18;
+    if (blocks > NYLES_STATIC_PARTIALS) blocks = NYLES_STATIC_PARTIALS;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_max_U2<double><<<(unsigned)blocks, 256, 0, st>>>(n, U, V, W, partial);
+    k_max_final<<<1, 1024, 0, st>>>(partial, (int)blocks, out);
+    note_launch(2);
+    return cuda_status(cudaGetLastError(), "max_U2_static kernel");
+}
