@@ -153,6 +153,16 @@ int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats);
 /* a fresh LFAM3 start (its first step is Euler forward, core/timescheme.py:129-140) */
 int nyles_model_reset_scheme(NylesModel* m);
 
+/* CUDA-graph replay of nsteps time steps of LES.forward with a fixed dt (no counterpart
+ * in the reference, whose step is a Python loop). The multigrid stop test runs on the
+ * device (a conditional while-node per pressure solve), so one launch advances nsteps
+ * steps with no host synchronisation; results equal nyles_model_forward's. LFAM3 must
+ * have taken its first (Euler) step before capture. nyles_model_mg_stats reads the
+ * device-side statistics after launches. */
+int nyles_model_capture(NylesModel* m, double dt, int nsteps);
+int nyles_model_graph_launch(NylesModel* m, void* stream);
+int nyles_model_graph_release(NylesModel* m);
+
 /* ---------------------------------------------------------------- instrumentation
  * No counterpart in the reference (its timing is core/timing.py's wall-clock decorator).
  * Phases: 0 right-hand side, 1 time-scheme update, 2 halo fill, 3 divergence,

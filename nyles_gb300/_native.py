@@ -92,6 +92,9 @@ SIGNATURES = {
     "nyles_model_max_U2": (_I, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_mg_stats": (_I, [_P, ctypes.POINTER(NylesMgStats)]),
     "nyles_model_reset_scheme": (_I, [_P]),
+    "nyles_model_capture": (_I, [_P, _D, _I]),
+    "nyles_model_graph_launch": (_I, [_P, _P]),
+    "nyles_model_graph_release": (_I, [_P]),
     "nyles_model_profile": (_I, [_P, _I]),
     "nyles_model_profile_read": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _I]),
     "nyles_launch_count": (ctypes.c_longlong, []),

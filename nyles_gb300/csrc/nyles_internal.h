@@ -117,4 +117,23 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision);
 int mg_solve(MgImpl* mg, cudaStream_t st);
 void* mg_level_ptr(MgImpl* mg, int lev, int var);
 
+// Incremental construction of a CUDA graph from captured segments. Between segments
+// the caller may add nodes by hand (conditional loops); `deps` is the frontier the next
+// segment depends on.
+struct GraphBuilder {
+    cudaGraph_t graph = nullptr;
+    cudaStream_t st = nullptr;
+    std::vector<cudaGraphNode_t> deps;
+    int error = 0;
+    long long body_kernels = 0; // kernel launches captured in the last multigrid loop body
+    void begin_segment();
+    void end_segment();
+};
+
+// multigrid solve recorded into a graph: stop test on the device, V-cycles in a
+// conditional while-node (solvers.f90:8-33)
+int mg_solve_graph(MgImpl* mg, GraphBuilder& gb);
+// device-side statistics of graph-mode solves: last nite, last res, total V-cycles
+int mg_read_device_stats(MgImpl* mg, cudaStream_t st, int* nite, double* res, long long* vcycles);
+
 }  // namespace nyles

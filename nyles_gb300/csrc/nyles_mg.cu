@@ -300,6 +300,36 @@ __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __
     }
 }
 
+// ---------------------------------------------------------------- device-side stop test
+// Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
+// [3] nite of the current solve, [4] V-cycles since creation.
+enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4 };
+
+// before the loop: res = sum(r^2)/sum(b^2) (0 when b = 0), continue while res >= tol
+__global__ void k_mg_ctl_begin(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol) {
+    const double normb = sc[SC_NORMB];
+    const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
+    sc[SC_RES] = res;
+    sc[SC_NITE] = 0.0;
+    cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
+}
+
+// after each V-cycle: nite += 1; stop at maxite (res keeps its previous value, as
+// solvers.f90:24-26 leaves the loop before recomputing it), else recompute res
+__global__ void k_mg_ctl_step(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol, int maxite) {
+    const double nite = sc[SC_NITE] + 1.0;
+    sc[SC_NITE] = nite;
+    sc[SC_TOTAL] = sc[SC_TOTAL] + 1.0;
+    if (nite >= (double)maxite) {
+        cudaGraphSetConditional(h, 0u);
+        return;
+    }
+    const double normb = sc[SC_NORMB];
+    const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
+    sc[SC_RES] = res;
+    cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
+}
+
 // ---------------------------------------------------------------- host side
 static inline dim3 grid_zc(const int n[3], int zc) {
     return dim3((n[2] + MG_BX - 1) / MG_BX, (n[1] + MG_BY - 1) / MG_BY, (n[0] + zc - 1) / zc);
@@ -440,33 +470,40 @@ static int read_scalar(MgImpl* mg, double* host_out, cudaStream_t st) {
     return cuda_status(e, "multigrid norm");
 }
 
+static double* scalars(MgImpl* mg) { return reinterpret_cast<double*>(mg->ws + mg->off_scalars); }
+
+// enqueue sum(v^2) (MODE 0) or sum(r^2) (MODE 1) of level 1 into *out
+template <typename T, int MODE>
+static void enqueue_sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* out, cudaStream_t st) {
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
+    ProfScope ps(mg->prof, 11, st);
+    note_launch(2);
+    k_mg_sumsq<T, MODE><<<grd, kBlk, 0, st>>>(g, v, b, part);
+    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
+}
+
+// mixed precision: enqueue the FP64 residual (also the next correction's rhs) into *out
+static void enqueue_resid64(MgImpl* mg, double* out, cudaStream_t st) {
+    MgGeom g = mgg(mg, 0);
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
+    ProfScope ps(mg->prof, 11, st);
+    note_launch(2);
+    k_mg_resid64<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
+                                       reinterpret_cast<const double*>(mg->ws + mg->off_b64),
+                                       lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
+    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
+}
+
 template <typename T, int MODE>
 static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* host_out, cudaStream_t st) {
-    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
-    double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
-    const dim3 grd = grid_zc(g.n, MG_ZC);
-    {
-        ProfScope ps(mg->prof, 11, st);
-        note_launch(2);
-        k_mg_sumsq<T, MODE><<<grd, kBlk, 0, st>>>(g, v, b, part);
-        k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
-    }
+    enqueue_sumsq<T, MODE>(mg, g, v, b, scalars(mg), st);
     return read_scalar(mg, host_out, st);
 }
 
 static int resid64(MgImpl* mg, double* host_out, cudaStream_t st) {
-    MgGeom g = mgg(mg, 0);
-    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
-    double* out = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
-    const dim3 grd = grid_zc(g.n, MG_ZC);
-    {
-        ProfScope ps(mg->prof, 11, st);
-        note_launch(2);
-        k_mg_resid64<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
-                                           reinterpret_cast<const double*>(mg->ws + mg->off_b64),
-                                           lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
-        k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
-    }
+    enqueue_resid64(mg, scalars(mg), st);
     return read_scalar(mg, host_out, st);
 }
 
@@ -523,6 +560,94 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
     mg->stats.vcycles += nite;
     if (res >= mg->tol && nite >= mg->maxite) mg->stats.not_converged += 1;
     return cuda_status(cudaGetLastError(), "multigrid solve");
+}
+
+// ---------------------------------------------------------------- graph mode
+void GraphBuilder::begin_segment() {
+    if (error) return;
+    cudaError_t e = cudaStreamBeginCaptureToGraph(st, graph, deps.empty() ? nullptr : deps.data(), nullptr,
+                                                  deps.size(), cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) error = cuda_status(e, "cudaStreamBeginCaptureToGraph");
+}
+
+void GraphBuilder::end_segment() {
+    if (error) return;
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t* d = nullptr;
+    size_t n = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &status, nullptr, nullptr, &d, nullptr, &n);
+    if (e == cudaSuccess) {
+        std::vector<cudaGraphNode_t> frontier(d, d + n);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(st, &g);
+        if (e == cudaSuccess) deps.swap(frontier);
+    }
+    if (e != cudaSuccess) error = cuda_status(e, "graph segment capture");
+}
+
+// The same solve as mg_solve with the stop test on the device: norms and the first
+// residual, then a while-node whose body is one V-cycle, the residual norm and the
+// control kernel. Called with a segment of gb open; leaves a new segment open.
+int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
+    if (!mg->ws) { set_error("multigrid: workspace not bound"); return NYLES_BAD_ARG; }
+    cudaStream_t st = gb.st;
+    MgGeom g0 = mgg(mg, 0);
+    double* sc = scalars(mg);
+    const bool mixed = mg->precision == NYLES_MIXED;
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, gb.graph, 0, 0);
+    if (e != cudaSuccess) return gb.error = cuda_status(e, "cudaGraphConditionalHandleCreate");
+    if (!mixed) {
+        enqueue_sumsq<double, 0>(mg, g0, lvp<double>(mg, 0, 2), (const double*)nullptr, sc + SC_NORMB, st);
+        enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
+    } else {
+        enqueue_sumsq<double, 0>(mg, g0, reinterpret_cast<const double*>(mg->ws + mg->off_b64),
+                                 (const double*)nullptr, sc + SC_NORMB, st);
+        enqueue_resid64(mg, sc + SC_RR, st);
+    }
+    k_mg_ctl_begin<<<1, 1, 0, st>>>(sc, h, mg->tol);
+    note_launch();
+    gb.end_segment();
+    if (gb.error) return gb.error;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, gb.graph, gb.deps.empty() ? nullptr : gb.deps.data(), nullptr, gb.deps.size(), &p);
+    if (e != cudaSuccess) return gb.error = cuda_status(e, "cudaGraphAddNode(while)");
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return gb.error = cuda_status(e, "capture of the multigrid loop body");
+    const long long l0 = nyles_launch_count();
+    if (!mixed) {
+        vcycle<double>(mg, st, false);
+        enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
+    } else {
+        vcycle<float>(mg, st, true);
+        enqueue_resid64(mg, sc + SC_RR, st);
+    }
+    k_mg_ctl_step<<<1, 1, 0, st>>>(sc, h, mg->tol, mg->maxite);
+    note_launch();
+    gb.body_kernels = nyles_launch_count() - l0;
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(st, &g);
+    if (e != cudaSuccess) return gb.error = cuda_status(e, "end of the multigrid loop body");
+    gb.deps.assign(1, node);
+    gb.begin_segment();
+    return gb.error;
+}
+
+int mg_read_device_stats(MgImpl* mg, cudaStream_t st, int* nite, double* res, long long* vcycles) {
+    double h[5];
+    cudaError_t e = cudaMemcpyAsync(h, scalars(mg), sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e, "multigrid statistics read-back");
+    *nite = (int)h[SC_NITE];
+    *res = h[SC_RES];
+    *vcycles = (long long)h[SC_TOTAL];
+    return NYLES_OK;
 }
 
 }  // namespace nyles

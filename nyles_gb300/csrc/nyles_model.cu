@@ -126,7 +126,29 @@ struct NylesModel {
     MgImpl mg;
     Prof prof;
     bool bound = false;
-    ~NylesModel() { prof.release(); }
+    // graph mode: one or more captured time steps replayed with one launch
+    GraphBuilder* gb = nullptr;          // set while capturing
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    long long graph_kernels = 0;         // kernels outside the multigrid loops per launch
+    long long graph_body_kernels = 0;    // kernels per V-cycle iteration of a loop
+    int graph_solves = 0;                // pressure solves per launch
+    long long graph_launches = 0;
+    long long vcycles_counted = 0;       // device V-cycles already added to the launch count
+    bool last_solve_graph = false;       // the latest solve ran inside a graph
+    cudaStream_t last_stream = nullptr;  // stream of the latest graph launch
+    void release_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        gexec = nullptr;
+        graph = nullptr;
+    }
+    ~NylesModel() {
+        prof.release();
+        release_graph();
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+    }
 };
 
 extern "C" {
@@ -329,6 +351,24 @@ int nyles_model_reset_scheme(NylesModel* m) {
 int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
     if (!m || !stats) { set_error("null argument"); return NYLES_BAD_ARG; }
     *stats = m->mg.stats;
+    if (m->graph_launches > 0) {   // solves run inside graphs keep their statistics on the device
+        NylesModel* mm = const_cast<NylesModel*>(m);
+        int nite = 0;
+        double res = 0.0;
+        long long vc = 0;
+        int rc = mg_read_device_stats(&mm->mg, mm->last_stream, &nite, &res, &vc);
+        if (rc) return rc;
+        if (vc > mm->vcycles_counted) {
+            note_launch((int)((vc - mm->vcycles_counted) * mm->graph_body_kernels));
+            mm->vcycles_counted = vc;
+        }
+        if (m->last_solve_graph) {
+            stats->nite = nite;
+            stats->res = res;
+        }
+        stats->vcycles += vc;
+        stats->solves += m->graph_launches * m->graph_solves;
+    }
     return NYLES_OK;
 }
 
@@ -364,7 +404,13 @@ static int model_diagnose(NylesModel* m, cudaStream_t st) {
     {
         ProfScope ps(&m->prof, 4, st);
         m->mg.prof = m->prof.on ? &m->prof : nullptr;
-        if ((rc = mg_solve(&m->mg, st))) return rc;
+        if (m->gb) {
+            if ((rc = mg_solve_graph(&m->mg, *m->gb))) return rc;
+            ++m->graph_solves;
+        } else {
+            if ((rc = mg_solve(&m->mg, st))) return rc;
+            m->last_solve_graph = false;
+        }
     }
     {
         ProfScope ps(&m->prof, 5, st);
@@ -486,5 +532,64 @@ int nyles_model_profile_read(NylesModel* m, double* ms, long long* count, int np
 }
 
 long long nyles_launch_count(void) { return g_launches.load(); }
+
+int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
+    if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
+    if (m->scheme == NYLES_SCHEME_LFAM3 && m->lf_first) {
+        set_error("LFAM3: run the first (Euler) step before capturing the steady step");
+        return NYLES_BAD_ARG;
+    }
+    cudaError_t e;
+    if (!m->cap_stream) {
+        e = cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_status(e, "capture stream");
+    }
+    m->release_graph();
+    e = cudaGraphCreate(&m->graph, 0);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphCreate");
+    GraphBuilder gb;
+    gb.graph = m->graph;
+    gb.st = m->cap_stream;
+    const bool prof_on = m->prof.on;
+    m->prof.on = false;   // event records are not allowed inside loop bodies
+    m->gb = &gb;
+    m->graph_solves = 0;
+    const long long l0 = g_launches.load();
+    gb.begin_segment();
+    int rc = NYLES_OK;
+    for (int s = 0; s < nsteps && !rc && !gb.error; ++s)
+        rc = m->precision == NYLES_FP64 ? model_forward<double>(m, 0.0, dt, gb.st)
+                                        : model_forward<float>(m, 0.0, dt, gb.st);
+    gb.end_segment();
+    m->gb = nullptr;
+    m->prof.on = prof_on;
+    const long long captured = g_launches.load() - l0;
+    g_launches.fetch_sub(captured);   // nothing ran yet: launches are counted at replay
+    if (!rc) rc = gb.error;
+    if (rc) { m->release_graph(); return rc; }
+    m->graph_body_kernels = gb.body_kernels;
+    m->graph_kernels = captured - (long long)m->graph_solves * gb.body_kernels;
+    e = cudaGraphInstantiate(&m->gexec, m->graph, 0);
+    if (e != cudaSuccess) { m->release_graph(); return cuda_status(e, "cudaGraphInstantiate"); }
+    return NYLES_OK;
+}
+
+int nyles_model_graph_launch(NylesModel* m, void* stream) {
+    if (!m || !m->gexec) { set_error("no captured graph"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaGraphLaunch(m->gexec, st);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphLaunch");
+    note_launch((int)m->graph_kernels);
+    m->graph_launches += 1;
+    m->last_solve_graph = true;
+    m->last_stream = st;
+    return NYLES_OK;
+}
+
+int nyles_model_graph_release(NylesModel* m) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    m->release_graph();
+    return NYLES_OK;
+}
 
 }  // extern "C"

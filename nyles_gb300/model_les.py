@@ -139,6 +139,20 @@ class LES(object):
         nat.check(self.lib.nyles_model_forward(self._h, float(t), float(dt), nat.stream_ptr()))
         return False
 
+    def capture_graph(self, dt, nsteps=1):
+        """Record `nsteps` time steps with fixed `dt` into one CUDA graph (the multigrid
+        stop test runs on the device). LFAM3 must have taken its first step."""
+        nat.check(self.lib.nyles_model_capture(self._h, float(dt), int(nsteps)))
+        self.graph = (float(dt), int(nsteps))
+
+    def replay(self, stream=None):
+        """Launch the captured graph: advances the state by its `nsteps` steps."""
+        nat.check(self.lib.nyles_model_graph_launch(self._h, nat.stream_ptr(stream)))
+
+    def release_graph(self):
+        nat.check(self.lib.nyles_model_graph_release(self._h))
+        self.graph = None
+
     def max_U2(self):
         """max of U^2+V^2+W^2 over the arrays; raises BlowUp on a non-finite value."""
         out = ctypes.c_double()
