@@ -38,6 +38,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=2, help="extra steps timed per phase with CUDA events")
+    ap.add_argument("--serving-requests", type=int, default=96, help="0 skips the serving ensemble")
+    ap.add_argument("--serving-steps", type=int, default=30, help="time steps of each ensemble run")
+    ap.add_argument("--serving-rate", type=float, default=20.0, help="Poisson arrivals per second")
+    ap.add_argument("--no-serving-baseline", action="store_true")
     return ap.parse_args()
 
 
@@ -311,6 +315,34 @@ def time_e2e(nyl, K, W):
     return (time.perf_counter() - t0) * 1e3, bytes_in
 
 
+def time_serving(a):
+    """Serving ensemble: seeded Poisson stream of lock-exchange and Taylor-Green runs on
+    n^3 grids, n in {32, 48, 64, 96, 128}, mixed precision, admitted against a 120 GB
+    budget and advanced by graph replays; baseline = the same runs one at a time with
+    eager FP64 stepping (queue-simulated latency)."""
+    import torch
+    from nyles_gb300 import serving as S
+    warm = [S.Request(i, c, n, i, 4, 0.0) for i, (c, n) in enumerate((("lock", 32), ("tgv", 32)))]
+    S.ServingEngine(precision="mixed").serve(warm, realtime=False)
+    reqs = S.make_requests(a.serving_requests, a.serving_rate, seed=5, steps=a.serving_steps)
+    eng = S.ServingEngine(hbm_budget_bytes=120e9, precision="mixed")
+    from nyles_gb300 import _native
+    l0 = _native.lib().nyles_launch_count()
+    torch.cuda.synchronize()
+    res, _ = eng.serve(reqs, realtime=True)
+    launches = _native.lib().nyles_launch_count() - l0
+    out = {"requests": len(reqs), "steps_per_run": a.serving_steps, "rate_per_s": a.serving_rate,
+           "stream_seed": 5, "sizes": [32, 48, 64, 96, 128], "precision": "mixed", "mg_tol_sq_ratio": 1e-6,
+           "hbm_budget_gb": 120, "max_resident_runs": eng.max_active, "peak_footprint_gb": eng.peak_used / 1e9,
+           "kernel_launches": launches}
+    out.update(S.summarize(res))
+    if not a.no_serving_baseline:
+        seq, _ = S.run_sequential(reqs, precision="fp64")
+        out["sequential_fp64"] = S.summarize(seq)
+    torch.cuda.empty_cache()
+    return out
+
+
 def cpu_baseline(nsample=64, steps=2):
     """The CPU oracle (single-threaded C++ restatement of the reference's numerics)
     on the same workload at a reduced grid, timed on one host core."""
@@ -453,6 +485,9 @@ def main():
             out["mixed"]["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in mph.items()}
             mdom = max((k for k in mph if k != "mg_solve"), key=lambda k: mph[k]["ms"])
             out["mixed"]["roofline"] = roofline(mdom, mph, n, 4, peak, peak_kind, None)
+    if a.serving_requests > 0:
+        out["serving"] = time_serving(a)
+        out["gpu_launches"] += out["serving"]["kernel_launches"]
     if rank == 0 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(64 if n >= 64 else n, 2)
     if dist:

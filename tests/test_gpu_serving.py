@@ -1,0 +1,60 @@
+"""Continuous batching on the GPU: every run's result is the same alone and in the mix.
+
+A handful of requests of different cases and sizes are served together (admitted
+while others are in flight, advanced by overlapping graph replays on their own
+streams); each is then run alone with eager stepping. The final fields must be
+identical: runs share no data, reductions are deterministic, and graph replay equals
+eager stepping bit for bit.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def test_results_identical_alone_and_in_the_mix():
+    from nyles_gb300 import serving as S
+    from nyles_gb300.nyles import Nyles
+    reqs = [S.Request(0, "lock", 32, 11, 20, 0.0), S.Request(1, "tgv", 16, 12, 20, 0.0),
+            S.Request(2, "tgv", 48, 13, 10, 0.0), S.Request(3, "lock", 16, 14, 30, 0.0),
+            S.Request(4, "lock", 32, 15, 20, 0.0)]
+    eng = S.ServingEngine(precision="mixed")
+    results, mixed_states = eng.serve(reqs, realtime=False, keep_states=True)
+    assert eng.max_active == len(reqs)
+    for req in reqs:
+        nyl = Nyles(S.build_params(req.case, req.n, "mixed"))
+        S.initial_state(nyl, req.case, req.seed)
+        m = nyl.model
+        m.diagnose_var(m.state)
+        for _ in range(req.steps):
+            m.forward(0.0, S.CASES[req.case]["dt"])
+        for s, arr in mixed_states[req.rid].items():
+            np.testing.assert_array_equal(m.state.get(s).view("i").double().cpu().numpy(), arr,
+                                          err_msg="run %d field %s" % (req.rid, s))
+
+
+def test_realtime_stream_latencies():
+    from nyles_gb300 import serving as S
+    reqs = S.make_requests(12, 40.0, seed=3, steps=10, sizes=(16, 32))
+    eng = S.ServingEngine(precision="mixed")
+    results, _ = eng.serve(reqs, realtime=True)
+    assert len(results) == 12
+    assert all(r.done >= r.admitted >= r.arrival - 1e-6 for r in results)
+    s = S.summarize(results)
+    assert 0 < s["p50_s"] <= s["p99_s"]
+
+
+@pytest.mark.parametrize("case,n,precision", [("lock", 32, "mixed"), ("tgv", 48, "mixed"), ("lock", 32, "fp64")])
+def test_footprint_model_covers_the_allocation(case, n, precision):
+    import gc
+    from nyles_gb300 import serving as S
+    gc.collect()
+    torch.cuda.synchronize()
+    before = torch.cuda.memory_allocated()
+    run = S.Run(S.Request(0, case, n, 1, 10, 0.0), precision, torch.device("cuda", 0), 1e-6)
+    torch.cuda.synchronize()
+    used = torch.cuda.memory_allocated() - before
+    need = S.footprint_bytes(case, n, precision)
+    assert used <= need <= 1.5 * used, (used, need)
+    del run
