@@ -7,9 +7,19 @@ at rest; RK3-SSP with dt = 1e-3; multigrid to sum(r^2)/sum(b^2) < 1e-20 (relativ
 residual 1e-10). A step = one full RK3 step (3 right-hand sides, 3 projections).
 `value` is the FP64 path with the state resident on the device; `mixed` reports the
 mixed-precision path (FP32 state and stencils, FP32 V-cycles in FP64 refinement) on
-the same workload with its error against FP64. `e2e` runs the same steps through the
-public API with the prognostic state copied in from pinned host memory and copied
-back every step.
+the same workload, and its error against the FP64 path after 100 steps from the same
+state (`mixed.accuracy`). `e2e` runs the same steps through the public API with the
+prognostic state copied in from pinned host memory and copied back every step.
+`step_roofline` = algorithmic bytes per cell-step (RK3 stencil part plus three
+multigrid solves at the measured V-cycle count) x cell-steps/s against the measured HBM
+copy bandwidth; `roofline` = the dominant kernel alone.
+
+`serving`: an ensemble of 96 lock-exchange and Taylor-Green runs on n^3 grids,
+n in {32, 48, 64, 96, 128}, arriving as a seeded Poisson stream at 20 per second,
+mixed precision, served by continuous batching under a 120 GB HBM budget; p50/p99
+completion latency and aggregate cell-steps/s, against the same runs one at a time
+with the eager FP64 path. Each run lasts --serving-steps steps (30 by default, so that
+the default bench stays within a few minutes).
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--n 256]
 """
@@ -42,6 +52,8 @@ def parse():
     ap.add_argument("--serving-steps", type=int, default=30, help="time steps of each ensemble run")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="Poisson arrivals per second")
     ap.add_argument("--no-serving-baseline", action="store_true")
+    ap.add_argument("--accuracy-steps", type=int, default=100,
+                    help="steps of the mixed-vs-FP64 error check (0 skips it)")
     return ap.parse_args()
 
 
@@ -343,15 +355,14 @@ def time_serving(a):
     return out
 
 
-def cpu_baseline(nsample=64, steps=2):
-    """The CPU oracle (single-threaded C++ restatement of the reference's numerics)
-    on the same workload at a reduced grid, timed on one host core."""
+def oracle_rt(n):
+    """The CPU oracle (single-threaded C++ restatement of the reference's numerics) set
+    up with the Rayleigh-Taylor workload at n^3 and projected once."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
     import numpy as np
     from nyles_gb300 import grid as grid_module
     from nyles_gb300 import topology as topo
-    n = nsample
     prm = dict(nx=n, ny=n, nz=n, nh=3, npx=1, npy=1, npz=1, Lx=1.0, Ly=1.0, Lz=1.0, loc=[0, 0, 0],
                neighbours=topo.get_neighbours([0, 0, 0], [1, 1, 1], "perio_xy"))
     g = grid_module.Grid(prm)
@@ -362,44 +373,98 @@ def cpu_baseline(nsample=64, steps=2):
     zb = g.z_b_1D[:, None, None]
     o.field("b")[...] = np.where(zb > 0.5 + eta[None, :, :], 0.5, -0.5)
     o.diagnose()
+    return o
+
+
+def cpu_baseline(nsample=128, steps=3):
+    """The oracle on one host core: `steps` RK3 steps of the workload at nsample^3."""
+    o = oracle_rt(nsample)
     t0 = time.perf_counter()
     for _ in range(steps):
         o.forward(0.0, 1e-3)
     el = time.perf_counter() - t0
-    return {"value": n ** 3 * steps / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
+    return {"value": nsample ** 3 * steps / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
             "sample": "oracle (C++ restatement of the reference numerics, 1 thread) on the same Rayleigh-Taylor "
-                      "setup at %d^3, %d RK3 steps, %.1f s" % (n, steps, el)}
+                      "setup at %d^3, %d RK3 steps, %.1f s" % (nsample, steps, el)}
 
 
 # ------------------------------------------------------------------ reference arm
 def _ref_worker(args):
-    n, steps = args
-    r = cpu_baseline(n, steps)
-    return r["value"]
+    n, warmup, steps = args
+    o = oracle_rt(n)
+    for _ in range(warmup):
+        o.forward(0.0, 1e-3)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.forward(0.0, 1e-3)
+    return n ** 3 * steps, time.perf_counter() - t0
 
 
 def run_reference(a, rank, world):
+    """The reference's numerics on the host cores: one single-threaded oracle per core
+    (the reference runs one thread per subdomain), each on the workload at 64^3, W
+    untimed and K timed RK3 steps; value = all cells x K / the slowest worker's time."""
     if rank != 0:
         return
     import multiprocessing as mp
     ncores = os.cpu_count() or 1
-    n = 48 if a.n >= 48 else a.n
+    n = 64 if a.n >= 64 else a.n
     ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
     with ctx.Pool(ncores) as pool:
-        vals = pool.map(_ref_worker, [(n, max(1, a.steps // 2))] * ncores)
-    el = time.perf_counter() - t0
-    value = float(sum(vals))
+        res = pool.map(_ref_worker, [(n, a.warmup, a.steps)] * ncores)
+    el = max(r[1] for r in res)
+    value = float(sum(r[0] for r in res) / el)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": el * 1e3 / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "rayleigh_taylor_perio_xy_rk3 (reference CPU numerics)", "grid": [n, n, n]},
+            "config": make_config(a.n, world),
             "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": ncores, "kind": "port",
-                             "sample": "%d independent single-thread oracle runs (one per host core) of the "
-                                       "Rayleigh-Taylor setup at %d^3, wall %.1f s; the reference itself has no "
-                                       "Fortran compiler here" % (ncores, n, el)},
+                             "sample": "%d concurrent single-thread oracle runs (one per host core) of the same "
+                                       "Rayleigh-Taylor setup at %d^3, %d timed RK3 steps each, %.1f s; the "
+                                       "reference's Fortran path cannot be built here" % (ncores, n, a.steps, el)},
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def make_config(n, world):
+    return {"workload": "rayleigh_taylor_%d^3_perio_xy_rk3" % n, "grid": [n, n, n], "box": [1, 1, 1],
+            "dt": 1e-3, "mg_tol_sq_ratio": 1e-20, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (state >> 129 MB)"}
+
+
+def accuracy(n, steps):
+    """Mixed path against the FP64 path after `steps` RK3 steps from the same state:
+    max|mixed - fp64| / max|fp64| for b and p, and over the three components for u."""
+    import numpy as np
+    import torch
+    fields = ("b", "p", "u_i", "u_j", "u_k")
+    out = {}
+    for prec in ("fp64", "mixed"):
+        nyl = build_model(n, prec)
+        m = nyl.model
+        m.diagnose_var(m.state)
+        for _ in range(steps):
+            m.forward(0.0, nyl.dt0)
+        torch.cuda.synchronize()
+        out[prec] = {s: m.state.get(s).view("i").double().cpu().numpy() for s in fields}
+        del nyl, m
+        torch.cuda.empty_cache()
+    a, b = out["mixed"], out["fp64"]
+    err = {s: float(np.abs(a[s] - b[s]).max() / max(np.abs(b[s]).max(), 1e-300)) for s in ("b", "p")}
+    us = max(np.abs(b[c]).max() for c in ("u_i", "u_j", "u_k"))
+    err["u"] = float(max(np.abs(a[c] - b[c]).max() for c in ("u_i", "u_j", "u_k")) / max(us, 1e-300))
+    return {"steps": steps, "rel_err_vs_fp64": err}
+
+
+def step_bytes(prec, nv, n_vcycles, refine=True):
+    """Algorithmic bytes per cell-step: RK3 stencil part w(11 nv + 6) plus 3 solves of
+    w_mg (4 + 24 n_V), and, in mixed precision, 40 B per cell and V-cycle of FP64
+    refinement (residual and correction)."""
+    w = 8 if prec == "fp64" else 4
+    q = w * (11 * nv + 6) + 3 * w * (4 + 24 * n_vcycles)
+    if prec != "fp64" and refine:
+        q += 3 * 40 * n_vcycles
+    return q
 
 
 # ------------------------------------------------------------------ main
@@ -424,9 +489,7 @@ def main():
     fp64_peak = fp64_peak_tflops() if a.precision in ("fp64", "both") else None
     out = {"metric": METRIC, "unit": "cell-steps/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic",
-           "config": {"workload": "rayleigh_taylor_%d^3_perio_xy_rk3" % n, "grid": [n, n, n], "box": [1, 1, 1],
-                      "dt": 1e-3, "mg_tol_sq_ratio": 1e-20, "parallelism": "replicas" if world > 1 else "single",
-                      "l2": "inputs larger than L2 (state >> 129 MB)"}}
+           "config": make_config(n, world)}
     results = {}
     precs = ["fp64", "mixed"] if a.precision == "both" else [a.precision]
     launches_total = 0
@@ -488,8 +551,16 @@ def main():
     if a.serving_requests > 0:
         out["serving"] = time_serving(a)
         out["gpu_launches"] += out["serving"]["kernel_launches"]
+    for prec, res in results.items():
+        q = step_bytes(prec, 4, res["mean_vcycles_per_solve"])
+        sr = {"bytes_per_cell_step": q, "achieved": q * res["value"] / world / 1e9, "peak": peak, "unit": "GB/s",
+              "peak_kind": peak_kind}
+        sr["frac"] = sr["achieved"] / peak
+        (out if prec == main_prec else out["mixed"])["step_roofline"] = sr
+    if a.accuracy_steps > 0 and len(results) == 2:
+        out["mixed"]["accuracy"] = accuracy(n, a.accuracy_steps)
     if rank == 0 and not a.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(64 if n >= 64 else n, 2)
+        out["cpu_baseline"] = cpu_baseline(128 if n >= 128 else n, 3)
     if dist:
         dist.barrier()
         dist.destroy_process_group()

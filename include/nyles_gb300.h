@@ -149,6 +149,11 @@ int nyles_model_diagnose(NylesModel* m, void* stream);
 int nyles_model_rhs(NylesModel* m, int reg, int last, void* stream);
 /* max over the arrays of U^2+V^2+W^2 (core/nyles.py:241-251), copied to *out */
 int nyles_model_max_U2(NylesModel* m, double* out, void* stream);
+/* VFwork.compute, core/online_diag.py:11-35: the u components of register set 0 are
+ * zeroed and receive the vortex force alone, the work field NYLES_F_WORK gets
+ * sum_d (U_d F_d / 2)(p) + (U_d F_d / 2)(p - e_d), and *worksum its sum (FP64) over the
+ * half-open box {z0, z1, y0, y1, x0, x1} of the arrays. Synchronises `stream`. */
+int nyles_model_vfwork(NylesModel* m, const long long* box, double* worksum, void* stream);
 int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats);
 /* a fresh LFAM3 start (its first step is Euler forward, core/timescheme.py:129-140) */
 int nyles_model_reset_scheme(NylesModel* m);

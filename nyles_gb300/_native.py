@@ -90,6 +90,7 @@ SIGNATURES = {
     "nyles_model_diagnose": (_I, [_P, _P]),
     "nyles_model_rhs": (_I, [_P, _I, _I, _P]),
     "nyles_model_max_U2": (_I, [_P, ctypes.POINTER(ctypes.c_double), _P]),
+    "nyles_model_vfwork": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_mg_stats": (_I, [_P, ctypes.POINTER(NylesMgStats)]),
     "nyles_model_reset_scheme": (_I, [_P]),
     "nyles_model_capture": (_I, [_P, _D, _I]),

@@ -89,6 +89,15 @@ template <typename T>
 int launch_max_U2(const Geom& g, const StencilPtrs<T>& s, double* partial, int npartial, double* out,
                   cudaStream_t st);
 
+// half-open index box of the (z, y, x) arrays summed by the vortex-force work diagnostic
+struct VfBox {
+    int lo[3], hi[3];
+};
+// work field of the vortex force held in ds.p[1..3] (u components), and its sum over box
+template <typename T>
+int launch_vfwork(const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, const VfBox& box, double* partial,
+                  int npartial, double* out, cudaStream_t st);
+
 // ------------------------------------------------------------------ multigrid
 struct MgLevelDesc {
     int n[3];         // interior extents z, y, x

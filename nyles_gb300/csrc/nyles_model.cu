@@ -512,6 +512,41 @@ int nyles_model_max_U2(NylesModel* m, double* out, void* stream) {
     return NYLES_OK;
 }
 
+extern "C++" {
+template <typename T>
+static int model_vfwork(NylesModel* m, const VfBox& box, double* out, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    ProgPtrs<T> ds = prog_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->regs[0]));
+    for (int c = 1; c <= 3; ++c) {
+        cudaError_t e = cudaMemsetAsync(ds.p[c], 0, (size_t)m->g.vol * sizeof(T), st);
+        if (e != cudaSuccess) return cuda_status(e, "vfwork register reset");
+    }
+    int rc = launch_rhs<T>(&m->d, m->g, s, ds, TERM_VF | TERM_ACCUMULATE, st);
+    if (rc) return rc;
+    double* part = reinterpret_cast<double*>(m->ws + m->off_partial);
+    double* dev = reinterpret_cast<double*>(m->ws + m->off_scalar);
+    return launch_vfwork<T>(m->g, s, ds, box, part, m->npartial, dev, st);
+}
+}  // extern "C++"
+
+int nyles_model_vfwork(NylesModel* m, const long long* box, double* worksum, void* stream) {
+    if (!m || !m->bound || !box || !worksum) { set_error("model not bound or null argument"); return NYLES_BAD_ARG; }
+    VfBox b;
+    for (int d = 0; d < 3; ++d) {
+        const long long lo = box[2 * d], hi = box[2 * d + 1];
+        if (lo < 0 || hi < lo || hi > m->g.N[d]) { set_error("vfwork: box outside the arrays"); return NYLES_BAD_ARG; }
+        b.lo[d] = (int)lo;
+        b.hi[d] = (int)hi;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    double* dev = reinterpret_cast<double*>(m->ws + m->off_scalar);
+    int rc = m->precision == NYLES_FP64 ? model_vfwork<double>(m, b, worksum, st) : model_vfwork<float>(m, b, worksum, st);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(worksum, dev, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e, "vfwork read-back");
+}
+
 int nyles_model_profile(NylesModel* m, int enable) {
     if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
     if (!enable) m->prof.flush();

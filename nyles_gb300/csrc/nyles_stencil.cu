@@ -733,6 +733,80 @@ int launch_max_U2(const Geom& g, const StencilPtrs<T>& s, double* partial, int n
     return cuda_status(cudaGetLastError(), "max_U2 kernel");
 }
 
+// ---------------------------------------------------------------- vortex-force work
+// core/online_diag.py:27-35: work(p) = sum over d = i, j, k (in that order) of
+// (U_d F_d / 2)(p) + (U_d F_d / 2)(p - e_d) where the index along d is >= 1; the products
+// and the sum of work over the box are taken in FP64 whatever the storage type. Each
+// block of a fixed grid strides over the array in a fixed order, so the partial sums,
+// and the total, are the same on every run.
+template <typename T>
+__global__ void __launch_bounds__(256) k_vfwork(Geom g, const T* __restrict__ U, const T* __restrict__ V,
+                                                const T* __restrict__ W, const T* __restrict__ FU,
+                                                const T* __restrict__ FV, const T* __restrict__ FW,
+                                                T* __restrict__ work, VfBox box, double* __restrict__ partial) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const int Nx = g.N[2], Ny = g.N[1];
+    double acc = 0.0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < g.vol; q += stride) {
+        const int i = (int)(q % Nx);
+        const long long r = q / Nx;
+        const int j = (int)(r % Ny);
+        const int k = (int)(r / Ny);
+        double w = 0.0;
+        if (i >= 1) {
+            const double a = __dmul_rn(__dmul_rn((double)U[q], (double)FU[q]), 0.5);
+            const double b = __dmul_rn(__dmul_rn((double)U[q - 1], (double)FU[q - 1]), 0.5);
+            w = __dadd_rn(w, __dadd_rn(a, b));
+        }
+        if (j >= 1) {
+            const double a = __dmul_rn(__dmul_rn((double)V[q], (double)FV[q]), 0.5);
+            const double b = __dmul_rn(__dmul_rn((double)V[q - g.sy], (double)FV[q - g.sy]), 0.5);
+            w = __dadd_rn(w, __dadd_rn(a, b));
+        }
+        if (k >= 1) {
+            const double a = __dmul_rn(__dmul_rn((double)W[q], (double)FW[q]), 0.5);
+            const double b = __dmul_rn(__dmul_rn((double)W[q - g.sz], (double)FW[q - g.sz]), 0.5);
+            w = __dadd_rn(w, __dadd_rn(a, b));
+        }
+        work[q] = (T)w;
+        if (k >= box.lo[0] && k < box.hi[0] && j >= box.lo[1] && j < box.hi[1] && i >= box.lo[2] && i < box.hi[2])
+            acc += w;
+    }
+    __shared__ double sm[8];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) partial[blockIdx.x] = v;
+    }
+}
+
+__global__ void k_sum_final(const double* __restrict__ partial, int n, double* out) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+    __shared__ double sm[32];
+    s = warp_sum(s);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x >> 5)) ? sm[threadIdx.x] : 0.0;
+        v = warp_sum(v);
+        if (threadIdx.x == 0) out[0] = v;
+    }
+}
+
+template <typename T>
+int launch_vfwork(const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, const VfBox& box, double* partial,
+                  int npartial, double* out, cudaStream_t st) {
+    k_vfwork<T><<<npartial, 256, 0, st>>>(g, s.f[NYLES_F_UC_I], s.f[NYLES_F_UC_J], s.f[NYLES_F_UC_K], ds.p[1],
+                                          ds.p[2], ds.p[3], s.f[NYLES_F_WORK], box, partial);
+    k_sum_final<<<1, 1024, 0, st>>>(partial, npartial, out);
+    note_launch(2);
+    return cuda_status(cudaGetLastError(), "vfwork kernel");
+}
+
 // ---------------------------------------------------------------- flux1d test entry
 template <typename T>
 __global__ void k_flux1d(const T* __restrict__ u, const T* __restrict__ q, T* __restrict__ flux, int nlines, int n) {
@@ -762,6 +836,8 @@ int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream
     template int launch_fill<T>(const Geom&, T* const*, int, cudaStream_t);                                    \
     template int launch_diag<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, int, cudaStream_t);      \
     template int launch_max_U2<T>(const Geom&, const StencilPtrs<T>&, double*, int, double*, cudaStream_t);   \
+    template int launch_vfwork<T>(const Geom&, const StencilPtrs<T>&, const ProgPtrs<T>&, const VfBox&, double*, \
+                                  int, double*, cudaStream_t);                                                 \
     template int launch_flux1d<T>(const T*, const T*, T*, int, int, cudaStream_t);
 NYLES_INST(double)
 NYLES_INST(float)

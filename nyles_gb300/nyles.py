@@ -14,6 +14,7 @@ import numpy as np
 
 from . import grid as grid_module
 from . import model_les
+from . import online_diag
 from . import topology as topo
 
 
@@ -59,6 +60,7 @@ class Nyles(object):
         self.dt_max = param["dt_max"]
         self.blowup_check = param.get("gpu", {}).get("blowup_check", True)
         self.gridcellpersubdom = param["nx"] * param["ny"] * param["nz"]
+        self.diag = online_diag.VFwork(self.model, self.grid)   # core/nyles.py:102
 
     def compute_dt(self):
         """cfl / max|U| bounded by dt_max, or the fixed dt (core/nyles.py:227-260)."""
@@ -72,10 +74,15 @@ class Nyles(object):
     def run(self, nsteps=None, verbose=True, callback=None):
         """Advance to tend (or `nsteps` steps). Returns (t, n, blowup).
 
-        `callback(nyles, t, n)` is called after every step (e.g. for snapshots).
+        `callback(nyles, t, n)` is called after every step (e.g. for snapshots). At
+        every history time (`timestep_history`) the vortex-force work is diagnosed and
+        (t, Kdiss) appended to `self.kdiss` (core/nyles.py:166-171).
         """
         from . import _native as nat
         t, n = 0.0, 0
+        dt_hist = float(self.param.get("timestep_history", 0.0))
+        t_next_hist = dt_hist
+        self.kdiss = []
         self.model.diagnose_var(self.model.state)
         realtime0 = time.time()
         blowup = False
@@ -88,6 +95,12 @@ class Nyles(object):
             self.model.forward(t, dt)
             t += dt
             n += 1
+            if t >= t_next_hist:
+                Kdiss = self.diag.compute()
+                self.kdiss.append((t, Kdiss))
+                if verbose:
+                    print(f"\nKdiss = {Kdiss}")
+                t_next_hist += dt_hist
             if callback is not None:
                 callback(self, t, n)
             if verbose:

@@ -956,4 +956,40 @@ double orc_model_max_U2(void* h) {
     return m;
 }
 
+// core/online_diag.py:11-35 (VFwork.compute): the u components of the first register
+// are zeroed (b is left as it is) and receive the vortex force; then, direction by
+// direction (i, j, k), work += (U*F*0.5)(p) + (U*F*0.5)(p - e_d) wherever the index
+// along d is >= 1, in numpy's association order; the result is summed over the box
+// {k0, k1, j0, j1, i0, i1} of the (k, j, i) arrays, in plain loop order.
+double orc_model_vfwork(void* h, const long long* box) {
+    Model* M = (Model*)h;
+    auto& ds = M->reg[0];
+    for (int q = 1; q <= 3; ++q) std::fill(ds[q].begin(), ds[q].end(), 0.0);
+    model_vortex_force(*M, ds);
+    const int Nz = M->N[0], Ny = M->N[1], Nx = M->N[2];
+    const long st[3] = {1, (long)Nx, (long)Nx * Ny};
+    double* w = M->f[WORK].data();
+    for (int k = 0; k < Nz; ++k)
+        for (int j = 0; j < Ny; ++j)
+            for (int i = 0; i < Nx; ++i) {
+                const long q = ((long)k * Ny + j) * Nx + i;
+                const int idx[3] = {i, j, k};
+                double r = 0.0;
+                for (int d = 0; d < 3; ++d) {
+                    if (idx[d] < 1) continue;
+                    const double* U = M->f[CX + d].data();
+                    const double* F = ds[1 + d].data();
+                    const double a = U[q] * F[q] * 0.5;
+                    const double b = U[q - st[d]] * F[q - st[d]] * 0.5;
+                    r = r + (a + b);
+                }
+                w[q] = r;
+            }
+    double s = 0.0;
+    for (long long k = box[0]; k < box[1]; ++k)
+        for (long long j = box[2]; j < box[3]; ++j)
+            for (long long i = box[4]; i < box[5]; ++i) s += w[(k * Ny + j) * Nx + i];
+    return s;
+}
+
 }  // extern "C"

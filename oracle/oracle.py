@@ -85,6 +85,7 @@ def lib():
             "orc_model_forward": (v, [p, d, d]),
             "orc_model_fill": (v, [p, i]),
             "orc_model_max_U2": (d, [p]),
+            "orc_model_vfwork": (d, [p, p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -251,6 +252,12 @@ class OracleModel:
     def vortex_force(self, reg=0):
         """register `reg` = vortex force only (core/vortex_force.py:69-81)"""
         lib().orc_model_vortex_force(self.h, reg)
+
+    def vfwork(self, box):
+        """vortex-force work into field `work` and its sum over `box` = (k0, k1, j0, j1,
+        i0, i1) (core/online_diag.py:11-35)"""
+        b = np.ascontiguousarray(box, dtype=np.int64)
+        return lib().orc_model_vfwork(self.h, b.ctypes.data)
 
     def rhs(self, reg=0, last=False):
         lib().orc_model_rhs(self.h, reg, 1 if last else 0)

@@ -297,6 +297,14 @@ def run_case(refparams, refnyles, mgmod, case, seed):
     names = progs + ["p", "ke", "U_i", "U_j", "U_k", "vor_i", "vor_j", "vor_k", "div"]
     for s in names:
         out["final_" + s] = state.get(s).view("i").copy()
+    # the reference's online diagnostic on the final state (core/online_diag.py:11-35)
+    import online_diag
+    diag = online_diag.VFwork(model, nyl.grid)
+    diag.compute()
+    out["vfwork_sum"] = np.array(diag.worksum)
+    out["vfwork_work"] = state.work.view("i").copy()
+    for c in "ijk":
+        out["vfwork_du_" + c] = model.timescheme.dstate.u[c].view("i").copy()
     meta = dict(case)
     meta["seed"] = seed
     meta["dx"], meta["dy"], meta["dz"] = nyl.grid.dx, nyl.grid.dy, nyl.grid.dz
