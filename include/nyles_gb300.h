@@ -119,7 +119,9 @@ int nyles_mg_workspace_bytes(const NylesMg* mg, size_t* bytes);
 int nyles_mg_bind(NylesMg* mg, void* workspace);      /* device memory of workspace_bytes */
 int nyles_mg_nlevels(const NylesMg* mg, int* nlevels);
 int nyles_mg_level_shape(const NylesMg* mg, int lev, int* shape3); /* lev 1 = finest */
-/* var 1 = x (solution; FP64 for lev 1 in both precisions), 2 = b (right-hand side) */
+/* var 1 = x (solution), 2 = b (right-hand side). Elements are double (NYLES_FP64) or
+ * float (NYLES_MIXED), except lev 1 in NYLES_MIXED: interleaved float pairs (hi, lo)
+ * whose value is hi + lo, |lo| <= ulp(hi)/2. */
 int nyles_mg_level_ptr(NylesMg* mg, int lev, int var, void** ptr);
 /* tol on the squared residual ratio (mg_types.f90:15-26; defaults 1e-6, 20, 0.9) */
 int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega);

@@ -163,6 +163,71 @@ __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, 
 __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
+// ---------------------------------------------------------------- float pairs
+// A value carried as hi + lo, two floats with |lo| <= ulp(hi)/2 (about 48 significant
+// bits), built from error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum
+// (|a| >= |b|) and the FMA-based TwoProduct. The mixed-precision projection keeps its
+// solution and right-hand side in this form, so that the extended-precision residual
+// and correction of iterative refinement run on the FP32 pipes (GB300 issues FP64
+// instructions at a small fraction of the FP32 rate). Every step rounds once
+// (explicit _rn intrinsics), so no contraction can break the error terms.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = __fmul_rn(a, b);
+    e = __fmaf_rn(a, b, -p);
+}
+// (a.hi + a.lo) + b, renormalised
+__device__ __forceinline__ float2 df_add_f(float2 a, float b) {
+    float s, e;
+    two_sum(a.x, b, s, e);
+    e = __fadd_rn(e, a.y);
+    float2 r;
+    fast_two_sum(s, e, r.x, r.y);
+    return r;
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    float2 r;
+    fast_two_sum(s, e, r.x, r.y);
+    return r;
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+// u * (c.hi + c.lo) for a float u
+__device__ __forceinline__ float2 df_mul_f(float u, float2 c) {
+    float p, e;
+    two_prod(u, c.x, p, e);
+    e = __fmaf_rn(u, c.y, e);
+    float2 r;
+    fast_two_sum(p, e, r.x, r.y);
+    return r;
+}
+// (a.hi + a.lo) * (c.hi + c.lo)
+__device__ __forceinline__ float2 df_mul(float2 a, float2 c) {
+    float p, e;
+    two_prod(a.x, c.x, p, e);
+    e = __fmaf_rn(a.x, c.y, e);
+    e = __fmaf_rn(a.y, c.x, e);
+    float2 r;
+    fast_two_sum(p, e, r.x, r.y);
+    return r;
+}
+__device__ __forceinline__ float df_value(float2 a) { return __fadd_rn(a.x, a.y); }
+// host: split a double into a float pair
+inline float2 df_split(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
 // ---------------------------------------------------------------- reductions
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {

@@ -77,6 +77,10 @@ int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* m
 template <typename T, typename TP>
 int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const TP* mg_x, double dx2,
                    cudaStream_t st);
+// mixed precision: divergence into a float-pair right-hand side, correction from a
+// float-pair solution
+int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st);
+int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st);
 
 // contravariant velocity, vorticity and kinetic energy from the filled velocity
 template <typename T>
@@ -112,8 +116,8 @@ struct MgImpl {
     double tol = 1e-6, omega = 0.9;
     int maxite = 20;
     MgLevelDesc lev[32];
-    // mixed precision: FP64 level-1 solution and right-hand side
-    size_t off_p64 = 0, off_b64 = 0;
+    // mixed precision: level-1 solution and right-hand side as float pairs (hi, lo)
+    size_t off_pdf = 0, off_bdf = 0;
     size_t off_partial = 0, off_scalars = 0;
     int npartial = 0;
     size_t bytes = 0;

@@ -28,6 +28,11 @@ struct MgGeom {
     double pcoef[8];   // 1/(Wx*Wy*Wz) indexed by the three "neighbour is wet" bits
 };
 
+// Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
+// [3] nite of the current solve, [4] V-cycles since creation, [5] and [6] the scale of
+// the mixed-precision residual sums and its inverse square.
+enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE = 5, SC_INVSCALE2 = 6 };
+
 constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
 constexpr int MG_RZC = 4;                          // restriction (coarse z per thread)
 
@@ -96,13 +101,13 @@ __device__ __forceinline__ bool mg_block_inside(const MgGeom& g, int z0, int z1,
 }
 
 // one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
-// (basicoperators.f90:379-398). With ACC, the result is added to the FP64 solution
-// `acc` instead of being stored (mixed precision: the correction of iterative
-// refinement, fused into the last half-sweep of the V-cycle).
+// (basicoperators.f90:379-398). With ACC, the result is added to the float-pair
+// solution `acc` instead of being stored (mixed precision: the correction of
+// iterative refinement, fused into the last half-sweep of the V-cycle).
 template <typename T, bool ACC>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
                                                             const T* __restrict__ b, T* __restrict__ out, T omega,
-                                                            double* __restrict__ acc) {
+                                                            float2* __restrict__ acc) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     const int z0 = blockIdx.z * MG_ZC;
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
             const T xp = in[c + sz];
             const T s = ((((in[c - 1] + in[c + 1]) + in[c - sy]) + in[c + sy]) + xm) + xp;
             const T v = cff1 * x0 + omega * (s - b[c]) * idg;
-            if (ACC) acc[c] = acc[c] + (double)v;
+            if (ACC) acc[c] = df_add_f(acc[c], (float)v);
             else out[c] = v;
             xm = x0;
             x0 = xp;
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
         const long long c = mg_at(g, z, y, x);
         const T idg = T(g.idiag[mg_diag(g, z, y, x)]);
         const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
-        if (ACC) acc[c] = acc[c] + (double)v;
+        if (ACC) acc[c] = df_add_f(acc[c], (float)v);
         else out[c] = v;
     }
 }
@@ -262,28 +267,120 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq(const MgGeom g, cons
     block_partial(s, partial);
 }
 
-// mixed precision: FP64 residual of the FP64 solution, its sum of squares, the FP32
-// right-hand side of the next correction V-cycle and a zero initial correction
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid64(const MgGeom g, const double* __restrict__ p,
-                                                             const double* __restrict__ b, float* __restrict__ r32,
-                                                             float* __restrict__ e32, double* __restrict__ partial) {
+// ---------------------------------------------------------------- mixed precision
+// Float-pair residual r = b + diag*p - sum(p_nb), neighbours in mgfor's order. The
+// neighbour sum and the centre product are error-free (TwoSum chain, TwoProduct); the
+// rounding errors and the low parts are added last, so r keeps ~2^-48 of the size of
+// the cancelling terms before its final rounding to float.
+__device__ __forceinline__ float df_resid(float2 bc, float2 pc, float dg, const float2* nb) {
+    float s, e, t;
+    two_sum(nb[0].x, nb[1].x, s, e);
+#pragma unroll
+    for (int k = 2; k < 6; ++k) {
+        two_sum(s, nb[k].x, s, t);
+        e = __fadd_rn(e, t);
+    }
+    float lo = nb[0].y;
+#pragma unroll
+    for (int k = 1; k < 6; ++k) lo = __fadd_rn(lo, nb[k].y);
+    float c, ce;
+    two_prod(dg, pc.x, c, ce);
+    float a1, t1, a2, t2;
+    two_sum(bc.x, c, a1, t1);
+    two_sum(a1, -s, a2, t2);
+    const float rest = __fsub_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bc.y, ce), t1), t2), __fmul_rn(dg, pc.y)),
+                                 __fadd_rn(e, lo));
+    return __fadd_rn(a2, rest);
+}
+
+// value of a float-pair level array one cell outside the interior at most: periodic
+// image, or 0 across a closed wall (branch-free, as mg_rd)
+__device__ __forceinline__ float2 mg_rd_df(const float2* __restrict__ a, const MgGeom& g, int z, int y, int x) {
+    bool ok = true;
+    int q[3] = {z, y, x};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int n = g.n[k];
+        const bool lo = q[k] < 0, hi = q[k] >= n;
+        ok = ok && (g.per[k] || !(lo || hi));
+        q[k] = lo ? q[k] + n : (hi ? q[k] - n : q[k]);
+        q[k] = min(max(q[k], 0), n - 1);
+    }
+    const float2 v = a[((long long)q[0] * g.n[1] + q[1]) * g.n[2] + q[2]];
+    return ok ? v : make_float2(0.f, 0.f);
+}
+
+// residual of the float-pair solution: its sum of squares (for the stop test), the
+// float right-hand side of the next correction V-cycle and a zero initial correction.
+// The squares are summed in float per thread on r * scale, scale = sc[SC_SCALE] a power
+// of two near 1/rms(b) (k_mg_scale), so that they neither underflow nor overflow; each
+// block partial is unscaled in double.
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, const float2* __restrict__ p,
+                                                              const float2* __restrict__ b, float* __restrict__ r32,
+                                                              float* __restrict__ e32, const double* __restrict__ sc,
+                                                              double* __restrict__ partial) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int z0 = blockIdx.z * MG_ZC;
+    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    const float scale = (float)sc[SC_SCALE];
+    float s = 0.f;
+    if (mg_block_inside(g, z0, z1, 1)) {
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        long long c = mg_at(g, z0, y, x);
+        float2 pm = p[c - sz], p0 = p[c];
+        for (int z = z0; z <= z1; ++z, c += sz) {
+            const float2 pp = p[c + sz];
+            const float2 nb[6] = {p[c - 1], p[c + 1], p[c - sy], p[c + sy], pm, pp};
+            const float r = df_resid(b[c], p0, 6.f, nb);
+            r32[c] = r;
+            e32[c] = 0.f;
+            const float rs = __fmul_rn(r, scale);
+            s = __fmaf_rn(rs, rs, s);
+            pm = p0;
+            p0 = pp;
+        }
+    } else if (x < g.n[2] && y < g.n[1]) {
+        for (int z = z0; z <= z1; ++z) {
+            const long long c = mg_at(g, z, y, x);
+            const float2 nb[6] = {mg_rd_df(p, g, z, y, x - 1), mg_rd_df(p, g, z, y, x + 1),
+                                  mg_rd_df(p, g, z, y - 1, x), mg_rd_df(p, g, z, y + 1, x),
+                                  mg_rd_df(p, g, z - 1, y, x), mg_rd_df(p, g, z + 1, y, x)};
+            const float r = df_resid(b[c], p[c], (float)mg_diag(g, z, y, x), nb);
+            r32[c] = r;
+            e32[c] = 0.f;
+            const float rs = __fmul_rn(r, scale);
+            s = __fmaf_rn(rs, rs, s);
+        }
+    }
+    block_partial((double)s * sc[SC_INVSCALE2], partial);
+}
+
+// sum of squares of a float-pair array (high parts, squared and summed in double)
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq_df(const MgGeom g, const float2* __restrict__ v,
+                                                              double* __restrict__ partial) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     const int z0 = blockIdx.z * MG_ZC;
     const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
     double s = 0.0;
-    const bool inside = mg_block_inside(g, z0, z1, 1);
-    if (inside || (x < g.n[2] && y < g.n[1])) {
-        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+    if (x < g.n[2] && y < g.n[1])
         for (int z = z0; z <= z1; ++z) {
-            const long long c = mg_at(g, z, y, x);
-            const double r = inside ? mg_resid_in(p, b, c, sy, sz) : mg_resid(p, b, g, z, y, x);
-            r32[c] = (float)r;
-            e32[c] = 0.0f;
-            s += r * r;
+            const double h = (double)v[mg_at(g, z, y, x)].x;
+            s += h * h;
         }
-    }
     block_partial(s, partial);
+}
+
+// scale of the float sums of squares: 2^-e with 2^e near rms(b) = sqrt(sum(b^2)/vol),
+// and its inverse square (both exact powers of two)
+__global__ void k_mg_scale(double* __restrict__ sc, double vol) {
+    const double nb = sc[SC_NORMB];
+    int e = 0;
+    if (nb > 0.0) frexp(sqrt(nb / vol), &e);
+    e = max(-120, min(120, e));
+    sc[SC_SCALE] = ldexp(1.0, -e);
+    sc[SC_INVSCALE2] = ldexp(1.0, 2 * e);
 }
 
 __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __restrict__ out) {
@@ -301,10 +398,6 @@ __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __
 }
 
 // ---------------------------------------------------------------- device-side stop test
-// Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
-// [3] nite of the current solve, [4] V-cycles since creation.
-enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4 };
-
 // before the loop: res = sum(r^2)/sum(b^2) (0 when b = 0), continue while res >= tol
 __global__ void k_mg_ctl_begin(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol) {
     const double normb = sc[SC_NORMB];
@@ -360,8 +453,8 @@ static T* lvp(MgImpl* mg, int l, int var) {
 void* mg_level_ptr(MgImpl* mg, int lev, int var) {
     if (!mg->ws || lev < 1 || lev > mg->nlevels) return nullptr;
     if (lev == 1 && mg->precision == NYLES_MIXED) {
-        if (var == 1) return mg->ws + mg->off_p64;
-        if (var == 2) return mg->ws + mg->off_b64;
+        if (var == 1) return mg->ws + mg->off_pdf;
+        if (var == 2) return mg->ws + mg->off_bdf;
     }
     size_t off = var == 1 ? mg->lev[lev - 1].off_x : (var == 2 ? mg->lev[lev - 1].off_b : mg->lev[lev - 1].off_y);
     return mg->ws + off;
@@ -408,8 +501,8 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         d.off_y = take(d.vol * es);
     }
     if (precision == NYLES_MIXED) {
-        mg->off_p64 = take(mg->lev[0].vol * sizeof(double));
-        mg->off_b64 = take(mg->lev[0].vol * sizeof(double));
+        mg->off_pdf = take(mg->lev[0].vol * sizeof(float2));
+        mg->off_bdf = take(mg->lev[0].vol * sizeof(float2));
     }
     const dim3 g0 = grid_zc(mg->lev[0].n, MG_ZC);
     mg->npartial = (int)(g0.x * g0.y * g0.z);
@@ -432,7 +525,7 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
     note_launch(2);
     k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr);
     if (acc_p64)
-        k_mg_jacobi<T, true><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<double*>(mg->ws + mg->off_p64));
+        k_mg_jacobi<T, true><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf));
     else
         k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr);
 }
@@ -483,17 +576,33 @@ static void enqueue_sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, d
     k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
 }
 
-// mixed precision: enqueue the FP64 residual (also the next correction's rhs) into *out
-static void enqueue_resid64(MgImpl* mg, double* out, cudaStream_t st) {
+// mixed precision: enqueue sum(b^2) of the float-pair right-hand side into
+// sc[SC_NORMB] and the scale of the residual sums
+static void enqueue_normb_df(MgImpl* mg, cudaStream_t st) {
     MgGeom g = mgg(mg, 0);
     double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
+    ProfScope ps(mg->prof, 11, st);
+    note_launch(3);
+    k_mg_sumsq_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_bdf), part);
+    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_NORMB);
+    k_mg_scale<<<1, 1, 0, st>>>(sc, (double)mg->lev[0].vol);
+}
+
+// mixed precision: enqueue the float-pair residual (also the next correction's rhs)
+// and its sum of squares into sc[SC_RR]
+static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
+    MgGeom g = mgg(mg, 0);
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
     const dim3 grd = grid_zc(g.n, MG_ZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(2);
-    k_mg_resid64<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const double*>(mg->ws + mg->off_p64),
-                                       reinterpret_cast<const double*>(mg->ws + mg->off_b64),
-                                       lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), part);
-    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), out);
+    k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
+                                        reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
+                                        lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), sc, part);
+    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
 }
 
 template <typename T, int MODE>
@@ -502,9 +611,10 @@ static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* ho
     return read_scalar(mg, host_out, st);
 }
 
-static int resid64(MgImpl* mg, double* host_out, cudaStream_t st) {
-    enqueue_resid64(mg, scalars(mg), st);
-    return read_scalar(mg, host_out, st);
+static int read_slot(MgImpl* mg, int slot, double* host_out, cudaStream_t st) {
+    cudaError_t e = cudaMemcpyAsync(host_out, scalars(mg) + slot, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return cuda_status(e, "multigrid norm");
 }
 
 // solvers.f90:8-33: stop when sum(r^2)/sum(b^2) < tol or after maxite V-cycles
@@ -535,19 +645,21 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
             }
         }
     } else {
-        const double* b64 = reinterpret_cast<const double*>(mg->ws + mg->off_b64);
-        if ((rc = sumsq<double, 0>(mg, g0, b64, nullptr, &normb, st))) return rc;
+        enqueue_normb_df(mg, st);
+        if ((rc = read_slot(mg, SC_NORMB, &normb, st))) return rc;
         if (normb > 0.0) {
-            if ((rc = resid64(mg, &rr, st))) return rc;
+            enqueue_resid_df(mg, st);
+            if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
             res = rr / normb;
         }
         while (true) {
             if (res < mg->tol) break;
-            vcycle<float>(mg, st, true);   // FP32 correction of the residual equation, added to p64
+            vcycle<float>(mg, st, true);   // FP32 correction of the residual equation, added to p
             ++nite;
             if (nite >= mg->maxite) break;
             if (normb > 0.0) {
-                if ((rc = resid64(mg, &rr, st))) return rc;
+                enqueue_resid_df(mg, st);
+                if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
                 res = rr / normb;
             } else {
                 res = 0.0;
@@ -601,9 +713,8 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         enqueue_sumsq<double, 0>(mg, g0, lvp<double>(mg, 0, 2), (const double*)nullptr, sc + SC_NORMB, st);
         enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
     } else {
-        enqueue_sumsq<double, 0>(mg, g0, reinterpret_cast<const double*>(mg->ws + mg->off_b64),
-                                 (const double*)nullptr, sc + SC_NORMB, st);
-        enqueue_resid64(mg, sc + SC_RR, st);
+        enqueue_normb_df(mg, st);
+        enqueue_resid_df(mg, st);
     }
     k_mg_ctl_begin<<<1, 1, 0, st>>>(sc, h, mg->tol);
     note_launch();
@@ -626,7 +737,7 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
     } else {
         vcycle<float>(mg, st, true);
-        enqueue_resid64(mg, sc + SC_RR, st);
+        enqueue_resid_df(mg, st);
     }
     k_mg_ctl_step<<<1, 1, 0, st>>>(sc, h, mg->tol, mg->maxite);
     note_launch();

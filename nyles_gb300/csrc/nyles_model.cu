@@ -395,11 +395,16 @@ static int model_diagnose(NylesModel* m, cudaStream_t st) {
         ProfScope ps(&m->prof, 2, st);
         if ((rc = launch_fill<T>(m->g, uf, 4, st))) return rc;
     }
-    double* mgb = reinterpret_cast<double*>(mg_level_ptr(&m->mg, 1, 2));
-    double* mgx = reinterpret_cast<double*>(mg_level_ptr(&m->mg, 1, 1));
+    void* mgb = mg_level_ptr(&m->mg, 1, 2);
+    void* mgx = mg_level_ptr(&m->mg, 1, 1);
     {
         ProfScope ps(&m->prof, 3, st);
-        if ((rc = launch_div<T, double>(&m->d, m->g, s, mgb, st))) return rc;
+        if constexpr (sizeof(T) == sizeof(double))
+            rc = launch_div<T, double>(&m->d, m->g, s, reinterpret_cast<double*>(mgb), st);
+        else
+            rc = launch_div_df(&m->d, m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)),
+                               reinterpret_cast<float2*>(mgb), st);
+        if (rc) return rc;
     }
     {
         ProfScope ps(&m->prof, 4, st);
@@ -414,7 +419,12 @@ static int model_diagnose(NylesModel* m, cudaStream_t st) {
     }
     {
         ProfScope ps(&m->prof, 5, st);
-        if ((rc = launch_correct<T, double>(&m->d, m->g, s, mgx, m->d.dx2, st))) return rc;
+        if constexpr (sizeof(T) == sizeof(double))
+            rc = launch_correct<T, double>(&m->d, m->g, s, reinterpret_cast<const double*>(mgx), m->d.dx2, st);
+        else
+            rc = launch_correct_df(m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)),
+                                   reinterpret_cast<const float2*>(mgx), m->d.dx2, st);
+        if (rc) return rc;
     }
     {
         ProfScope ps(&m->prof, 2, st);

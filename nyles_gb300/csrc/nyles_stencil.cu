@@ -531,11 +531,48 @@ __global__ void __launch_bounds__(256) k_div(const Geom g, const T* __restrict__
     }
 }
 
+// mixed precision: the same divergence of the FP32 velocity carried as a float pair
+// (products by the metric factor and differences are exact to ~2^-48), written to the
+// multigrid right-hand side as (hi, lo); the model's div field gets hi + lo rounded.
+__global__ void __launch_bounds__(256) k_div_df(const Geom g, const float* __restrict__ ux,
+                                                const float* __restrict__ uy, const float* __restrict__ uz,
+                                                float2 idx2, float2 idy2, float2 idz2, float* __restrict__ div,
+                                                float2* __restrict__ mgb) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const int zz = g.wrap(0, z), yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const long long c = g.at(zz, yy, xx);
+    float2 acc = df_mul_f(ux[c], idx2);
+    if (xx != 0) acc = df_add(acc, df_neg(df_mul_f(ux[c - 1], idx2)));
+    float2 t = df_mul_f(uy[c], idy2);
+    if (yy != 0) t = df_add(t, df_neg(df_mul_f(uy[c - g.sy], idy2)));
+    acc = df_add(acc, t);
+    t = df_mul_f(uz[c], idz2);
+    if (zz != 0) t = df_add(t, df_neg(df_mul_f(uz[c - g.sz], idz2)));
+    acc = df_add(acc, t);
+    div[g.at(z, y, x)] = df_value(acc);
+    if (zz == z && yy == y && xx == x) {
+        const int iz = zz - (g.per[0] ? g.nh : 0), iy = yy - (g.per[1] ? g.nh : 0), ix = xx - (g.per[2] ? g.nh : 0);
+        mgb[((long long)iz * g.n[1] + iy) * g.n[2] + ix] = acc;
+    }
+}
+
 template <typename T, typename TB>
 int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* mg_b, cudaStream_t st) {
     dim3 blk(32, 4, 2);
     k_div<T, TB><<<grid3(g, blk), blk, 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
                                                  TB(d->idx2), TB(d->idy2), TB(d->idz2), s.f[NYLES_F_DIV], mg_b);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "div kernel");
+}
+
+int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st) {
+    dim3 blk(32, 4, 2);
+    k_div_df<<<grid3(g, blk), blk, 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
+                                             df_split(d->idx2), df_split(d->idy2), df_split(d->idz2),
+                                             s.f[NYLES_F_DIV], mg_b);
     note_launch();
     return cuda_status(cudaGetLastError(), "div kernel");
 }
@@ -590,6 +627,55 @@ int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, c
     a.dx2 = dx2;
     dim3 blk(32, 4, 2);
     k_correct<T, TP><<<grid3(g, blk), blk, 0, st>>>(a);
+    note_launch();
+    return cuda_status(cudaGetLastError(), "correct kernel");
+}
+
+// mixed precision: the same correction from the float-pair solution; differences of
+// neighbouring pressures and the dx^2 scaling are taken on the pairs, then rounded.
+struct CorrDfArgs {
+    Geom g;
+    float* u[3];
+    const float2* x;
+    float* p;
+    float2 dx2;
+};
+
+__device__ __forceinline__ float2 pres_df(const CorrDfArgs& a, int z, int y, int x) {
+    const Geom& g = a.g;
+    z = g.wrap(0, z); y = g.wrap(1, y); x = g.wrap(2, x);
+    const int iz = z - (g.per[0] ? g.nh : 0), iy = y - (g.per[1] ? g.nh : 0), ix = x - (g.per[2] ? g.nh : 0);
+    return a.x[((long long)iz * g.n[1] + iy) * g.n[2] + ix];
+}
+
+__global__ void __launch_bounds__(256) k_correct_df(const CorrDfArgs a) {
+    const Geom& g = a.g;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const long long c = g.at(z, y, x);
+    const float2 p0 = pres_df(a, z, y, x);
+    a.p[c] = df_value(df_mul(p0, a.dx2));
+    if (g.wrap(0, z) != z || g.wrap(1, y) != y || g.wrap(2, x) != x) return;   // halo: filled later
+    const float2 np0 = df_neg(p0);
+    if (x < g.N[2] - 1)
+        a.u[0][c] = __fsub_rn(a.u[0][c], df_value(df_mul(df_add(pres_df(a, z, y, x + 1), np0), a.dx2)));
+    if (y < g.N[1] - 1)
+        a.u[1][c] = __fsub_rn(a.u[1][c], df_value(df_mul(df_add(pres_df(a, z, y + 1, x), np0), a.dx2)));
+    if (z < g.N[0] - 1)
+        a.u[2][c] = __fsub_rn(a.u[2][c], df_value(df_mul(df_add(pres_df(a, z + 1, y, x), np0), a.dx2)));
+}
+
+int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st) {
+    CorrDfArgs a;
+    a.g = g;
+    for (int i = 0; i < 3; ++i) a.u[i] = s.f[NYLES_F_U_I + i];
+    a.x = mg_x;
+    a.p = s.f[NYLES_F_P];
+    a.dx2 = df_split(dx2);
+    dim3 blk(32, 4, 2);
+    k_correct_df<<<grid3(g, blk), blk, 0, st>>>(a);
     note_launch();
     return cuda_status(cudaGetLastError(), "correct kernel");
 }
@@ -842,11 +928,8 @@ int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream
 NYLES_INST(double)
 NYLES_INST(float)
 template int launch_div<double, double>(const NylesDesc*, const Geom&, const StencilPtrs<double>&, double*, cudaStream_t);
-template int launch_div<float, double>(const NylesDesc*, const Geom&, const StencilPtrs<float>&, double*, cudaStream_t);
 template int launch_correct<double, double>(const NylesDesc*, const Geom&, const StencilPtrs<double>&, const double*,
                                             double, cudaStream_t);
-template int launch_correct<float, double>(const NylesDesc*, const Geom&, const StencilPtrs<float>&, const double*,
-                                           double, cudaStream_t);
 
 // ---------------------------------------------------------------- allocation-free CFL reduction
 // The reduction's block partials live in this file-scope array instead of a caller

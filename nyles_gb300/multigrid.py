@@ -47,28 +47,52 @@ class MG(object):
         return (s[0], s[1], s[2])
 
     def level_tensor(self, lev, var):
-        """Device tensor aliasing a level array (var 1 = x, 2 = b). Level 1 is float64;
-        coarser levels are float64 (fp64) or float32 (mixed)."""
+        """Device tensor aliasing a level array (var 1 = x, 2 = b): float64 (fp64) or
+        float32 (mixed); level 1 of the mixed solver holds float pairs (hi, lo), shape
+        (nz, ny, nx, 2), whose value is hi + lo."""
         p = ctypes.c_void_p()
         nat.check(self.lib.nyles_mg_level_ptr(self._h, lev, var, ctypes.byref(p)))
         shape = self.level_shape(lev)
         n = shape[0] * shape[1] * shape[2]
-        dtype = torch.float64 if (lev == 1 or self.precision == "fp64") else torch.float32
-        return _alias(self.workspace, p.value - self.workspace.data_ptr(), n, dtype).view(shape)
+        if self.precision == "fp64":
+            return _alias(self.workspace, p.value - self.workspace.data_ptr(), n, torch.float64).view(shape)
+        if lev == 1:
+            return _alias(self.workspace, p.value - self.workspace.data_ptr(), 2 * n, torch.float32).view(shape + (2,))
+        return _alias(self.workspace, p.value - self.workspace.data_ptr(), n, torch.float32).view(shape)
+
+    def get(self, lev, var):
+        """float64 copy of a level array (pairs summed)."""
+        t = self.level_tensor(lev, var)
+        if self.precision != "fp64" and lev == 1:
+            return t[..., 0].double() + t[..., 1].double()
+        return t.double()
+
+    def set(self, lev, var, value):
+        """write a level array from any float tensor (split into pairs where needed)"""
+        t = self.level_tensor(lev, var)
+        v = torch.as_tensor(value, device=self.device).reshape(self.level_shape(lev)).double()
+        if self.precision != "fp64" and lev == 1:
+            hi = v.float()
+            t[..., 0].copy_(hi)
+            t[..., 1].copy_((v - hi.double()).float())
+        else:
+            t.copy_(v)
 
     def set_params(self, tol=1e-6, maxite=20, omega=0.9):
         nat.check(self.lib.nyles_mg_set_params(self._h, float(tol), int(maxite), float(omega)))
 
     def solve(self, b=None):
         """Solve with the current warm start; `b` (interior, any dtype) replaces the
-        right-hand side when given. Returns (x view, stats dict)."""
+        right-hand side when given. Returns (x, stats dict): x aliases the solution in
+        fp64 and is a float64 copy in mixed precision."""
         if b is not None:
-            self.level_tensor(1, 2).copy_(torch.as_tensor(b, device=self.device).reshape(self.shape))
+            self.set(1, 2, b)
         st = nat.NylesMgStats()
         rc = self.lib.nyles_mg_solve(self._h, ctypes.byref(st), nat.stream_ptr())
         if rc not in (nat.NYLES_OK, nat.NYLES_NOT_CONVERGED):
             nat.check(rc)
-        return self.level_tensor(1, 1), {"nite": st.nite, "res": st.res, "converged": rc == nat.NYLES_OK}
+        x = self.level_tensor(1, 1) if self.precision == "fp64" else self.get(1, 1)
+        return x, {"nite": st.nite, "res": st.res, "converged": rc == nat.NYLES_OK}
 
 
 def _alias(buf, byte_offset, n, dtype):
