@@ -116,6 +116,8 @@ struct MgImpl {
     double tol = 1e-6, omega = 0.9;
     int maxite = 20;
     MgLevelDesc lev[32];
+    int bottom = 0;                   // first level of the one-block coarse solve (nlevels: none)
+    size_t bottom_smem = 0;           // its shared memory bytes
     // mixed precision: level-1 solution and right-hand side as float pairs (hi, lo)
     size_t off_pdf = 0, off_bdf = 0;
     size_t off_partial = 0, off_scalars = 0;

@@ -92,6 +92,48 @@ __device__ __forceinline__ T mg_resid_in(const T* __restrict__ x, const T* __res
     return (b[c] + T(6) * x[c]) - (((((x[c - 1] + x[c + 1]) + x[c - sy]) + x[c + sy]) + x[c - sz]) + x[c + sz]);
 }
 
+// ---- per-cell operators with the ghost logic (used at level faces and on the levels
+// held in shared memory by k_mg_bottom)
+// damped Jacobi value at (z, y, x): (1-omega)*in + omega*(sum(in_nb) - b)*idiag
+template <typename T>
+__device__ __forceinline__ T mg_jacobi_cell(const MgGeom& g, const T* __restrict__ in, const T* __restrict__ b, int z,
+                                            int y, int x, T cff1, T omega) {
+    const long long c = mg_at(g, z, y, x);
+    const T idg = T(g.idiag[mg_diag(g, z, y, x)]);
+    return cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
+}
+// sum of the residuals of the 8 children of coarse cell (z, y, x)
+template <typename T>
+__device__ __forceinline__ T mg_restrict_cell(const MgGeom& gf, const T* __restrict__ xf, const T* __restrict__ bf,
+                                              int z, int y, int x) {
+    const int i = 2 * x, j = 2 * y, k = 2 * z;
+    T s = mg_resid(xf, bf, gf, k, j, i);
+    s = s + mg_resid(xf, bf, gf, k, j, i + 1);
+    s = s + mg_resid(xf, bf, gf, k, j + 1, i);
+    s = s + mg_resid(xf, bf, gf, k, j + 1, i + 1);
+    s = s + mg_resid(xf, bf, gf, k + 1, j, i);
+    s = s + mg_resid(xf, bf, gf, k + 1, j, i + 1);
+    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i);
+    s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i + 1);
+    return s;
+}
+// 9-3-3-1 prolongation increment of fine cell (z, y, x)
+template <typename T>
+__device__ __forceinline__ T mg_prolong_cell(const MgGeom& gf, const MgGeom& gc, const T* __restrict__ xc, int z,
+                                             int y, int x) {
+    const int ic = x >> 1, jc = y >> 1, kc = z >> 1;
+    const int si = (x & 1) ? 1 : -1, sj = (y & 1) ? 1 : -1, sk = (z & 1) ? 1 : -1;
+    auto plane = [&](int kk) -> T {
+        return ((T(9) * mg_rd(xc, gc, kk, jc, ic) + T(3) * mg_rd(xc, gc, kk, jc, ic + si)) +
+                T(3) * mg_rd(xc, gc, kk, jc + sj, ic)) + mg_rd(xc, gc, kk, jc + sj, ic + si);
+    };
+    const T bpl = plane(kc);
+    const T opl = plane(kc + sk);
+    auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
+    const T pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
+    return pcoef * (T(3) * bpl + opl);
+}
+
 // this block's cells plus a margin of `r` cells lie inside the level in every direction
 __device__ __forceinline__ bool mg_block_inside(const MgGeom& g, int z0, int z1, int r) {
     const int x0 = blockIdx.x * MG_BX, y0 = blockIdx.y * MG_BY;
@@ -132,8 +174,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
     if (x >= g.n[2] || y >= g.n[1]) return;
     for (int z = z0; z <= z1; ++z) {
         const long long c = mg_at(g, z, y, x);
-        const T idg = T(g.idiag[mg_diag(g, z, y, x)]);
-        const T v = cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
+        const T v = mg_jacobi_cell(g, in, b, z, y, x, cff1, omega);
         if (ACC) acc[c] = df_add_f(acc[c], (float)v);
         else out[c] = v;
     }
@@ -170,14 +211,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, 
             s = s + mg_resid_in(xf, bf, c + sz + sy, sy, sz);
             s = s + mg_resid_in(xf, bf, c + sz + sy + 1, sy, sz);
         } else {
-            s = mg_resid(xf, bf, gf, k, j, i);
-            s = s + mg_resid(xf, bf, gf, k, j, i + 1);
-            s = s + mg_resid(xf, bf, gf, k, j + 1, i);
-            s = s + mg_resid(xf, bf, gf, k, j + 1, i + 1);
-            s = s + mg_resid(xf, bf, gf, k + 1, j, i);
-            s = s + mg_resid(xf, bf, gf, k + 1, j, i + 1);
-            s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i);
-            s = s + mg_resid(xf, bf, gf, k + 1, j + 1, i + 1);
+            s = mg_restrict_cell(gf, xf, bf, z, y, x);
         }
         const long long c = mg_at(gc, z, y, x);
         bc[c] = T(0.5) * s;
@@ -225,6 +259,88 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
         const long long c = mg_at(gf, z, y, x);
         xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
     }
+}
+
+// ---------------------------------------------------------------- coarse levels in one block
+// Levels l0..L-1 of a V-cycle (solvers.f90:35-55 from level l0 down and back up) run in
+// one thread block: the level arrays live in shared memory, and each half-sweep,
+// restriction and prolongation is one pass of the block over a level followed by a
+// barrier, instead of one grid launch each. Input: b of level l0 (its x is zero after
+// the restriction that produced b); output: x of level l0. The per-cell arithmetic is
+// that of the grid kernels' ghost paths.
+constexpr int MG_BOTTOM_MAXLEV = 12;
+constexpr int MG_BOTTOM_THREADS = 512;
+constexpr size_t MG_BOTTOM_SMEM = 200 * 1024;
+
+template <typename T>
+struct MgBottom {
+    int nlev;                          // levels held: l0..L-1
+    MgGeom g[MG_BOTTOM_MAXLEV];
+    int off[MG_BOTTOM_MAXLEV];         // element offset of each level's x in shared memory; b, y follow
+    T* xg;                             // x of level l0 (global)
+    const T* bg;                       // b of level l0 (global)
+    T omega;
+};
+
+__device__ __forceinline__ int mg_vol(const MgGeom& g) { return g.n[0] * g.n[1] * g.n[2]; }
+
+template <typename T>
+__device__ __forceinline__ void bottom_smooth(const MgGeom& g, T* x, const T* b, T* y, T cff1, T om) {
+    const int vol = mg_vol(g);
+    if (vol == 0) return;
+    for (int q = threadIdx.x; q < vol; q += blockDim.x) {
+        const int xx = q % g.n[2], r = q / g.n[2];
+        y[q] = mg_jacobi_cell(g, x, b, r / g.n[1], r % g.n[1], xx, cff1, om);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < vol; q += blockDim.x) {
+        const int xx = q % g.n[2], r = q / g.n[2];
+        x[q] = mg_jacobi_cell(g, y, b, r / g.n[1], r % g.n[1], xx, cff1, om);
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const MgBottom<T> a) {
+    extern __shared__ __align__(16) unsigned char mg_smem[];
+    T* sm = reinterpret_cast<T*>(mg_smem);
+    const T om = a.omega, cff1 = T(1) - om;
+    const int L = a.nlev;
+    auto X = [&](int l) { return sm + a.off[l]; };
+    auto Bv = [&](int l) { return sm + a.off[l] + mg_vol(a.g[l]); };
+    auto Y = [&](int l) { return sm + a.off[l] + 2 * mg_vol(a.g[l]); };
+    const int v0 = mg_vol(a.g[0]);
+    for (int q = threadIdx.x; q < v0; q += blockDim.x) {
+        X(0)[q] = T(0);
+        Bv(0)[q] = a.bg[q];
+    }
+    __syncthreads();
+    for (int l = 0; l < L - 1; ++l) {
+        bottom_smooth(a.g[l], X(l), Bv(l), Y(l), cff1, om);
+        const MgGeom& gc = a.g[l + 1];
+        const int vc = mg_vol(gc);
+        if (vc == 0) continue;
+        for (int q = threadIdx.x; q < vc; q += blockDim.x) {
+            const int xx = q % gc.n[2], r = q / gc.n[2];
+            Bv(l + 1)[q] = T(0.5) * mg_restrict_cell(a.g[l], X(l), Bv(l), r / gc.n[1], r % gc.n[1], xx);
+            X(l + 1)[q] = T(0);
+        }
+        __syncthreads();
+    }
+    bottom_smooth(a.g[L - 1], X(L - 1), Bv(L - 1), Y(L - 1), cff1, om);
+    for (int l = L - 2; l >= 0; --l) {
+        const MgGeom& gf = a.g[l];
+        if (mg_vol(a.g[l + 1]) > 0) {
+            const int vf = mg_vol(gf);
+            for (int q = threadIdx.x; q < vf; q += blockDim.x) {
+                const int xx = q % gf.n[2], r = q / gf.n[2];
+                X(l)[q] = X(l)[q] + mg_prolong_cell(gf, a.g[l + 1], X(l + 1), r / gf.n[1], r % gf.n[1], xx);
+            }
+            __syncthreads();
+        }
+        bottom_smooth(gf, X(l), Bv(l), Y(l), cff1, om);
+    }
+    for (int q = threadIdx.x; q < v0; q += blockDim.x) a.xg[q] = X(0)[q];
 }
 
 // ---------------------------------------------------------------- reductions
@@ -504,6 +620,29 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         mg->off_pdf = take(mg->lev[0].vol * sizeof(float2));
         mg->off_bdf = take(mg->lev[0].vol * sizeof(float2));
     }
+    // the coarsest levels whose arrays fit in one block's shared memory (two levels at
+    // least, never level 0) run as one k_mg_bottom launch per V-cycle
+    mg->bottom = L;
+    mg->bottom_smem = 0;
+    {
+        size_t bytes = 0;
+        for (int l = L - 1; l >= 1 && L - l <= MG_BOTTOM_MAXLEV; --l) {
+            bytes += 3 * (size_t)mg->lev[l].vol * es;
+            if (bytes > MG_BOTTOM_SMEM) break;
+            if (L - l >= 2) {
+                mg->bottom = l;
+                mg->bottom_smem = bytes;
+            }
+        }
+        if (mg->bottom < L) {
+            cudaError_t e = precision == NYLES_MIXED
+                                ? cudaFuncSetAttribute(k_mg_bottom<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)MG_BOTTOM_SMEM)
+                                : cudaFuncSetAttribute(k_mg_bottom<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)MG_BOTTOM_SMEM);
+            if (e != cudaSuccess) return cuda_status(e, "multigrid coarse-level kernel attribute");
+        }
+    }
     const dim3 g0 = grid_zc(mg->lev[0].n, MG_ZC);
     mg->npartial = (int)(g0.x * g0.y * g0.z);
     mg->off_partial = take(mg->npartial * sizeof(double));
@@ -531,10 +670,32 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
 }
 
 // solvers.f90:35-55
+// levels mg->bottom..L-1 of the V-cycle in one block (k_mg_bottom)
+template <typename T>
+static void bottom(MgImpl* mg, cudaStream_t st) {
+    const int l0 = mg->bottom;
+    if (empty(mg, l0)) return;
+    MgBottom<T> a;
+    a.nlev = mg->nlevels - l0;
+    int off = 0;
+    for (int k = 0; k < a.nlev; ++k) {
+        a.g[k] = mgg(mg, l0 + k);
+        a.off[k] = off;
+        off += 3 * (int)mg->lev[l0 + k].vol;
+    }
+    a.xg = lvp<T>(mg, l0, 1);
+    a.bg = lvp<T>(mg, l0, 2);
+    a.omega = T(mg->omega);
+    ProfScope ps(mg->prof, 8, st);
+    note_launch();
+    k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, mg->bottom_smem, st>>>(a);
+}
+
 template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     const int L = mg->nlevels;
-    for (int l = 0; l < L - 1; ++l) {
+    const int B = mg->bottom;   // < L: levels B..L-1 in one block
+    for (int l = 0; l < L - 1 && l < B; ++l) {
         smooth<T>(mg, l, st, false);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -544,8 +705,11 @@ static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
                                                                     lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 1));
         }
     }
-    smooth<T>(mg, L - 1, st, L == 1 && mixed);
-    for (int l = L - 2; l >= 0; --l) {
+    if (B < L)
+        bottom<T>(mg, st);
+    else
+        smooth<T>(mg, L - 1, st, L == 1 && mixed);
+    for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 10, st);
