@@ -34,7 +34,7 @@ struct MgGeom {
 enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE = 5, SC_INVSCALE2 = 6 };
 
 constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
-constexpr int MG_RZC = 4;                          // restriction (coarse z per thread)
+constexpr int MG_RZC = 2;                          // restriction (coarse z per thread)
 
 __device__ __forceinline__ long long mg_at(const MgGeom& g, int z, int y, int x) {
     return ((long long)z * g.n[1] + y) * g.n[2] + x;
@@ -134,12 +134,28 @@ __device__ __forceinline__ T mg_prolong_cell(const MgGeom& gf, const MgGeom& gc,
     return pcoef * (T(3) * bpl + opl);
 }
 
-// this block's cells plus a margin of `r` cells lie inside the level in every direction
-__device__ __forceinline__ bool mg_block_inside(const MgGeom& g, int z0, int z1, int r) {
-    const int x0 = blockIdx.x * MG_BX, y0 = blockIdx.y * MG_BY;
-    const int x1 = min(x0 + MG_BX, g.n[2]) - 1, y1 = min(y0 + MG_BY, g.n[1]) - 1;
-    return x0 >= r && x1 <= g.n[2] - 1 - r && y0 >= r && y1 <= g.n[1] - 1 - r && z0 >= r && z1 <= g.n[0] - 1 - r &&
-           (x0 + MG_BX <= g.n[2]) && (y0 + MG_BY <= g.n[1]);
+// ---- grid kernels: one thread per (x, y) column and chunk of z
+// The neighbours of a thread's fixed coordinate along one direction: element offsets
+// of the cells at c-1 and c+1 and whether they are wet. Outside the level a neighbour
+// is the periodic image or, across a closed wall, dry: its offset is then 0 (the cell
+// itself, a valid address) and the value read is replaced by 0 — loads are never
+// skipped (see mg_rd).
+struct MgNb {
+    long long om, op;
+    bool wm, wp;
+};
+__device__ __forceinline__ MgNb mg_nb(int c, int n, int per, long long stride) {
+    MgNb r;
+    r.wm = c > 0 || per;
+    r.wp = c < n - 1 || per;
+    r.om = c > 0 ? -stride : (per ? (long long)(n - 1) * stride : 0);
+    r.op = c < n - 1 ? stride : (per ? -(long long)(n - 1) * stride : 0);
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ T mg_ldw(const T* __restrict__ a, long long c, bool wet) {
+    const T v = a[c];
+    return wet ? v : T(0);
 }
 
 // one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
@@ -152,70 +168,131 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
                                                             float2* __restrict__ acc) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_ZC;
-    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    if (x >= g.n[2] || y >= g.n[1]) return;
+    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+    const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+    const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+    const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
     const T cff1 = T(1) - omega;
-    if (mg_block_inside(g, z0, z1, 1)) {
-        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
-        const T idg = T(g.idiag[6]);
-        long long c = mg_at(g, z0, y, x);
-        T xm = in[c - sz], x0 = in[c];
-        for (int z = z0; z <= z1; ++z, c += sz) {
-            const T xp = in[c + sz];
-            const T s = ((((in[c - 1] + in[c + 1]) + in[c - sy]) + in[c + sy]) + xm) + xp;
-            const T v = cff1 * x0 + omega * (s - b[c]) * idg;
-            if (ACC) acc[c] = df_add_f(acc[c], (float)v);
-            else out[c] = v;
-            xm = x0;
-            x0 = xp;
+    const long long c0 = mg_at(g, z0, y, x);
+    // neighbour sum in mgfor's order x-1, x+1, y-1, y+1, z-1, z+1
+    auto cell = [&](long long c, T zm, T x0, T zp, T idg) -> T {
+        const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) + mg_ldw(in, c + ny.om, ny.wm)) +
+                      mg_ldw(in, c + ny.op, ny.wp)) + zm) + zp;
+        return cff1 * x0 + omega * (s - b[c]) * idg;
+    };
+    auto put = [&](long long c, T v) {
+        if (ACC) acc[c] = df_add_f(acc[c], (float)v);
+        else out[c] = v;
+    };
+    if (z0 + MG_ZC <= nz) {
+        // full chunk: fixed trip count, fully unrolled, so that every load of the chunk
+        // is issued before the first result is needed
+        const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+        T col[MG_ZC + 2];
+        col[0] = mg_ldw(in, c0 + lo.om, lo.wm);
+#pragma unroll
+        for (int k = 1; k <= MG_ZC; ++k) col[k] = in[c0 + (k - 1) * sz];
+        col[MG_ZC + 1] = mg_ldw(in, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+        const T idg = T(g.idiag[dxy + 2]);
+        const T idg_lo = T(g.idiag[dxy + 1 + (int)lo.wm]);
+        const T idg_hi = T(g.idiag[dxy + 1 + (int)hi.wp]);
+#pragma unroll
+        for (int k = 0; k < MG_ZC; ++k) {
+            const long long c = c0 + k * sz;
+            put(c, cell(c, col[k], col[k + 1], col[k + 2], k == 0 ? idg_lo : (k == MG_ZC - 1 ? idg_hi : idg)));
         }
         return;
     }
-    if (x >= g.n[2] || y >= g.n[1]) return;
-    for (int z = z0; z <= z1; ++z) {
+    for (int z = z0; z < nz; ++z) {   // last, partial chunk
         const long long c = mg_at(g, z, y, x);
-        const T v = mg_jacobi_cell(g, in, b, z, y, x, cff1, omega);
-        if (ACC) acc[c] = df_add_f(acc[c], (float)v);
-        else out[c] = v;
+        const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
+        const T idg = T(g.idiag[dxy + (int)nzb.wm + (int)nzb.wp]);
+        put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg));
     }
+}
+
+// First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
+// depends on the cell's own b alone, so the kernel that produces b writes it.
+template <typename T>
+__device__ __forceinline__ T mg_jacobi_from_zero(T b, T omega, T idg) {
+    return omega * (T(0) - b) * idg;
 }
 
 // residual of the fine level restricted to the coarse right-hand side,
 // bc = Rcoef*(sum of the 8 children) with Rcoef = 1/2 (basicoperators.f90:32-60,
-// operators.f90:172-213); the coarse solution is zeroed (operators.f90:209)
+// operators.f90:172-213). The coarse solution is zero at this point (operators.f90:209),
+// so the first half-sweep of the coarse smoothing is written here, into yc.
 template <typename T>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, const T* __restrict__ xf,
                                                               const T* __restrict__ bf, const MgGeom gc,
-                                                              T* __restrict__ bc, T* __restrict__ xc) {
+                                                              T* __restrict__ bc, T* __restrict__ yc, T omega) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_RZC;
-    const int z1 = min(z0 + MG_RZC, gc.n[0]) - 1;
     if (x >= gc.n[2] || y >= gc.n[1]) return;
-    // fast path when every child and its face neighbours are inside the fine level
-    const int bx0 = blockIdx.x * MG_BX, by0 = blockIdx.y * MG_BY;
-    const bool inside = bx0 >= 1 && 2 * (bx0 + MG_BX) + 1 <= gf.n[2] - 1 && by0 >= 1 &&
-                        2 * (by0 + MG_BY) + 1 <= gf.n[1] - 1 && z0 >= 1 && 2 * z1 + 2 <= gf.n[0] - 1;
-    const long long sy = gf.n[2], sz = (long long)gf.n[1] * gf.n[2];
-    for (int z = z0; z <= z1; ++z) {
-        const int i = 2 * x, j = 2 * y, k = 2 * z;
-        T s;
-        if (inside) {
-            const long long c = mg_at(gf, k, j, i);
-            s = mg_resid_in(xf, bf, c, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + 1, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sy, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sy + 1, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sz, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sz + 1, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sz + sy, sy, sz);
-            s = s + mg_resid_in(xf, bf, c + sz + sy + 1, sy, sz);
-        } else {
-            s = mg_restrict_cell(gf, xf, bf, z, y, x);
-        }
+    const int nzc = gc.n[0], z0 = blockIdx.z * MG_RZC;
+    auto emit = [&](int z, T s) {
         const long long c = mg_at(gc, z, y, x);
-        bc[c] = T(0.5) * s;
-        xc[c] = T(0);
+        const T bv = T(0.5) * s;
+        bc[c] = bv;
+        yc[c] = mg_jacobi_from_zero(bv, omega, T(gc.idiag[mg_diag(gc, z, y, x)]));
+    };
+    if (z0 + MG_RZC > nzc) {   // last, partial chunk
+        for (int z = z0; z < nzc; ++z) emit(z, mg_restrict_cell(gf, xf, bf, z, y, x));
+        return;
+    }
+    // Full chunk, unrolled: the 2 x 2 children of each fine plane 2*z0-1 .. 2*(z0+RZC)
+    // and their x/y neighbours are loaded up front; residuals of the children in
+    // mgfor's neighbour order, summed in the order (k,j,i), (k,j,i+1), (k,j+1,i),
+    // (k,j+1,i+1), then the same at k+1.
+    const long long sy = gf.n[2], sz = (long long)gf.n[1] * gf.n[2];
+    const int i0 = 2 * x, j0 = 2 * y, k0 = 2 * z0;
+    const MgNb xl = mg_nb(i0, gf.n[2], gf.per[2], 1), xh = mg_nb(i0 + 1, gf.n[2], gf.per[2], 1);
+    const MgNb yl = mg_nb(j0, gf.n[1], gf.per[1], sy), yh = mg_nb(j0 + 1, gf.n[1], gf.per[1], sy);
+    const MgNb zl = mg_nb(k0, gf.n[0], gf.per[0], sz), zh = mg_nb(k0 + 2 * MG_RZC - 1, gf.n[0], gf.per[0], sz);
+    // wet x/y neighbours of the children (j0,i0), (j0,i1), (j1,i0), (j1,i1)
+    const int dxy[4] = {(int)xl.wm + 1 + (int)yl.wm + 1, 1 + (int)xh.wp + (int)yl.wm + 1,
+                        (int)xl.wm + 1 + 1 + (int)yh.wp, 1 + (int)xh.wp + 1 + (int)yh.wp};
+    const long long cb = mg_at(gf, k0, j0, i0);
+    constexpr int NP = 2 * MG_RZC + 2;   // fine planes k0-1 .. k0+2*RZC
+    T v[NP][4];
+    auto ld4 = [&](long long c, bool wet, T* o) {
+        o[0] = mg_ldw(xf, c, wet);
+        o[1] = mg_ldw(xf, c + 1, wet);
+        o[2] = mg_ldw(xf, c + sy, wet);
+        o[3] = mg_ldw(xf, c + sy + 1, wet);
+    };
+    ld4(cb + zl.om, zl.wm, v[0]);
+#pragma unroll
+    for (int q = 1; q < NP - 1; ++q) ld4(cb + (q - 1) * sz, true, v[q]);
+    ld4(cb + (2 * MG_RZC - 1) * sz + zh.op, zh.wp, v[NP - 1]);
+#pragma unroll
+    for (int zc = 0; zc < MG_RZC; ++zc) {
+        T s = T(0);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = 2 * zc + 1 + h;   // plane index in v
+            const long long c = cb + (q - 1) * sz;
+            const int dz = (q == 1 ? (int)zl.wm : 1) + (q == NP - 2 ? (int)zh.wp : 1);
+            // x/y ring of the plane
+            const T xm0 = mg_ldw(xf, c + xl.om, xl.wm), xm1 = mg_ldw(xf, c + sy + xl.om, xl.wm);
+            const T xp0 = mg_ldw(xf, c + 1 + xh.op, xh.wp), xp1 = mg_ldw(xf, c + sy + 1 + xh.op, xh.wp);
+            const T ym0 = mg_ldw(xf, c + yl.om, yl.wm), ym1 = mg_ldw(xf, c + 1 + yl.om, yl.wm);
+            const T yp0 = mg_ldw(xf, c + sy + yh.op, yh.wp), yp1 = mg_ldw(xf, c + sy + 1 + yh.op, yh.wp);
+            const T* p = v[q];
+            const T r00 = (bf[c] + T(dxy[0] + dz) * p[0]) - (((((xm0 + p[1]) + ym0) + p[2]) + v[q - 1][0]) + v[q + 1][0]);
+            const T r01 = (bf[c + 1] + T(dxy[1] + dz) * p[1]) -
+                          (((((p[0] + xp0) + ym1) + p[3]) + v[q - 1][1]) + v[q + 1][1]);
+            const T r10 = (bf[c + sy] + T(dxy[2] + dz) * p[2]) -
+                          (((((xm1 + p[3]) + p[0]) + yp0) + v[q - 1][2]) + v[q + 1][2]);
+            const T r11 = (bf[c + sy + 1] + T(dxy[3] + dz) * p[3]) -
+                          (((((p[2] + xp1) + p[1]) + yp1) + v[q - 1][3]) + v[q + 1][3]);
+            s = (h == 0) ? r00 : s + r00;
+            s = s + r01;
+            s = s + r10;
+            s = s + r11;
+        }
+        emit(z0 + zc, s);
     }
 }
 
@@ -225,39 +302,48 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
                                                              const T* __restrict__ xc) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_ZC;
-    const int z1 = min(z0 + MG_ZC, gf.n[0]) - 1;
     if (x >= gf.n[2] || y >= gf.n[1]) return;
-    const int ic = x >> 1, jc = y >> 1;
-    const int si = (x & 1) ? 1 : -1, sj = (y & 1) ? 1 : -1;
-    // fast path: all coarse neighbours of the block inside the coarse level
-    const int bx0 = blockIdx.x * MG_BX, by0 = blockIdx.y * MG_BY;
-    const bool inside = (bx0 >> 1) >= 1 && ((bx0 + MG_BX - 1) >> 1) + 1 <= gc.n[2] - 1 && (by0 >> 1) >= 1 &&
-                        ((by0 + MG_BY - 1) >> 1) + 1 <= gc.n[1] - 1 && (z0 >> 1) >= 1 && (z1 >> 1) + 1 <= gc.n[0] - 1;
-    const long long csy = gc.n[2], csz = (long long)gc.n[1] * gc.n[2];
-    for (int z = z0; z <= z1; ++z) {
-        const int kc = z >> 1, sk = (z & 1) ? 1 : -1;
-        T bpl, opl, pcoef;
-        if (inside) {
-            const long long c0 = mg_at(gc, kc, jc, ic);
-            auto plane = [&](long long c) -> T {
-                return ((T(9) * xc[c] + T(3) * xc[c + si]) + T(3) * xc[c + sj * csy]) + xc[c + sj * csy + si];
-            };
-            bpl = plane(c0);
-            opl = plane(c0 + sk * csz);
-            pcoef = T(gf.pcoef[7]);
-        } else {
-            auto plane = [&](int kk) -> T {
-                return ((T(9) * mg_rd(xc, gc, kk, jc, ic) + T(3) * mg_rd(xc, gc, kk, jc, ic + si)) +
-                        T(3) * mg_rd(xc, gc, kk, jc + sj, ic)) + mg_rd(xc, gc, kk, jc + sj, ic + si);
-            };
-            bpl = plane(kc);
-            opl = plane(kc + sk);
-            auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
-            pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
+    const int nzf = gf.n[0], z0 = blockIdx.z * MG_ZC;   // z0 even
+    if (z0 + MG_ZC > nzf) {   // last, partial chunk
+        for (int z = z0; z < nzf; ++z) {
+            const long long c = mg_at(gf, z, y, x);
+            xf[c] = xf[c] + mg_prolong_cell(gf, gc, xc, z, y, x);
         }
-        const long long c = mg_at(gf, z, y, x);
-        xf[c] = xf[c] + pcoef * (T(3) * bpl + opl);
+        return;
+    }
+    // Full chunk, unrolled: the in-plane 9-3-3-1 sums of the coarse planes z0/2-1 ..
+    // z0/2+ZC/2 (each used by two fine planes) are formed once; a coarse neighbour
+    // outside the level is the periodic image or 0.
+    const int ic = x >> 1, jc = y >> 1;
+    const long long csy = gc.n[2], csz = (long long)gc.n[1] * gc.n[2];
+    const MgNb cx = mg_nb(ic, gc.n[2], gc.per[2], 1), cy = mg_nb(jc, gc.n[1], gc.per[1], csy);
+    const long long ox = (x & 1) ? cx.op : cx.om, oy = (y & 1) ? cy.op : cy.om;
+    const bool wx = (x & 1) ? cx.wp : cx.wm, wy = (y & 1) ? cy.wp : cy.wm;
+    const int kc0 = z0 >> 1;
+    const MgNb zl = mg_nb(kc0, gc.n[0], gc.per[0], csz), zh = mg_nb(kc0 + MG_ZC / 2 - 1, gc.n[0], gc.per[0], csz);
+    const long long cc = mg_at(gc, kc0, jc, ic);
+    auto plane = [&](long long c, bool wet) -> T {
+        const T a = mg_ldw(xc, c, wet), b = mg_ldw(xc, c + ox, wet && wx);
+        const T d = mg_ldw(xc, c + oy, wet && wy), e = mg_ldw(xc, c + ox + oy, wet && wx && wy);
+        return ((T(9) * a + T(3) * b) + T(3) * d) + e;
+    };
+    constexpr int NP = MG_ZC / 2 + 2;
+    T P[NP];
+    P[0] = plane(cc + zl.om, zl.wm);
+#pragma unroll
+    for (int q = 1; q < NP - 1; ++q) P[q] = plane(cc + (q - 1) * csz, true);
+    P[NP - 1] = plane(cc + (MG_ZC / 2 - 1) * csz + zh.op, zh.wp);
+    const int bxy = (int)wx | ((int)wy << 1);
+    const T pc_wet = T(gf.pcoef[bxy | 4]), pc_lo = T(gf.pcoef[bxy | ((int)zl.wm << 2)]);
+    const T pc_hi = T(gf.pcoef[bxy | ((int)zh.wp << 2)]);
+    const long long c0 = mg_at(gf, z0, y, x), sz = (long long)gf.n[1] * gf.n[2];
+#pragma unroll
+    for (int k = 0; k < MG_ZC; ++k) {
+        const int m = (k >> 1) + 1;                  // plane of z>>1 in P
+        const T bpl = P[m], opl = P[(k & 1) ? m + 1 : m - 1];
+        const T pc = (k == 0) ? pc_lo : (k == MG_ZC - 1 ? pc_hi : pc_wet);
+        const long long c = c0 + k * sz;
+        xf[c] = xf[c] + pc * (T(3) * bpl + opl);
     }
 }
 
@@ -365,19 +451,46 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq(const MgGeom g, cons
                                                            const T* __restrict__ b, double* __restrict__ partial) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_ZC;
-    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
     double s = 0.0;
-    if (MODE == 1 && mg_block_inside(g, z0, z1, 1)) {
+    if (x < g.n[2] && y < g.n[1]) {
         const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
-        for (int z = z0; z <= z1; ++z) {
-            const double r = (double)mg_resid_in(v, b, mg_at(g, z, y, x), sy, sz);
-            s += r * r;
-        }
-    } else if (x < g.n[2] && y < g.n[1]) {
-        for (int z = z0; z <= z1; ++z) {
-            const double r = MODE == 0 ? (double)v[mg_at(g, z, y, x)] : (double)mg_resid(v, b, g, z, y, x);
-            s += r * r;
+        const long long c0 = mg_at(g, z0, y, x);
+        if (MODE == 0) {
+            for (int z = z0; z < min(z0 + MG_ZC, nz); ++z) {
+                const double r = (double)v[c0 + (z - z0) * sz];
+                s += r * r;
+            }
+        } else {
+            const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+            const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
+            auto res = [&](long long c, T zm, T x0, T zp, T dg) -> T {
+                return (b[c] + dg * x0) - (((((mg_ldw(v, c + nx.om, nx.wm) + mg_ldw(v, c + nx.op, nx.wp)) +
+                                              mg_ldw(v, c + ny.om, ny.wm)) + mg_ldw(v, c + ny.op, ny.wp)) + zm) + zp);
+            };
+            if (z0 + MG_ZC <= nz) {
+                const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+                T col[MG_ZC + 2];
+                col[0] = mg_ldw(v, c0 + lo.om, lo.wm);
+#pragma unroll
+                for (int k = 1; k <= MG_ZC; ++k) col[k] = v[c0 + (k - 1) * sz];
+                col[MG_ZC + 1] = mg_ldw(v, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+                const T d_mid = T(dxy + 2), d_lo = T(dxy + 1 + (int)lo.wm), d_hi = T(dxy + 1 + (int)hi.wp);
+#pragma unroll
+                for (int k = 0; k < MG_ZC; ++k) {
+                    const double r = (double)res(c0 + k * sz, col[k], col[k + 1], col[k + 2],
+                                                 k == 0 ? d_lo : (k == MG_ZC - 1 ? d_hi : d_mid));
+                    s += r * r;
+                }
+            } else {
+                for (int z = z0; z < nz; ++z) {
+                    const long long c = c0 + (z - z0) * sz;
+                    const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
+                    const double r = (double)res(c, mg_ldw(v, c + nzb.om, nzb.wm), v[c], mg_ldw(v, c + nzb.op, nzb.wp),
+                                                 T(dxy + (int)nzb.wm + (int)nzb.wp));
+                    s += r * r;
+                }
+            }
         }
     }
     block_partial(s, partial);
@@ -409,64 +522,60 @@ __device__ __forceinline__ float df_resid(float2 bc, float2 pc, float dg, const 
     return __fadd_rn(a2, rest);
 }
 
-// value of a float-pair level array one cell outside the interior at most: periodic
-// image, or 0 across a closed wall (branch-free, as mg_rd)
-__device__ __forceinline__ float2 mg_rd_df(const float2* __restrict__ a, const MgGeom& g, int z, int y, int x) {
-    bool ok = true;
-    int q[3] = {z, y, x};
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int n = g.n[k];
-        const bool lo = q[k] < 0, hi = q[k] >= n;
-        ok = ok && (g.per[k] || !(lo || hi));
-        q[k] = lo ? q[k] + n : (hi ? q[k] - n : q[k]);
-        q[k] = min(max(q[k], 0), n - 1);
-    }
-    const float2 v = a[((long long)q[0] * g.n[1] + q[1]) * g.n[2] + q[2]];
-    return ok ? v : make_float2(0.f, 0.f);
+// float-pair neighbour read with the wet flag of mg_nb (always loads, 0 when dry)
+__device__ __forceinline__ float2 mg_ldw_df(const float2* __restrict__ a, long long c, bool wet) {
+    const float2 v = a[c];
+    return wet ? v : make_float2(0.f, 0.f);
 }
 
 // residual of the float-pair solution: its sum of squares (for the stop test), the
-// float right-hand side of the next correction V-cycle and a zero initial correction.
-// The squares are summed in float per thread on r * scale, scale = sc[SC_SCALE] a power
-// of two near 1/rms(b) (k_mg_scale), so that they neither underflow nor overflow; each
-// block partial is unscaled in double.
+// float right-hand side r32 of the next correction V-cycle, and the first half-sweep
+// of that V-cycle from its zero initial correction, y32. The squares are summed in
+// float per thread on r * scale, scale = sc[SC_SCALE] a power of two near 1/rms(b)
+// (k_mg_scale), so that they neither underflow nor overflow; each block partial is
+// unscaled in double.
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, const float2* __restrict__ p,
                                                               const float2* __restrict__ b, float* __restrict__ r32,
-                                                              float* __restrict__ e32, const double* __restrict__ sc,
+                                                              float* __restrict__ y32, float omega,
+                                                              const double* __restrict__ sc,
                                                               double* __restrict__ partial) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_ZC;
-    const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
+    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
     const float scale = (float)sc[SC_SCALE];
     float s = 0.f;
-    if (mg_block_inside(g, z0, z1, 1)) {
+    if (x < g.n[2] && y < g.n[1]) {
         const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
-        long long c = mg_at(g, z0, y, x);
-        float2 pm = p[c - sz], p0 = p[c];
-        for (int z = z0; z <= z1; ++z, c += sz) {
-            const float2 pp = p[c + sz];
-            const float2 nb[6] = {p[c - 1], p[c + 1], p[c - sy], p[c + sy], pm, pp};
-            const float r = df_resid(b[c], p0, 6.f, nb);
+        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+        const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
+        const long long c0 = mg_at(g, z0, y, x);
+        auto cell = [&](long long c, float2 zm, float2 p0, float2 zp, int dg) {
+            const float2 nb[6] = {mg_ldw_df(p, c + nx.om, nx.wm), mg_ldw_df(p, c + nx.op, nx.wp),
+                                  mg_ldw_df(p, c + ny.om, ny.wm), mg_ldw_df(p, c + ny.op, ny.wp), zm, zp};
+            const float r = df_resid(b[c], p0, (float)dg, nb);
             r32[c] = r;
-            e32[c] = 0.f;
+            y32[c] = mg_jacobi_from_zero(r, omega, (float)g.idiag[dg]);
             const float rs = __fmul_rn(r, scale);
             s = __fmaf_rn(rs, rs, s);
-            pm = p0;
-            p0 = pp;
-        }
-    } else if (x < g.n[2] && y < g.n[1]) {
-        for (int z = z0; z <= z1; ++z) {
-            const long long c = mg_at(g, z, y, x);
-            const float2 nb[6] = {mg_rd_df(p, g, z, y, x - 1), mg_rd_df(p, g, z, y, x + 1),
-                                  mg_rd_df(p, g, z, y - 1, x), mg_rd_df(p, g, z, y + 1, x),
-                                  mg_rd_df(p, g, z - 1, y, x), mg_rd_df(p, g, z + 1, y, x)};
-            const float r = df_resid(b[c], p[c], (float)mg_diag(g, z, y, x), nb);
-            r32[c] = r;
-            e32[c] = 0.f;
-            const float rs = __fmul_rn(r, scale);
-            s = __fmaf_rn(rs, rs, s);
+        };
+        if (z0 + MG_ZC <= nz) {
+            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+            float2 col[MG_ZC + 2];
+            col[0] = mg_ldw_df(p, c0 + lo.om, lo.wm);
+#pragma unroll
+            for (int k = 1; k <= MG_ZC; ++k) col[k] = p[c0 + (k - 1) * sz];
+            col[MG_ZC + 1] = mg_ldw_df(p, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+#pragma unroll
+            for (int k = 0; k < MG_ZC; ++k)
+                cell(c0 + k * sz, col[k], col[k + 1], col[k + 2],
+                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == MG_ZC - 1 ? 1 + (int)hi.wp : 2)));
+        } else {
+            for (int z = z0; z < nz; ++z) {
+                const long long c = c0 + (z - z0) * sz;
+                const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
+                cell(c, mg_ldw_df(p, c + nzb.om, nzb.wm), p[c], mg_ldw_df(p, c + nzb.op, nzb.wp),
+                     dxy + (int)nzb.wm + (int)nzb.wp);
+            }
         }
     }
     block_partial((double)s * sc[SC_INVSCALE2], partial);
@@ -652,7 +761,9 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
 }
 
 template <typename T>
-static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
+// smoothing of level l: half-sweeps x -> y -> x; with from_y the first one was already
+// written into y by the kernel that set b from a zero solution
+static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64, bool from_y = false) {
     if (empty(mg, l)) return;
     MgGeom g = mgg(mg, l);
     const dim3 grd = grid_zc(g.n, MG_ZC);
@@ -661,8 +772,8 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64) {
     T* y = lvp<T>(mg, l, 3);
     const T om = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
-    note_launch(2);
-    k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr);
+    note_launch(from_y ? 1 : 2);
+    if (!from_y) k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr);
     if (acc_p64)
         k_mg_jacobi<T, true><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf));
     else
@@ -695,20 +806,24 @@ template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     const int L = mg->nlevels;
     const int B = mg->bottom;   // < L: levels B..L-1 in one block
+    // level 0 of a mixed-precision correction starts from zero: the residual kernel
+    // wrote its first half-sweep; every restricted level likewise gets it from the
+    // restriction
     for (int l = 0; l < L - 1 && l < B; ++l) {
-        smooth<T>(mg, l, st, false);
+        smooth<T>(mg, l, st, false, l > 0 || mixed);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 9, st);
             note_launch();
             k_mg_restrict<T><<<grid_zc(gc.n, MG_RZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
-                                                                    lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 1));
+                                                                    lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 3),
+                                                                    T(mg->omega));
         }
     }
     if (B < L)
         bottom<T>(mg, st);
     else
-        smooth<T>(mg, L - 1, st, L == 1 && mixed);
+        smooth<T>(mg, L - 1, st, L == 1 && mixed, L > 1 || mixed);
     for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -765,7 +880,7 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     note_launch(2);
     k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
                                         reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
-                                        lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 1), sc, part);
+                                        lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
     k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
 }
 
