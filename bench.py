@@ -260,9 +260,13 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
 
 
 # ------------------------------------------------------------------ timed runs
-def time_steps(nyl, K, W, stream):
+def time_steps(nyl, K, W, stream, graphs=True):
+    """K timed steps of model.forward after W warm-up steps; with graphs, forward
+    replays its captured fixed-dt step (the path Nyles.run takes), without them every
+    step is launched eagerly with the multigrid stop test on the host."""
     import torch
     m = nyl.model
+    m.use_graphs = graphs
     for _ in range(W):
         m.forward(0.0, nyl.dt0)
     torch.cuda.synchronize()
@@ -288,14 +292,14 @@ def profile_phases(nyl, steps):
     from nyles_gb300 import _native as nat
     m = nyl.model
     lib = nat.lib()
-    nat.check(lib.nyles_model_profile(m._h, 1))
+    m.profile(True)
     for _ in range(steps):
         m.forward(0.0, nyl.dt0)
     torch.cuda.synchronize()
     ms = (ctypes.c_double * nat.NPHASE)()
     cnt = (ctypes.c_longlong * nat.NPHASE)()
     nat.check(lib.nyles_model_profile_read(m._h, ms, cnt, nat.NPHASE))
-    nat.check(lib.nyles_model_profile(m._h, 0))
+    m.profile(False)
     return {nat.PHASES[i]: {"ms": ms[i], "count": cnt[i]} for i in range(nat.NPHASE)}
 
 
@@ -507,9 +511,14 @@ def main():
                 ms = float(t.item())
             launches_total += launches
             res = {"ms_per_step": ms / a.steps, "value": world * cells * a.steps / (ms * 1e-3),
-                   "mean_vcycles_per_solve": vc, "kernel_launches": launches}
+                   "mean_vcycles_per_solve": vc, "kernel_launches": launches, "path": "graph replay"}
+            ems_eager, _, _ = time_steps(nyl, a.steps, 1, stream, graphs=False)
+            res["eager"] = {"ms_per_step": ems_eager / a.steps,
+                            "value": world * cells * a.steps / (ems_eager * 1e-3),
+                            "note": "same steps launched one kernel at a time, multigrid stop test on the host"}
             if a.profile_steps > 0:
                 res["phases"] = profile_phases(nyl, a.profile_steps)
+            nyl.model.use_graphs = True
             if not a.no_e2e:
                 ems, bts = time_e2e(nyl, max(1, a.steps // 2), 1)
                 k = max(1, a.steps // 2)
@@ -523,7 +532,8 @@ def main():
     r = results[main_prec]
     out.update({"value": r["value"], "ms_per_step": r["ms_per_step"],
                 "dtype": "f64" if main_prec == "fp64" else "f32+f64", "clocks": clocks,
-                "gpu_launches": launches_total, "mg": {"mean_vcycles_per_solve": r["mean_vcycles_per_solve"]}})
+                "gpu_launches": launches_total, "mg": {"mean_vcycles_per_solve": r["mean_vcycles_per_solve"]},
+                "path": r["path"], "eager": r["eager"]})
     if "e2e" in r:
         out["e2e"] = r["e2e"]
     # roofline of the dominant kernel (largest share of device time)
@@ -540,7 +550,7 @@ def main():
         mr = results["mixed"]
         out["mixed"] = {"value": mr["value"], "ms_per_step": mr["ms_per_step"],
                         "speedup_vs_fp64": mr["value"] / r["value"],
-                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"]}
+                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"], "eager": mr["eager"]}
         if "e2e" in mr:
             out["mixed"]["e2e"] = mr["e2e"]
         if "phases" in mr:

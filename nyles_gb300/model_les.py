@@ -91,6 +91,12 @@ class LES(object):
         self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9))
         self.forcing = None
         self.stats = []
+        # graph replay of fixed-dt steps (see forward)
+        self.use_graphs = bool(gpu.get("graphs", True))
+        self.graph = None
+        self._last_dt = None
+        self._first_step_pending = param["timestepping"] == "LFAM3"
+        self._profiling = False
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -133,11 +139,32 @@ class LES(object):
         nat.check(fn(ctypes.byref(self.desc), fields, ds, 1 if last else 0, nat.stream_ptr()))
 
     def forward(self, t, dt):
-        """One time step (core/model_les.py:147-149). Returns the blow-up flag."""
+        """One time step (core/model_les.py:147-149). Returns the blow-up flag.
+
+        With graphs on (gpu parameter `graphs`), the second consecutive call with the same
+        dt captures the step into a CUDA graph, and every later call with that dt replays
+        it: the same kernels, with the multigrid stop test on the device instead of one
+        host round trip per V-cycle. A call with another dt runs eagerly."""
         if self.forced and self.forcing is not None:
             raise NotImplementedError("user forcing hooks are not supported on the GPU path")
-        nat.check(self.lib.nyles_model_forward(self._h, float(t), float(dt), nat.stream_ptr()))
+        dt = float(dt)
+        if self.use_graphs and not self._profiling and not self._first_step_pending:
+            if self.graph == (dt, 1):
+                self.replay()
+                return False
+            if self._last_dt == dt:
+                self.capture_graph(dt, 1)
+                self.replay()
+                return False
+        self._last_dt = dt
+        nat.check(self.lib.nyles_model_forward(self._h, float(t), dt, nat.stream_ptr()))
+        self._first_step_pending = False
         return False
+
+    def profile(self, enable=True):
+        """Per-phase CUDA-event timing of eager steps (graph replay is off meanwhile)."""
+        self._profiling = bool(enable)
+        nat.check(self.lib.nyles_model_profile(self._h, 1 if enable else 0))
 
     def capture_graph(self, dt, nsteps=1):
         """Record `nsteps` time steps with fixed `dt` into one CUDA graph (the multigrid
@@ -161,6 +188,8 @@ class LES(object):
 
     def reset_timescheme(self):
         nat.check(self.lib.nyles_model_reset_scheme(self._h))
+        self._first_step_pending = self.param["timestepping"] == "LFAM3"
+        self._last_dt = None
 
 
 class Euler3d(LES):

@@ -266,8 +266,8 @@ class ServingEngine:
 
 
 def run_sequential(requests, precision="fp64", mg_tol=1e-6, device=None, keep_states=False):
-    """Baseline: the same runs one at a time, eager stepping (no graph), in arrival
-    order; a run starts at max(arrival, end of the previous run)."""
+    """Baseline: the same runs one at a time through model.forward (by default FP64),
+    in arrival order; a run starts at max(arrival, end of the previous run)."""
     results, states = [], {}
     clock = 0.0
     for req in sorted(requests, key=lambda r: r.arrival):

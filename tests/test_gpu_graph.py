@@ -23,13 +23,39 @@ CASES = [
 ]
 
 
-def _model(cfg, kind, seed):
+def _model(cfg, kind, seed, graphs=False):
     from nyles_gb300.nyles import Nyles
     nyl = Nyles(helpers.make_params(**cfg))
+    nyl.model.use_graphs = graphs
     for k, v in helpers.seeded_state(nyl, kind, seed).items():
         nyl.model.state.get(k).view("i")[...] = torch.from_numpy(v)
     nyl.model.diagnose_var(nyl.model.state)
     return nyl
+
+
+def _assert_same_state(a, b):
+    for s in a.model.state.toc:
+        for comp in (["i", "j", "k"] if a.model.state.toc[s] != "scalar" else [None]):
+            name = s if comp is None else s + "_" + comp
+            np.testing.assert_array_equal(a.model.state.get(name).view("i").cpu().numpy(),
+                                          b.model.state.get(name).view("i").cpu().numpy(), err_msg=name)
+
+
+@pytest.mark.parametrize("k", [0, 2, 3])
+def test_forward_switches_to_graph_replay(k):
+    """model.forward with graphs on: eager, then capture on the second call with the
+    same dt, replay after; a new dt runs eagerly. Same bits as eager stepping."""
+    cfg, kind, _ = CASES[k]
+    dt = cfg["dt"]
+    eager = _model(cfg, kind, 70 + k)
+    auto = _model(cfg, kind, 70 + k, graphs=True)
+    for dts in (dt, dt, dt, 0.5 * dt, dt, dt):
+        eager.model.forward(0.0, dts)
+        auto.model.forward(0.0, dts)
+        assert auto.model.mg_stats()["nite"] == eager.model.mg_stats()["nite"]
+    assert auto.model.graph == (dt, 1)
+    torch.cuda.synchronize()
+    _assert_same_state(auto, eager)
 
 
 @pytest.mark.parametrize("k", range(len(CASES)))
@@ -52,8 +78,4 @@ def test_graph_replay_equals_eager(k):
         nite_g.append(graph.model.mg_stats()["nite"])
     assert nite_g == nite_e[per_graph - 1::per_graph]
     assert graph.model.mg_stats()["vcycles"] == eager.model.mg_stats()["vcycles"]
-    for s in graph.model.state.toc:
-        for comp in (["i", "j", "k"] if graph.model.state.toc[s] != "scalar" else [None]):
-            a = graph.model.state.get(s if comp is None else s + "_" + comp).view("i").cpu().numpy()
-            b = eager.model.state.get(s if comp is None else s + "_" + comp).view("i").cpu().numpy()
-            np.testing.assert_array_equal(a, b, err_msg="%s %s" % (s, comp))
+    _assert_same_state(graph, eager)
