@@ -128,6 +128,41 @@ __device__ __forceinline__ double weno5<double>(double qmm, double qm, double q0
     return (A * qi1 + B * qi2 + C * qi3) / (A + B + C);
 }
 
+// Single precision (mixed-precision path): the four-division form with the hardware
+// reciprocal-based division (__fdividef, within 2 ulp): every denominator here is at
+// least 1e-14 or 1e-16 (eps) and far below 2^126, the limit of its accurate range, and
+// the weights only scale the stencils.
+template <>
+__device__ __forceinline__ float weno3<float>(float qm, float q0, float qp) {
+    typedef WenoK<float> K;
+    const float qi1 = (-qm + 3.f * q0) * 0.5f;
+    const float qi2 = (q0 + qp) * 0.5f;
+    const float d1 = q0 - qm, d2 = qp - q0;
+    const float beta1 = d1 * d1, beta2 = d2 * d2;
+    const float tau = fabsf(beta2 - beta1);
+    const float w1 = 1.f + __fdividef(tau, beta1 + K::eps3());
+    const float w2 = (1.f + __fdividef(tau, beta2 + K::eps3())) * 2.f;
+    return __fdividef(w1 * qi1 + w2 * qi2, w1 + w2);
+}
+template <>
+__device__ __forceinline__ float weno5<float>(float qmm, float qm, float q0, float qp, float qpp) {
+    typedef WenoK<float> K;
+    const float qi1 = K::c13() * qmm - K::c76() * qm + K::c116() * q0;
+    const float qi2 = -(K::c16() * qm) + K::c56() * q0 + K::c13() * qp;
+    const float qi3 = K::c13() * q0 + K::c56() * qp - K::c16() * qpp;
+    const float a1 = qmm - 2.f * qm + q0, b1 = qmm - 4.f * qm + 3.f * q0;
+    const float a2 = qm - 2.f * q0 + qp, b2 = qm - qp;
+    const float a3 = q0 - 2.f * qp + qpp, b3 = 3.f * q0 - 4.f * qp + qpp;
+    const float beta1 = K::k1() * (a1 * a1) + 0.25f * (b1 * b1);
+    const float beta2 = K::k1() * (a2 * a2) + 0.25f * (b2 * b2);
+    const float beta3 = K::k1() * (a3 * a3) + 0.25f * (b3 * b3);
+    const float tau5 = fabsf(beta1 - beta3);
+    const float w1 = 1.f + __fdividef(tau5, beta1 + K::eps5());
+    const float w2 = 6.f * (1.f + __fdividef(tau5, beta2 + K::eps5()));
+    const float w3 = 3.f * (1.f + __fdividef(tau5, beta3 + K::eps5()));
+    return __fdividef(w1 * qi1 + w2 * qi2 + w3 * qi3, w1 + w2 + w3);
+}
+
 // Value of core/weno.f90:106-153 `flux1d` at index i (0-based) of a line of length n
 // (n >= 5), given the velocity u at i and an accessor Q(j) for the advected quantity.
 // Branch precedence follows the Fortran statement order (later statements win).

@@ -355,8 +355,9 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
 // the restriction that produced b); output: x of level l0. The per-cell arithmetic is
 // that of the grid kernels' ghost paths.
 constexpr int MG_BOTTOM_MAXLEV = 12;
-constexpr int MG_BOTTOM_THREADS = 512;
 constexpr size_t MG_BOTTOM_SMEM = 200 * 1024;
+template <typename T> struct MgBottomThreads { static constexpr int n = 1024; };
+template <> struct MgBottomThreads<double> { static constexpr int n = 512; };   // register budget
 
 template <typename T>
 struct MgBottom {
@@ -370,24 +371,47 @@ struct MgBottom {
 
 __device__ __forceinline__ int mg_vol(const MgGeom& g) { return g.n[0] * g.n[1] * g.n[2]; }
 
+// Visit every cell of a level: threads take (x, y) columns, split in z when the block
+// has more threads than the level has columns; f(z, y, x, nx, ny) gets the column's
+// x/y neighbours.
+template <typename F>
+__device__ __forceinline__ void bottom_cells(const MgGeom& g, F f) {
+    const int ncol = g.n[1] * g.n[2], nz = g.n[0];
+    if (ncol == 0 || nz == 0) return;
+    const int groups = max(1, (int)blockDim.x / ncol);
+    const int zc = (nz + groups - 1) / groups;
+    for (int t = threadIdx.x; t < ncol * groups; t += blockDim.x) {
+        const int col = t % ncol, grp = t / ncol;
+        const int x = col % g.n[2], y = col / g.n[2];
+        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], g.n[2]);
+        const int ze = min(nz, (grp + 1) * zc);
+        for (int z = grp * zc; z < ze; ++z) f(z, y, x, nx, ny);
+    }
+}
+
+// one half-sweep in -> out over a level held in shared memory
 template <typename T>
-__device__ __forceinline__ void bottom_smooth(const MgGeom& g, T* x, const T* b, T* y, T cff1, T om) {
-    const int vol = mg_vol(g);
-    if (vol == 0) return;
-    for (int q = threadIdx.x; q < vol; q += blockDim.x) {
-        const int xx = q % g.n[2], r = q / g.n[2];
-        y[q] = mg_jacobi_cell(g, x, b, r / g.n[1], r % g.n[1], xx, cff1, om);
-    }
-    __syncthreads();
-    for (int q = threadIdx.x; q < vol; q += blockDim.x) {
-        const int xx = q % g.n[2], r = q / g.n[2];
-        x[q] = mg_jacobi_cell(g, y, b, r / g.n[1], r % g.n[1], xx, cff1, om);
-    }
+__device__ __forceinline__ void bottom_sweep(const MgGeom& g, const T* in, const T* b, T* out, T cff1, T om) {
+    const long long sz = (long long)g.n[1] * g.n[2];
+    bottom_cells(g, [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
+        const long long c = mg_at(g, z, y, x);
+        const MgNb nzb = mg_nb(z, g.n[0], g.per[0], sz);
+        const T idg = T(g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp]);
+        const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) + mg_ldw(in, c + ny.om, ny.wm)) +
+                      mg_ldw(in, c + ny.op, ny.wp)) + mg_ldw(in, c + nzb.om, nzb.wm)) + mg_ldw(in, c + nzb.op, nzb.wp);
+        out[c] = cff1 * in[c] + om * (s - b[c]) * idg;
+    });
     __syncthreads();
 }
 
+// 1/diag of a cell from its column's x/y neighbours and its z position
+__device__ __forceinline__ double bottom_idiag(const MgGeom& g, int z, const MgNb& nx, const MgNb& ny) {
+    const MgNb nzb = mg_nb(z, g.n[0], g.per[0], 0);
+    return g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp];
+}
+
 template <typename T>
-__global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const MgBottom<T> a) {
+__global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const MgBottom<T> a) {
     extern __shared__ __align__(16) unsigned char mg_smem[];
     T* sm = reinterpret_cast<T*>(mg_smem);
     const T om = a.omega, cff1 = T(1) - om;
@@ -395,37 +419,43 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const MgBottom<
     auto X = [&](int l) { return sm + a.off[l]; };
     auto Bv = [&](int l) { return sm + a.off[l] + mg_vol(a.g[l]); };
     auto Y = [&](int l) { return sm + a.off[l] + 2 * mg_vol(a.g[l]); };
-    const int v0 = mg_vol(a.g[0]);
-    for (int q = threadIdx.x; q < v0; q += blockDim.x) {
-        X(0)[q] = T(0);
-        Bv(0)[q] = a.bg[q];
-    }
+    // level l0 starts from x = 0: its first half-sweep is y = from_zero(b)
+    bottom_cells(a.g[0], [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
+        const long long c = mg_at(a.g[0], z, y, x);
+        const T bv = a.bg[c];
+        Bv(0)[c] = bv;
+        Y(0)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(a.g[0], z, nx, ny)));
+    });
     __syncthreads();
     for (int l = 0; l < L - 1; ++l) {
-        bottom_smooth(a.g[l], X(l), Bv(l), Y(l), cff1, om);
+        if (mg_vol(a.g[l]) == 0) break;
+        bottom_sweep(a.g[l], Y(l), Bv(l), X(l), cff1, om);   // second half of the pre-smoothing
         const MgGeom& gc = a.g[l + 1];
-        const int vc = mg_vol(gc);
-        if (vc == 0) continue;
-        for (int q = threadIdx.x; q < vc; q += blockDim.x) {
-            const int xx = q % gc.n[2], r = q / gc.n[2];
-            Bv(l + 1)[q] = T(0.5) * mg_restrict_cell(a.g[l], X(l), Bv(l), r / gc.n[1], r % gc.n[1], xx);
-            X(l + 1)[q] = T(0);
-        }
+        if (mg_vol(gc) == 0) break;
+        // restriction; the coarse level starts from zero, so its first half-sweep is written too
+        bottom_cells(gc, [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
+            const long long c = mg_at(gc, z, y, x);
+            const T bv = T(0.5) * mg_restrict_cell(a.g[l], X(l), Bv(l), z, y, x);
+            Bv(l + 1)[c] = bv;
+            Y(l + 1)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(gc, z, nx, ny)));
+        });
         __syncthreads();
     }
-    bottom_smooth(a.g[L - 1], X(L - 1), Bv(L - 1), Y(L - 1), cff1, om);
+    if (mg_vol(a.g[L - 1]) > 0) bottom_sweep(a.g[L - 1], Y(L - 1), Bv(L - 1), X(L - 1), cff1, om);
     for (int l = L - 2; l >= 0; --l) {
         const MgGeom& gf = a.g[l];
+        if (mg_vol(gf) == 0) continue;
         if (mg_vol(a.g[l + 1]) > 0) {
-            const int vf = mg_vol(gf);
-            for (int q = threadIdx.x; q < vf; q += blockDim.x) {
-                const int xx = q % gf.n[2], r = q / gf.n[2];
-                X(l)[q] = X(l)[q] + mg_prolong_cell(gf, a.g[l + 1], X(l + 1), r / gf.n[1], r % gf.n[1], xx);
-            }
+            bottom_cells(gf, [&](int z, int y, int x, const MgNb&, const MgNb&) {
+                const long long c = mg_at(gf, z, y, x);
+                X(l)[c] = X(l)[c] + mg_prolong_cell(gf, a.g[l + 1], X(l + 1), z, y, x);
+            });
             __syncthreads();
         }
-        bottom_smooth(gf, X(l), Bv(l), Y(l), cff1, om);
+        bottom_sweep(gf, X(l), Bv(l), Y(l), cff1, om);
+        bottom_sweep(gf, Y(l), Bv(l), X(l), cff1, om);
     }
+    const int v0 = mg_vol(a.g[0]);
     for (int q = threadIdx.x; q < v0; q += blockDim.x) a.xg[q] = X(0)[q];
 }
 
@@ -799,7 +829,7 @@ static void bottom(MgImpl* mg, cudaStream_t st) {
     a.omega = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch();
-    k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, mg->bottom_smem, st>>>(a);
+    k_mg_bottom<T><<<1, MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a);
 }
 
 template <typename T>
