@@ -159,6 +159,11 @@ int nyles_model_vfwork(NylesModel* m, const long long* box, double* worksum, voi
 int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats);
 /* a fresh LFAM3 start (its first step is Euler forward, core/timescheme.py:129-140) */
 int nyles_model_reset_scheme(NylesModel* m);
+/* LFAM3's `first` flag (core/timescheme.py:94, the Euler first step still to take),
+ * read and restored with a snapshot of the device state. No counterpart in the
+ * reference (its LFAM3 state is not checkpointable). */
+int nyles_model_get_first_step(const NylesModel* m, int* pending);
+int nyles_model_set_first_step(NylesModel* m, int pending);
 
 /* CUDA-graph replay of nsteps time steps of LES.forward with a fixed dt (no counterpart
  * in the reference, whose step is a Python loop). The multigrid stop test runs on the

@@ -93,6 +93,8 @@ SIGNATURES = {
     "nyles_model_vfwork": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_mg_stats": (_I, [_P, ctypes.POINTER(NylesMgStats)]),
     "nyles_model_reset_scheme": (_I, [_P]),
+    "nyles_model_get_first_step": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "nyles_model_set_first_step": (_I, [_P, ctypes.c_int]),
     "nyles_model_capture": (_I, [_P, _D, _I]),
     "nyles_model_graph_launch": (_I, [_P, _P]),
     "nyles_model_graph_release": (_I, [_P]),

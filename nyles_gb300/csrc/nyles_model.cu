@@ -348,6 +348,18 @@ int nyles_model_reset_scheme(NylesModel* m) {
     return NYLES_OK;
 }
 
+int nyles_model_get_first_step(const NylesModel* m, int* pending) {
+    if (!m || !pending) { set_error("null argument"); return NYLES_BAD_ARG; }
+    *pending = m->lf_first ? 1 : 0;
+    return NYLES_OK;
+}
+
+int nyles_model_set_first_step(NylesModel* m, int pending) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    m->lf_first = pending != 0;
+    return NYLES_OK;
+}
+
 int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
     if (!m || !stats) { set_error("null argument"); return NYLES_BAD_ARG; }
     *stats = m->mg.stats;

@@ -85,6 +85,8 @@ class LES(object):
         self.workspace = torch.zeros(nbytes.value + 256, dtype=torch.uint8, device=self.device)
         ws = self.workspace.data_ptr()
         ws = (ws + 255) & ~255
+        off = ws - self.workspace.data_ptr()
+        self._ws_used = self.workspace[off:off + nbytes.value]   # the aligned bytes the library uses
         self._fields = nat.ptr_array([s.data_ptr() for s in self.state.scalars()])
         self._regs = nat.ptr_array(self.timescheme.register_pointers())
         nat.check(self.lib.nyles_model_bind(h, self._fields, self._regs, ctypes.c_void_p(ws)))
@@ -185,6 +187,30 @@ class LES(object):
         out = ctypes.c_double()
         nat.check(self.lib.nyles_model_max_U2(self._h, ctypes.byref(out), nat.stream_ptr()))
         return out.value
+
+    def snapshot(self):
+        """Host copy of everything a continued run depends on: all state fields, the
+        time-scheme registers, the multigrid workspace (warm-started solution) and the
+        LFAM3 first-step flag. `restore` on a model built from the same parameters
+        continues bit for bit."""
+        torch.cuda.synchronize(self.device)
+        first = ctypes.c_int()
+        nat.check(self.lib.nyles_model_get_first_step(self._h, ctypes.byref(first)))
+        return {"state": self.state.storage.cpu(), "registers": self.timescheme.storage.cpu(),
+                "workspace": self._ws_used.cpu(), "first_step": first.value}
+
+    def restore(self, snap):
+        for key, dst in (("state", self.state.storage), ("registers", self.timescheme.storage),
+                         ("workspace", self._ws_used)):
+            src = snap[key]
+            if tuple(src.shape) != tuple(dst.shape) or src.dtype != dst.dtype:
+                raise ValueError("snapshot %s does not match this model (%s %s vs %s %s)"
+                                 % (key, tuple(src.shape), src.dtype, tuple(dst.shape), dst.dtype))
+            dst.copy_(src)
+        nat.check(self.lib.nyles_model_set_first_step(self._h, int(snap["first_step"])))
+        self._first_step_pending = bool(snap["first_step"])
+        self._last_dt = None
+        torch.cuda.synchronize(self.device)
 
     def reset_timescheme(self):
         nat.check(self.lib.nyles_model_reset_scheme(self._h))
