@@ -430,6 +430,21 @@ def run_reference(a, rank, world):
     print(json.dumps(line))
 
 
+def job_time_ms(ms, dist=None, device="cpu"):
+    """Time of the whole job: the maximum over ranks of each rank's timed region."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(cells, steps, ms, world):
+    """Whole-job cell-steps/s: every replica advances `cells` cells by `steps` steps."""
+    return world * cells * steps / (ms * 1e-3)
+
+
 def make_config(n, world):
     return {"workload": "rayleigh_taylor_%d^3_perio_xy_rk3" % n, "grid": [n, n, n], "box": [1, 1, 1],
             "dt": 1e-3, "mg_tol_sq_ratio": 1e-20, "parallelism": "replicas" if world > 1 else "single",
@@ -505,12 +520,9 @@ def main():
                 dist.barrier()
             torch.cuda.synchronize()
             ms, launches, vc = time_steps(nyl, a.steps, a.warmup, stream)
-            if dist:
-                t = torch.tensor([ms], device="cuda")
-                dist.all_reduce(t, op=dist.ReduceOp.MAX)
-                ms = float(t.item())
+            ms = job_time_ms(ms, dist, "cuda")
             launches_total += launches
-            res = {"ms_per_step": ms / a.steps, "value": world * cells * a.steps / (ms * 1e-3),
+            res = {"ms_per_step": ms / a.steps, "value": job_value(cells, a.steps, ms, world),
                    "mean_vcycles_per_solve": vc, "kernel_launches": launches, "path": "graph replay"}
             ems_eager, _, _ = time_steps(nyl, a.steps, 1, stream, graphs=False)
             res["eager"] = {"ms_per_step": ems_eager / a.steps,

@@ -147,7 +147,7 @@ def _mg_rhs(om, b, topo_name):
     om.set(2, full)
 
 
-@pytest.mark.parametrize("shape", [(4, 4, 4), (16, 8, 4), (8, 16, 8), (32, 16, 16)])
+@pytest.mark.parametrize("shape", [(4, 4, 4), (16, 8, 4), (8, 16, 8), (32, 16, 16), (64, 32, 32), (48, 48, 48)])
 @pytest.mark.parametrize("topo", MG_TOPOLOGIES)
 def test_multigrid_vcycles_match_oracle(topo, shape):
     """Each of the first V-cycles (smoothing, residual+restriction, prolongation on
@@ -195,3 +195,27 @@ def test_multigrid_solver_matches_oracle():
         assert st["nite"] == n_o
         xo = om.get(1)[3:-3, 3:-3, 3:-3]
         assert helpers.relerr(x.cpu().numpy(), xo) < 1e-12, topo_name
+
+
+@pytest.mark.parametrize("topo", MG_TOPOLOGIES)
+def test_mixed_multigrid_matches_fp64_solve(topo):
+    """Float-pair refinement with FP32 V-cycles reaches the same tolerance in the same
+    number of V-cycles as the FP64 solver, and the same solution."""
+    from nyles_gb300.multigrid import MG
+    topo_name, _ = topo
+    nx, ny, nz = (64, 32, 32) if topo_name != "perio_xyz" else (32, 32, 32)
+    rng = np.random.Generator(np.random.PCG64(17))
+    b = rng.standard_normal((nz, ny, nx))
+    b -= b.mean()
+    sols, nites = {}, {}
+    for prec in ("fp64", "mixed"):
+        mg = MG(nx, ny, nz, topo_name, precision=prec)
+        mg.set_params(1e-20, 60, 0.9)
+        x, st = mg.solve(b)
+        assert st["converged"], (prec, st)
+        sols[prec] = x.double().cpu().numpy()
+        nites[prec] = st["nite"]
+    assert abs(nites["mixed"] - nites["fp64"]) <= 1, nites
+    if topo_name == "perio_xyz":   # the solution is defined up to a constant
+        sols = {k: v - v.mean() for k, v in sols.items()}
+    assert helpers.relerr(sols["mixed"], sols["fp64"]) < 1e-8
