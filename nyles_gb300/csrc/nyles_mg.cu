@@ -35,6 +35,7 @@ enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE 
 
 constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
 constexpr int MG_RZC = 2;                          // restriction (coarse z per thread)
+constexpr int MG_DFZC = 8;                         // float-pair residual
 
 __device__ __forceinline__ long long mg_at(const MgGeom& g, int z, int y, int x) {
     return ((long long)z * g.n[1] + y) * g.n[2] + x;
@@ -327,6 +328,10 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
         const T d = mg_ldw(xc, c + oy, wet && wy), e = mg_ldw(xc, c + ox + oy, wet && wx && wy);
         return ((T(9) * a + T(3) * b) + T(3) * d) + e;
     };
+    const long long c0 = mg_at(gf, z0, y, x), sz = (long long)gf.n[1] * gf.n[2];
+    T xv[MG_ZC];   // the fine values, loaded together with the coarse ones
+#pragma unroll
+    for (int k = 0; k < MG_ZC; ++k) xv[k] = xf[c0 + k * sz];
     constexpr int NP = MG_ZC / 2 + 2;
     T P[NP];
     P[0] = plane(cc + zl.om, zl.wm);
@@ -336,14 +341,12 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
     const int bxy = (int)wx | ((int)wy << 1);
     const T pc_wet = T(gf.pcoef[bxy | 4]), pc_lo = T(gf.pcoef[bxy | ((int)zl.wm << 2)]);
     const T pc_hi = T(gf.pcoef[bxy | ((int)zh.wp << 2)]);
-    const long long c0 = mg_at(gf, z0, y, x), sz = (long long)gf.n[1] * gf.n[2];
 #pragma unroll
     for (int k = 0; k < MG_ZC; ++k) {
         const int m = (k >> 1) + 1;                  // plane of z>>1 in P
         const T bpl = P[m], opl = P[(k & 1) ? m + 1 : m - 1];
         const T pc = (k == 0) ? pc_lo : (k == MG_ZC - 1 ? pc_hi : pc_wet);
-        const long long c = c0 + k * sz;
-        xf[c] = xf[c] + pc * (T(3) * bpl + opl);
+        xf[c0 + k * sz] = xv[k] + pc * (T(3) * bpl + opl);
     }
 }
 
@@ -371,6 +374,25 @@ struct MgBottom {
 
 __device__ __forceinline__ int mg_vol(const MgGeom& g) { return g.n[0] * g.n[1] * g.n[2]; }
 
+// neighbours along one direction with 32-bit offsets (levels held in shared memory)
+struct MgNbI {
+    int om, op;
+    bool wm, wp;
+};
+__device__ __forceinline__ MgNbI mg_nbi(int c, int n, int per, int stride) {
+    MgNbI r;
+    r.wm = c > 0 || per;
+    r.wp = c < n - 1 || per;
+    r.om = c > 0 ? -stride : (per ? (n - 1) * stride : 0);
+    r.op = c < n - 1 ? stride : (per ? -(n - 1) * stride : 0);
+    return r;
+}
+template <typename T>
+__device__ __forceinline__ T sm_ldw(const T* a, int c, bool wet) {
+    const T v = a[c];
+    return wet ? v : T(0);
+}
+
 // Visit every cell of a level: threads take (x, y) columns, split in z when the block
 // has more threads than the level has columns; f(z, y, x, nx, ny) gets the column's
 // x/y neighbours.
@@ -383,7 +405,7 @@ __device__ __forceinline__ void bottom_cells(const MgGeom& g, F f) {
     for (int t = threadIdx.x; t < ncol * groups; t += blockDim.x) {
         const int col = t % ncol, grp = t / ncol;
         const int x = col % g.n[2], y = col / g.n[2];
-        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], g.n[2]);
+        const MgNbI nx = mg_nbi(x, g.n[2], g.per[2], 1), ny = mg_nbi(y, g.n[1], g.per[1], g.n[2]);
         const int ze = min(nz, (grp + 1) * zc);
         for (int z = grp * zc; z < ze; ++z) f(z, y, x, nx, ny);
     }
@@ -392,22 +414,92 @@ __device__ __forceinline__ void bottom_cells(const MgGeom& g, F f) {
 // one half-sweep in -> out over a level held in shared memory
 template <typename T>
 __device__ __forceinline__ void bottom_sweep(const MgGeom& g, const T* in, const T* b, T* out, T cff1, T om) {
-    const long long sz = (long long)g.n[1] * g.n[2];
-    bottom_cells(g, [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
-        const long long c = mg_at(g, z, y, x);
-        const MgNb nzb = mg_nb(z, g.n[0], g.per[0], sz);
+    const int sz = g.n[1] * g.n[2];
+    bottom_cells(g, [&](int z, int y, int x, const MgNbI& nx, const MgNbI& ny) {
+        const int c = (z * g.n[1] + y) * g.n[2] + x;
+        const MgNbI nzb = mg_nbi(z, g.n[0], g.per[0], sz);
         const T idg = T(g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp]);
-        const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) + mg_ldw(in, c + ny.om, ny.wm)) +
-                      mg_ldw(in, c + ny.op, ny.wp)) + mg_ldw(in, c + nzb.om, nzb.wm)) + mg_ldw(in, c + nzb.op, nzb.wp);
+        const T s = ((((sm_ldw(in, c + nx.om, nx.wm) + sm_ldw(in, c + nx.op, nx.wp)) + sm_ldw(in, c + ny.om, ny.wm)) +
+                      sm_ldw(in, c + ny.op, ny.wp)) + sm_ldw(in, c + nzb.om, nzb.wm)) + sm_ldw(in, c + nzb.op, nzb.wp);
         out[c] = cff1 * in[c] + om * (s - b[c]) * idg;
     });
     __syncthreads();
 }
 
 // 1/diag of a cell from its column's x/y neighbours and its z position
-__device__ __forceinline__ double bottom_idiag(const MgGeom& g, int z, const MgNb& nx, const MgNb& ny) {
-    const MgNb nzb = mg_nb(z, g.n[0], g.per[0], 0);
+__device__ __forceinline__ double bottom_idiag(const MgGeom& g, int z, const MgNbI& nx, const MgNbI& ny) {
+    const MgNbI nzb = mg_nbi(z, g.n[0], g.per[0], 0);
     return g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp];
+}
+
+// sum of the residuals of the 8 children of coarse cell (z, y, x), shared-memory level
+// (mg_restrict_cell with direct neighbour offsets)
+template <typename T>
+__device__ __forceinline__ T bottom_restrict(const MgGeom& gf, const T* xf, const T* bf, int z, int y, int x) {
+    const int nx = gf.n[2], ny = gf.n[1], nz = gf.n[0], sy = nx, sz = nx * ny;
+    const int i0 = 2 * x, j0 = 2 * y, k0 = 2 * z;
+    const MgNbI xl = mg_nbi(i0, nx, gf.per[2], 1), xh = mg_nbi(i0 + 1, nx, gf.per[2], 1);
+    const MgNbI yl = mg_nbi(j0, ny, gf.per[1], sy), yh = mg_nbi(j0 + 1, ny, gf.per[1], sy);
+    const MgNbI zl = mg_nbi(k0, nz, gf.per[0], sz), zh = mg_nbi(k0 + 1, nz, gf.per[0], sz);
+    const int dxy[4] = {(int)xl.wm + 1 + (int)yl.wm + 1, 1 + (int)xh.wp + (int)yl.wm + 1,
+                        (int)xl.wm + 1 + 1 + (int)yh.wp, 1 + (int)xh.wp + 1 + (int)yh.wp};
+    const int cb = (k0 * ny + j0) * nx + i0;
+    T v[4][4];   // the 2 x 2 children positions on planes k0-1 .. k0+2
+    auto ld4 = [&](int c, bool wet, T* o) {
+        o[0] = sm_ldw(xf, c, wet);
+        o[1] = sm_ldw(xf, c + 1, wet);
+        o[2] = sm_ldw(xf, c + sy, wet);
+        o[3] = sm_ldw(xf, c + sy + 1, wet);
+    };
+    ld4(cb + zl.om, zl.wm, v[0]);
+    ld4(cb, true, v[1]);
+    ld4(cb + sz, true, v[2]);
+    ld4(cb + sz + zh.op, zh.wp, v[3]);
+    T s = T(0);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = h + 1;
+        const int c = cb + h * sz;
+        const int dz = (h == 0 ? (int)zl.wm : 1) + (h == 1 ? (int)zh.wp : 1);
+        const T xm0 = sm_ldw(xf, c + xl.om, xl.wm), xm1 = sm_ldw(xf, c + sy + xl.om, xl.wm);
+        const T xp0 = sm_ldw(xf, c + 1 + xh.op, xh.wp), xp1 = sm_ldw(xf, c + sy + 1 + xh.op, xh.wp);
+        const T ym0 = sm_ldw(xf, c + yl.om, yl.wm), ym1 = sm_ldw(xf, c + 1 + yl.om, yl.wm);
+        const T yp0 = sm_ldw(xf, c + sy + yh.op, yh.wp), yp1 = sm_ldw(xf, c + sy + 1 + yh.op, yh.wp);
+        const T* p = v[q];
+        const T r00 = (bf[c] + T(dxy[0] + dz) * p[0]) - (((((xm0 + p[1]) + ym0) + p[2]) + v[q - 1][0]) + v[q + 1][0]);
+        const T r01 = (bf[c + 1] + T(dxy[1] + dz) * p[1]) -
+                      (((((p[0] + xp0) + ym1) + p[3]) + v[q - 1][1]) + v[q + 1][1]);
+        const T r10 = (bf[c + sy] + T(dxy[2] + dz) * p[2]) -
+                      (((((xm1 + p[3]) + p[0]) + yp0) + v[q - 1][2]) + v[q + 1][2]);
+        const T r11 = (bf[c + sy + 1] + T(dxy[3] + dz) * p[3]) -
+                      (((((p[2] + xp1) + p[1]) + yp1) + v[q - 1][3]) + v[q + 1][3]);
+        s = (h == 0) ? r00 : s + r00;
+        s = s + r01;
+        s = s + r10;
+        s = s + r11;
+    }
+    return s;
+}
+
+// prolongation increment of fine cell (z, y, x) from a shared-memory coarse level
+// (mg_prolong_cell with direct neighbour offsets)
+template <typename T>
+__device__ __forceinline__ T bottom_prolong(const MgGeom& gf, const MgGeom& gc, const T* xc, int z, int y, int x) {
+    const int ic = x >> 1, jc = y >> 1, kc = z >> 1;
+    const int csy = gc.n[2], csz = gc.n[1] * gc.n[2];
+    const MgNbI cx = mg_nbi(ic, gc.n[2], gc.per[2], 1), cy = mg_nbi(jc, gc.n[1], gc.per[1], csy);
+    const MgNbI cz = mg_nbi(kc, gc.n[0], gc.per[0], csz);
+    const int ox = (x & 1) ? cx.op : cx.om, oy = (y & 1) ? cy.op : cy.om, oz = (z & 1) ? cz.op : cz.om;
+    const bool wx = (x & 1) ? cx.wp : cx.wm, wy = (y & 1) ? cy.wp : cy.wm, wz = (z & 1) ? cz.wp : cz.wm;
+    const int c0 = (kc * gc.n[1] + jc) * gc.n[2] + ic;
+    auto plane = [&](int c, bool w) -> T {
+        const T a = sm_ldw(xc, c, w), b = sm_ldw(xc, c + ox, w && wx);
+        const T d = sm_ldw(xc, c + oy, w && wy), e = sm_ldw(xc, c + ox + oy, w && wx && wy);
+        return ((T(9) * a + T(3) * b) + T(3) * d) + e;
+    };
+    const T bpl = plane(c0, true), opl = plane(c0 + oz, wz);
+    const T pcoef = T(gf.pcoef[(int)wx | ((int)wy << 1) | ((int)wz << 2)]);
+    return pcoef * (T(3) * bpl + opl);
 }
 
 template <typename T>
@@ -420,8 +512,8 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
     auto Bv = [&](int l) { return sm + a.off[l] + mg_vol(a.g[l]); };
     auto Y = [&](int l) { return sm + a.off[l] + 2 * mg_vol(a.g[l]); };
     // level l0 starts from x = 0: its first half-sweep is y = from_zero(b)
-    bottom_cells(a.g[0], [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
-        const long long c = mg_at(a.g[0], z, y, x);
+    bottom_cells(a.g[0], [&](int z, int y, int x, const MgNbI& nx, const MgNbI& ny) {
+        const int c = (z * a.g[0].n[1] + y) * a.g[0].n[2] + x;
         const T bv = a.bg[c];
         Bv(0)[c] = bv;
         Y(0)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(a.g[0], z, nx, ny)));
@@ -433,9 +525,9 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
         const MgGeom& gc = a.g[l + 1];
         if (mg_vol(gc) == 0) break;
         // restriction; the coarse level starts from zero, so its first half-sweep is written too
-        bottom_cells(gc, [&](int z, int y, int x, const MgNb& nx, const MgNb& ny) {
-            const long long c = mg_at(gc, z, y, x);
-            const T bv = T(0.5) * mg_restrict_cell(a.g[l], X(l), Bv(l), z, y, x);
+        bottom_cells(gc, [&](int z, int y, int x, const MgNbI& nx, const MgNbI& ny) {
+            const int c = (z * gc.n[1] + y) * gc.n[2] + x;
+            const T bv = T(0.5) * bottom_restrict(a.g[l], X(l), Bv(l), z, y, x);
             Bv(l + 1)[c] = bv;
             Y(l + 1)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(gc, z, nx, ny)));
         });
@@ -446,9 +538,9 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
         const MgGeom& gf = a.g[l];
         if (mg_vol(gf) == 0) continue;
         if (mg_vol(a.g[l + 1]) > 0) {
-            bottom_cells(gf, [&](int z, int y, int x, const MgNb&, const MgNb&) {
-                const long long c = mg_at(gf, z, y, x);
-                X(l)[c] = X(l)[c] + mg_prolong_cell(gf, a.g[l + 1], X(l + 1), z, y, x);
+            bottom_cells(gf, [&](int z, int y, int x, const MgNbI&, const MgNbI&) {
+                const int c = (z * gf.n[1] + y) * gf.n[2] + x;
+                X(l)[c] = X(l)[c] + bottom_prolong(gf, a.g[l + 1], X(l + 1), z, y, x);
             });
             __syncthreads();
         }
@@ -565,13 +657,14 @@ __device__ __forceinline__ float2 mg_ldw_df(const float2* __restrict__ a, long l
 // (k_mg_scale), so that they neither underflow nor overflow; each block partial is
 // unscaled in double.
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, const float2* __restrict__ p,
-                                                              const float2* __restrict__ b, float* __restrict__ r32,
-                                                              float* __restrict__ y32, float omega,
-                                                              const double* __restrict__ sc,
-                                                              double* __restrict__ partial) {
+                                                                 const float2* __restrict__ b, float* __restrict__ r32,
+                                                                 float* __restrict__ y32, float omega,
+                                                                 const double* __restrict__ sc,
+                                                                 double* __restrict__ partial) {
+    constexpr int ZC = MG_DFZC;
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+    const int nz = g.n[0], z0 = blockIdx.z * ZC;
     const float scale = (float)sc[SC_SCALE];
     float s = 0.f;
     if (x < g.n[2] && y < g.n[1]) {
@@ -588,17 +681,17 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
             const float rs = __fmul_rn(r, scale);
             s = __fmaf_rn(rs, rs, s);
         };
-        if (z0 + MG_ZC <= nz) {
-            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
-            float2 col[MG_ZC + 2];
+        if (z0 + ZC <= nz) {
+            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + ZC - 1, nz, g.per[0], sz);
+            float2 col[ZC + 2];
             col[0] = mg_ldw_df(p, c0 + lo.om, lo.wm);
 #pragma unroll
-            for (int k = 1; k <= MG_ZC; ++k) col[k] = p[c0 + (k - 1) * sz];
-            col[MG_ZC + 1] = mg_ldw_df(p, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+            for (int k = 1; k <= ZC; ++k) col[k] = p[c0 + (k - 1) * sz];
+            col[ZC + 1] = mg_ldw_df(p, c0 + (ZC - 1) * sz + hi.op, hi.wp);
 #pragma unroll
-            for (int k = 0; k < MG_ZC; ++k)
+            for (int k = 0; k < ZC; ++k)
                 cell(c0 + k * sz, col[k], col[k + 1], col[k + 2],
-                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == MG_ZC - 1 ? 1 + (int)hi.wp : 2)));
+                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == ZC - 1 ? 1 + (int)hi.wp : 2)));
         } else {
             for (int z = z0; z < nz; ++z) {
                 const long long c = c0 + (z - z0) * sz;
@@ -782,7 +875,8 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
             if (e != cudaSuccess) return cuda_status(e, "multigrid coarse-level kernel attribute");
         }
     }
-    const dim3 g0 = grid_zc(mg->lev[0].n, MG_ZC);
+    // one partial per block of the largest reduction grid (the float-pair residual's)
+    const dim3 g0 = grid_zc(mg->lev[0].n, MG_DFZC < MG_ZC ? MG_DFZC : MG_ZC);
     mg->npartial = (int)(g0.x * g0.y * g0.z);
     mg->off_partial = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
@@ -905,7 +999,7 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     MgGeom g = mgg(mg, 0);
     double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
     double* sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
-    const dim3 grd = grid_zc(g.n, MG_ZC);
+    const dim3 grd = grid_zc(g.n, MG_DFZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(2);
     k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
