@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--serving-steps", type=int, default=30, help="time steps of each ensemble run")
     ap.add_argument("--serving-rate", type=float, default=20.0, help="Poisson arrivals per second")
     ap.add_argument("--no-serving-baseline", action="store_true")
+    ap.add_argument("--no-eager", action="store_true", help="skip the eager (no graph) timing beside the headline")
     ap.add_argument("--accuracy-steps", type=int, default=100,
                     help="steps of the mixed-vs-FP64 error check (0 skips it)")
     return ap.parse_args()
@@ -524,10 +525,12 @@ def main():
             launches_total += launches
             res = {"ms_per_step": ms / a.steps, "value": job_value(cells, a.steps, ms, world),
                    "mean_vcycles_per_solve": vc, "kernel_launches": launches, "path": "graph replay"}
-            ems_eager, _, _ = time_steps(nyl, a.steps, 1, stream, graphs=False)
-            res["eager"] = {"ms_per_step": ems_eager / a.steps,
-                            "value": world * cells * a.steps / (ems_eager * 1e-3),
-                            "note": "same steps launched one kernel at a time, multigrid stop test on the host"}
+            if not a.no_eager:
+                ems_eager, _, _ = time_steps(nyl, a.steps, 1, stream, graphs=False)
+                ems_eager = job_time_ms(ems_eager, dist, "cuda")
+                res["eager"] = {"ms_per_step": ems_eager / a.steps,
+                                "value": job_value(cells, a.steps, ems_eager, world),
+                                "note": "same steps launched one kernel at a time, multigrid stop test on the host"}
             if a.profile_steps > 0:
                 res["phases"] = profile_phases(nyl, a.profile_steps)
             nyl.model.use_graphs = True
@@ -545,7 +548,7 @@ def main():
     out.update({"value": r["value"], "ms_per_step": r["ms_per_step"],
                 "dtype": "f64" if main_prec == "fp64" else "f32+f64", "clocks": clocks,
                 "gpu_launches": launches_total, "mg": {"mean_vcycles_per_solve": r["mean_vcycles_per_solve"]},
-                "path": r["path"], "eager": r["eager"]})
+                "path": r["path"], "eager": r.get("eager")})
     if "e2e" in r:
         out["e2e"] = r["e2e"]
     # roofline of the dominant kernel (largest share of device time)
@@ -562,7 +565,7 @@ def main():
         mr = results["mixed"]
         out["mixed"] = {"value": mr["value"], "ms_per_step": mr["ms_per_step"],
                         "speedup_vs_fp64": mr["value"] / r["value"],
-                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"], "eager": mr["eager"]}
+                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"], "eager": mr.get("eager")}
         if "e2e" in mr:
             out["mixed"]["e2e"] = mr["e2e"]
         if "phases" in mr:

@@ -26,7 +26,15 @@ struct MgGeom {
     int per[3];
     double idiag[8];   // 1/diag for diag = 0..6 (0 -> 0), computed once on the host
     double pcoef[8];   // 1/(Wx*Wy*Wz) indexed by the three "neighbour is wet" bits
+    float fidiag[8];   // the same tables rounded to float: single-precision kernels read
+    float fpcoef[8];   // these instead of converting (FP64 conversions use the FP64 pipe)
 };
+template <typename T> __device__ __forceinline__ T mg_idiag(const MgGeom& g, int k);
+template <> __device__ __forceinline__ double mg_idiag<double>(const MgGeom& g, int k) { return g.idiag[k]; }
+template <> __device__ __forceinline__ float mg_idiag<float>(const MgGeom& g, int k) { return g.fidiag[k]; }
+template <typename T> __device__ __forceinline__ T mg_pcoef(const MgGeom& g, int k);
+template <> __device__ __forceinline__ double mg_pcoef<double>(const MgGeom& g, int k) { return g.pcoef[k]; }
+template <> __device__ __forceinline__ float mg_pcoef<float>(const MgGeom& g, int k) { return g.fpcoef[k]; }
 
 // Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
 // [3] nite of the current solve, [4] V-cycles since creation, [5] and [6] the scale of
@@ -100,7 +108,7 @@ template <typename T>
 __device__ __forceinline__ T mg_jacobi_cell(const MgGeom& g, const T* __restrict__ in, const T* __restrict__ b, int z,
                                             int y, int x, T cff1, T omega) {
     const long long c = mg_at(g, z, y, x);
-    const T idg = T(g.idiag[mg_diag(g, z, y, x)]);
+    const T idg = mg_idiag<T>(g, mg_diag(g, z, y, x));
     return cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
 }
 // sum of the residuals of the 8 children of coarse cell (z, y, x)
@@ -131,7 +139,7 @@ __device__ __forceinline__ T mg_prolong_cell(const MgGeom& gf, const MgGeom& gc,
     const T bpl = plane(kc);
     const T opl = plane(kc + sk);
     auto wet = [&](int d, int v) -> int { return (gc.per[d] || (v >= 0 && v < gc.n[d])) ? 1 : 0; };
-    const T pcoef = T(gf.pcoef[wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2)]);
+    const T pcoef = mg_pcoef<T>(gf, wet(2, ic + si) | (wet(1, jc + sj) << 1) | (wet(0, kc + sk) << 2));
     return pcoef * (T(3) * bpl + opl);
 }
 
@@ -195,9 +203,9 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 #pragma unroll
         for (int k = 1; k <= MG_ZC; ++k) col[k] = in[c0 + (k - 1) * sz];
         col[MG_ZC + 1] = mg_ldw(in, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
-        const T idg = T(g.idiag[dxy + 2]);
-        const T idg_lo = T(g.idiag[dxy + 1 + (int)lo.wm]);
-        const T idg_hi = T(g.idiag[dxy + 1 + (int)hi.wp]);
+        const T idg = mg_idiag<T>(g, dxy + 2);
+        const T idg_lo = mg_idiag<T>(g, dxy + 1 + (int)lo.wm);
+        const T idg_hi = mg_idiag<T>(g, dxy + 1 + (int)hi.wp);
 #pragma unroll
         for (int k = 0; k < MG_ZC; ++k) {
             const long long c = c0 + k * sz;
@@ -208,7 +216,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
     for (int z = z0; z < nz; ++z) {   // last, partial chunk
         const long long c = mg_at(g, z, y, x);
         const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
-        const T idg = T(g.idiag[dxy + (int)nzb.wm + (int)nzb.wp]);
+        const T idg = mg_idiag<T>(g, dxy + (int)nzb.wm + (int)nzb.wp);
         put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg));
     }
 }
@@ -236,7 +244,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, 
         const long long c = mg_at(gc, z, y, x);
         const T bv = T(0.5) * s;
         bc[c] = bv;
-        yc[c] = mg_jacobi_from_zero(bv, omega, T(gc.idiag[mg_diag(gc, z, y, x)]));
+        yc[c] = mg_jacobi_from_zero(bv, omega, mg_idiag<T>(gc, mg_diag(gc, z, y, x)));
     };
     if (z0 + MG_RZC > nzc) {   // last, partial chunk
         for (int z = z0; z < nzc; ++z) emit(z, mg_restrict_cell(gf, xf, bf, z, y, x));
@@ -339,8 +347,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
     for (int q = 1; q < NP - 1; ++q) P[q] = plane(cc + (q - 1) * csz, true);
     P[NP - 1] = plane(cc + (MG_ZC / 2 - 1) * csz + zh.op, zh.wp);
     const int bxy = (int)wx | ((int)wy << 1);
-    const T pc_wet = T(gf.pcoef[bxy | 4]), pc_lo = T(gf.pcoef[bxy | ((int)zl.wm << 2)]);
-    const T pc_hi = T(gf.pcoef[bxy | ((int)zh.wp << 2)]);
+    const T pc_wet = mg_pcoef<T>(gf, bxy | 4), pc_lo = mg_pcoef<T>(gf, bxy | ((int)zl.wm << 2));
+    const T pc_hi = mg_pcoef<T>(gf, bxy | ((int)zh.wp << 2));
 #pragma unroll
     for (int k = 0; k < MG_ZC; ++k) {
         const int m = (k >> 1) + 1;                  // plane of z>>1 in P
@@ -418,7 +426,7 @@ __device__ __forceinline__ void bottom_sweep(const MgGeom& g, const T* in, const
     bottom_cells(g, [&](int z, int y, int x, const MgNbI& nx, const MgNbI& ny) {
         const int c = (z * g.n[1] + y) * g.n[2] + x;
         const MgNbI nzb = mg_nbi(z, g.n[0], g.per[0], sz);
-        const T idg = T(g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp]);
+        const T idg = mg_idiag<T>(g, (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp);
         const T s = ((((sm_ldw(in, c + nx.om, nx.wm) + sm_ldw(in, c + nx.op, nx.wp)) + sm_ldw(in, c + ny.om, ny.wm)) +
                       sm_ldw(in, c + ny.op, ny.wp)) + sm_ldw(in, c + nzb.om, nzb.wm)) + sm_ldw(in, c + nzb.op, nzb.wp);
         out[c] = cff1 * in[c] + om * (s - b[c]) * idg;
@@ -427,9 +435,10 @@ __device__ __forceinline__ void bottom_sweep(const MgGeom& g, const T* in, const
 }
 
 // 1/diag of a cell from its column's x/y neighbours and its z position
-__device__ __forceinline__ double bottom_idiag(const MgGeom& g, int z, const MgNbI& nx, const MgNbI& ny) {
+template <typename T>
+__device__ __forceinline__ T bottom_idiag(const MgGeom& g, int z, const MgNbI& nx, const MgNbI& ny) {
     const MgNbI nzb = mg_nbi(z, g.n[0], g.per[0], 0);
-    return g.idiag[(int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp];
+    return mg_idiag<T>(g, (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp);
 }
 
 // sum of the residuals of the 8 children of coarse cell (z, y, x), shared-memory level
@@ -498,7 +507,7 @@ __device__ __forceinline__ T bottom_prolong(const MgGeom& gf, const MgGeom& gc, 
         return ((T(9) * a + T(3) * b) + T(3) * d) + e;
     };
     const T bpl = plane(c0, true), opl = plane(c0 + oz, wz);
-    const T pcoef = T(gf.pcoef[(int)wx | ((int)wy << 1) | ((int)wz << 2)]);
+    const T pcoef = mg_pcoef<T>(gf, (int)wx | ((int)wy << 1) | ((int)wz << 2));
     return pcoef * (T(3) * bpl + opl);
 }
 
@@ -516,7 +525,7 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
         const int c = (z * a.g[0].n[1] + y) * a.g[0].n[2] + x;
         const T bv = a.bg[c];
         Bv(0)[c] = bv;
-        Y(0)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(a.g[0], z, nx, ny)));
+        Y(0)[c] = mg_jacobi_from_zero(bv, om, bottom_idiag<T>(a.g[0], z, nx, ny));
     });
     __syncthreads();
     for (int l = 0; l < L - 1; ++l) {
@@ -529,7 +538,7 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
             const int c = (z * gc.n[1] + y) * gc.n[2] + x;
             const T bv = T(0.5) * bottom_restrict(a.g[l], X(l), Bv(l), z, y, x);
             Bv(l + 1)[c] = bv;
-            Y(l + 1)[c] = mg_jacobi_from_zero(bv, om, T(bottom_idiag(gc, z, nx, ny)));
+            Y(l + 1)[c] = mg_jacobi_from_zero(bv, om, bottom_idiag<T>(gc, z, nx, ny));
         });
         __syncthreads();
     }
@@ -677,7 +686,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
                                   mg_ldw_df(p, c + ny.om, ny.wm), mg_ldw_df(p, c + ny.op, ny.wp), zm, zp};
             const float r = df_resid(b[c], p0, (float)dg, nb);
             r32[c] = r;
-            y32[c] = mg_jacobi_from_zero(r, omega, (float)g.idiag[dg]);
+            y32[c] = mg_jacobi_from_zero(r, omega, mg_idiag<float>(g, dg));
             const float rs = __fmul_rn(r, scale);
             s = __fmaf_rn(rs, rs, s);
         };
@@ -787,6 +796,10 @@ static inline MgGeom mgg(const MgImpl* mg, int l) {
     for (int bits = 0; bits < 8; ++bits) {
         const int W = (3 + (bits & 1)) * (3 + ((bits >> 1) & 1)) * (3 + ((bits >> 2) & 1));
         g.pcoef[bits] = 1.0 / (double)W;
+    }
+    for (int k = 0; k < 8; ++k) {
+        g.fidiag[k] = (float)g.idiag[k];
+        g.fpcoef[k] = (float)g.pcoef[k];
     }
     return g;
 }
