@@ -214,8 +214,31 @@ def mg_levels(n):
 
 # FP64 flops (DADD + DMUL + 2 x DFMA thread instructions) per array cell of one
 # k_rhs_march<double, 1, 1> launch, counted by ncu on the 128^3 case of this workload
-# (profiles/k_rhs_march_fp64_rayleigh_taylor_128.md: 237 + 251 + 2 x 252).
+# (237 + 251 + 2 x 252 per cell).
 RHS_FP64_OPS_PER_CELL = 992
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per array cell of one
+# right-hand-side launch, from ncu --set full captures of this workload: FP64 at 128^3
+# (158.4 + 47.1 MB over 128 x 134 x 134 cells), FP32 at 256^3 (574.1 + 263.8 MB over
+# 256 x 262 x 262 cells). Traffic grows with the cells processed.
+RHS_DRAM_BYTES_PER_CELL = {8: 205.5e6 / (128 * 134 * 134), 4: 837.9e6 / (256 * 262 * 262)}
+# DRAM bytes of one level-0 Jacobi half-sweep launch at 256^3, mixed (ncu: 134.2 +
+# 41.6 MB; algorithmic 201.3 MB, the rest of the output still in L2 at the end)
+JACOBI_F32_L0_DRAM_BYTES_256 = 175.8e6
+
+
+def mg_bottom_level(levels, elem, smem=200 * 1024):
+    """First level of the one-block coarse solve (the library's rule: the coarsest
+    levels whose x, b, y fit in `smem` bytes, two levels at least, never level 0)."""
+    L = len(levels)
+    bottom, total = L, 0
+    for l in range(L - 1, 0, -1):
+        z, y, x = levels[l]
+        total += 3 * z * y * x * elem
+        if total > smem:
+            break
+        if L - l >= 2:
+            bottom = l
+    return bottom
 
 
 def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
@@ -223,9 +246,13 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
 
     rhs       : one launch reads b, U(3), vor(3), ke and writes 4 registers: 12 words
                 per cell of the (n+6)^2 n array.
-    mg_smooth : each Jacobi half-sweep reads its input and b and writes its output:
-                3 words per level cell; per V-cycle 4 half-sweeps on every level but
-                the coarsest (2).
+    mg_smooth : each Jacobi half-sweep reads its input and b and writes its output, 3
+                words per level cell; per V-cycle, on each grid level above the
+                one-block coarse levels: 3 half-sweeps (the first of the pre-smoothing
+                is written by the kernel that sets b; FP64 level 0, warm-started: 4),
+                plus, in mixed precision, the float-pair solution read and written by
+                the last level-0 half-sweep (16 B per cell); the one-block coarse solve
+                reads b and writes x of its first level.
     """
     if ph.get(kernel, {}).get("count", 0) == 0:
         return None
@@ -237,7 +264,9 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
         per_launch = 12 * elem * vol
         avg = ms / launches
         out.update({"kernel": "k_rhs_march", "bytes_per_launch": per_launch, "avg_launch_ms": avg,
-                    "achieved": per_launch / (avg * 1e-3) / 1e9})
+                    "achieved": per_launch / (avg * 1e-3) / 1e9,
+                    "traffic": RHS_DRAM_BYTES_PER_CELL[elem] * vol,
+                    "traffic_source": "ncu dram bytes per cell of the same kernel, scaled to this grid"})
         if elem == 8 and fp64_peak:
             ops = RHS_FP64_OPS_PER_CELL
             out["fp64"] = {"peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM)",
@@ -247,12 +276,22 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
                 out["fp64"]["frac"] = out["fp64"]["achieved_tflops"] / fp64_peak
     elif kernel == "mg_smooth":
         lev = mg_levels(n)
-        per_vcycle = sum((4 if i < len(lev) - 1 else 2) * 3 * elem * (z * y * x) for i, (z, y, x) in enumerate(lev))
-        calls_per_vcycle = 2 * (len(lev) - 1) + 1
+        B = mg_bottom_level(lev, elem)
+        vol = [z * y * x for (z, y, x) in lev]
+        per_vcycle = sum((4 if (l == 0 and elem == 8) else 3) * 3 * elem * vol[l] for l in range(B))
+        if elem == 4:
+            per_vcycle += 16 * vol[0]
+        if B < len(lev):
+            per_vcycle += 2 * elem * vol[B]
+        calls_per_vcycle = 2 * B + 1   # one bracketed call per smoothing and the coarse solve
         vcycles = ph[kernel]["count"] / calls_per_vcycle
         total = per_vcycle * vcycles
-        out.update({"kernel": "k_mg_jacobi", "bytes_per_vcycle": per_vcycle, "vcycles": vcycles,
-                    "avg_launch_ms": ms / (2 * ph[kernel]["count"]), "achieved": total / (ms * 1e-3) / 1e9})
+        out.update({"kernel": "k_mg_jacobi (+ k_mg_bottom)", "bytes_per_vcycle": per_vcycle, "vcycles": vcycles,
+                    "ms_per_vcycle": ms / vcycles, "achieved": total / (ms * 1e-3) / 1e9})
+        if elem == 4 and n == 256:
+            out["traffic"] = JACOBI_F32_L0_DRAM_BYTES_256
+            out["traffic_source"] = ("ncu dram bytes of one level-0 half-sweep launch (algorithmic %.1f MB)"
+                                     % (3 * 4 * vol[0] / 1e6))
     else:
         out["achieved"] = None
     if out.get("achieved") is not None:
