@@ -627,6 +627,55 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq(const MgGeom g, cons
     block_partial(s, partial);
 }
 
+// Stop-test residual of the level-1 solution together with the first half-sweep of the
+// next V-cycle: both need the same neighbour sum, so one pass gives sum(r^2) (same
+// partials, same order as k_mg_sumsq MODE 1) and y = (1-omega)*x + omega*(sum - b)*idiag.
+// If the solve then stops, y is simply not used.
+template <typename T>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_sweep(const MgGeom g, const T* __restrict__ v,
+                                                                 const T* __restrict__ b, T* __restrict__ y_out,
+                                                                 T omega, double* __restrict__ partial) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+    const T cff1 = T(1) - omega;
+    double s = 0.0;
+    if (x < g.n[2] && y < g.n[1]) {
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        const long long c0 = mg_at(g, z0, y, x);
+        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+        const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
+        auto cell = [&](long long c, T zm, T x0, T zp, int dg) {
+            const T nsum = ((((mg_ldw(v, c + nx.om, nx.wm) + mg_ldw(v, c + nx.op, nx.wp)) + mg_ldw(v, c + ny.om, ny.wm)) +
+                             mg_ldw(v, c + ny.op, ny.wp)) + zm) + zp;
+            const T bv = b[c];
+            const double r = (double)((bv + T(dg) * x0) - nsum);
+            s += r * r;
+            y_out[c] = cff1 * x0 + omega * (nsum - bv) * mg_idiag<T>(g, dg);
+        };
+        if (z0 + MG_ZC <= nz) {
+            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+            T col[MG_ZC + 2];
+            col[0] = mg_ldw(v, c0 + lo.om, lo.wm);
+#pragma unroll
+            for (int k = 1; k <= MG_ZC; ++k) col[k] = v[c0 + (k - 1) * sz];
+            col[MG_ZC + 1] = mg_ldw(v, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+#pragma unroll
+            for (int k = 0; k < MG_ZC; ++k)
+                cell(c0 + k * sz, col[k], col[k + 1], col[k + 2],
+                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == MG_ZC - 1 ? 1 + (int)hi.wp : 2)));
+        } else {
+            for (int z = z0; z < nz; ++z) {
+                const long long c = c0 + (z - z0) * sz;
+                const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
+                cell(c, mg_ldw(v, c + nzb.om, nzb.wm), v[c], mg_ldw(v, c + nzb.op, nzb.wp),
+                     dxy + (int)nzb.wm + (int)nzb.wp);
+            }
+        }
+    }
+    block_partial(s, partial);
+}
+
 // ---------------------------------------------------------------- mixed precision
 // Float-pair residual r = b + diag*p - sum(p_nb), neighbours in mgfor's order. The
 // neighbour sum and the centre product are error-free (TwoSum chain, TwoProduct); the
@@ -943,11 +992,12 @@ template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     const int L = mg->nlevels;
     const int B = mg->bottom;   // < L: levels B..L-1 in one block
-    // level 0 of a mixed-precision correction starts from zero: the residual kernel
-    // wrote its first half-sweep; every restricted level likewise gets it from the
-    // restriction
+    // The first half-sweep of level 0 was written by the stop-test residual kernel that
+    // precedes every V-cycle (k_mg_resid_sweep; mixed: k_mg_resid_df, from a zero
+    // correction); every restricted level gets it from the restriction.
+    (void)mixed;
     for (int l = 0; l < L - 1 && l < B; ++l) {
-        smooth<T>(mg, l, st, false, l > 0 || mixed);
+        smooth<T>(mg, l, st, false, true);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 9, st);
@@ -960,7 +1010,7 @@ static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     if (B < L)
         bottom<T>(mg, st);
     else
-        smooth<T>(mg, L - 1, st, L == 1 && mixed, L > 1 || mixed);
+        smooth<T>(mg, L - 1, st, L == 1 && mixed, true);
     for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -1021,6 +1071,20 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
 }
 
+// FP64: enqueue the stop-test sum(r^2) into sc[SC_RR] together with the next V-cycle's
+// first level-0 half-sweep (k_mg_resid_sweep)
+static void enqueue_resid_sweep(MgImpl* mg, cudaStream_t st) {
+    MgGeom g = mgg(mg, 0);
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+    const dim3 grd = grid_zc(g.n, MG_ZC);
+    ProfScope ps(mg->prof, 11, st);
+    note_launch(2);
+    k_mg_resid_sweep<double><<<grd, kBlk, 0, st>>>(g, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2),
+                                                   lvp<double>(mg, 0, 3), mg->omega, part);
+    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
+}
+
 template <typename T, int MODE>
 static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* host_out, cudaStream_t st) {
     enqueue_sumsq<T, MODE>(mg, g, v, b, scalars(mg), st);
@@ -1041,11 +1105,11 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
     double normb = 0.0, rr = 0.0, res = 0.0;
     int rc;
     if (mg->precision == NYLES_FP64) {
-        double* x = lvp<double>(mg, 0, 1);
         double* b = lvp<double>(mg, 0, 2);
         if ((rc = sumsq<double, 0>(mg, g0, b, nullptr, &normb, st))) return rc;
         if (normb > 0.0) {
-            if ((rc = sumsq<double, 1>(mg, g0, x, b, &rr, st))) return rc;
+            enqueue_resid_sweep(mg, st);
+            if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
             res = rr / normb;
         }
         while (true) {
@@ -1054,7 +1118,8 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
             ++nite;
             if (nite >= mg->maxite) break;
             if (normb > 0.0) {
-                if ((rc = sumsq<double, 1>(mg, g0, x, b, &rr, st))) return rc;
+                enqueue_resid_sweep(mg, st);
+                if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
                 res = rr / normb;
             } else {
                 res = 0.0;
@@ -1127,7 +1192,7 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
     if (e != cudaSuccess) return gb.error = cuda_status(e, "cudaGraphConditionalHandleCreate");
     if (!mixed) {
         enqueue_sumsq<double, 0>(mg, g0, lvp<double>(mg, 0, 2), (const double*)nullptr, sc + SC_NORMB, st);
-        enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
+        enqueue_resid_sweep(mg, st);
     } else {
         enqueue_normb_df(mg, st);
         enqueue_resid_df(mg, st);
@@ -1150,7 +1215,7 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
     const long long l0 = nyles_launch_count();
     if (!mixed) {
         vcycle<double>(mg, st, false);
-        enqueue_sumsq<double, 1>(mg, g0, lvp<double>(mg, 0, 1), lvp<double>(mg, 0, 2), sc + SC_RR, st);
+        enqueue_resid_sweep(mg, st);
     } else {
         vcycle<float>(mg, st, true);
         enqueue_resid_df(mg, st);
