@@ -147,8 +147,16 @@ int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omeg
 int nyles_model_forward(NylesModel* m, double t, double dt, void* stream);
 /* LES.diagnose_var, core/model_les.py:98-127 (core/model_les_euler.py:96-125) */
 int nyles_model_diagnose(NylesModel* m, void* stream);
-/* LES.rhs into register set `reg`, core/model_les.py:130-144 */
-int nyles_model_rhs(NylesModel* m, int reg, int last, void* stream);
+/* LES.rhs(state, t, dstate, last) into register set `reg`, core/model_les.py:130-144 */
+int nyles_model_rhs(NylesModel* m, int reg, double t, int last, void* stream);
+/* User forcing (core/model_les.py:143-144, `forcing.add(state, dstate, t)` when the
+ * parameter `forced` is set): `fn(user, reg, t, stream)` is called on the host after
+ * every right-hand side of forward/rhs, with the register set holding that stage's
+ * tendencies and the stage time (RK3: t, t + dt, t + dt/2; LFAM3: t, t + dt/2; EF: t);
+ * it adds its tendencies by work enqueued on `stream`. NULL detaches it. A model with
+ * a forcing cannot be captured into a graph. */
+typedef void (*nyles_forcing_fn)(void* user, int reg, double t, void* stream);
+int nyles_model_set_forcing(NylesModel* m, nyles_forcing_fn fn, void* user);
 /* max over the arrays of U^2+V^2+W^2 (core/nyles.py:241-251), copied to *out */
 int nyles_model_max_U2(NylesModel* m, double* out, void* stream);
 /* VFwork.compute, core/online_diag.py:11-35: the u components of register set 0 are

@@ -58,6 +58,9 @@ class NylesMgStats(ctypes.Structure):
                 ("vcycles", ctypes.c_longlong), ("not_converged", ctypes.c_int)]
 
 
+# user forcing callback: fn(user, reg, t, stream)
+FORCING_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)
+
 # exported symbol -> (restype, argtypes); the complete list of include/nyles_gb300.h
 _P, _I, _D, _VP = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
 _PP = ctypes.POINTER(ctypes.c_void_p)
@@ -88,7 +91,8 @@ SIGNATURES = {
     "nyles_model_set_mg_params": (_I, [_P, _D, _I, _D]),
     "nyles_model_forward": (_I, [_P, _D, _D, _P]),
     "nyles_model_diagnose": (_I, [_P, _P]),
-    "nyles_model_rhs": (_I, [_P, _I, _I, _P]),
+    "nyles_model_rhs": (_I, [_P, _I, _D, _I, _P]),
+    "nyles_model_set_forcing": (_I, [_P, _P, _P]),
     "nyles_model_max_U2": (_I, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_vfwork": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_mg_stats": (_I, [_P, ctypes.POINTER(NylesMgStats)]),

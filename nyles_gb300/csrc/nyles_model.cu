@@ -138,6 +138,8 @@ struct NylesModel {
     long long vcycles_counted = 0;       // device V-cycles already added to the launch count
     bool last_solve_graph = false;       // the latest solve ran inside a graph
     cudaStream_t last_stream = nullptr;  // stream of the latest graph launch
+    nyles_forcing_fn forcing = nullptr;  // user forcing called after each right-hand side
+    void* forcing_user = nullptr;
     void release_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
@@ -390,11 +392,15 @@ int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
 namespace nyles {
 
 template <typename T>
-static int model_rhs(NylesModel* m, int reg, int last, cudaStream_t st) {
+static int model_rhs(NylesModel* m, int reg, int last, double t, cudaStream_t st) {
     StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
     ProgPtrs<T> ds = prog_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->regs[reg]));
     ProfScope ps(&m->prof, 0, st);
-    return launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st);
+    int rc = launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st);
+    // user forcing, core/model_les.py:143-144: called with the stage's register set and
+    // time; it enqueues its own work on `st`
+    if (!rc && m->forcing) m->forcing(m->forcing_user, reg, t, (void*)st);
+    return rc;
 }
 
 // core/model_les.py:98-127 ; core/model_les_euler.py:96-125
@@ -458,26 +464,25 @@ static int model_update(NylesModel* m, int kind, int ra, int rb, int rc_, double
 // core/timescheme.py:113-221
 template <typename T>
 static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
-    (void)t;
     int rc;
     if (m->scheme == NYLES_SCHEME_RK3_SSP) {
-        if ((rc = model_rhs<T>(m, 0, 0, st))) return rc;
+        if ((rc = model_rhs<T>(m, 0, 0, t, st))) return rc;
         if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
         if ((rc = model_diagnose<T>(m, st))) return rc;
-        if ((rc = model_rhs<T>(m, 1, 0, st))) return rc;
+        if ((rc = model_rhs<T>(m, 1, 0, t + dt, st))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_2, 0, 1, -1, dt, st))) return rc;
         if ((rc = model_diagnose<T>(m, st))) return rc;
-        if ((rc = model_rhs<T>(m, 2, 1, st))) return rc;
+        if ((rc = model_rhs<T>(m, 2, 1, t + dt * 0.5, st))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_3, 0, 1, 2, dt, st))) return rc;
         return model_diagnose<T>(m, st);
     }
     if (m->scheme == NYLES_SCHEME_EF) {
-        if ((rc = model_rhs<T>(m, 0, 1, st))) return rc;
+        if ((rc = model_rhs<T>(m, 0, 1, t, st))) return rc;
         if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
         return model_diagnose<T>(m, st);
     }
     // LFAM3: registers 0 = dstate, 1 = stateb, 2 = state (n)
-    if ((rc = model_rhs<T>(m, 0, 0, st))) return rc;
+    if ((rc = model_rhs<T>(m, 0, 0, t, st))) return rc;
     if (m->lf_first) {
         if ((rc = model_update<T>(m, UPD_LF_FIRST, 0, 1, 2, dt, st))) return rc;
         m->lf_first = false;
@@ -485,7 +490,7 @@ static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
     }
     if ((rc = model_update<T>(m, UPD_LF_PRED, 0, 1, 2, dt, st))) return rc;
     if ((rc = model_diagnose<T>(m, st))) return rc;
-    if ((rc = model_rhs<T>(m, 0, 1, st))) return rc;
+    if ((rc = model_rhs<T>(m, 0, 1, t + dt * 0.5, st))) return rc;
     if ((rc = model_update<T>(m, UPD_LF_CORR, 0, 1, 2, dt, st))) return rc;
     return model_diagnose<T>(m, st);
 }
@@ -506,10 +511,18 @@ int nyles_model_diagnose(NylesModel* m, void* stream) {
     return m->precision == NYLES_FP64 ? model_diagnose<double>(m, st) : model_diagnose<float>(m, st);
 }
 
-int nyles_model_rhs(NylesModel* m, int reg, int last, void* stream) {
+int nyles_model_rhs(NylesModel* m, int reg, double t, int last, void* stream) {
     if (!m || !m->bound || reg < 0 || reg > 2) { set_error("model not bound or bad register"); return NYLES_BAD_ARG; }
     cudaStream_t st = (cudaStream_t)stream;
-    return m->precision == NYLES_FP64 ? model_rhs<double>(m, reg, last, st) : model_rhs<float>(m, reg, last, st);
+    return m->precision == NYLES_FP64 ? model_rhs<double>(m, reg, last, t, st) : model_rhs<float>(m, reg, last, t, st);
+}
+
+int nyles_model_set_forcing(NylesModel* m, nyles_forcing_fn fn, void* user) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    if (fn && m->gexec) { set_error("release the captured graph before attaching a forcing"); return NYLES_BAD_ARG; }
+    m->forcing = fn;
+    m->forcing_user = user;
+    return NYLES_OK;
 }
 
 int nyles_model_max_U2(NylesModel* m, double* out, void* stream) {
@@ -594,6 +607,10 @@ int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
     if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
     if (m->scheme == NYLES_SCHEME_LFAM3 && m->lf_first) {
         set_error("LFAM3: run the first (Euler) step before capturing the steady step");
+        return NYLES_BAD_ARG;
+    }
+    if (m->forcing) {
+        set_error("a model with a user forcing cannot be captured (the forcing runs on the host)");
         return NYLES_BAD_ARG;
     }
     cudaError_t e;

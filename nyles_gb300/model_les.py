@@ -91,7 +91,6 @@ class LES(object):
         self._regs = nat.ptr_array(self.timescheme.register_pointers())
         nat.check(self.lib.nyles_model_bind(h, self._fields, self._regs, ctypes.c_void_p(ws)))
         self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9))
-        self.forcing = None
         self.stats = []
         # graph replay of fixed-dt steps (see forward)
         self.use_graphs = bool(gpu.get("graphs", True))
@@ -99,6 +98,46 @@ class LES(object):
         self._last_dt = None
         self._first_step_pending = param["timestepping"] == "LFAM3"
         self._profiling = False
+        self._forcing_cb = None
+        self._forcing_error = None
+        self.forcing = None
+
+    # ------------------------------------------------------------------ user forcing
+    @property
+    def forcing(self):
+        """User forcing (core/model_les.py:143-144): an object with
+        `add(state, dstate, t)` that adds its tendencies into `dstate` with device tensor
+        operations; it is called after every right-hand side when the parameter
+        `forced` is set. Forced steps are never replayed from a graph."""
+        return self._forcing
+
+    @forcing.setter
+    def forcing(self, f):
+        self._forcing = f
+        if self.forced and f is not None:
+            if self.graph is not None:
+                self.release_graph()
+
+            def call(user, reg, t, stream):
+                try:
+                    if stream:
+                        with torch.cuda.stream(torch.cuda.ExternalStream(stream, device=self.device)):
+                            f.add(self.state, self.timescheme.registers[reg], t)
+                    else:
+                        f.add(self.state, self.timescheme.registers[reg], t)
+                except BaseException as e:   # raised again by forward(): nothing propagates through C
+                    self._forcing_error = e
+
+            self._forcing_cb = nat.FORCING_FN(call)
+            nat.check(self.lib.nyles_model_set_forcing(self._h, ctypes.cast(self._forcing_cb, ctypes.c_void_p), None))
+        else:
+            self._forcing_cb = None
+            nat.check(self.lib.nyles_model_set_forcing(self._h, None, None))
+
+    def _raise_forcing_error(self):
+        e, self._forcing_error = self._forcing_error, None
+        if e is not None:
+            raise e
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -133,12 +172,17 @@ class LES(object):
     def rhs(self, state, t, dstate, last=False):
         """Right-hand side into `dstate` (core/model_les.py:130-144)."""
         self._check_state(state)
-        if self.forced and self.forcing is not None:
-            raise NotImplementedError("user forcing hooks are not supported on the GPU path")
         fields = nat.ptr_array([s.data_ptr() for s in state.scalars()])
         ds = nat.ptr_array([s.data_ptr() for s in dstate.scalars()])
         fn = self.lib.nyles_rhs_f64 if self.precision == "fp64" else self.lib.nyles_rhs_f32
         nat.check(fn(ctypes.byref(self.desc), fields, ds, 1 if last else 0, nat.stream_ptr()))
+        if self.forced:
+            self._require_forcing()
+            self.forcing.add(state, dstate, t)
+
+    def _require_forcing(self):
+        if self._forcing is None:
+            raise RuntimeError("the parameter `forced` is set but no forcing is attached (model.forcing = ...)")
 
     def forward(self, t, dt):
         """One time step (core/model_les.py:147-149). Returns the blow-up flag.
@@ -147,10 +191,10 @@ class LES(object):
         dt captures the step into a CUDA graph, and every later call with that dt replays
         it: the same kernels, with the multigrid stop test on the device instead of one
         host round trip per V-cycle. A call with another dt runs eagerly."""
-        if self.forced and self.forcing is not None:
-            raise NotImplementedError("user forcing hooks are not supported on the GPU path")
+        if self.forced:
+            self._require_forcing()
         dt = float(dt)
-        if self.use_graphs and not self._profiling and not self._first_step_pending:
+        if self.use_graphs and not self._profiling and not self._first_step_pending and not self.forced:
             if self.graph == (dt, 1):
                 self.replay()
                 return False
@@ -159,7 +203,9 @@ class LES(object):
                 self.replay()
                 return False
         self._last_dt = dt
-        nat.check(self.lib.nyles_model_forward(self._h, float(t), dt, nat.stream_ptr()))
+        rc = self.lib.nyles_model_forward(self._h, float(t), dt, nat.stream_ptr())
+        self._raise_forcing_error()
+        nat.check(rc)
         self._first_step_pending = False
         return False
 

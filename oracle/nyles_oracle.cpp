@@ -610,6 +610,8 @@ struct Model {
     std::vector<std::vector<std::vector<double>>> reg;   // ds0, ds1, ds2 (RK3) / dstate, stateb, staten
     Mg* mg = nullptr;
     std::vector<double> mgx, mgb;   // level-1 numpy buffers of MG.preallocate_for_nyles
+    void (*forcing)(void* user, int reg, double t, void* stream) = nullptr;   // forcing.add hook
+    void* forcing_user = nullptr;
     int nprog() const { return 4 + ntr; }
 };
 
@@ -802,36 +804,42 @@ void model_diagnose(Model& M) {
     }
 }
 
+// right-hand side into register set `reg` at stage time t, then the user forcing
+// (core/model_les.py:143-144)
+void model_rhs_at(Model& M, int reg, bool last, double t) {
+    model_rhs(M, M.reg[reg], last);
+    if (M.forcing) M.forcing(M.forcing_user, reg, t, nullptr);
+}
+
 // core/timescheme.py:113-221
 void model_forward(Model& M, double t, double dt) {
-    (void)t;
     const int np = M.nprog();
     auto S = [&](int q) { return M.f[prog_field(q)].data(); };
     if (M.scheme == 2) {   // RK3_SSP
         auto& ds0 = M.reg[0]; auto& ds1 = M.reg[1]; auto& ds2 = M.reg[2];
-        model_rhs(M, ds0, false);
+        model_rhs_at(M, 0, false, t);
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data();
             for (long c = 0; c < M.vol; ++c) s[c] = s[c] + dt * a[c]; }
         model_diagnose(M);
-        model_rhs(M, ds1, false);
+        model_rhs_at(M, 1, false, t + dt);
         const double c2 = dt / 4.0;
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data(); const double* b = ds1[q].data();
             for (long c = 0; c < M.vol; ++c) s[c] = s[c] + c2 * (b[c] - 3.0 * a[c]); }
         model_diagnose(M);
-        model_rhs(M, ds2, true);
+        model_rhs_at(M, 2, true, t + dt * 0.5);
         const double c3 = dt / 12.0;
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data(); const double* b = ds1[q].data(); const double* e = ds2[q].data();
             for (long c = 0; c < M.vol; ++c) s[c] = s[c] + c3 * (8.0 * e[c] - a[c] - b[c]); }
         model_diagnose(M);
     } else if (M.scheme == 0) {   // EF
         auto& ds = M.reg[0];
-        model_rhs(M, ds, true);
+        model_rhs_at(M, 0, true, t);
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds[q].data();
             for (long c = 0; c < M.vol; ++c) s[c] = s[c] + dt * a[c]; }
         model_diagnose(M);
     } else {   // LFAM3
         auto& ds = M.reg[0]; auto& sb = M.reg[1]; auto& sn = M.reg[2];
-        model_rhs(M, ds, false);
+        model_rhs_at(M, 0, false, t);
         if (M.lfam3_first) {
             for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds[q].data();
                 for (long c = 0; c < M.vol; ++c) { sn[q][c] = s[c]; sb[q][c] = s[c]; s[c] = s[c] + dt * a[c]; } }
@@ -847,7 +855,7 @@ void model_forward(Model& M, double t, double dt) {
                     sb[q][c] = sn[q][c];
                 } }
             model_diagnose(M);
-            model_rhs(M, ds, true);
+            model_rhs_at(M, 0, true, t + dt * 0.5);
             for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds[q].data();
                 for (long c = 0; c < M.vol; ++c) s[c] = sn[q][c] + dt * a[c]; }
             model_diagnose(M);
@@ -947,6 +955,8 @@ void orc_model_vortex_force(void* h, int reg) {
     Model* M = (Model*)h; for (auto& a : M->reg[reg]) std::fill(a.begin(), a.end(), 0.0); model_vortex_force(*M, M->reg[reg]); }
 void orc_model_rhs(void* h, int reg, int last) { Model* M = (Model*)h; model_rhs(*M, M->reg[reg], last != 0); }
 void orc_model_forward(void* h, double t, double dt) { model_forward(*(Model*)h, t, dt); }
+void orc_model_set_forcing(void* h, void (*fn)(void*, int, double, void*), void* user) {
+    Model* M = (Model*)h; M->forcing = fn; M->forcing_user = user; }
 void orc_model_fill(void* h, int fld) { Model* M = (Model*)h; model_fill(*M, M->f[fld].data()); }
 // core/nyles.py:227-260
 double orc_model_max_U2(void* h) {

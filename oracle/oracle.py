@@ -86,6 +86,7 @@ def lib():
             "orc_model_fill": (v, [p, i]),
             "orc_model_max_U2": (d, [p]),
             "orc_model_vfwork": (d, [p, p]),
+            "orc_model_set_forcing": (v, [p, p, p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -264,6 +265,17 @@ class OracleModel:
 
     def forward(self, t, dt):
         lib().orc_model_forward(self.h, float(t), float(dt))
+
+    def set_forcing(self, fn):
+        """fn(reg, t) adds tendencies into register set `reg` (numpy views from
+        `register`) after each right-hand side; None detaches it."""
+        if fn is None:
+            self._forcing_cb = None
+            lib().orc_model_set_forcing(self.h, None, None)
+            return
+        proto = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)
+        self._forcing_cb = proto(lambda user, reg, t, stream: fn(reg, t))
+        lib().orc_model_set_forcing(self.h, ctypes.cast(self._forcing_cb, ctypes.c_void_p), None)
 
     def fill(self, name):
         lib().orc_model_fill(self.h, FIELDS[name])

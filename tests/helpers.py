@@ -14,7 +14,7 @@ DIAG = ["p", "ke", "U_i", "U_j", "U_k", "vor_i", "vor_j", "vor_k", "div"]
 
 def make_params(geometry="closed", modelname="LES", timestepping="RK3_SSP", n=(16, 8, 8), L=(1.0, 1.0, 1.0),
                 n_tracers=0, auto_dt=False, dt=1e-3, cfl=0.8, dt_max=1.0, rotating=False, coriolis=1.0,
-                diff_coef=None, precision="fp64", mg_tol=1e-6, mg_maxite=20):
+                diff_coef=None, precision="fp64", mg_tol=1e-6, mg_maxite=20, forced=False):
     from nyles_gb300 import parameters
     parameters.InextensibleDict.unfreeze()
     p = parameters.UserParameters()
@@ -30,6 +30,7 @@ def make_params(geometry="closed", modelname="LES", timestepping="RK3_SSP", n=(1
     p.physics["rotating"] = rotating
     p.physics["coriolis"] = coriolis
     p.physics["diff_coef"] = dict(diff_coef or {})
+    p.physics["forced"] = forced
     p.discretization["global_nx"], p.discretization["global_ny"], p.discretization["global_nz"] = n
     p.gpu["precision"] = precision
     p.gpu["mg_tol"] = mg_tol
