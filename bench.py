@@ -75,6 +75,7 @@ def rt_params(n, precision):
     p.gpu["precision"] = precision
     p.gpu["mg_tol"] = 1e-20
     p.gpu["mg_maxite"] = 40
+    p.gpu["history"] = False
     return p
 
 

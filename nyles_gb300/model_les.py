@@ -159,6 +159,20 @@ class LES(object):
         return {"nite": s.nite, "res": s.res, "solves": s.solves, "vcycles": s.vcycles,
                 "not_converged": s.not_converged}
 
+    def update_stats(self):
+        """Append the multigrid statistics and max|div| of the state to `stats`
+        (core/model_les.py:151-160; the reference's run loop does not call it)."""
+        s = self.mg_stats()
+        s["maxdiv"] = float(self.state.div.view().abs().max())
+        self.stats.append(s)
+
+    def write_stats(self, path):
+        """Pickle `stats` to <path>/stats.pkl (core/model_les.py:162-164)."""
+        import os
+        import pickle
+        with open(os.path.join(path, "stats.pkl"), "wb") as fid:
+            pickle.dump(self.stats, fid)
+
     # ------------------------------------------------------------------ model API
     def _check_state(self, state):
         if state is not self.state:

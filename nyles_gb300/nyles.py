@@ -3,17 +3,22 @@
 Interface of the reference's core/nyles.py:22-260: the constructor checks and freezes
 the parameters, derives nx/ny/nz, the neighbours and the grid, and builds the model
 (``LES``, ``Euler3d`` or ``linear``); ``run()`` projects the initial state and advances
-it to ``tend`` with ``compute_dt()`` (CFL) and ``model.forward``.
+it to ``tend`` with ``compute_dt()`` (CFL) and ``model.forward``, writing the netCDF
+history file (nylesIO) when the gpu parameter `history` is on (the default).
 
-Not part of this build: netCDF history files, the interactive animation, and MPI
-decomposition (one subdomain per process; npx = npy = npz = 1).
+Not part of this build: the interactive animation, and MPI decomposition (one subdomain
+per process; npx = npy = npz = 1).
 """
+import os
+import pickle
+import sys
 import time
 
 import numpy as np
 
 from . import grid as grid_module
 from . import model_les
+from . import nylesIO
 from . import online_diag
 from . import topology as topo
 
@@ -61,6 +66,13 @@ class Nyles(object):
         self.blowup_check = param.get("gpu", {}).get("blowup_check", True)
         self.gridcellpersubdom = param["nx"] * param["ny"] * param["nz"]
         self.diag = online_diag.VFwork(self.model, self.grid)   # core/nyles.py:102
+        # history files and param.pkl (core/nyles.py:78-87), unless the gpu parameter
+        # `history` is off
+        self.IO = None
+        if param.get("gpu", {}).get("history", True):
+            self.IO = nylesIO.NylesIO(param)
+            with open(os.path.join(self.IO.output_directory, "param.pkl"), "wb") as fid:
+                pickle.dump(param, fid)
 
     def compute_dt(self):
         """cfl / max|U| bounded by dt_max, or the fixed dt (core/nyles.py:227-260)."""
@@ -83,7 +95,17 @@ class Nyles(object):
         dt_hist = float(self.param.get("timestep_history", 0.0))
         t_next_hist = dt_hist
         self.kdiss = []
-        self.model.diagnose_var(self.model.state)
+        self.model.diagnose_var(self.model.state)   # core/nyles.py:122
+        if self.IO is not None:                      # core/nyles.py:131-139
+            if verbose:
+                print("Creating output file:", self.IO.hist_path)
+            self.IO.init(self.model.state, self.grid, t, n)
+            t_next_hist = self.IO.t_next_hist
+            script = sys.argv[0] if sys.argv else ""
+            if script.endswith(".py") and os.path.isfile(script):
+                if verbose:
+                    print("Backing up script to:", self.IO.script_path)
+                self.IO.backup_scriptfile(script)
         realtime0 = time.time()
         blowup = False
         while True:
@@ -91,15 +113,22 @@ class Nyles(object):
                 dt = self.compute_dt()
             except nat.BlowUp:
                 blowup = True
+                if self.IO is not None:              # last frame at blow-up (core/nyles.py:186-201)
+                    self.IO.t_next_hist = t
+                    self.IO.write(self.model.state, t, n)
                 break
             self.model.forward(t, dt)
             t += dt
             n += 1
-            if t >= t_next_hist:
+            if t >= t_next_hist:                     # core/nyles.py:166-171
                 Kdiss = self.diag.compute()
                 self.kdiss.append((t, Kdiss))
                 if verbose:
                     print(f"\nKdiss = {Kdiss}")
+            if self.IO is not None:
+                self.IO.write(self.model.state, t, n)
+                t_next_hist = self.IO.t_next_hist
+            elif t >= t_next_hist:
                 t_next_hist += dt_hist
             if callback is not None:
                 callback(self, t, n)
@@ -116,6 +145,11 @@ class Nyles(object):
                 self.model.max_U2()
             except nat.BlowUp:
                 blowup = True
+        if self.IO is not None:                      # core/nyles.py:217-222
+            self.IO.finalize(self.model.state, t, n)
+            self.model.write_stats(self.IO.output_directory)
+            if verbose:
+                print("Output written to:", self.IO.hist_path)
         if verbose:
             print()
             print("BLOW UP!" if blowup else "Job completed as expected")

@@ -92,6 +92,7 @@ def build_params(case, n, precision="mixed", mg_tol=1e-6):
     p.discretization["global_nz"] = n
     p.gpu["precision"] = precision
     p.gpu["mg_tol"] = mg_tol
+    p.gpu["history"] = False
     return p
 
 

@@ -35,6 +35,7 @@ def make_params(geometry="closed", modelname="LES", timestepping="RK3_SSP", n=(1
     p.gpu["precision"] = precision
     p.gpu["mg_tol"] = mg_tol
     p.gpu["mg_maxite"] = mg_maxite
+    p.gpu["history"] = False
     return p
 
 
