@@ -66,6 +66,13 @@ typedef struct NylesDesc {
     double dx2;              /* dx**2 as computed by the host, core/mgfordriver.py:78 */
     double fparam;           /* covariant Coriolis coriolis*dx*dy (0 when not rotating), core/model_les.py:61-67 */
     double viscosity;        /* diff_coef['u'], core/viscosity.py:3-9 */
+    /* Tracer diffusion (core/tracer.py:74-76): diff_coef of b, t0, t1.. added as
+     * add_laplacian after each direction's advection on the last stage. The reference
+     * never passes `last` to rhstrac (core/model_les.py:133), so its tracer diffusion
+     * never runs; it runs here only when bit q of tracer_diffusion is set (q = 0 for b,
+     * 1 + k for tk). 0 = the reference's behaviour. */
+    double tracer_diffusivity[NYLES_MAX_TRACERS + 1];
+    int tracer_diffusion;
 } NylesDesc;
 
 typedef struct NylesMgStats {

@@ -50,7 +50,8 @@ class NylesDesc(ctypes.Structure):
                 ("n_tracers", ctypes.c_int), ("model", ctypes.c_int), ("add_viscosity", ctypes.c_int),
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("idx2", ctypes.c_double), ("idy2", ctypes.c_double), ("idz2", ctypes.c_double),
-                ("dx2", ctypes.c_double), ("fparam", ctypes.c_double), ("viscosity", ctypes.c_double)]
+                ("dx2", ctypes.c_double), ("fparam", ctypes.c_double), ("viscosity", ctypes.c_double),
+                ("tracer_diffusivity", ctypes.c_double * (MAX_TRACERS + 1)), ("tracer_diffusion", ctypes.c_int)]
 
 
 class NylesMgStats(ctypes.Structure):

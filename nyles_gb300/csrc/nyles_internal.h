@@ -53,7 +53,7 @@ struct ProgPtrs {
 };
 
 // term bits of launch_rhs
-enum { TERM_TRACER = 1, TERM_VF = 2, TERM_BERNOULLI = 4, TERM_VISC = 8, TERM_ACCUMULATE = 16 };
+enum { TERM_TRACER = 1, TERM_VF = 2, TERM_BERNOULLI = 4, TERM_VISC = 8, TERM_ACCUMULATE = 16, TERM_TRDIFF = 32 };
 
 template <typename T>
 int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,

@@ -64,6 +64,10 @@ static int check_desc(const NylesDesc* d, Geom* g) {
     if (!d) { set_error("null descriptor"); return NYLES_BAD_ARG; }
     if (d->n_tracers < 0 || d->n_tracers > NYLES_MAX_TR) { set_error("n_tracers out of range (0..8)"); return NYLES_BAD_ARG; }
     if (d->model < 0 || d->model > 2) { set_error("unknown model"); return NYLES_BAD_ARG; }
+    if (d->tracer_diffusion < 0 || (d->tracer_diffusion >> (d->n_tracers + 1)) != 0) {
+        set_error("tracer_diffusion names a tracer beyond b, t0..t{n_tracers-1}");
+        return NYLES_BAD_ARG;
+    }
     if ((d->periodic_x || d->periodic_y || d->periodic_z) && d->nh != 3) {
         set_error("periodic directions need nh == 3 (the multigrid halo width, mg_types.f90:18)");
         return NYLES_UNSUPPORTED;
@@ -100,6 +104,8 @@ static int rhs_terms(const NylesDesc* d, int last) {
     if (d->model != NYLES_MODEL_EULER3D) t |= TERM_TRACER;   // model_les_euler.py:131
     if (d->model != NYLES_MODEL_LINEAR) t |= TERM_VF;        // model_les.py:135-136
     if (last && d->add_viscosity) t |= TERM_VISC;            // model_les.py:140-141
+    // tracer.py:74-76 (opt-in: the reference's rhs never passes last to rhstrac)
+    if (last && d->tracer_diffusion && d->model != NYLES_MODEL_EULER3D) t |= TERM_TRDIFF;
     return t;
 }
 

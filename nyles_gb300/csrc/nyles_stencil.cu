@@ -45,25 +45,6 @@ __device__ __forceinline__ T tr_flux(const T* __restrict__ Uf, const T* __restri
     return flux1d_at(i, n, __ldg(Uf + c), Q);
 }
 
-// -(flux divergence) of one tracer at a cell, accumulated direction by direction in
-// the reference's order (x pass assigns, y and z passes add), core/tracer.py:59-72
-template <typename T>
-__device__ __forceinline__ T tracer_rhs(const T* __restrict__ q, const T* const* U, const Geom& g, long long c,
-                                        const int* pos) {
-    T acc = T(0);
-    for (int pass = 0; pass < 3; ++pass) {
-        const int d = 2 - pass;            // x, then y, then z
-        const int i = pos[d];
-        const T Fi = tr_flux(U[d], q, g, c, i, d);
-        if (i > 0) {
-            const T Fm = tr_flux(U[d], q, g, c - g.stride(d), i - 1, d);
-            acc = (acc + Fm) - Fi;
-        } else {
-            acc = acc - Fi;
-        }
-    }
-    return acc;
-}
 
 template <typename T>
 struct RhsArgs {
@@ -80,6 +61,8 @@ struct RhsArgs {
     int euler;        // Euler3d: no buoyancy in Bernoulli
     T half_dz;        // 0.5*dz, fortran_bernoulli.f90:49
     T vcoef[3];       // viscosity*ids2 for directions x, y, z
+    T kcoef[NYLES_MAX_TR + 1][3];   // tracer diffusivity*ids2 of b, t0.. for x, y, z
+    int kmask;        // bit q: diffuse tracer q (b = 0) when TERM_TRDIFF is set
 };
 
 // viscosity along direction d of component field u at c, core/fortran_dissipation.f90:18-33
@@ -90,6 +73,29 @@ __device__ __forceinline__ T lap1d(const T* __restrict__ u, const Geom& g, long 
     T fx = (i < n - 1) ? (__ldg(u + c + s) - __ldg(u + c)) : T(0);
     T fxm = (i > 0) ? (__ldg(u + c) - __ldg(u + c - s)) : T(0);
     return fx - fxm;
+}
+
+// -(flux divergence) of one tracer at a cell, accumulated direction by direction in
+// the reference's order (x pass assigns, y and z passes add), core/tracer.py:59-72;
+// with `diff`, each direction's diffusion k[pass]*lap follows its advection
+// (core/tracer.py:74-76)
+template <typename T>
+__device__ __forceinline__ T tracer_rhs(const T* __restrict__ q, const T* const* U, const Geom& g, long long c,
+                                        const int* pos, bool diff, T kx, T ky, T kz) {
+    T acc = T(0);
+    for (int pass = 0; pass < 3; ++pass) {
+        const int d = 2 - pass;            // x, then y, then z
+        const int i = pos[d];
+        const T Fi = tr_flux(U[d], q, g, c, i, d);
+        if (i > 0) {
+            const T Fm = tr_flux(U[d], q, g, c - g.stride(d), i - 1, d);
+            acc = (acc + Fm) - Fi;
+        } else {
+            acc = acc - Fi;
+        }
+        if (diff) acc = acc + (pass == 0 ? kx : (pass == 1 ? ky : kz)) * lap1d(q, g, c, i, d);
+    }
+    return acc;
 }
 
 template <typename T>
@@ -109,7 +115,8 @@ __global__ void __launch_bounds__(128) k_rhs(const RhsArgs<T> a) {
         for (int t = 0; t <= a.ntr; ++t) {
             const T* q = (t == 0) ? a.b : a.tr[t - 1];
             const int slot = (t == 0) ? 0 : 3 + t;
-            T v = tracer_rhs(q, Uxyz, g, c, pos);
+            const bool diff = (a.terms & TERM_TRDIFF) && ((a.kmask >> t) & 1);
+            T v = tracer_rhs(q, Uxyz, g, c, pos, diff, a.kcoef[t][0], a.kcoef[t][1], a.kcoef[t][2]);
             if (a.ds[slot]) a.ds[slot][c] = acc ? a.ds[slot][c] + v : v;
         }
     } else if (!acc) {
@@ -169,13 +176,15 @@ template <typename T>
 struct TracerMarch {
     T fz_prev;
     // -(flux divergence) at (z, ys, xs); all threads of the block must call it
+    // with `diff`, k[pass]*lap follows each direction's advection (core/tracer.py:74-76)
     __device__ __forceinline__ T step(const T* __restrict__ q, const T* const* U, const Geom& g, long long c, int z,
-                                      int ys, int xs, T (*sfy)[RZ_BX]) {
+                                      int ys, int xs, T (*sfy)[RZ_BX], bool diff, T kx, T ky, T kz) {
         const int tx = threadIdx.x, ty = threadIdx.y;
         const T fx = tr_flux(U[2], q, g, c, xs, 2);
         T fxm = __shfl_up_sync(0xffffffffu, fx, 1);
         if (tx == 0 && xs > 0) fxm = tr_flux(U[2], q, g, c - 1, xs - 1, 2);
         T acc = (xs > 0) ? (T(0) + fxm) - fx : T(0) - fx;
+        if (diff) acc = acc + kx * lap1d(q, g, c, xs, 2);
         const T fy = tr_flux(U[1], q, g, c, ys, 1);
         sfy[ty][tx] = fy;
         __syncthreads();
@@ -183,15 +192,19 @@ struct TracerMarch {
         __syncthreads();
         if (ty == 0 && ys > 0) fym = tr_flux(U[1], q, g, c - g.sy, ys - 1, 1);
         acc = (ys > 0) ? (acc + fym) - fy : acc - fy;
+        if (diff) acc = acc + ky * lap1d(q, g, c, ys, 1);
         const T fz = tr_flux(U[0], q, g, c, z, 0);
         acc = (z > 0) ? (acc + fz_prev) - fz : acc - fz;
+        if (diff) acc = acc + kz * lap1d(q, g, c, z, 0);
         fz_prev = fz;
         return acc;
     }
 };
 
-// TR: buoyancy advection on; VF: vortex force on. ds[0..3] are written.
-template <typename T, bool TR, bool VF>
+// TR: buoyancy advection on; VF: vortex force on; BDIFF: buoyancy diffusion on (a
+// template flag so that the default instances carry none of its registers). ds[0..3]
+// are written.
+template <typename T, bool TR, bool VF, bool BDIFF>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a) {
     __shared__ T sfy[RZ_BY][RZ_BX];
     const Geom& g = a.g;
@@ -210,7 +223,7 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a)
         const long long c = g.at(z, ys, xs);
         const int pos[3] = {z, ys, xs};
         T db = T(0);
-        if (TR) db = tm.step(a.b, Uzyx, g, c, z, ys, xs, sfy);
+        if (TR) db = tm.step(a.b, Uzyx, g, c, z, ys, xs, sfy, BDIFF, a.kcoef[0][0], a.kcoef[0][1], a.kcoef[0][2]);
         T dux = T(0), duy = T(0), duz = T(0);
         if (VF) {
             if (ys < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, xs, 2, 1);
@@ -248,10 +261,11 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a)
 }
 
 // advection of one passive tracer (core/tracer.py:59-72) with the same flux sharing
-template <typename T>
+template <typename T, bool DIFF>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, const T* __restrict__ Ux,
                                                                 const T* __restrict__ Uy, const T* __restrict__ Uz,
-                                                                const T* __restrict__ q, T* __restrict__ dq) {
+                                                                const T* __restrict__ q, T* __restrict__ dq,
+                                                                T kx, T ky, T kz) {
     __shared__ T sfy[RZ_BY][RZ_BX];
     const int x = blockIdx.x * RZ_BX + threadIdx.x;
     const int y = blockIdx.y * RZ_BY + threadIdx.y;
@@ -264,7 +278,7 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, co
     tm.fz_prev = z0 > 0 ? tr_flux(U[0], q, g, g.at(z0 - 1, ys, xs), z0 - 1, 0) : T(0);
     for (int z = z0; z <= z1; ++z) {
         const long long c = g.at(z, ys, xs);
-        const T v = tm.step(q, U, g, c, z, ys, xs, sfy);
+        const T v = tm.step(q, U, g, c, z, ys, xs, sfy, DIFF, kx, ky, kz);
         if (valid) dq[c] = v;
     }
 }
@@ -311,6 +325,12 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     a.vcoef[0] = T(d->viscosity * d->idx2);
     a.vcoef[1] = T(d->viscosity * d->idy2);
     a.vcoef[2] = T(d->viscosity * d->idz2);
+    a.kmask = d->tracer_diffusion;
+    for (int q = 0; q <= NYLES_MAX_TR; ++q) {   // diff_coef[name]*ids2[direction], core/tracer.py:75
+        a.kcoef[q][0] = T(d->tracer_diffusivity[q] * d->idx2);
+        a.kcoef[q][1] = T(d->tracer_diffusivity[q] * d->idy2);
+        a.kcoef[q][2] = T(d->tracer_diffusivity[q] * d->idz2);
+    }
     if (terms & TERM_ACCUMULATE) {   // add into existing registers (vortex force alone)
         dim3 blk(32, 2, 2);
         k_rhs<T><<<grid3(g, blk), blk, 0, st>>>(a);
@@ -320,14 +340,23 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     const dim3 blk(RZ_BX, RZ_BY, 1);
     const dim3 grd((g.N[2] + RZ_BX - 1) / RZ_BX, (g.N[1] + RZ_BY - 1) / RZ_BY, (g.N[0] + RZ_ZC - 1) / RZ_ZC);
     const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
-    if (tr && vf) k_rhs_march<T, true, true><<<grd, blk, 0, st>>>(a);
-    else if (tr) k_rhs_march<T, true, false><<<grd, blk, 0, st>>>(a);
-    else if (vf) k_rhs_march<T, false, true><<<grd, blk, 0, st>>>(a);
-    else k_rhs_march<T, false, false><<<grd, blk, 0, st>>>(a);
+    const bool bdiff = tr && (terms & TERM_TRDIFF) && (d->tracer_diffusion & 1);
+    if (tr && vf && bdiff) k_rhs_march<T, true, true, true><<<grd, blk, 0, st>>>(a);
+    else if (tr && vf) k_rhs_march<T, true, true, false><<<grd, blk, 0, st>>>(a);
+    else if (tr && bdiff) k_rhs_march<T, true, false, true><<<grd, blk, 0, st>>>(a);
+    else if (tr) k_rhs_march<T, true, false, false><<<grd, blk, 0, st>>>(a);
+    else if (vf) k_rhs_march<T, false, true, false><<<grd, blk, 0, st>>>(a);
+    else k_rhs_march<T, false, false, false><<<grd, blk, 0, st>>>(a);
     note_launch();
     for (int t = 0; t < d->n_tracers; ++t) {
         if (tr) {
-            k_tracer_march<T><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.tr[t], a.ds[4 + t]);
+            const T* kc = a.kcoef[t + 1];
+            if ((terms & TERM_TRDIFF) && ((d->tracer_diffusion >> (t + 1)) & 1))
+                k_tracer_march<T, true><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.tr[t], a.ds[4 + t],
+                                                             kc[0], kc[1], kc[2]);
+            else
+                k_tracer_march<T, false><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.tr[t], a.ds[4 + t],
+                                                              T(0), T(0), T(0));
             note_launch();
         } else {   // Euler3d: tracers are not advected, their tendency is zero (reset_state)
             cudaMemsetAsync(a.ds[4 + t], 0, sizeof(T) * g.vol, st);

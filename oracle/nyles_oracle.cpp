@@ -603,6 +603,9 @@ struct Model {
     double dx, dy, dz, idx2, idy2, idz2;
     double fparam = 0.0;  // covariant Coriolis (coriolis * dx * dy), 0 if not rotating
     double visc = 0.0; int add_visc = 0;
+    // tracer diffusion (core/tracer.py:74-76), applied only when bit q of trdiff_mask is
+    // set (q = 0 for b): the reference's rhs never passes `last` to rhstrac
+    double kappa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}; int trdiff_mask = 0;
     bool lfam3_first = true;
     long vol;
     std::vector<std::vector<double>> f;    // state fields (14 + ntr)
@@ -669,8 +672,9 @@ void model_vortex_force(Model& M, std::vector<std::vector<double>>& ds) {
     }
 }
 
-// core/tracer.py:44-78
-void model_rhstrac(Model& M, std::vector<std::vector<double>>& ds) {
+// core/tracer.py:44-78; `last` with a tracer's bit in trdiff_mask adds its diffusion
+// after each direction's advection (core/tracer.py:74-76)
+void model_rhstrac(Model& M, std::vector<std::vector<double>>& ds, bool last) {
     if (M.model == 1) return;   // Euler3d: tracer step commented out (model_les_euler.py:131)
     for (int tr = 0; tr <= M.ntr; ++tr) {
         int fld = (tr == 0) ? B : T0 + tr - 1;
@@ -680,6 +684,10 @@ void model_rhstrac(Model& M, std::vector<std::vector<double>>& ds) {
             V3 dfield = rv(M, ds, fld, d);
             if (d == 'i') { double* p = ds[fld == B ? 0 : 4 + (fld - T0)].data(); std::fill(p, p + M.vol, 0.0); }
             upwind(field, vel, dfield);
+            if (last && ((M.trdiff_mask >> tr) & 1)) {
+                double ids2 = d == 'i' ? M.idx2 : (d == 'j' ? M.idy2 : M.idz2);
+                add_laplacian(field, dfield, M.kappa[tr] * ids2);
+            }
         }
     }
 }
@@ -707,7 +715,7 @@ void model_viscosity(Model& M, std::vector<std::vector<double>>& ds) {
 // core/model_les.py:130-144, :167-175
 void model_rhs(Model& M, std::vector<std::vector<double>>& ds, bool last) {
     for (auto& a : ds) std::fill(a.begin(), a.end(), 0.0);
-    model_rhstrac(M, ds);
+    model_rhstrac(M, ds, last);
     if (M.model != 2) model_vortex_force(M, ds);
     model_bernoulli(M, ds);
     if (last && M.add_visc) model_viscosity(M, ds);
@@ -945,7 +953,11 @@ void* orc_model_create(int nx, int ny, int nz, int nh, int per_bits, int ntr, in
 }
 void orc_model_destroy(void* h) { Model* M = (Model*)h; delete M->mg; delete M; }
 double* orc_model_field(void* h, int fld) { return ((Model*)h)->f[fld].data(); }
-double* orc_model_reg(void* h, int r, int q) { return ((Model*)h)->reg[r][q].data(); }
+double* orc_model_reg(void* h, int r, int q) {
+    Model* M = (Model*)h;
+    if (r < 0 || r >= (int)M->reg.size() || q < 0 || q >= M->nprog()) return nullptr;
+    return M->reg[r][q].data();
+}
 void orc_model_mg_params(void* h, double tol, int maxite, double omega) {
     Model* M = (Model*)h; M->mg->tol = tol; M->mg->maxite = maxite; M->mg->omega = omega; }
 void orc_model_mg_stats(void* h, int* nite, double* res) { Model* M = (Model*)h; *nite = M->mg->nite; *res = M->mg->res; }
@@ -953,6 +965,11 @@ void* orc_model_mg(void* h) { return ((Model*)h)->mg; }
 void orc_model_diagnose(void* h) { model_diagnose(*(Model*)h); }
 void orc_model_vortex_force(void* h, int reg) {
     Model* M = (Model*)h; for (auto& a : M->reg[reg]) std::fill(a.begin(), a.end(), 0.0); model_vortex_force(*M, M->reg[reg]); }
+void orc_model_set_tracer_diffusion(void* h, const double* kappa, int mask) {
+    Model* M = (Model*)h;
+    for (int q = 0; q <= M->ntr; ++q) M->kappa[q] = kappa[q];
+    M->trdiff_mask = mask;
+}
 void orc_model_rhs(void* h, int reg, int last) { Model* M = (Model*)h; model_rhs(*M, M->reg[reg], last != 0); }
 void orc_model_forward(void* h, double t, double dt) { model_forward(*(Model*)h, t, dt); }
 void orc_model_set_forcing(void* h, void (*fn)(void*, int, double, void*), void* user) {

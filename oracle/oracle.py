@@ -87,6 +87,7 @@ def lib():
             "orc_model_max_U2": (d, [p]),
             "orc_model_vfwork": (d, [p, p]),
             "orc_model_set_forcing": (v, [p, p, p]),
+            "orc_model_set_tracer_diffusion": (v, [p, p, i]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -197,7 +198,9 @@ class OracleModel:
     """One subdomain of the LES model (core/model_les.py) on the CPU.
 
     ``desc`` holds: nx, ny, nz, nh, geometry, n_tracers, modelname, timestepping,
-    dx, dy, dz, idx2, idy2, idz2, fparam, visc (None = off).
+    dx, dy, dz, idx2, idy2, idz2, fparam, visc (None = off), and optionally
+    tracer_diffusion = {"b": kappa, "t0": kappa, ...} for the opt-in tracer diffusion
+    on the last stage (core/tracer.py:74-76; never applied by the reference's rhs).
     """
 
     def __init__(self, desc):
@@ -217,6 +220,16 @@ class OracleModel:
                       desc["ny"] + (2 * nh if per & 2 else 0),
                       desc["nx"] + (2 * nh if per & 1 else 0))
         self.ntr = desc.get("n_tracers", 0)
+        trd = desc.get("tracer_diffusion") or {}
+        if trd:
+            names = ["b"] + ["t%d" % k for k in range(self.ntr)]
+            kappa = (ctypes.c_double * 9)()
+            mask = 0
+            for q, name in enumerate(names):
+                if name in trd:
+                    kappa[q] = float(trd[name])
+                    mask |= 1 << q
+            lib().orc_model_set_tracer_diffusion(self.h, kappa, mask)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -235,6 +248,8 @@ class OracleModel:
 
     def register(self, r, q):
         ptr = lib().orc_model_reg(self.h, r, q)
+        if not ptr:
+            raise IndexError("register %d, prognostic %d out of range" % (r, q))
         n = int(np.prod(self.shape))
         return np.ctypeslib.as_array(ptr, shape=(n,)).reshape(self.shape)
 

@@ -65,6 +65,11 @@ STEP_CASES = [
           timestepping="LFAM3", dt=5e-3), "tgv"),
     (dict(geometry="closed", n=(16, 16, 16), timestepping="EF", dt=1e-3, diff_coef={"u": 1e-3},
           rotating=True), "noise"),
+    # opt-in tracer diffusion on the last stage (core/tracer.py:74-76)
+    (dict(geometry="perio_xy", n=(16, 16, 16), n_tracers=2, dt=1e-3, diff_coef={"u": 1e-3, "b": 2e-3, "t1": 1e-3},
+          tracer_diffusion=True), "noise"),
+    (dict(geometry="closed", n=(16, 16, 16), n_tracers=1, timestepping="LFAM3", dt=1e-3,
+          diff_coef={"b": 5e-3, "t0": 1e-3}, tracer_diffusion=True), "noise"),
 ]
 
 
@@ -112,10 +117,18 @@ def test_lock_exchange_100_steps():
         assert errs[s] < 1e-9, (s, errs[s])
 
 
-def test_mixed_precision_error_small():
+MIXED_CASES = [
+    dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30),
+    dict(geometry="closed", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
+         diff_coef={"u": 1e-3, "b": 2e-3, "t0": 1e-3}, tracer_diffusion=True),
+]
+
+
+@pytest.mark.parametrize("k", range(len(MIXED_CASES)))
+def test_mixed_precision_error_small(k):
     """Mixed path (FP32 state/stencils, FP32 V-cycles in FP64 refinement) against FP64."""
     from nyles_gb300.nyles import Nyles
-    cfg = dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30)
+    cfg = MIXED_CASES[k]
     runs = {}
     for prec in ("fp64", "mixed"):
         p = helpers.make_params(precision=prec, **cfg)
@@ -128,8 +141,9 @@ def test_mixed_precision_error_small():
         for n in range(20):
             nyl.model.forward(t, 1e-3)
             t += 1e-3
-        runs[prec] = {s: nyl.model.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k")}
-    for s in ("b", "u_i", "u_j", "u_k"):
+        names = ["b", "u_i", "u_j", "u_k"] + ["t%d" % i for i in range(cfg.get("n_tracers", 0))]
+        runs[prec] = {s: nyl.model.state.get(s).view("i").double().cpu().numpy() for s in names}
+    for s in runs["fp64"]:
         assert helpers.relerr(runs["mixed"][s], runs["fp64"][s]) < 1e-5, s
 
 

@@ -132,3 +132,44 @@ def test_compute_dt_cases():
     o.field("U_k")[...] = 1.0
     assert o.compute_dt(True, 0.1, cfl, dt_max) == pytest.approx(cfl / np.sqrt(3))
     assert o.compute_dt(False, 0.1, cfl, dt_max) == 0.1
+
+
+def test_tracer_diffusion_adds_laplacians_on_last_stage():
+    """Opt-in tracer diffusion (core/tracer.py:74-76): on the last stage the tendency of
+    each named tracer gains sum_d kappa*ids2[d]*(phi[i+1]-2phi[i]+phi[i-1]) with no flux
+    through the array ends (core/fortran_dissipation.f90:2-35); tracers without a
+    coefficient and the velocity are unchanged, and without `last` nothing changes."""
+    nx, ny, nz = 8, 6, 5
+    L = (2.0, 1.5, 1.0)
+    dx, dy, dz = L[0] / nx, L[1] / ny, L[2] / nz
+    base = dict(nx=nx, ny=ny, nz=nz, nh=3, geometry="closed", n_tracers=2, modelname="LES",
+                timestepping="RK3_SSP", dx=dx, dy=dy, dz=dz, idx2=1 / dx ** 2, idy2=1 / dy ** 2, idz2=1 / dz ** 2)
+    kappa = {"b": 1e-2, "t1": 3e-3}
+    plain = oracle.OracleModel(base)
+    diff = oracle.OracleModel(dict(base, tracer_diffusion=kappa))
+    rng = np.random.default_rng(4)
+    for name in ("b", "t0", "t1", "u_i", "u_j", "u_k"):
+        a = rng.standard_normal(plain.shape)
+        plain.field(name)[...] = a
+        diff.field(name)[...] = a
+    for m in (plain, diff):
+        m.diagnose()
+    plain.rhs(0, last=True)
+    diff.rhs(0, last=False)
+    for q in range(6):                           # b, u_i, u_j, u_k, t0, t1
+        np.testing.assert_array_equal(diff.register(0, q), plain.register(0, q))
+    diff.rhs(0, last=True)
+
+    def lap(phi, axis, coef):
+        f = np.diff(phi, axis=axis)
+        pad = [(0, 0)] * 3
+        pad[axis] = (1, 1)
+        f = np.pad(f, pad)                       # zero flux through both array ends
+        return coef * np.diff(f, axis=axis)
+
+    for q, name in ((0, "b"), (5, "t1")):
+        phi = diff.field(name)
+        expect = sum(lap(phi, ax, kappa[name] * c) for ax, c in ((2, 1 / dx ** 2), (1, 1 / dy ** 2), (0, 1 / dz ** 2)))
+        np.testing.assert_allclose(diff.register(0, q) - plain.register(0, q), expect, rtol=1e-9, atol=1e-12)
+    for q in (1, 2, 3, 4):                       # u_i, u_j, u_k and t0 (no coefficient)
+        np.testing.assert_array_equal(diff.register(0, q), plain.register(0, q))
