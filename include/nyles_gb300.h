@@ -34,7 +34,9 @@ enum {
 };
 
 /* ---------------------------------------------------------------- enumerations */
-enum { NYLES_MODEL_LES = 0, NYLES_MODEL_EULER3D = 1, NYLES_MODEL_LINEAR = 2 }; /* core/nyles.py:92-100 */
+/* core/nyles.py:92-100; NYLES_MODEL_ADVECTION is core/model_advection.py (b advected by
+ * the stored contravariant velocity U, which the model never changes) */
+enum { NYLES_MODEL_LES = 0, NYLES_MODEL_EULER3D = 1, NYLES_MODEL_LINEAR = 2, NYLES_MODEL_ADVECTION = 3 };
 enum { NYLES_SCHEME_EF = 0, NYLES_SCHEME_LFAM3 = 1, NYLES_SCHEME_RK3_SSP = 2 };  /* core/timescheme.py:80-90 */
 enum { NYLES_FP64 = 0, NYLES_MIXED = 1 };
 /* multigrid topology, core/mgfor/mg_enums.f90:6 */
@@ -73,6 +75,12 @@ typedef struct NylesDesc {
      * 1 + k for tk). 0 = the reference's behaviour. */
     double tracer_diffusivity[NYLES_MAX_TRACERS + 1];
     int tracer_diffusion;
+    /* Tracer advection scheme: 0 = WENO (core/fortran_upwind.f90:63-80, the only branch
+     * the reference runs: `linear` is hard-coded .false. at :28); 1..5 = the linear
+     * branch of core/fortran_upwind.f90:32-61 with the interpolation of that order
+     * from core/interpolate_tracer.f90 (odd: upwind-biased, even: centred), i.e.
+     * param orderA. */
+    int tracer_order;
 } NylesDesc;
 
 typedef struct NylesMgStats {
@@ -154,8 +162,14 @@ int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omeg
 int nyles_model_forward(NylesModel* m, double t, double dt, void* stream);
 /* LES.diagnose_var, core/model_les.py:98-127 (core/model_les_euler.py:96-125) */
 int nyles_model_diagnose(NylesModel* m, void* stream);
-/* LES.rhs(state, t, dstate, last) into register set `reg`, core/model_les.py:130-144 */
+/* LES.rhs(state, t, dstate, last) into register set `reg`, core/model_les.py:130-144
+ * (advection model: Advection.rhs, core/model_advection.py:59-61, b only; the velocity
+ * registers are left as they are) */
 int nyles_model_rhs(NylesModel* m, int reg, double t, int last, void* stream);
+/* Advection.make_u_divergentfree, core/model_advection.py:38-53: fill u, project u with
+ * the multigrid (p = x*dx^2, u -= grad p, as LES.diagnose_var), fill u, U = u/dx^2 and
+ * div of the new U (halo filled). Any model kind. */
+int nyles_model_project(NylesModel* m, void* stream);
 /* User forcing (core/model_les.py:143-144, `forcing.add(state, dstate, t)` when the
  * parameter `forced` is set): `fn(user, reg, t, stream)` is called on the host after
  * every right-hand side of forward/rhs, with the register set holding that stage's

@@ -18,7 +18,7 @@ NYLES_BLOWUP = 4
 NYLES_TIMEOUT = 5
 NYLES_UNSUPPORTED = 6
 
-MODEL = {"LES": 0, "Euler3d": 1, "linear": 2}
+MODEL = {"LES": 0, "Euler3d": 1, "linear": 2, "advection": 3}
 SCHEME = {"EF": 0, "LFAM3": 1, "RK3_SSP": 2}
 PRECISION = {"fp64": 0, "mixed": 1}
 MG_TOPOLOGY = {"closed": 1, "perio_x": 2, "perio_y": 3, "perio_xy": 5, "perio_xyz": 6}
@@ -51,7 +51,8 @@ class NylesDesc(ctypes.Structure):
                 ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
                 ("idx2", ctypes.c_double), ("idy2", ctypes.c_double), ("idz2", ctypes.c_double),
                 ("dx2", ctypes.c_double), ("fparam", ctypes.c_double), ("viscosity", ctypes.c_double),
-                ("tracer_diffusivity", ctypes.c_double * (MAX_TRACERS + 1)), ("tracer_diffusion", ctypes.c_int)]
+                ("tracer_diffusivity", ctypes.c_double * (MAX_TRACERS + 1)), ("tracer_diffusion", ctypes.c_int),
+                ("tracer_order", ctypes.c_int)]
 
 
 class NylesMgStats(ctypes.Structure):
@@ -93,6 +94,7 @@ SIGNATURES = {
     "nyles_model_forward": (_I, [_P, _D, _D, _P]),
     "nyles_model_diagnose": (_I, [_P, _P]),
     "nyles_model_rhs": (_I, [_P, _I, _D, _I, _P]),
+    "nyles_model_project": (_I, [_P, _P]),
     "nyles_model_set_forcing": (_I, [_P, _P, _P]),
     "nyles_model_max_U2": (_I, [_P, ctypes.POINTER(ctypes.c_double), _P]),
     "nyles_model_vfwork": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double), _P]),

@@ -63,7 +63,15 @@ void Prof::release() {
 static int check_desc(const NylesDesc* d, Geom* g) {
     if (!d) { set_error("null descriptor"); return NYLES_BAD_ARG; }
     if (d->n_tracers < 0 || d->n_tracers > NYLES_MAX_TR) { set_error("n_tracers out of range (0..8)"); return NYLES_BAD_ARG; }
-    if (d->model < 0 || d->model > 2) { set_error("unknown model"); return NYLES_BAD_ARG; }
+    if (d->model < 0 || d->model > 3) { set_error("unknown model"); return NYLES_BAD_ARG; }
+    if (d->model == NYLES_MODEL_ADVECTION && d->n_tracers != 0) {
+        set_error("the advection model advects b only (n_tracers must be 0)");
+        return NYLES_BAD_ARG;
+    }
+    if (d->tracer_order < 0 || d->tracer_order > 5) {
+        set_error("tracer_order must be 0 (WENO) or an interpolation order 1..5");
+        return NYLES_BAD_ARG;
+    }
     if (d->tracer_diffusion < 0 || (d->tracer_diffusion >> (d->n_tracers + 1)) != 0) {
         set_error("tracer_diffusion names a tracer beyond b, t0..t{n_tracers-1}");
         return NYLES_BAD_ARG;
@@ -100,6 +108,9 @@ static ProgPtrs<T> state_prog(const NylesDesc* d, const StencilPtrs<T>& s) {
 }
 
 static int rhs_terms(const NylesDesc* d, int last) {
+    // Advection.rhs passes `last` to rhstrac, so its diffusion of b is live
+    // (core/model_advection.py:59-61)
+    if (d->model == NYLES_MODEL_ADVECTION) return TERM_TRACER | ((last && (d->tracer_diffusion & 1)) ? TERM_TRDIFF : 0);
     int t = TERM_BERNOULLI;
     if (d->model != NYLES_MODEL_EULER3D) t |= TERM_TRACER;   // model_les_euler.py:131
     if (d->model != NYLES_MODEL_LINEAR) t |= TERM_VF;        // model_les.py:135-136
@@ -409,16 +420,13 @@ static int model_rhs(NylesModel* m, int reg, int last, double t, cudaStream_t st
     return rc;
 }
 
-// core/model_les.py:98-127 ; core/model_les_euler.py:96-125
+// compute_p (core/projection.py:39-87): divergence of U = u/dx^2 into the multigrid
+// right-hand side (and div), solve, p = x*dx^2, u -= grad p; then fill u
 template <typename T>
-static int model_diagnose(NylesModel* m, cudaStream_t st) {
+static int model_pressure_projection(NylesModel* m, cudaStream_t st) {
     StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
     int rc;
-    T* uf[4] = {s.f[NYLES_F_B], s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
-    if (m->d.model != NYLES_MODEL_EULER3D) {
-        ProfScope ps(&m->prof, 2, st);
-        if ((rc = launch_fill<T>(m->g, uf, 4, st))) return rc;
-    }
+    T* uf[3] = {s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
     void* mgb = mg_level_ptr(&m->mg, 1, 2);
     void* mgx = mg_level_ptr(&m->mg, 1, 1);
     {
@@ -450,12 +458,47 @@ static int model_diagnose(NylesModel* m, cudaStream_t st) {
                                    reinterpret_cast<const float2*>(mgx), m->d.dx2, st);
         if (rc) return rc;
     }
-    {
+    ProfScope ps(&m->prof, 2, st);
+    return launch_fill<T>(m->g, uf, 3, st);
+}
+
+// core/model_les.py:98-127 ; core/model_les_euler.py:96-125 ; the advection model fills
+// b only (core/model_advection.py:33-35)
+template <typename T>
+static int model_diagnose(NylesModel* m, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    int rc;
+    T* uf[4] = {s.f[NYLES_F_B], s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
+    if (m->d.model == NYLES_MODEL_ADVECTION) {
         ProfScope ps(&m->prof, 2, st);
-        if ((rc = launch_fill<T>(m->g, uf + 1, 3, st))) return rc;
+        return launch_fill<T>(m->g, uf, 1, st);
     }
+    if (m->d.model != NYLES_MODEL_EULER3D) {
+        ProfScope ps(&m->prof, 2, st);
+        if ((rc = launch_fill<T>(m->g, uf, 4, st))) return rc;
+    }
+    if ((rc = model_pressure_projection<T>(m, st))) return rc;
     ProfScope ps(&m->prof, 6, st);
     return launch_diag<T>(&m->d, m->g, s, m->d.model != NYLES_MODEL_LINEAR, st);
+}
+
+// Advection.make_u_divergentfree (core/model_advection.py:38-53) with the projection of
+// diagnose_var: fill u, project, U = u/dx^2, div of U (evaluated at the periodic
+// image, i.e. with its halo filled)
+template <typename T>
+static int model_project(NylesModel* m, cudaStream_t st) {
+    StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
+    int rc;
+    T* uf[3] = {s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
+    if ((rc = launch_fill<T>(m->g, uf, 3, st))) return rc;
+    if ((rc = model_pressure_projection<T>(m, st))) return rc;
+    if ((rc = launch_diag<T>(&m->d, m->g, s, 0, st))) return rc;
+    void* mgb = mg_level_ptr(&m->mg, 1, 2);   // overwritten: the right-hand side is scratch
+    if constexpr (sizeof(T) == sizeof(double))
+        return launch_div<T, double>(&m->d, m->g, s, reinterpret_cast<double*>(mgb), st);
+    else
+        return launch_div_df(&m->d, m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)),
+                             reinterpret_cast<float2*>(mgb), st);
 }
 
 template <typename T>
@@ -515,6 +558,12 @@ int nyles_model_diagnose(NylesModel* m, void* stream) {
     if (!m || !m->bound) { set_error("model not bound"); return NYLES_BAD_ARG; }
     cudaStream_t st = (cudaStream_t)stream;
     return m->precision == NYLES_FP64 ? model_diagnose<double>(m, st) : model_diagnose<float>(m, st);
+}
+
+int nyles_model_project(NylesModel* m, void* stream) {
+    if (!m || !m->bound) { set_error("model not bound"); return NYLES_BAD_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    return m->precision == NYLES_FP64 ? model_project<double>(m, st) : model_project<float>(m, st);
 }
 
 int nyles_model_rhs(NylesModel* m, int reg, double t, int last, void* stream) {

@@ -283,6 +283,86 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, co
     }
 }
 
+// ---------------------------------------------------------------- linear tracer schemes
+// core/interpolate_tracer.f90:3-116 (coefficients: REAL(4) literals widened) and the
+// linear branch of core/fortran_upwind.f90:32-61, which the reference never takes
+// (`linear = .false.`, :28): selected by NylesDesc.tracer_order (param orderA).
+template <typename T>
+struct LinK {
+    static __device__ __forceinline__ T c1() { return T(-1.0f / 6.0f); }
+    static __device__ __forceinline__ T c2() { return T(5.0f / 6.0f); }
+    static __device__ __forceinline__ T c3() { return T(2.0f / 6.0f); }
+    static __device__ __forceinline__ T e1() { return T(-1.0f / 12.0f); }
+    static __device__ __forceinline__ T e2() { return T(7.0f / 12.0f); }
+    static __device__ __forceinline__ T b1() { return T(2.0f / 60.0f); }
+    static __device__ __forceinline__ T b2() { return T(-13.0f / 60.0f); }
+    static __device__ __forceinline__ T b3() { return T(47.0f / 60.0f); }
+    static __device__ __forceinline__ T b4() { return T(27.0f / 60.0f); }
+    static __device__ __forceinline__ T b5() { return T(-3.0f / 60.0f); }
+};
+
+// interpolation qp(j) (plus) or qm(j) of an odd order at 0-based position j of a line
+// of n values
+template <typename T, typename Q>
+__device__ __forceinline__ T lin_interp_odd(int j, int n, int order, bool plus, Q q) {
+    using K = LinK<T>;
+    if (order == 1 || j == 0 || j == n - 1) return q(j);
+    if (order == 3 || j == 1 || j == n - 2)
+        return plus ? K::c1() * q(j - 1) + K::c2() * q(j) + K::c3() * q(j + 1)
+                    : K::c3() * q(j - 1) + K::c2() * q(j) + K::c1() * q(j + 1);
+    return plus ? K::b1() * q(j - 2) + K::b2() * q(j - 1) + K::b3() * q(j) + K::b4() * q(j + 1) + K::b5() * q(j + 2)
+                : K::b5() * q(j - 2) + K::b4() * q(j - 1) + K::b3() * q(j) + K::b2() * q(j + 1) + K::b1() * q(j + 2);
+}
+
+// flux through the face to the right of 0-based cell i of a line (none at the last cell)
+template <typename T, typename Q>
+__device__ __forceinline__ T lin_flux(int i, int n, int order, T u, Q q) {
+    using K = LinK<T>;
+    if (i >= n - 1) return T(0);
+    if (order == 2) return u * (T(0.5) * (q(i) + q(i + 1)));
+    if (order == 4) {
+        T qp;
+        if (i == 0) qp = K::e2() * (q(0) + q(1)) + K::e1() * q(2);
+        else if (i == n - 2) qp = K::e2() * (q(i) + q(i + 1)) + K::e1() * q(i - 1);
+        else qp = K::e2() * (q(i) + q(i + 1)) + K::e1() * (q(i - 1) + q(i + 2));
+        return u * qp;
+    }
+    const T uu = fabs(u);
+    const T up = T(0.5) * (u + uu), um = T(0.5) * (u - uu);
+    return up * lin_interp_odd<T>(i, n, order, true, q) + um * lin_interp_odd<T>(i + 1, n, order, false, q);
+}
+
+// -(flux divergence) of one tracer with a linear scheme, one thread per stored point,
+// direction by direction in the reference's order; with `diff`, each direction's
+// diffusion k*lap follows its advection (core/tracer.py:74-76)
+template <typename T>
+__global__ void __launch_bounds__(256) k_tracer_linear(const Geom g, const T* __restrict__ Ux,
+                                                       const T* __restrict__ Uy, const T* __restrict__ Uz,
+                                                       const T* __restrict__ q, T* __restrict__ dq, int order,
+                                                       int diff, T kx, T ky, T kz) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z * blockDim.z + threadIdx.z;
+    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
+    const long long c = g.at(z, y, x);
+    const int pos[3] = {z, y, x};
+    const T* U[3] = {Uz, Uy, Ux};
+    const T kc[3] = {kz, ky, kx};
+    T acc = T(0);
+    for (int pass = 0; pass < 3; ++pass) {
+        const int d = 2 - pass;   // x, then y, then z
+        const int i = pos[d], n = g.N[d];
+        const long long st = g.stride(d);
+        const long long base = c - (long long)i * st;
+        auto Q = [&](int k) -> T { return __ldg(q + base + (long long)k * st); };
+        const T fx = lin_flux<T>(i, n, order, __ldg(U[d] + c), Q);
+        const T fxm = (i > 0) ? lin_flux<T>(i - 1, n, order, __ldg(U[d] + c - st), Q) : T(0);
+        acc = (acc + fxm) - fx;
+        if (diff) acc = acc + kc[d] * lap1d(q, g, c, i, d);
+    }
+    dq[c] = acc;
+}
+
 bool make_geom(const NylesDesc* d, Geom* g) {
     if (!d || d->nx < 1 || d->ny < 1 || d->nz < 1 || d->nh < 0) return false;
     const int per[3] = {d->periodic_z ? 1 : 0, d->periodic_y ? 1 : 0, d->periodic_x ? 1 : 0};
@@ -339,6 +419,34 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     }
     const dim3 blk(RZ_BX, RZ_BY, 1);
     const dim3 grd((g.N[2] + RZ_BX - 1) / RZ_BX, (g.N[1] + RZ_BY - 1) / RZ_BY, (g.N[0] + RZ_ZC - 1) / RZ_ZC);
+    const int order = d->tracer_order;
+    const dim3 lblk(32, 4, 2);
+    auto tracer_linear = [&](const T* q, T* dq, int qi) {
+        const bool diff = (terms & TERM_TRDIFF) && ((d->tracer_diffusion >> qi) & 1);
+        const T* kc = a.kcoef[qi];
+        k_tracer_linear<T><<<grid3(g, lblk), lblk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], q, dq, order, diff ? 1 : 0,
+                                                            kc[0], kc[1], kc[2]);
+        note_launch();
+    };
+    if (d->model == NYLES_MODEL_ADVECTION) {
+        // Advection.rhs (core/model_advection.py:59-61): b only; the velocity registers
+        // are not touched (the reference never writes them)
+        if (order > 0) {
+            tracer_linear(a.b, a.ds[0], 0);
+        } else {
+            const T* kc = a.kcoef[0];
+            if ((terms & TERM_TRDIFF) && (d->tracer_diffusion & 1))
+                k_tracer_march<T, true><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.b, a.ds[0], kc[0], kc[1],
+                                                             kc[2]);
+            else
+                k_tracer_march<T, false><<<grd, blk, 0, st>>>(g, a.U[0], a.U[1], a.U[2], a.b, a.ds[0], T(0), T(0),
+                                                              T(0));
+            note_launch();
+        }
+        return cuda_status(cudaGetLastError(), "rhs kernel");
+    }
+    const bool linear_tr = (terms & TERM_TRACER) && order > 0;
+    if (linear_tr) terms &= ~TERM_TRACER;   // b's tendency comes from k_tracer_linear after the march
     const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
     const bool bdiff = tr && (terms & TERM_TRDIFF) && (d->tracer_diffusion & 1);
     if (tr && vf && bdiff) k_rhs_march<T, true, true, true><<<grd, blk, 0, st>>>(a);
@@ -348,6 +456,11 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     else if (vf) k_rhs_march<T, false, true, false><<<grd, blk, 0, st>>>(a);
     else k_rhs_march<T, false, false, false><<<grd, blk, 0, st>>>(a);
     note_launch();
+    if (linear_tr) {
+        tracer_linear(a.b, a.ds[0], 0);
+        for (int t = 0; t < d->n_tracers; ++t) tracer_linear(a.tr[t], a.ds[4 + t], t + 1);
+        return cuda_status(cudaGetLastError(), "rhs kernel");
+    }
     for (int t = 0; t < d->n_tracers; ++t) {
         if (tr) {
             const T* kc = a.kcoef[t + 1];

@@ -30,13 +30,19 @@ def make_desc(param, grid, modelname):
     diff = param.get("diff_coef", {}) or {}
     d.add_viscosity = int("u" in diff)
     d.viscosity = float(diff.get("u", 0.0))
-    # tracer diffusion (core/tracer.py:74-76) only with the gpu parameter
-    # tracer_diffusion: the reference never applies it
-    if param.get("gpu", {}).get("tracer_diffusion", False):
+    # tracer diffusion (core/tracer.py:74-76): live in the advection model, whose rhs
+    # passes `last` (core/model_advection.py:59-61); in LES only with the gpu parameter
+    # tracer_diffusion (the reference's LES.rhs never applies it)
+    gpu = param.get("gpu", {}) or {}
+    if modelname == "advection" or gpu.get("tracer_diffusion", False):
         for q, name in enumerate(["b"] + ["t%d" % k for k in range(d.n_tracers)]):
             if name in diff:
                 d.tracer_diffusivity[q] = float(diff[name])
                 d.tracer_diffusion |= 1 << q
+    # tracer_scheme "linear": the orderA interpolation of the linear branch of
+    # core/fortran_upwind.f90:32-61 instead of WENO (the reference hard-codes WENO)
+    if gpu.get("tracer_scheme", "weno") == "linear":
+        d.tracer_order = int(param.get("orderA", 5))
     d.dx, d.dy, d.dz = grid.dx, grid.dy, grid.dz
     d.idx2, d.idy2, d.idz2 = grid.idx2, grid.idy2, grid.idz2
     d.dx2 = grid.dx ** 2

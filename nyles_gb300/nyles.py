@@ -2,7 +2,7 @@
 
 Interface of the reference's core/nyles.py:22-260: the constructor checks and freezes
 the parameters, derives nx/ny/nz, the neighbours and the grid, and builds the model
-(``LES``, ``Euler3d`` or ``linear``); ``run()`` projects the initial state and advances
+(``LES``, ``Euler3d``, ``linear`` or ``advection``); ``run()`` projects the initial state and advances
 it to ``tend`` with ``compute_dt()`` (CFL) and ``model.forward``, writing the netCDF
 history file (nylesIO) when the gpu parameter `history` is on (the default).
 
@@ -17,6 +17,7 @@ import time
 import numpy as np
 
 from . import grid as grid_module
+from . import model_advection
 from . import model_les
 from . import nylesIO
 from . import online_diag
@@ -56,6 +57,8 @@ class Nyles(object):
             self.model = model_les.Euler3d(param, self.grid, device=device)
         elif name == "linear":
             self.model = model_les.LES(param, self.grid, linear=True, device=device)
+        elif name == "advection":
+            self.model = model_advection.Advection(param, self.grid, device=device)
         else:
             raise NotImplementedError("modelname %r is not provided by the GPU build" % name)
         self.tend = param["tend"]

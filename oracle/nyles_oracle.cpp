@@ -175,6 +175,68 @@ void upwind(const V3& trac, const V3& u, const V3& dtrac) {
         }
 }
 
+// core/interpolate_tracer.f90:3-116 on one line of n values (0-based here; the source is
+// 1-based). The coefficients are REAL(4) literals widened to double.
+void interpolate_tracer(const double* q, double* qp, double* qm, int order, int n) {
+    const double c1 = -1.0f / 6.0f, c2 = 5.0f / 6.0f, c3 = 2.0f / 6.0f;
+    const double e1 = -1.0f / 12.0f, e2 = 7.0f / 12.0f;
+    const double b1 = 2.0f / 60.0f, b2 = -13.0f / 60.0f, b3 = 47.0f / 60.0f, b4 = 27.0f / 60.0f,
+                 b5 = -3.0f / 60.0f;
+    auto cstencil = [&](int i) {
+        qp[i] = c1 * q[i - 1] + c2 * q[i] + c3 * q[i + 1];
+        qm[i] = c3 * q[i - 1] + c2 * q[i] + c1 * q[i + 1];
+    };
+    if (order == 5) {
+        qp[0] = q[0]; qm[0] = q[0];
+        cstencil(1);
+        for (int i = 2; i <= n - 3; ++i) {
+            qp[i] = b1 * q[i - 2] + b2 * q[i - 1] + b3 * q[i] + b4 * q[i + 1] + b5 * q[i + 2];
+            qm[i] = b5 * q[i - 2] + b4 * q[i - 1] + b3 * q[i] + b2 * q[i + 1] + b1 * q[i + 2];
+        }
+        cstencil(n - 2);
+        qp[n - 1] = q[n - 1]; qm[n - 1] = q[n - 1];
+    } else if (order == 3) {
+        qp[0] = q[0]; qm[0] = q[0];
+        for (int i = 1; i <= n - 2; ++i) cstencil(i);
+        qp[n - 1] = q[n - 1]; qm[n - 1] = q[n - 1];
+    } else if (order == 1) {
+        for (int i = 0; i < n; ++i) { qp[i] = q[i]; qm[i] = q[i]; }
+    } else if (order == 2) {
+        for (int i = 0; i < n - 1; ++i) qp[i] = 0.5 * (q[i] + q[i + 1]);
+    } else if (order == 4) {
+        qp[0] = e2 * (q[0] + q[1]) + e1 * (q[2]);
+        for (int i = 1; i <= n - 3; ++i) qp[i] = e2 * (q[i] + q[i + 1]) + e1 * (q[i - 1] + q[i + 2]);
+        qp[n - 2] = e2 * (q[n - 2] + q[n - 1]) + e1 * (q[n - 3]);
+    }
+}
+
+// core/fortran_upwind.f90:32-61, the linear branch (`linear` is .false. in the
+// reference, so only an explicit order > 0 reaches it): odd orders upwind the
+// interpolations qp(i) / qm(i+1) with the split velocity, even orders take the centred
+// qp(i); the last face carries no flux.
+void upwind_linear(const V3& trac, const V3& u, const V3& dtrac, int order) {
+    const int l = trac.n0, m = trac.n1, n = trac.n2;
+    std::vector<double> up(n), um(n), phi(n), qp(n, 0.0), qm(n, 0.0);
+    for (int k = 0; k < l; ++k)
+        for (int j = 0; j < m; ++j) {
+            for (int i = 0; i < n; ++i) {
+                double uu = std::fabs(u(k, j, i));
+                up[i] = 0.5 * (u(k, j, i) + uu);
+                um[i] = 0.5 * (u(k, j, i) - uu);
+                phi[i] = trac(k, j, i);
+            }
+            interpolate_tracer(phi.data(), qp.data(), qm.data(), order, n);
+            double fxm = 0.0, fx;
+            for (int i = 0; i < n - 1; ++i) {
+                fx = (order % 2 == 0) ? u(k, j, i) * qp[i] : up[i] * qp[i] + um[i] * qm[i + 1];
+                dtrac(k, j, i) = dtrac(k, j, i) + fxm - fx;
+                fxm = fx;
+            }
+            fx = 0.0;
+            dtrac(k, j, n - 1) = dtrac(k, j, n - 1) + fxm - fx;
+        }
+}
+
 // ---------------------------------------------------------------- vorticity
 // core/fortran_vorticity.f90:2-28
 void vorticity_k(const V3& ui, const V3& uj, const V3& wk) {
@@ -598,7 +660,7 @@ struct Model {
     int per[3];           // periodic flags (z, y, x)
     int nh = 3;
     int ntr = 0;
-    int model = 0;        // 0 LES, 1 Euler3d, 2 linear
+    int model = 0;        // 0 LES, 1 Euler3d, 2 linear, 3 advection (core/model_advection.py)
     int scheme = 2;       // 0 EF, 1 LFAM3, 2 RK3_SSP
     double dx, dy, dz, idx2, idy2, idz2;
     double fparam = 0.0;  // covariant Coriolis (coriolis * dx * dy), 0 if not rotating
@@ -606,6 +668,7 @@ struct Model {
     // tracer diffusion (core/tracer.py:74-76), applied only when bit q of trdiff_mask is
     // set (q = 0 for b): the reference's rhs never passes `last` to rhstrac
     double kappa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}; int trdiff_mask = 0;
+    int tr_order = 0;     // 0 WENO (the reference); 1..5 the linear branch of order orderA
     bool lfam3_first = true;
     long vol;
     std::vector<std::vector<double>> f;    // state fields (14 + ntr)
@@ -683,7 +746,8 @@ void model_rhstrac(Model& M, std::vector<std::vector<double>>& ds, bool last) {
             V3 field = fv(M, fld, d);
             V3 dfield = rv(M, ds, fld, d);
             if (d == 'i') { double* p = ds[fld == B ? 0 : 4 + (fld - T0)].data(); std::fill(p, p + M.vol, 0.0); }
-            upwind(field, vel, dfield);
+            if (M.tr_order > 0) upwind_linear(field, vel, dfield, M.tr_order);
+            else upwind(field, vel, dfield);
             if (last && ((M.trdiff_mask >> tr) & 1)) {
                 double ids2 = d == 'i' ? M.idx2 : (d == 'j' ? M.idy2 : M.idz2);
                 add_laplacian(field, dfield, M.kappa[tr] * ids2);
@@ -714,6 +778,10 @@ void model_viscosity(Model& M, std::vector<std::vector<double>>& ds) {
 
 // core/model_les.py:130-144, :167-175
 void model_rhs(Model& M, std::vector<std::vector<double>>& ds, bool last) {
+    if (M.model == 3) {   // Advection.rhs, core/model_advection.py:59-61: b only, no reset_state
+        model_rhstrac(M, ds, last);
+        return;
+    }
     for (auto& a : ds) std::fill(a.begin(), a.end(), 0.0);
     model_rhstrac(M, ds, last);
     if (M.model != 2) model_vortex_force(M, ds);
@@ -796,6 +864,10 @@ void model_kinenergy(Model& M) {
 
 // core/model_les.py:98-127 ; core/model_les_euler.py:96-125
 void model_diagnose(Model& M) {
+    if (M.model == 3) {   // Advection.diagnose_var, core/model_advection.py:33-35
+        model_fill(M, M.f[B].data());
+        return;
+    }
     if (M.model != 1) {
         model_fill(M, M.f[B].data());
         for (int d = 0; d < 3; ++d) model_fill(M, M.f[UX + d].data());
@@ -810,6 +882,19 @@ void model_diagnose(Model& M) {
         for (int d = 0; d < 3; ++d) model_fill(M, M.f[WX + d].data());
         model_fill(M, M.f[KE].data());
     }
+}
+
+// Advection.make_u_divergentfree, core/model_advection.py:38-53, with the projection of
+// LES.diagnose_var (the reference method calls compute_p without its `ngbs` argument and
+// builds the superseded Python multigrid, so it cannot run as written)
+void model_project(Model& M) {
+    for (int d = 0; d < 3; ++d) model_fill(M, M.f[UX + d].data());
+    model_U_from_u(M);
+    model_compute_p(M);
+    for (int d = 0; d < 3; ++d) model_fill(M, M.f[UX + d].data());
+    model_U_from_u(M);
+    model_compute_div(M);
+    model_fill(M, M.f[DIV].data());
 }
 
 // right-hand side into register set `reg` at stage time t, then the user forcing
@@ -965,6 +1050,10 @@ void* orc_model_mg(void* h) { return ((Model*)h)->mg; }
 void orc_model_diagnose(void* h) { model_diagnose(*(Model*)h); }
 void orc_model_vortex_force(void* h, int reg) {
     Model* M = (Model*)h; for (auto& a : M->reg[reg]) std::fill(a.begin(), a.end(), 0.0); model_vortex_force(*M, M->reg[reg]); }
+void orc_model_project(void* h) { model_project(*(Model*)h); }
+void orc_model_set_tracer_order(void* h, int order) { ((Model*)h)->tr_order = order; }
+void orc_upwind_linear(double* trac, double* u, double* dtrac, int order, int l, int m, int n) {
+    upwind_linear(contig(trac, l, m, n), contig(u, l, m, n), contig(dtrac, l, m, n), order); }
 void orc_model_set_tracer_diffusion(void* h, const double* kappa, int mask) {
     Model* M = (Model*)h;
     for (int q = 0; q <= M->ntr; ++q) M->kappa[q] = kappa[q];

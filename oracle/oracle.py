@@ -26,7 +26,7 @@ FIELDS = {"b": 0, "p": 1, "ke": 2, "div": 3, "u_i": 4, "u_j": 5, "u_k": 6,
           "U_i": 7, "U_j": 8, "U_k": 9, "vor_i": 10, "vor_j": 11, "vor_k": 12,
           "work": 13}
 SCHEMES = {"EF": 0, "LFAM3": 1, "RK3_SSP": 2}
-MODELS = {"LES": 0, "Euler3d": 1, "linear": 2}
+MODELS = {"LES": 0, "Euler3d": 1, "linear": 2, "advection": 3}
 # mg_enums.f90:6
 MG_TOPOLOGY = {"closed": 1, "perio_x": 2, "perio_y": 3, "perio_xy": 5, "perio_xyz": 6}
 
@@ -52,6 +52,7 @@ def lib():
             "orc_vortex_force_direc": (v, [p, p, p, i, i, i]),
             "orc_vortex_force_flip": (v, [p, p, p, i, i, i]),
             "orc_upwind": (v, [p, p, p, i, i, i]),
+            "orc_upwind_linear": (v, [p, p, p, i, i, i, i]),
             "orc_vorticity": (v, [p, p, p, i, i, i]),
             "orc_kin": (v, [p, p, d, i, i, i]),
             "orc_gradke": (v, [p, p, i, i, i]),
@@ -88,6 +89,8 @@ def lib():
             "orc_model_vfwork": (d, [p, p]),
             "orc_model_set_forcing": (v, [p, p, p]),
             "orc_model_set_tracer_diffusion": (v, [p, p, i]),
+            "orc_model_set_tracer_order": (v, [p, i]),
+            "orc_model_project": (v, [p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -129,6 +132,11 @@ def vortex_force_flip(U, vort, res):
 
 def upwind(trac, u, dtrac):
     lib().orc_upwind(_ptr(trac), _ptr(u), _ptr(dtrac), *dtrac.shape)
+
+
+def upwind_linear(trac, u, dtrac, order):
+    """the linear branch of core/fortran_upwind.f90:32-61 with core/interpolate_tracer.f90"""
+    lib().orc_upwind_linear(_ptr(trac), _ptr(u), _ptr(dtrac), int(order), *dtrac.shape)
 
 
 def vorticity(ui, uj, wk):
@@ -200,7 +208,9 @@ class OracleModel:
     ``desc`` holds: nx, ny, nz, nh, geometry, n_tracers, modelname, timestepping,
     dx, dy, dz, idx2, idy2, idz2, fparam, visc (None = off), and optionally
     tracer_diffusion = {"b": kappa, "t0": kappa, ...} for the opt-in tracer diffusion
-    on the last stage (core/tracer.py:74-76; never applied by the reference's rhs).
+    on the last stage (core/tracer.py:74-76; never applied by the reference's rhs), and
+    tracer_order = 1..5 for the linear advection branch (0 = WENO, the reference).
+    modelname "advection" is core/model_advection.py.
     """
 
     def __init__(self, desc):
@@ -230,6 +240,8 @@ class OracleModel:
                     kappa[q] = float(trd[name])
                     mask |= 1 << q
             lib().orc_model_set_tracer_diffusion(self.h, kappa, mask)
+        if desc.get("tracer_order", 0):
+            lib().orc_model_set_tracer_order(self.h, int(desc["tracer_order"]))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -274,6 +286,10 @@ class OracleModel:
         i0, i1) (core/online_diag.py:11-35)"""
         b = np.ascontiguousarray(box, dtype=np.int64)
         return lib().orc_model_vfwork(self.h, b.ctypes.data)
+
+    def project(self):
+        """Advection.make_u_divergentfree (core/model_advection.py:38-53)"""
+        lib().orc_model_project(self.h)
 
     def rhs(self, reg=0, last=False):
         lib().orc_model_rhs(self.h, reg, 1 if last else 0)
