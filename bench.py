@@ -217,6 +217,7 @@ def mg_levels(n):
 # k_rhs_march<double, 1, 1> launch, counted by ncu on the 128^3 case of this workload
 # (237 + 251 + 2 x 252 per cell).
 RHS_FP64_OPS_PER_CELL = 992
+RHS_FP64_INSTR_PER_CELL = 237 + 251 + 252
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per array cell of one
 # right-hand-side launch, from ncu --set full captures of this workload: FP64 at 128^3
 # (158.4 + 47.1 MB over 128 x 134 x 134 cells), FP32 at 256^3 (574.1 + 263.8 MB over
@@ -242,18 +243,26 @@ def mg_bottom_level(levels, elem, smem=200 * 1024):
     return bottom
 
 
-def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
-    """Algorithmic-bytes roofline of one kernel family from the CUDA-event phase times.
+def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak, nv=None, solves=None, krylov=False):
+    """Roofline of one kernel family from the CUDA-event phase times.
 
     rhs       : one launch reads b, U(3), vor(3), ke and writes 4 registers: 12 words
-                per cell of the (n+6)^2 n array.
+                per cell of the (n+6)^2 n array. In FP64 the kernel is bound by the FP64
+                pipe (GB300 issues FP64 at 1/64 of its FP32 rate): the roofline is
+                then the FP64 arithmetic rate against cuBLAS DGEMM, with the
+                issue-slot fraction (DADD and DMUL take a slot for one flop, DFMA for
+                two) and the HBM figures beside it.
     mg_smooth : each Jacobi half-sweep reads its input and b and writes its output, 3
                 words per level cell; per V-cycle, on each grid level above the
                 one-block coarse levels: 3 half-sweeps (the first of the pre-smoothing
                 is written by the kernel that sets b; FP64 level 0, warm-started: 4),
                 plus, in mixed precision, the float-pair solution read and written by
-                the last level-0 half-sweep (16 B per cell); the one-block coarse solve
-                reads b and writes x of its first level.
+                the last level-0 half-sweep (16 B per cell; the Krylov solve instead
+                reads q, 4 B); the one-block coarse solve reads b and writes x of its
+                first level.
+    mg_norm   : mixed precision, the float-pair outer iteration per solve and level-0
+                cell: sum(b^2) 8 B, nv + 1 residuals of 24 B, and per Krylov iteration
+                the direction update (24 B) and the solution update (20 B).
     """
     if ph.get(kernel, {}).get("count", 0) == 0:
         return None
@@ -264,24 +273,28 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
         launches = ph[kernel]["count"]
         per_launch = 12 * elem * vol
         avg = ms / launches
-        out.update({"kernel": "k_rhs_march", "bytes_per_launch": per_launch, "avg_launch_ms": avg,
-                    "achieved": per_launch / (avg * 1e-3) / 1e9,
-                    "traffic": RHS_DRAM_BYTES_PER_CELL[elem] * vol,
-                    "traffic_source": "ncu dram bytes per cell of the same kernel, scaled to this grid"})
+        hbm = {"achieved": per_launch / (avg * 1e-3) / 1e9, "peak": peak, "unit": "GB/s", "peak_kind": peak_kind,
+               "bytes_per_launch": per_launch, "traffic": RHS_DRAM_BYTES_PER_CELL[elem] * vol,
+               "traffic_source": "ncu dram bytes per cell of the same kernel, scaled to this grid"}
+        hbm["frac"] = hbm["achieved"] / peak
         if elem == 8 and fp64_peak:
-            ops = RHS_FP64_OPS_PER_CELL
-            out["fp64"] = {"peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM)",
-                           "achieved_tflops": (ops * vol / (avg * 1e-3) / 1e12) if ops else None,
-                           "ops_per_cell": ops}
-            if ops:
-                out["fp64"]["frac"] = out["fp64"]["achieved_tflops"] / fp64_peak
+            flops = RHS_FP64_OPS_PER_CELL * vol / (avg * 1e-3) / 1e12
+            issue = RHS_FP64_INSTR_PER_CELL * vol / (avg * 1e-3) / 1e12
+            return {"kernel": "k_rhs_march", "bound": "fp64", "achieved": flops, "peak": fp64_peak,
+                    "unit": "TFLOP/s", "peak_kind": "measured (cuBLAS DGEMM, torch.mm float64 8192^3)",
+                    "frac": flops / fp64_peak, "fp64_flops_per_cell": RHS_FP64_OPS_PER_CELL,
+                    "fp64_instructions_per_cell": RHS_FP64_INSTR_PER_CELL,
+                    "fp64_issue_frac": issue / (fp64_peak / 2), "avg_launch_ms": avg,
+                    "traffic": hbm["traffic"], "hbm": hbm}
+        out.update({"kernel": "k_rhs_march", "avg_launch_ms": avg})
+        out.update({k: v for k, v in hbm.items() if k not in ("peak", "unit", "peak_kind", "frac")})
     elif kernel == "mg_smooth":
         lev = mg_levels(n)
         B = mg_bottom_level(lev, elem)
         vol = [z * y * x for (z, y, x) in lev]
         per_vcycle = sum((4 if (l == 0 and elem == 8) else 3) * 3 * elem * vol[l] for l in range(B))
         if elem == 4:
-            per_vcycle += 16 * vol[0]
+            per_vcycle += (4 if krylov else 16) * vol[0]
         if B < len(lev):
             per_vcycle += 2 * elem * vol[B]
         calls_per_vcycle = 2 * B + 1   # one bracketed call per smoothing and the coarse solve
@@ -293,6 +306,12 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak):
             out["traffic"] = JACOBI_F32_L0_DRAM_BYTES_256
             out["traffic_source"] = ("ncu dram bytes of one level-0 half-sweep launch (algorithmic %.1f MB)"
                                      % (3 * 4 * vol[0] / 1e6))
+    elif kernel == "mg_norm" and elem == 4 and nv is not None and solves:
+        v0 = n ** 3
+        per_solve = v0 * (8 + (nv + 1) * 24 + (nv * 44 if krylov else 0))
+        out.update({"kernel": "k_mg_resid_df" + (" + k_fcg_direction + k_fcg_xupdate" if krylov else ""),
+                    "bytes_per_solve": per_solve, "solves": solves,
+                    "achieved": per_solve * solves / (ms * 1e-3) / 1e9})
     else:
         out["achieved"] = None
     if out.get("achieved") is not None:
@@ -494,7 +513,11 @@ def make_config(n, world):
 
 def accuracy(n, steps):
     """Mixed path against the FP64 path after `steps` RK3 steps from the same state:
-    max|mixed - fp64| / max|fp64| for b and p, and over the three components for u."""
+    max|mixed - fp64| / max|fp64| for b and p, and over the three components for u.
+    The pressure of a box closed or periodic on every side is defined up to a constant,
+    which the Krylov solve and the stationary V-cycle iteration fix differently (the
+    velocity correction uses its gradient only): p is compared after removing each
+    field's mean."""
     import numpy as np
     import torch
     fields = ("b", "p", "u_i", "u_j", "u_k")
@@ -510,20 +533,24 @@ def accuracy(n, steps):
         del nyl, m
         torch.cuda.empty_cache()
     a, b = out["mixed"], out["fp64"]
+    for d in (a, b):
+        d["p"] = d["p"] - d["p"].mean()
     err = {s: float(np.abs(a[s] - b[s]).max() / max(np.abs(b[s]).max(), 1e-300)) for s in ("b", "p")}
     us = max(np.abs(b[c]).max() for c in ("u_i", "u_j", "u_k"))
     err["u"] = float(max(np.abs(a[c] - b[c]).max() for c in ("u_i", "u_j", "u_k")) / max(us, 1e-300))
     return {"steps": steps, "rel_err_vs_fp64": err}
 
 
-def step_bytes(prec, nv, n_vcycles, refine=True):
+def step_bytes(prec, nv, n_vcycles, refine=True, krylov=False):
     """Algorithmic bytes per cell-step: RK3 stencil part w(11 nv + 6) plus 3 solves of
-    w_mg (4 + 24 n_V), and, in mixed precision, 40 B per cell and V-cycle of FP64
-    refinement (residual and correction)."""
+    w_mg (4 + 24 n_V), and, in mixed precision, per cell and V-cycle of the float-pair
+    outer iteration: 40 B for iterative refinement (residual 24, correction 16), 72 B
+    for the Krylov solve (residual 24, z.q read 4, direction and image update 24,
+    solution update 20)."""
     w = 8 if prec == "fp64" else 4
     q = w * (11 * nv + 6) + 3 * w * (4 + 24 * n_vcycles)
     if prec != "fp64" and refine:
-        q += 3 * 40 * n_vcycles
+        q += 3 * (72 if krylov else 40) * n_vcycles
     return q
 
 
@@ -564,7 +591,8 @@ def main():
             ms = job_time_ms(ms, dist, "cuda")
             launches_total += launches
             res = {"ms_per_step": ms / a.steps, "value": job_value(cells, a.steps, ms, world),
-                   "mean_vcycles_per_solve": vc, "kernel_launches": launches, "path": "graph replay"}
+                   "mean_vcycles_per_solve": vc, "kernel_launches": launches, "path": "graph replay",
+                   "krylov": bool(getattr(nyl.model, "krylov", False))}
             if not a.no_eager:
                 ems_eager, _, _ = time_steps(nyl, a.steps, 1, stream, graphs=False)
                 ems_eager = job_time_ms(ems_eager, dist, "cuda")
@@ -598,26 +626,32 @@ def main():
         dom = max(kernels, key=lambda k: kernels[k]["ms"])
         elem = 8 if main_prec == "fp64" else 4
         out["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in ph.items()}
-        out["roofline"] = roofline(dom, ph, n, elem, peak, peak_kind, fp64_peak)
-        out["roofline_kernels"] = {k: roofline(k, ph, n, elem, peak, peak_kind, fp64_peak)
-                                   for k in ("rhs", "mg_smooth") if k != dom}
+        kw = dict(nv=r["mean_vcycles_per_solve"], solves=3 * a.profile_steps, krylov=r.get("krylov", False))
+        out["roofline"] = roofline(dom, ph, n, elem, peak, peak_kind, fp64_peak, **kw)
+        out["roofline_kernels"] = {k: roofline(k, ph, n, elem, peak, peak_kind, fp64_peak, **kw)
+                                   for k in ("rhs", "mg_smooth", "mg_norm") if k != dom}
     if "mixed" in results and main_prec != "mixed":
         mr = results["mixed"]
         out["mixed"] = {"value": mr["value"], "ms_per_step": mr["ms_per_step"],
                         "speedup_vs_fp64": mr["value"] / r["value"],
-                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"], "eager": mr.get("eager")}
+                        "mean_vcycles_per_solve": mr["mean_vcycles_per_solve"], "eager": mr.get("eager"),
+                        "solver": ("FCG(1) preconditioned by the FP32 V-cycle" if mr["krylov"]
+                                   else "stationary V-cycle iteration (iterative refinement)")}
         if "e2e" in mr:
             out["mixed"]["e2e"] = mr["e2e"]
         if "phases" in mr:
             mph = mr["phases"]
             out["mixed"]["phases"] = {k: round(v["ms"] / max(1, a.profile_steps), 3) for k, v in mph.items()}
             mdom = max((k for k in mph if k != "mg_solve"), key=lambda k: mph[k]["ms"])
-            out["mixed"]["roofline"] = roofline(mdom, mph, n, 4, peak, peak_kind, None)
+            kw = dict(nv=mr["mean_vcycles_per_solve"], solves=3 * a.profile_steps, krylov=mr.get("krylov", False))
+            out["mixed"]["roofline"] = roofline(mdom, mph, n, 4, peak, peak_kind, None, **kw)
+            out["mixed"]["roofline_kernels"] = {k: roofline(k, mph, n, 4, peak, peak_kind, None, **kw)
+                                                for k in ("rhs", "mg_smooth", "mg_norm") if k != mdom}
     if a.serving_requests > 0:
         out["serving"] = time_serving(a)
         out["gpu_launches"] += out["serving"]["kernel_launches"]
     for prec, res in results.items():
-        q = step_bytes(prec, 4, res["mean_vcycles_per_solve"])
+        q = step_bytes(prec, 4, res["mean_vcycles_per_solve"], krylov=res.get("krylov", False))
         sr = {"bytes_per_cell_step": q, "achieved": q * res["value"] / world / 1e9, "peak": peak, "unit": "GB/s",
               "peak_kind": peak_kind}
         sr["frac"] = sr["achieved"] / peak

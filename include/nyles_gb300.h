@@ -140,6 +140,14 @@ int nyles_mg_level_shape(const NylesMg* mg, int lev, int* shape3); /* lev 1 = fi
 int nyles_mg_level_ptr(NylesMg* mg, int lev, int var, void** ptr);
 /* tol on the squared residual ratio (mg_types.f90:15-26; defaults 1e-6, 20, 0.9) */
 int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega);
+/* Mixed precision only: with on = 1 the solve is flexible conjugate gradients (FCG(1))
+ * on the level-1 equation, preconditioned by one FP32 V-cycle per iteration, with the
+ * float-pair solution and the float-pair true residual of the stop test (same rule:
+ * sum(r^2)/sum(b^2) < tol or maxite iterations). It reaches a tight tolerance in about
+ * half the V-cycles of the reference's stationary iteration (mgfor solvers.f90:8-33),
+ * whose iterates it no longer follows; 0 (default) keeps that iteration.
+ * NYLES_UNSUPPORTED for an FP64 solver. */
+int nyles_mg_set_krylov(NylesMg* mg, int on);
 int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream);
 
 /* ---------------------------------------------------------------- whole model
@@ -157,6 +165,8 @@ int nyles_model_destroy(NylesModel* m);
 int nyles_model_workspace_bytes(const NylesModel* m, size_t* bytes);
 int nyles_model_bind(NylesModel* m, void* const* fields, void* const* regs, void* workspace);
 int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omega);
+/* nyles_mg_set_krylov for the model's pressure solve (refused while a graph is captured) */
+int nyles_model_set_mg_krylov(NylesModel* m, int on);
 /* LES.forward: one time step, core/model_les.py:147-149 -> core/timescheme.py:113-221.
  * Returns NYLES_BLOWUP when the new state holds a non-finite value. */
 int nyles_model_forward(NylesModel* m, double t, double dt, void* stream);

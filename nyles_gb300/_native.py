@@ -85,12 +85,14 @@ SIGNATURES = {
     "nyles_mg_level_shape": (_I, [_P, _I, ctypes.POINTER(ctypes.c_int)]),
     "nyles_mg_level_ptr": (_I, [_P, _I, _I, _PP]),
     "nyles_mg_set_params": (_I, [_P, _D, _I, _D]),
+    "nyles_mg_set_krylov": (_I, [_P, _I]),
     "nyles_mg_solve": (_I, [_P, ctypes.POINTER(NylesMgStats), _P]),
     "nyles_model_create": (_I, [ctypes.POINTER(NylesDesc), _I, _I, _PP]),
     "nyles_model_destroy": (_I, [_P]),
     "nyles_model_workspace_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "nyles_model_bind": (_I, [_P, _PP, _PP, _P]),
     "nyles_model_set_mg_params": (_I, [_P, _D, _I, _D]),
+    "nyles_model_set_mg_krylov": (_I, [_P, _I]),
     "nyles_model_forward": (_I, [_P, _D, _D, _P]),
     "nyles_model_diagnose": (_I, [_P, _P]),
     "nyles_model_rhs": (_I, [_P, _I, _D, _I, _P]),

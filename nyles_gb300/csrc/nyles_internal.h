@@ -120,7 +120,11 @@ struct MgImpl {
     size_t bottom_smem = 0;           // its shared memory bytes
     // mixed precision: level-1 solution and right-hand side as float pairs (hi, lo)
     size_t off_pdf = 0, off_bdf = 0;
-    size_t off_partial = 0, off_scalars = 0;
+    // mixed precision, Krylov acceleration (FCG(1) preconditioned by the V-cycle): the
+    // search direction and its image under the operator, level-1 floats
+    int krylov = 0;
+    size_t off_fp = 0, off_fq = 0;
+    size_t off_partial = 0, off_partial2 = 0, off_scalars = 0;
     int npartial = 0;
     size_t bytes = 0;
     char* ws = nullptr;

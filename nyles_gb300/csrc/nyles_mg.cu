@@ -167,58 +167,111 @@ __device__ __forceinline__ T mg_ldw(const T* __restrict__ a, long long c, bool w
     return wet ? v : T(0);
 }
 
+// per-block partial sum (one double per block, block index order)
+__device__ __forceinline__ void block_partial(double s, double* __restrict__ partial) {
+    __shared__ double sm[MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
+    s = warp_sum(s);
+    if ((tid & 31) == 0) sm[tid >> 5] = s;
+    __syncthreads();
+    if (tid < 32) {
+        double t = (tid < MG_BX * MG_BY / 32) ? sm[tid] : 0.0;
+        t = warp_sum(t);
+        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+// two per-block partial sums at once
+__device__ __forceinline__ void block_partial2(double s, double t, double* __restrict__ ps,
+                                               double* __restrict__ pt) {
+    __shared__ double sm[2][MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
+    s = warp_sum(s);
+    t = warp_sum(t);
+    if ((tid & 31) == 0) {
+        sm[0][tid >> 5] = s;
+        sm[1][tid >> 5] = t;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        double a = (tid < MG_BX * MG_BY / 32) ? sm[0][tid] : 0.0;
+        double b = (tid < MG_BX * MG_BY / 32) ? sm[1][tid] : 0.0;
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (tid == 0) {
+            const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            ps[blk] = a;
+            pt[blk] = b;
+        }
+    }
+}
+
 // one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
-// (basicoperators.f90:379-398). With ACC, the result is added to the float-pair
-// solution `acc` instead of being stored (mixed precision: the correction of
-// iterative refinement, fused into the last half-sweep of the V-cycle).
-template <typename T, bool ACC>
+// (basicoperators.f90:379-398). MODE 0 stores it; MODE 1 adds it to the float-pair
+// solution `acc` instead (mixed precision: the correction of iterative refinement,
+// fused into the last half-sweep of the V-cycle); MODE 2 stores it and sums out*dot
+// and out per block into `partial` and `partial2` (the Krylov solve: z.q of the new
+// preconditioned residual against the previous direction's image, and the sum of z).
+template <typename T, int MODE>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
                                                             const T* __restrict__ b, T* __restrict__ out, T omega,
-                                                            float2* __restrict__ acc) {
+                                                            float2* __restrict__ acc, const T* __restrict__ dot,
+                                                            double* __restrict__ partial,
+                                                            double* __restrict__ partial2) {
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    if (x >= g.n[2] || y >= g.n[1]) return;
-    const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
-    const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
-    const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
-    const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
-    const T cff1 = T(1) - omega;
-    const long long c0 = mg_at(g, z0, y, x);
-    // neighbour sum in mgfor's order x-1, x+1, y-1, y+1, z-1, z+1
-    auto cell = [&](long long c, T zm, T x0, T zp, T idg) -> T {
-        const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) + mg_ldw(in, c + ny.om, ny.wm)) +
-                      mg_ldw(in, c + ny.op, ny.wp)) + zm) + zp;
-        return cff1 * x0 + omega * (s - b[c]) * idg;
-    };
-    auto put = [&](long long c, T v) {
-        if (ACC) acc[c] = df_add_f(acc[c], (float)v);
-        else out[c] = v;
-    };
-    if (z0 + MG_ZC <= nz) {
-        // full chunk: fixed trip count, fully unrolled, so that every load of the chunk
-        // is issued before the first result is needed
-        const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
-        T col[MG_ZC + 2];
-        col[0] = mg_ldw(in, c0 + lo.om, lo.wm);
+    float sdot = 0.f, ssum = 0.f;
+    if (x < g.n[2] && y < g.n[1]) {
+        const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+        const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
+        const T cff1 = T(1) - omega;
+        const long long c0 = mg_at(g, z0, y, x);
+        // neighbour sum in mgfor's order x-1, x+1, y-1, y+1, z-1, z+1
+        auto cell = [&](long long c, T zm, T x0, T zp, T idg) -> T {
+            const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) +
+                           mg_ldw(in, c + ny.om, ny.wm)) + mg_ldw(in, c + ny.op, ny.wp)) + zm) + zp;
+            return cff1 * x0 + omega * (s - b[c]) * idg;
+        };
+        auto put = [&](long long c, T v) {
+            if (MODE == 1) {
+                acc[c] = df_add_f(acc[c], (float)v);
+            } else {
+                out[c] = v;
+                if (MODE == 2) {
+                    sdot = __fmaf_rn((float)v, (float)dot[c], sdot);
+                    ssum = __fadd_rn(ssum, (float)v);
+                }
+            }
+        };
+        if (z0 + MG_ZC <= nz) {
+            // full chunk: fixed trip count, fully unrolled, so that every load of the chunk
+            // is issued before the first result is needed
+            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+            T col[MG_ZC + 2];
+            col[0] = mg_ldw(in, c0 + lo.om, lo.wm);
 #pragma unroll
-        for (int k = 1; k <= MG_ZC; ++k) col[k] = in[c0 + (k - 1) * sz];
-        col[MG_ZC + 1] = mg_ldw(in, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
-        const T idg = mg_idiag<T>(g, dxy + 2);
-        const T idg_lo = mg_idiag<T>(g, dxy + 1 + (int)lo.wm);
-        const T idg_hi = mg_idiag<T>(g, dxy + 1 + (int)hi.wp);
+            for (int k = 1; k <= MG_ZC; ++k) col[k] = in[c0 + (k - 1) * sz];
+            col[MG_ZC + 1] = mg_ldw(in, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+            const T idg = mg_idiag<T>(g, dxy + 2);
+            const T idg_lo = mg_idiag<T>(g, dxy + 1 + (int)lo.wm);
+            const T idg_hi = mg_idiag<T>(g, dxy + 1 + (int)hi.wp);
 #pragma unroll
-        for (int k = 0; k < MG_ZC; ++k) {
-            const long long c = c0 + k * sz;
-            put(c, cell(c, col[k], col[k + 1], col[k + 2], k == 0 ? idg_lo : (k == MG_ZC - 1 ? idg_hi : idg)));
+            for (int k = 0; k < MG_ZC; ++k) {
+                const long long c = c0 + k * sz;
+                put(c, cell(c, col[k], col[k + 1], col[k + 2], k == 0 ? idg_lo : (k == MG_ZC - 1 ? idg_hi : idg)));
+            }
+        } else {
+            for (int z = z0; z < nz; ++z) {   // last, partial chunk
+                const long long c = mg_at(g, z, y, x);
+                const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
+                const T idg = mg_idiag<T>(g, dxy + (int)nzb.wm + (int)nzb.wp);
+                put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg));
+            }
         }
-        return;
     }
-    for (int z = z0; z < nz; ++z) {   // last, partial chunk
-        const long long c = mg_at(g, z, y, x);
-        const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
-        const T idg = mg_idiag<T>(g, dxy + (int)nzb.wm + (int)nzb.wp);
-        put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg));
-    }
+    if (MODE == 2) block_partial2((double)sdot, (double)ssum, partial, partial2);
 }
 
 // First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
@@ -563,18 +616,6 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
 // ---------------------------------------------------------------- reductions
 // Deterministic sums: one partial per block of the (x, y, z-chunk) grid, then one
 // block adds the partials in a fixed order.
-__device__ __forceinline__ void block_partial(double s, double* __restrict__ partial) {
-    __shared__ double sm[MG_BX * MG_BY / 32];
-    const int tid = threadIdx.y * MG_BX + threadIdx.x;
-    s = warp_sum(s);
-    if ((tid & 31) == 0) sm[tid >> 5] = s;
-    __syncthreads();
-    if (tid < 32) {
-        double t = (tid < MG_BX * MG_BY / 32) ? sm[tid] : 0.0;
-        t = warp_sum(t);
-        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
-    }
-}
 
 // MODE 0: sum v^2 ; MODE 1: sum r^2 with r = b + diag*x - sum(x_nb)
 template <typename T, int MODE>
@@ -762,6 +803,157 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
     block_partial((double)s * sc[SC_INVSCALE2], partial);
 }
 
+// ---------------------------------------------------------------- Krylov acceleration
+// Mixed precision with mg_krylov: flexible conjugate gradients FCG(1) on the level-0
+// equation, preconditioned by the FP32 V-cycle (zero initial guess), with the float-pair
+// solution x and the float-pair true residual of iterative refinement:
+//   r = b - A x (k_mg_resid_df; stop test), z = V(r), p = z + beta p with
+//   beta = -(z.q)/(p.q) of the previous direction (0 on the first iteration),
+//   q = A p, alpha = (p.r)/(p.q), x += alpha p.
+// A x = sum(x_nb) - diag*x is the operator whose residual k_mg_resid_df forms; it is
+// negative definite, which leaves alpha and beta unchanged against the positive form.
+// The V-cycle is not symmetric (the restriction is not the transposed prolongation),
+// hence the flexible beta. Scalars live in the solve's slots: SC_ZQ, SC_PQ, SC_PR as
+// doubles, beta as a float and alpha as a float pair (so that the elementwise kernels
+// do no FP64 work).
+constexpr int SC_ZQ = 7, SC_PQ = 8, SC_PR = 9, SC_BETA = 10, SC_ALPHA = 11, SC_ZMEAN = 12;
+
+
+// sums of the partials of z.q and of z, then beta = -(z.q)/(p.q) of the previous
+// iteration (0 on the first: k = iteration of this solve, or sc[SC_NITE] when k < 0),
+// stored as a float, and the mean of z (float)
+__global__ void k_fcg_final_beta(const double* __restrict__ pzq, const double* __restrict__ pz, int n, double vol,
+                                 double* __restrict__ sc, int k) {
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a += pzq[i];
+        b += pz[i];
+    }
+    __shared__ double sm[2][32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((threadIdx.x & 31) == 0) {
+        sm[0][threadIdx.x >> 5] = a;
+        sm[1][threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const bool in = threadIdx.x < (blockDim.x >> 5);
+        double zq = in ? sm[0][threadIdx.x] : 0.0, zs = in ? sm[1][threadIdx.x] : 0.0;
+        zq = warp_sum(zq);
+        zs = warp_sum(zs);
+        if (threadIdx.x == 0) {
+            const int it = k >= 0 ? k : (int)sc[SC_NITE];
+            const double pq = sc[SC_PQ];
+            double beta = (it > 0 && pq != 0.0) ? -zq / pq : 0.0;
+            if (!isfinite(beta)) beta = 0.0;
+            double zmean = zs / vol;
+            if (!isfinite(zmean)) zmean = 0.0;
+            sc[SC_ZQ] = zq;
+            reinterpret_cast<float*>(sc + SC_BETA)[0] = (float)beta;
+            reinterpret_cast<float*>(sc + SC_ZMEAN)[0] = (float)zmean;
+        }
+    }
+}
+
+// New direction and its image, in place: p = (z - mean z) + beta p and
+// q = A p = A z + beta q (A is linear and A 1 = 0, so only z is read at the
+// neighbours), with the partial sums of p.q and p.r. A z = sum(z_nb) - diag*z.
+// Walls and periodic directions leave A the constant null space: a right-hand side with
+// a component along it (the reference's viscosity moves wall-face velocities) makes the
+// stationary iteration stall at a residual floor, and would make the directions drift
+// along the constant without the mean removal.
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g, const float* __restrict__ z,
+                                                                 const float* __restrict__ r, float* __restrict__ p,
+                                                                 float* __restrict__ q, const double* __restrict__ sc,
+                                                                 double* __restrict__ ppq, double* __restrict__ ppr) {
+    const int x = blockIdx.x * MG_BX + threadIdx.x;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const float beta = reinterpret_cast<const float*>(sc + SC_BETA)[0];
+    const float zmean = reinterpret_cast<const float*>(sc + SC_ZMEAN)[0];
+    float spq = 0.f, spr = 0.f;
+    if (x < g.n[2] && y < g.n[1]) {
+        const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+        const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
+        const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
+        const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
+        const long long c0 = mg_at(g, z0, y, x);
+        auto cell = [&](long long c, float zm, float z0v, float zp, int dg) {
+            const float s = ((((mg_ldw(z, c + nx.om, nx.wm) + mg_ldw(z, c + nx.op, nx.wp)) +
+                               mg_ldw(z, c + ny.om, ny.wm)) + mg_ldw(z, c + ny.op, ny.wp)) + zm) + zp;
+            const float az = __fmaf_rn(-(float)dg, z0v, s);
+            const float pv = __fmaf_rn(beta, p[c], __fsub_rn(z0v, zmean));
+            const float qv = __fmaf_rn(beta, q[c], az);
+            p[c] = pv;
+            q[c] = qv;
+            spq = __fmaf_rn(pv, qv, spq);
+            spr = __fmaf_rn(pv, r[c], spr);
+        };
+        if (z0 + MG_ZC <= nz) {
+            const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
+            float col[MG_ZC + 2];
+            col[0] = mg_ldw(z, c0 + lo.om, lo.wm);
+#pragma unroll
+            for (int k = 1; k <= MG_ZC; ++k) col[k] = z[c0 + (k - 1) * sz];
+            col[MG_ZC + 1] = mg_ldw(z, c0 + (MG_ZC - 1) * sz + hi.op, hi.wp);
+#pragma unroll
+            for (int k = 0; k < MG_ZC; ++k)
+                cell(c0 + k * sz, col[k], col[k + 1], col[k + 2],
+                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == MG_ZC - 1 ? 1 + (int)hi.wp : 2)));
+        } else {
+            for (int zz = z0; zz < nz; ++zz) {
+                const long long c = c0 + (zz - z0) * sz;
+                const MgNb nzb = mg_nb(zz, nz, g.per[0], sz);
+                cell(c, mg_ldw(z, c + nzb.om, nzb.wm), z[c], mg_ldw(z, c + nzb.op, nzb.wp),
+                     dxy + (int)nzb.wm + (int)nzb.wp);
+            }
+        }
+    }
+    block_partial2((double)spq, (double)spr, ppq, ppr);
+}
+
+// sums of p.q and p.r, then alpha = (p.r)/(p.q) stored as a float pair
+__global__ void k_fcg_final_alpha(const double* __restrict__ ppq, const double* __restrict__ ppr, int n,
+                                  double* __restrict__ sc) {
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a += ppq[i];
+        b += ppr[i];
+    }
+    __shared__ double sm[2][32];
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((threadIdx.x & 31) == 0) {
+        sm[0][threadIdx.x >> 5] = a;
+        sm[1][threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const bool in = threadIdx.x < (blockDim.x >> 5);
+        double pq = in ? sm[0][threadIdx.x] : 0.0, pr = in ? sm[1][threadIdx.x] : 0.0;
+        pq = warp_sum(pq);
+        pr = warp_sum(pr);
+        if (threadIdx.x == 0) {
+            double alpha = pq != 0.0 ? pr / pq : 0.0;
+            if (!isfinite(alpha)) alpha = 0.0;
+            sc[SC_PQ] = pq;
+            sc[SC_PR] = pr;
+            const float hi = (float)alpha;
+            float2* a2 = reinterpret_cast<float2*>(sc + SC_ALPHA);
+            *a2 = make_float2(hi, (float)(alpha - (double)hi));
+        }
+    }
+}
+
+// x += alpha p on the float-pair solution (level 0, elementwise)
+__global__ void __launch_bounds__(256) k_fcg_xupdate(float2* __restrict__ xdf, const float* __restrict__ p,
+                                                     long long n, const double* __restrict__ sc) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2 alpha = reinterpret_cast<const float2*>(sc + SC_ALPHA)[0];
+    xdf[i] = df_add(xdf[i], df_mul_f(p[i], alpha));
+}
+
 // sum of squares of a float-pair array (high parts, squared and summed in double)
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq_df(const MgGeom g, const float2* __restrict__ v,
                                                               double* __restrict__ partial) {
@@ -913,6 +1105,8 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
     if (precision == NYLES_MIXED) {
         mg->off_pdf = take(mg->lev[0].vol * sizeof(float2));
         mg->off_bdf = take(mg->lev[0].vol * sizeof(float2));
+        mg->off_fp = take(mg->lev[0].vol * sizeof(float));
+        mg->off_fq = take(mg->lev[0].vol * sizeof(float));
     }
     // the coarsest levels whose arrays fit in one block's shared memory (two levels at
     // least, never level 0) run as one k_mg_bottom launch per V-cycle
@@ -941,15 +1135,18 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
     const dim3 g0 = grid_zc(mg->lev[0].n, MG_DFZC < MG_ZC ? MG_DFZC : MG_ZC);
     mg->npartial = (int)(g0.x * g0.y * g0.z);
     mg->off_partial = take(mg->npartial * sizeof(double));
+    mg->off_partial2 = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
     mg->bytes = off;
     return NYLES_OK;
 }
 
-template <typename T>
 // smoothing of level l: half-sweeps x -> y -> x; with from_y the first one was already
-// written into y by the kernel that set b from a zero solution
-static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64, bool from_y = false) {
+// written into y by the kernel that set b from a zero solution. The last half-sweep
+// runs in `last_mode` (k_mg_jacobi: 0 store, 1 add to the float-pair solution, 2 store
+// and sum its dot product with the Krylov vector q).
+template <typename T>
+static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_y = false) {
     if (empty(mg, l)) return;
     MgGeom g = mgg(mg, l);
     const dim3 grd = grid_zc(g.n, MG_ZC);
@@ -959,11 +1156,17 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, bool acc_p64, bool from_y
     const T om = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch(from_y ? 1 : 2);
-    if (!from_y) k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr);
-    if (acc_p64)
-        k_mg_jacobi<T, true><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf));
+    if (!from_y) k_mg_jacobi<T, 0><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
+    if (last_mode == 1)
+        k_mg_jacobi<T, 1><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf),
+                                                nullptr, nullptr, nullptr);
+    else if (last_mode == 2)
+        k_mg_jacobi<T, 2><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr,
+                                                reinterpret_cast<const T*>(mg->ws + mg->off_fq),
+                                                reinterpret_cast<double*>(mg->ws + mg->off_partial),
+                                                reinterpret_cast<double*>(mg->ws + mg->off_partial2));
     else
-        k_mg_jacobi<T, false><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr);
+        k_mg_jacobi<T, 0><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr);
 }
 
 // solvers.f90:35-55
@@ -988,16 +1191,16 @@ static void bottom(MgImpl* mg, cudaStream_t st) {
     k_mg_bottom<T><<<1, MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a);
 }
 
+// level0_last: mode of the last level-0 half-sweep (see smooth)
 template <typename T>
-static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
+static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
     const int L = mg->nlevels;
     const int B = mg->bottom;   // < L: levels B..L-1 in one block
     // The first half-sweep of level 0 was written by the stop-test residual kernel that
     // precedes every V-cycle (k_mg_resid_sweep; mixed: k_mg_resid_df, from a zero
     // correction); every restricted level gets it from the restriction.
-    (void)mixed;
     for (int l = 0; l < L - 1 && l < B; ++l) {
-        smooth<T>(mg, l, st, false, true);
+        smooth<T>(mg, l, st, 0, true);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 9, st);
@@ -1010,7 +1213,7 @@ static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
     if (B < L)
         bottom<T>(mg, st);
     else
-        smooth<T>(mg, L - 1, st, L == 1 && mixed, true);
+        smooth<T>(mg, L - 1, st, L == 1 ? level0_last : 0, true);
     for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -1018,7 +1221,7 @@ static void vcycle(MgImpl* mg, cudaStream_t st, bool mixed) {
             note_launch();
             k_mg_prolong<T><<<grid_zc(gf.n, MG_ZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
         }
-        smooth<T>(mg, l, st, l == 0 && mixed);
+        smooth<T>(mg, l, st, l == 0 ? level0_last : 0);
     }
 }
 
@@ -1085,6 +1288,32 @@ static void enqueue_resid_sweep(MgImpl* mg, cudaStream_t st) {
     k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
 }
 
+// mixed precision with krylov: after the V-cycle left z = V(r) in level 0's x (and the
+// partial sums of z.q), one FCG(1) update of the direction p and q = A p, and
+// x += alpha p on the float-pair solution (k: iteration of this solve, or -1 to read it
+// on the device)
+static void enqueue_fcg_update(MgImpl* mg, cudaStream_t st, int k) {
+    MgGeom g = mgg(mg, 0);
+    double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
+    double* part2 = reinterpret_cast<double*>(mg->ws + mg->off_partial2);
+    double* sc = scalars(mg);
+    float* z = lvp<float>(mg, 0, 1);
+    float* r = lvp<float>(mg, 0, 2);
+    float* P = reinterpret_cast<float*>(mg->ws + mg->off_fp);
+    float* Q = reinterpret_cast<float*>(mg->ws + mg->off_fq);
+    const long long n = mg->lev[0].vol;
+    const dim3 grd = grid_zc(g.n, MG_ZC);
+    const int nb = (int)(grd.x * grd.y * grd.z);
+    const unsigned eb = (unsigned)((n + 255) / 256);
+    ProfScope ps(mg->prof, 11, st);
+    note_launch(4);
+    // the partial sums of z.q and z were written by the V-cycle's last level-0 half-sweep
+    k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, nb, (double)n, sc, k);
+    k_fcg_direction<<<grd, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
+    k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, nb, sc);
+    k_fcg_xupdate<<<eb, 256, 0, st>>>(reinterpret_cast<float2*>(mg->ws + mg->off_pdf), P, n, sc);
+}
+
 template <typename T, int MODE>
 static int sumsq(MgImpl* mg, const MgGeom& g, const T* v, const T* b, double* host_out, cudaStream_t st) {
     enqueue_sumsq<T, MODE>(mg, g, v, b, scalars(mg), st);
@@ -1114,7 +1343,7 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
         }
         while (true) {
             if (res < mg->tol) break;
-            vcycle<double>(mg, st, false);
+            vcycle<double>(mg, st, 0);
             ++nite;
             if (nite >= mg->maxite) break;
             if (normb > 0.0) {
@@ -1135,7 +1364,12 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
         }
         while (true) {
             if (res < mg->tol) break;
-            vcycle<float>(mg, st, true);   // FP32 correction of the residual equation, added to p
+            if (mg->krylov) {              // z = V(r) preconditions an FCG(1) update of p
+                vcycle<float>(mg, st, 2);
+                enqueue_fcg_update(mg, st, nite);
+            } else {
+                vcycle<float>(mg, st, 1);   // FP32 correction of the residual equation, added to p
+            }
             ++nite;
             if (nite >= mg->maxite) break;
             if (normb > 0.0) {
@@ -1214,10 +1448,14 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
     if (e != cudaSuccess) return gb.error = cuda_status(e, "capture of the multigrid loop body");
     const long long l0 = nyles_launch_count();
     if (!mixed) {
-        vcycle<double>(mg, st, false);
+        vcycle<double>(mg, st, 0);
         enqueue_resid_sweep(mg, st);
+    } else if (mg->krylov) {
+        vcycle<float>(mg, st, 2);
+        enqueue_fcg_update(mg, st, -1);
+        enqueue_resid_df(mg, st);
     } else {
-        vcycle<float>(mg, st, true);
+        vcycle<float>(mg, st, 1);
         enqueue_resid_df(mg, st);
     }
     k_mg_ctl_step<<<1, 1, 0, st>>>(sc, h, mg->tol, mg->maxite);

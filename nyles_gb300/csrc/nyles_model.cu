@@ -280,6 +280,19 @@ int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega) {
     mg->impl.tol = tol; mg->impl.maxite = maxite; mg->impl.omega = omega;
     return NYLES_OK;
 }
+static int set_krylov(MgImpl* mg, int on) {
+    if (on && mg->precision != NYLES_MIXED) {
+        set_error("Krylov acceleration is provided for the mixed-precision solve only (the FP64 solve keeps "
+                  "the reference's iteration)");
+        return NYLES_UNSUPPORTED;
+    }
+    mg->krylov = on ? 1 : 0;
+    return NYLES_OK;
+}
+int nyles_mg_set_krylov(NylesMg* mg, int on) {
+    if (!mg) { set_error("null multigrid"); return NYLES_BAD_ARG; }
+    return set_krylov(&mg->impl, on);
+}
 int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream) {
     if (!mg) { set_error("null multigrid"); return NYLES_BAD_ARG; }
     int rc = mg_solve(&mg->impl, (cudaStream_t)stream);
@@ -359,6 +372,12 @@ int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omeg
     if (!m || maxite < 0 || !(tol >= 0.0) || !(omega > 0.0)) { set_error("bad multigrid parameters"); return NYLES_BAD_ARG; }
     m->mg.tol = tol; m->mg.maxite = maxite; m->mg.omega = omega;
     return NYLES_OK;
+}
+
+int nyles_model_set_mg_krylov(NylesModel* m, int on) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    if (m->gexec) { set_error("release the captured graph before changing the solver"); return NYLES_BAD_ARG; }
+    return set_krylov(&m->mg, on);
 }
 
 int nyles_model_reset_scheme(NylesModel* m) {

@@ -51,6 +51,11 @@ def make_desc(param, grid, modelname):
     return d
 
 
+# mixed precision, mg_krylov "auto": FCG at squared residual ratios at or below this
+# (relative residual 1e-8)
+KRYLOV_AUTO_TOL = 1e-16
+
+
 class LES(object):
     """One subdomain of the LES / Euler3d / linear model on cuda:0 (or `device`)."""
 
@@ -103,7 +108,8 @@ class LES(object):
         self._fields = nat.ptr_array([s.data_ptr() for s in self.state.scalars()])
         self._regs = nat.ptr_array(self.timescheme.register_pointers())
         nat.check(self.lib.nyles_model_bind(h, self._fields, self._regs, ctypes.c_void_p(ws)))
-        self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9))
+        self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9),
+                           krylov=gpu.get("mg_krylov", "auto"))
         self.stats = []
         # graph replay of fixed-dt steps (see forward)
         self.use_graphs = bool(gpu.get("graphs", True))
@@ -162,9 +168,31 @@ class LES(object):
             self._h = None
 
     # ------------------------------------------------------------------ settings
-    def set_mg_params(self, tol=1e-6, maxite=20, omega=0.9):
-        """Multigrid stop rule: sum(r^2)/sum(b^2) < tol or maxite V-cycles."""
+    def set_mg_params(self, tol=1e-6, maxite=20, omega=0.9, krylov=None):
+        """Multigrid stop rule: sum(r^2)/sum(b^2) < tol or maxite V-cycles. `krylov`
+        ("auto", "on", "off"; None keeps the current mode) selects the mixed-precision
+        solver: FCG(1) preconditioned by the V-cycle, or the reference's stationary
+        iteration; "auto" takes FCG when tol <= KRYLOV_AUTO_TOL, where both solvers land
+        within the tolerance of the exact solution (at looser tolerances the stationary
+        iterates are the ones that track the FP64 solve). A captured graph holds the
+        solver and its parameters, so it is released first."""
+        if getattr(self, "graph", None) is not None:
+            self.release_graph()
+        if krylov is not None:
+            if krylov not in ("auto", "on", "off"):
+                raise ValueError("mg_krylov must be 'auto', 'on' or 'off'")
+            self.mg_krylov = krylov
+        mode = getattr(self, "mg_krylov", "auto")
         nat.check(self.lib.nyles_model_set_mg_params(self._h, float(tol), int(maxite), float(omega)))
+        if self.precision == "fp64":
+            if mode == "on":
+                raise ValueError("mg_krylov = 'on' needs the mixed precision (the FP64 solve keeps the reference's "
+                                 "iteration)")
+            use = False
+        else:
+            use = mode == "on" or (mode == "auto" and float(tol) <= KRYLOV_AUTO_TOL)
+        nat.check(self.lib.nyles_model_set_mg_krylov(self._h, 1 if use else 0))
+        self.krylov = use
 
     def mg_stats(self):
         s = nat.NylesMgStats()

@@ -81,6 +81,11 @@ class MG(object):
     def set_params(self, tol=1e-6, maxite=20, omega=0.9):
         nat.check(self.lib.nyles_mg_set_params(self._h, float(tol), int(maxite), float(omega)))
 
+    def set_krylov(self, on=True):
+        """Mixed precision: FCG(1) preconditioned by the FP32 V-cycle instead of the
+        stationary V-cycle iteration (same stop rule)."""
+        nat.check(self.lib.nyles_mg_set_krylov(self._h, 1 if on else 0))
+
     def solve(self, b=None):
         """Solve with the current warm start; `b` (interior, any dtype) replaces the
         right-hand side when given. Returns (x, stats dict): x aliases the solution in
