@@ -234,13 +234,14 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
                            mg_ldw(in, c + ny.om, ny.wm)) + mg_ldw(in, c + ny.op, ny.wp)) + zm) + zp;
             return cff1 * x0 + omega * (s - b[c]) * idg;
         };
-        auto put = [&](long long c, T v) {
+        // dv: the cell's value of `dot` (MODE 2)
+        auto put = [&](long long c, T v, T dv) {
             if (MODE == 1) {
                 acc[c] = df_add_f(acc[c], (float)v);
             } else {
                 out[c] = v;
                 if (MODE == 2) {
-                    sdot = __fmaf_rn((float)v, (float)dot[c], sdot);
+                    sdot = __fmaf_rn((float)v, (float)dv, sdot);
                     ssum = __fadd_rn(ssum, (float)v);
                 }
             }
@@ -260,14 +261,16 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 #pragma unroll
             for (int k = 0; k < MG_ZC; ++k) {
                 const long long c = c0 + k * sz;
-                put(c, cell(c, col[k], col[k + 1], col[k + 2], k == 0 ? idg_lo : (k == MG_ZC - 1 ? idg_hi : idg)));
+                put(c, cell(c, col[k], col[k + 1], col[k + 2], k == 0 ? idg_lo : (k == MG_ZC - 1 ? idg_hi : idg)),
+                    (MODE == 2) ? dot[c] : T(0));
             }
         } else {
             for (int z = z0; z < nz; ++z) {   // last, partial chunk
                 const long long c = mg_at(g, z, y, x);
                 const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
                 const T idg = mg_idiag<T>(g, dxy + (int)nzb.wm + (int)nzb.wp);
-                put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg));
+                put(c, cell(c, mg_ldw(in, c + nzb.om, nzb.wm), in[c], mg_ldw(in, c + nzb.op, nzb.wp), idg),
+                    (MODE == 2) ? dot[c] : T(0));
             }
         }
     }
@@ -771,10 +774,11 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
         const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
         const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
         const long long c0 = mg_at(g, z0, y, x);
-        auto cell = [&](long long c, float2 zm, float2 p0, float2 zp, int dg) {
+        // bc: the cell's right-hand side (loaded ahead by the caller)
+        auto cell = [&](long long c, float2 zm, float2 p0, float2 zp, int dg, float2 bc) {
             const float2 nb[6] = {mg_ldw_df(p, c + nx.om, nx.wm), mg_ldw_df(p, c + nx.op, nx.wp),
                                   mg_ldw_df(p, c + ny.om, ny.wm), mg_ldw_df(p, c + ny.op, ny.wp), zm, zp};
-            const float r = df_resid(b[c], p0, (float)dg, nb);
+            const float r = df_resid(bc, p0, (float)dg, nb);
             r32[c] = r;
             y32[c] = mg_jacobi_from_zero(r, omega, mg_idiag<float>(g, dg));
             const float rs = __fmul_rn(r, scale);
@@ -787,16 +791,19 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
 #pragma unroll
             for (int k = 1; k <= ZC; ++k) col[k] = p[c0 + (k - 1) * sz];
             col[ZC + 1] = mg_ldw_df(p, c0 + (ZC - 1) * sz + hi.op, hi.wp);
+            float2 bcol[ZC];
+#pragma unroll
+            for (int k = 0; k < ZC; ++k) bcol[k] = b[c0 + k * sz];
 #pragma unroll
             for (int k = 0; k < ZC; ++k)
                 cell(c0 + k * sz, col[k], col[k + 1], col[k + 2],
-                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == ZC - 1 ? 1 + (int)hi.wp : 2)));
+                     dxy + (k == 0 ? 1 + (int)lo.wm : (k == ZC - 1 ? 1 + (int)hi.wp : 2)), bcol[k]);
         } else {
             for (int z = z0; z < nz; ++z) {
                 const long long c = c0 + (z - z0) * sz;
                 const MgNb nzb = mg_nb(z, nz, g.per[0], sz);
                 cell(c, mg_ldw_df(p, c + nzb.om, nzb.wm), p[c], mg_ldw_df(p, c + nzb.op, nzb.wp),
-                     dxy + (int)nzb.wm + (int)nzb.wp);
+                     dxy + (int)nzb.wm + (int)nzb.wp, b[c]);
             }
         }
     }
