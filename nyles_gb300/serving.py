@@ -150,9 +150,10 @@ def steps_per_graph(steps, kmax=10):
 
 
 class Run:
-    """One admitted request: resident state, its stream and its captured graph."""
+    """One admitted request: resident state, its stream (of CUDA priority `priority`,
+    lower = scheduled first) and its captured graph."""
 
-    def __init__(self, req, precision, device, mg_tol):
+    def __init__(self, req, precision, device, mg_tol, priority=0):
         self.req = req
         self.nyl = Nyles(build_params(req.case, req.n, precision, mg_tol), device=device)
         initial_state(self.nyl, req.case, req.seed)
@@ -160,7 +161,7 @@ class Run:
         m.diagnose_var(m.state)                       # core/nyles.py:122
         self.k = steps_per_graph(req.steps)
         m.capture_graph(CASES[req.case]["dt"], self.k)
-        self.stream = torch.cuda.Stream(device=device)
+        self.stream = torch.cuda.Stream(device=device, priority=priority)
         self.stream.wait_stream(torch.cuda.current_stream(device))
         self.launched = 0
         self.inflight = []                            # events of launches not yet seen complete
@@ -194,11 +195,29 @@ class Run:
         return {s: st.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k", "p")}
 
 
+def remaining_work(run):
+    """cells x steps not yet launched"""
+    return run.req.n ** 3 * max(0, run.req.steps - run.launched)
+
+
 class ServingEngine:
-    """Admission against an HBM budget, resident runs, overlapping graph replays."""
+    """Admission against an HBM budget, resident runs, overlapping graph replays.
+
+    priority "work" (default) gives each run's stream a CUDA priority by its total work
+    (cells x steps): the GPU schedules the blocks of small runs first; "none" gives every
+    stream the same priority. `window` = W advances only the W runs with the least
+    remaining work at each tick (shortest remaining work first): small runs complete
+    soon after they arrive, the large ones, which set the makespan, fill the device once
+    the small ones are done; None advances every resident run."""
 
     def __init__(self, hbm_budget_bytes=120e9, precision="mixed", mg_tol=1e-6, device=None, inflight=2,
-                 clock=time.perf_counter, run_factory=None):
+                 clock=time.perf_counter, run_factory=None, priority="work", window=None):
+        if priority not in ("work", "none"):
+            raise ValueError("priority must be 'work' or 'none'")
+        if window is not None and window < 1:
+            raise ValueError("window must be None or >= 1")
+        self.priority = priority
+        self.window = window
         self.budget = float(hbm_budget_bytes)
         self.precision = precision
         self.mg_tol = mg_tol
@@ -217,6 +236,7 @@ class ServingEngine:
         once). Returns (results, final_states) with final_states[rid] = dict of numpy
         prognostic fields when keep_states."""
         pending = sorted(requests, key=lambda r: r.arrival)
+        prio = self.stream_priorities(requests)
         queue, active, results, states = [], [], [], {}
         t0 = self.clock()
         nxt = 0
@@ -232,15 +252,17 @@ class ServingEngine:
                 if self.used + need > self.budget and active:
                     break
                 queue.pop(0)
-                run = self.run_factory(req, self.precision, self.device, self.mg_tol)
+                run = self.run_factory(req, self.precision, self.device, self.mg_tol, priority=prio[req.rid])
                 run.admitted = self.clock() - t0
                 run.need = need
                 self.used += need
                 self.peak_used = max(self.peak_used, self.used)
                 active.append(run)
             self.max_active = max(self.max_active, len(active))
-            # advance: keep up to `inflight` graph launches queued per run
-            for run in active:
+            # advance: keep up to `inflight` graph launches queued per run, for the
+            # `window` runs with the least remaining work (all runs without a window)
+            order = active if self.window is None else sorted(active, key=remaining_work)[:self.window]
+            for run in order:
                 if not run.all_launched and run.poll() < self.inflight:
                     run.launch()
             # completion
@@ -258,13 +280,30 @@ class ServingEngine:
                 else:
                     still.append(run)
             active = still
-            if active and all(r.all_launched or r.poll() >= self.inflight for r in active):
+            waiting = order if self.window is None else [r for r in order if r in active]
+            if waiting and all(r.all_launched or r.poll() >= self.inflight for r in waiting):
                 time.sleep(2e-4)
             elif not active and not queue and nxt < len(pending):
                 time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
         if self.device is not None and self.device.type == "cuda":
             torch.cuda.synchronize(self.device)
         return sorted(results, key=lambda r: r.rid), states
+
+    def stream_priorities(self, requests, levels=None):
+        """{rid: stream priority}: the distinct work values (n^3 x steps) of the requests,
+        smallest first, spread over the device's priority range (greatest priority to
+        the least work); 0 for all with priority "none"."""
+        if self.priority == "none" or not requests:
+            return {r.rid: 0 for r in requests}
+        if levels is None:
+            least, greatest = (torch.cuda.Stream.priority_range() if self.device is not None
+                               and self.device.type == "cuda" else (0, 0))
+        else:
+            least, greatest = levels
+        nlev = least - greatest + 1
+        works = sorted({r.n ** 3 * r.steps for r in requests})
+        rank = {w: i for i, w in enumerate(works)}
+        return {r.rid: greatest + min(nlev - 1, rank[r.n ** 3 * r.steps] * nlev // len(works)) for r in requests}
 
 
 def run_sequential(requests, precision="fp64", mg_tol=1e-6, device=None, keep_states=False):
@@ -293,6 +332,46 @@ def run_sequential(requests, precision="fp64", mg_tol=1e-6, device=None, keep_st
                                for s in ("b", "u_i", "u_j", "u_k", "p")}
         del nyl, m
     return results, states
+
+
+def sequential_estimate(requests, precision="fp64", mg_tol=1e-6, device=None, sample_steps=10, warmup=2):
+    """The baseline of run_sequential without running every step: for each bucket (case,
+    grid) of the requests, the setup (model build, initial projection) and `sample_steps`
+    eager steps after `warmup` are timed once; the arrival queue is then replayed with
+    duration = setup + steps x step time per run, one run at a time. Returns (results,
+    {bucket: {"setup_s", "step_s"}})."""
+    timing = {}
+    for case, n in sorted({r.bucket for r in requests}):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        nyl = Nyles(build_params(case, n, precision, mg_tol), device=device)
+        initial_state(nyl, case, 0)
+        m = nyl.model
+        m.diagnose_var(m.state)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        dt = CASES[case]["dt"]
+        for _ in range(warmup):
+            m.forward(0.0, dt)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(sample_steps):
+            m.forward(0.0, dt)
+        torch.cuda.synchronize()
+        timing[(case, n)] = {"setup_s": setup, "step_s": (time.perf_counter() - t0) / sample_steps}
+        del nyl, m
+    return replay_queue(requests, lambda r: timing[r.bucket]["setup_s"] + r.steps * timing[r.bucket]["step_s"]), timing
+
+
+def replay_queue(requests, duration):
+    """One run at a time in arrival order: a run starts at max(arrival, end of the
+    previous run) and lasts duration(request) seconds."""
+    results, clock = [], 0.0
+    for req in sorted(requests, key=lambda r: r.arrival):
+        start = max(clock, req.arrival)
+        clock = start + duration(req)
+        results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival, start, clock, req.n ** 3))
+    return results
 
 
 def summarize(results, makespan=None):

@@ -58,3 +58,17 @@ def test_footprint_model_covers_the_allocation(case, n, precision):
     need = S.footprint_bytes(case, n, precision)
     assert used <= need <= 1.5 * used, (used, need)
     del run
+
+
+def test_sequential_estimate_tracks_the_sequential_run():
+    """The bucketed baseline (setup + steps x measured step time, queue replayed) stays
+    within a factor of two of actually running the same requests one at a time."""
+    from nyles_gb300 import serving as S
+    reqs = [S.Request(0, "lock", 48, 11, 40, 0.0), S.Request(1, "tgv", 32, 12, 40, 0.0),
+            S.Request(2, "lock", 48, 13, 40, 0.0)]
+    est, timing = S.sequential_estimate(reqs, precision="fp64", sample_steps=10)
+    run, _ = S.run_sequential(reqs, precision="fp64")
+    assert set(timing) == {("lock", 48), ("tgv", 32)}
+    span_est = max(r.done for r in est)
+    span_run = max(r.done for r in run)
+    assert 0.5 < span_est / span_run < 2.0, (span_est, span_run)

@@ -26,8 +26,9 @@ class FakeRun:
     live = 0
     peak = 0
 
-    def __init__(self, req, precision, device, mg_tol):
+    def __init__(self, req, precision, device, mg_tol, priority=0):
         self.req = req
+        self.priority = priority
         self.k = S.steps_per_graph(req.steps)
         self.launched = 0
         self.pending = 0
@@ -71,3 +72,39 @@ def test_admission_respects_the_budget_and_serves_everything():
     assert FakeRun.live == 0
     summary = S.summarize(results)
     assert summary["runs"] == 20 and summary["p99_s"] >= summary["p50_s"]
+
+
+def test_replay_queue_one_at_a_time():
+    """The sequential baseline's queue: starts at max(arrival, previous end)."""
+    from nyles_gb300 import serving as S
+    reqs = [S.Request(0, "lock", 32, 1, 10, 0.0), S.Request(1, "tgv", 64, 2, 10, 0.5),
+            S.Request(2, "lock", 32, 3, 10, 5.0)]
+    res = S.replay_queue(reqs, lambda r: 1.0 if r.n == 32 else 2.0)
+    assert [(r.rid, r.admitted, r.done) for r in res] == [(0, 0.0, 1.0), (1, 1.0, 3.0), (2, 5.0, 6.0)]
+    assert [r.latency for r in res] == [1.0, 2.5, 1.0]
+
+
+def test_stream_priorities_by_work():
+    """Smallest work gets the greatest (numerically lowest) priority; equal work, equal
+    priority; "none" leaves every stream at 0."""
+    from nyles_gb300 import serving as S
+    reqs = [S.Request(i, "lock", n, i, 300, 0.0) for i, n in enumerate((32, 48, 64, 96, 128, 32))]
+    eng = S.ServingEngine(device="cpu", run_factory=FakeRun)
+    pr = eng.stream_priorities(reqs, levels=(0, -5))
+    assert pr[0] == pr[5] == -5 and pr[4] > pr[3] > pr[2] > pr[1] > pr[0] and pr[4] <= 0
+    assert set(S.ServingEngine(device="cpu", run_factory=FakeRun, priority="none")
+               .stream_priorities(reqs).values()) == {0}
+
+
+def test_window_serves_shortest_remaining_work_first():
+    """With a window of one run and every request available at once, runs complete in
+    the order of their work; every run completes."""
+    from nyles_gb300 import serving as S
+    sizes = [96, 32, 128, 48, 64]
+    reqs = [S.Request(i, "lock", n, i, 20, 0.0) for i, n in enumerate(sizes)]
+    ticks = iter(range(10 ** 6))
+    eng = S.ServingEngine(device="cpu", run_factory=FakeRun, window=1, clock=lambda: float(next(ticks)))
+    results, _ = eng.serve(reqs, realtime=False)
+    order = [r.rid for r in sorted(results, key=lambda r: r.done)]
+    assert order == sorted(range(5), key=lambda i: sizes[i])
+    assert FakeRun.live == 0
