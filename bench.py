@@ -221,16 +221,15 @@ def mg_levels(n):
     return levels
 
 
-# FP64 flops (DADD + DMUL + 2 x DFMA thread instructions) per array cell of one
-# k_rhs_march<double, 1, 1> launch, counted by ncu on the 128^3 case of this workload
-# (237 + 251 + 2 x 252 per cell).
-RHS_FP64_OPS_PER_CELL = 992
-RHS_FP64_INSTR_PER_CELL = 237 + 251 + 252
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per array cell of one
-# right-hand-side launch, from ncu --set full captures of this workload: FP64 at 128^3
-# (158.4 + 47.1 MB over 128 x 134 x 134 cells), FP32 at 256^3 (574.1 + 263.8 MB over
-# 256 x 262 x 262 cells). Traffic grows with the cells processed.
-RHS_DRAM_BYTES_PER_CELL = {8: 205.5e6 / (128 * 134 * 134), 4: 837.9e6 / (256 * 262 * 262)}
+# FP64 flops (DADD + DMUL + 2 x DFMA thread instructions) per interior cell of one
+# k_rhs_march<double, 1, 1, 0> launch, counted by ncu on the 128^3 case of this workload
+# (smsp__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on: 223.5 + 237.8 + 2 x 237.5
+# per cell), and the FP64 instructions (issue slots) behind them
+RHS_FP64_OPS_PER_CELL = 936
+RHS_FP64_INSTR_PER_CELL = 699
+# DRAM bytes (read + write) per interior cell of one launch: ncu, FP64 at 128^3
+# (159.0 + 43.7 MB), mixed at 256^3 (591.1 + 252.4 MB)
+RHS_DRAM_BYTES_PER_CELL = {8: 202.72e6 / 128 ** 3, 4: 843.45e6 / 256 ** 3}
 # DRAM bytes of one level-0 Jacobi half-sweep launch at 256^3, mixed (ncu: 134.2 +
 # 41.6 MB; algorithmic 201.3 MB, the rest of the output still in L2 at the end)
 JACOBI_F32_L0_DRAM_BYTES_256 = 175.8e6
@@ -255,7 +254,7 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak, nv=None, solves=No
     """Roofline of one kernel family from the CUDA-event phase times.
 
     rhs       : one launch reads b, U(3), vor(3), ke and writes 4 registers: 12 words
-                per cell of the (n+6)^2 n array. In FP64 the kernel is bound by the FP64
+                per interior cell (the periodic halo's tendencies are not computed). In FP64 the kernel is bound by the FP64
                 pipe (GB300 issues FP64 at 1/64 of its FP32 rate): the roofline is
                 then the FP64 arithmetic rate against cuBLAS DGEMM, with the
                 issue-slot fraction (DADD and DMUL take a slot for one flop, DFMA for
@@ -277,7 +276,7 @@ def roofline(kernel, ph, n, elem, peak, peak_kind, fp64_peak, nv=None, solves=No
     ms = ph[kernel]["ms"]
     out = {"kernel": kernel, "bound": "hbm", "peak": peak, "unit": "GB/s", "peak_kind": peak_kind, "traffic": None}
     if kernel == "rhs":
-        vol = (n + 6) * (n + 6) * n
+        vol = n ** 3   # the time step computes the b and u tendencies of interior cells only
         launches = ph[kernel]["count"]
         per_launch = 12 * elem * vol
         avg = ms / launches

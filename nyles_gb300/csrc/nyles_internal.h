@@ -55,9 +55,11 @@ struct ProgPtrs {
 // term bits of launch_rhs
 enum { TERM_TRACER = 1, TERM_VF = 2, TERM_BERNOULLI = 4, TERM_VISC = 8, TERM_ACCUMULATE = 16, TERM_TRDIFF = 32 };
 
+// interior = true skips the b and u tendencies of periodic halo cells (the time step
+// refills those halos before it reads them); false covers every stored cell
 template <typename T>
 int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
-               cudaStream_t st);
+               cudaStream_t st, bool interior = false);
 
 // time-scheme elementwise updates (core/timescheme.py:113-221)
 enum { UPD_EULER = 0, UPD_RK3_2 = 1, UPD_RK3_3 = 2, UPD_LF_PRED = 3, UPD_LF_FIRST = 4, UPD_LF_CORR = 5 };

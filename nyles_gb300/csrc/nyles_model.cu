@@ -428,11 +428,14 @@ int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
 namespace nyles {
 
 template <typename T>
-static int model_rhs(NylesModel* m, int reg, int last, double t, cudaStream_t st) {
+static int model_rhs(NylesModel* m, int reg, int last, double t, cudaStream_t st, bool interior = false) {
     StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
     ProgPtrs<T> ds = prog_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->regs[reg]));
+    // Euler3d projects before its halo fill (core/model_les_euler.py:96-125): the
+    // divergence next to the halo reads updated halo velocities, so their tendencies count
+    if (m->d.model == NYLES_MODEL_EULER3D) interior = false;
     ProfScope ps(&m->prof, 0, st);
-    int rc = launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st);
+    int rc = launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st, interior);
     // user forcing, core/model_les.py:143-144: called with the stage's register set and
     // time; it enqueues its own work on `st`
     if (!rc && m->forcing) m->forcing(m->forcing_user, reg, t, (void*)st);
@@ -534,23 +537,23 @@ template <typename T>
 static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
     int rc;
     if (m->scheme == NYLES_SCHEME_RK3_SSP) {
-        if ((rc = model_rhs<T>(m, 0, 0, t, st))) return rc;
+        if ((rc = model_rhs<T>(m, 0, 0, t, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
         if ((rc = model_diagnose<T>(m, st))) return rc;
-        if ((rc = model_rhs<T>(m, 1, 0, t + dt, st))) return rc;
+        if ((rc = model_rhs<T>(m, 1, 0, t + dt, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_2, 0, 1, -1, dt, st))) return rc;
         if ((rc = model_diagnose<T>(m, st))) return rc;
-        if ((rc = model_rhs<T>(m, 2, 1, t + dt * 0.5, st))) return rc;
+        if ((rc = model_rhs<T>(m, 2, 1, t + dt * 0.5, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_3, 0, 1, 2, dt, st))) return rc;
         return model_diagnose<T>(m, st);
     }
     if (m->scheme == NYLES_SCHEME_EF) {
-        if ((rc = model_rhs<T>(m, 0, 1, t, st))) return rc;
+        if ((rc = model_rhs<T>(m, 0, 1, t, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
         return model_diagnose<T>(m, st);
     }
     // LFAM3: registers 0 = dstate, 1 = stateb, 2 = state (n)
-    if ((rc = model_rhs<T>(m, 0, 0, t, st))) return rc;
+    if ((rc = model_rhs<T>(m, 0, 0, t, st, true))) return rc;
     if (m->lf_first) {
         if ((rc = model_update<T>(m, UPD_LF_FIRST, 0, 1, 2, dt, st))) return rc;
         m->lf_first = false;
@@ -558,7 +561,7 @@ static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
     }
     if ((rc = model_update<T>(m, UPD_LF_PRED, 0, 1, 2, dt, st))) return rc;
     if ((rc = model_diagnose<T>(m, st))) return rc;
-    if ((rc = model_rhs<T>(m, 0, 1, t + dt * 0.5, st))) return rc;
+    if ((rc = model_rhs<T>(m, 0, 1, t + dt * 0.5, st, true))) return rc;
     if ((rc = model_update<T>(m, UPD_LF_CORR, 0, 1, 2, dt, st))) return rc;
     return model_diagnose<T>(m, st);
 }

@@ -63,6 +63,7 @@ struct RhsArgs {
     T vcoef[3];       // viscosity*ids2 for directions x, y, z
     T kcoef[NYLES_MAX_TR + 1][3];   // tracer diffusivity*ids2 of b, t0.. for x, y, z
     int kmask;        // bit q: diffuse tracer q (b = 0) when TERM_TRDIFF is set
+    int lo[3], hi[3]; // k_rhs_march: index box (z, y, x) of the cells it computes
 };
 
 // viscosity along direction d of component field u at c, core/fortran_dissipation.f90:18-33
@@ -208,13 +209,13 @@ template <typename T, bool TR, bool VF, bool BDIFF>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a) {
     __shared__ T sfy[RZ_BY][RZ_BX];
     const Geom& g = a.g;
-    const int x = blockIdx.x * RZ_BX + threadIdx.x;
-    const int y = blockIdx.y * RZ_BY + threadIdx.y;
-    const int z0 = blockIdx.z * RZ_ZC;
-    const int z1 = min(z0 + RZ_ZC, g.N[0]) - 1;
+    const int x = a.lo[2] + blockIdx.x * RZ_BX + threadIdx.x;
+    const int y = a.lo[1] + blockIdx.y * RZ_BY + threadIdx.y;
+    const int z0 = a.lo[0] + blockIdx.z * RZ_ZC;
+    const int z1 = min(z0 + RZ_ZC, a.hi[0]) - 1;
     const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
-    const bool valid = x < Nx && y < Ny;
-    const int xs = min(x, Nx - 1), ys = min(y, Ny - 1);   // idle lanes shadow a real cell
+    const bool valid = x < a.hi[2] && y < a.hi[1];
+    const int xs = min(x, a.hi[2] - 1), ys = min(y, a.hi[1] - 1);   // idle lanes shadow a real cell
     const T* Uzyx[3] = {a.U[2], a.U[1], a.U[0]};
     TracerMarch<T> tm;
     tm.fz_prev = T(0);
@@ -386,9 +387,15 @@ static dim3 grid3(const Geom& g, dim3 blk) {
 
 template <typename T>
 int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
-               cudaStream_t st) {
+               cudaStream_t st, bool interior) {
     RhsArgs<T> a;
     a.g = g;
+    // interior: the b and u tendencies of the periodic halo are not computed (the time
+    // step refills those halos before reading them); tracers always cover every cell
+    for (int k = 0; k < 3; ++k) {
+        a.lo[k] = (interior && g.per[k]) ? g.nh : 0;
+        a.hi[k] = (interior && g.per[k]) ? g.nh + g.n[k] : g.N[k];
+    }
     a.b = s.f[NYLES_F_B];
     for (int t = 0; t < NYLES_MAX_TR; ++t) a.tr[t] = (t < d->n_tracers) ? s.f[NYLES_F_T0 + t] : nullptr;
     for (int i = 0; i < 3; ++i) {
@@ -419,6 +426,8 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     }
     const dim3 blk(RZ_BX, RZ_BY, 1);
     const dim3 grd((g.N[2] + RZ_BX - 1) / RZ_BX, (g.N[1] + RZ_BY - 1) / RZ_BY, (g.N[0] + RZ_ZC - 1) / RZ_ZC);
+    const dim3 grd_box((a.hi[2] - a.lo[2] + RZ_BX - 1) / RZ_BX, (a.hi[1] - a.lo[1] + RZ_BY - 1) / RZ_BY,
+                       (a.hi[0] - a.lo[0] + RZ_ZC - 1) / RZ_ZC);
     const int order = d->tracer_order;
     const dim3 lblk(32, 4, 2);
     auto tracer_linear = [&](const T* q, T* dq, int qi) {
@@ -449,12 +458,12 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     if (linear_tr) terms &= ~TERM_TRACER;   // b's tendency comes from k_tracer_linear after the march
     const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
     const bool bdiff = tr && (terms & TERM_TRDIFF) && (d->tracer_diffusion & 1);
-    if (tr && vf && bdiff) k_rhs_march<T, true, true, true><<<grd, blk, 0, st>>>(a);
-    else if (tr && vf) k_rhs_march<T, true, true, false><<<grd, blk, 0, st>>>(a);
-    else if (tr && bdiff) k_rhs_march<T, true, false, true><<<grd, blk, 0, st>>>(a);
-    else if (tr) k_rhs_march<T, true, false, false><<<grd, blk, 0, st>>>(a);
-    else if (vf) k_rhs_march<T, false, true, false><<<grd, blk, 0, st>>>(a);
-    else k_rhs_march<T, false, false, false><<<grd, blk, 0, st>>>(a);
+    if (tr && vf && bdiff) k_rhs_march<T, true, true, true><<<grd_box, blk, 0, st>>>(a);
+    else if (tr && vf) k_rhs_march<T, true, true, false><<<grd_box, blk, 0, st>>>(a);
+    else if (tr && bdiff) k_rhs_march<T, true, false, true><<<grd_box, blk, 0, st>>>(a);
+    else if (tr) k_rhs_march<T, true, false, false><<<grd_box, blk, 0, st>>>(a);
+    else if (vf) k_rhs_march<T, false, true, false><<<grd_box, blk, 0, st>>>(a);
+    else k_rhs_march<T, false, false, false><<<grd_box, blk, 0, st>>>(a);
     note_launch();
     if (linear_tr) {
         tracer_linear(a.b, a.ds[0], 0);
@@ -1058,7 +1067,7 @@ int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream
 // ---------------------------------------------------------------- instantiations
 #define NYLES_INST(T)                                                                                          \
     template int launch_rhs<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, const ProgPtrs<T>&, int, \
-                               cudaStream_t);                                                                  \
+                               cudaStream_t, bool);                                                            \
     template int launch_update<T>(const Geom&, int, const ProgPtrs<T>&, const ProgPtrs<T>&, const ProgPtrs<T>&, \
                                   const ProgPtrs<T>&, int, double, cudaStream_t);                              \
     template int launch_fill<T>(const Geom&, T* const*, int, cudaStream_t);                                    \
