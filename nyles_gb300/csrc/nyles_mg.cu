@@ -24,7 +24,7 @@ namespace nyles {
 struct MgGeom {
     int n[3];          // interior extents z, y, x
     int per[3];
-    double idiag[8];   // 1/diag for diag = 0..6 (0 -> 0), computed once on the host
+    double idiag[8];   // omega/diag for diag = 0..6 (0 -> 0): the damped inverse diagonal, host-computed
     double pcoef[8];   // 1/(Wx*Wy*Wz) indexed by the three "neighbour is wet" bits
     float fidiag[8];   // the same tables rounded to float: single-precision kernels read
     float fpcoef[8];   // these instead of converting (FP64 conversions use the FP64 pipe)
@@ -109,7 +109,8 @@ __device__ __forceinline__ T mg_jacobi_cell(const MgGeom& g, const T* __restrict
                                             int y, int x, T cff1, T omega) {
     const long long c = mg_at(g, z, y, x);
     const T idg = mg_idiag<T>(g, mg_diag(g, z, y, x));
-    return cff1 * in[c] + omega * (mg_nsum(in, g, z, y, x) - b[c]) * idg;
+    (void)omega;
+    return cff1 * in[c] + (mg_nsum(in, g, z, y, x) - b[c]) * idg;
 }
 // sum of the residuals of the 8 children of coarse cell (z, y, x)
 template <typename T>
@@ -232,7 +233,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
         auto cell = [&](long long c, T zm, T x0, T zp, T idg) -> T {
             const T s = ((((mg_ldw(in, c + nx.om, nx.wm) + mg_ldw(in, c + nx.op, nx.wp)) +
                            mg_ldw(in, c + ny.om, ny.wm)) + mg_ldw(in, c + ny.op, ny.wp)) + zm) + zp;
-            return cff1 * x0 + omega * (s - b[c]) * idg;
+            return cff1 * x0 + (s - b[c]) * idg;
         };
         // dv: the cell's value of `dot` (MODE 2)
         auto put = [&](long long c, T v, T dv) {
@@ -281,7 +282,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // depends on the cell's own b alone, so the kernel that produces b writes it.
 template <typename T>
 __device__ __forceinline__ T mg_jacobi_from_zero(T b, T omega, T idg) {
-    return omega * (T(0) - b) * idg;
+    (void)omega;   // idg = omega/diag
+    return (T(0) - b) * idg;
 }
 
 // residual of the fine level restricted to the coarse right-hand side,
@@ -485,7 +487,7 @@ __device__ __forceinline__ void bottom_sweep(const MgGeom& g, const T* in, const
         const T idg = mg_idiag<T>(g, (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp + (int)nzb.wm + (int)nzb.wp);
         const T s = ((((sm_ldw(in, c + nx.om, nx.wm) + sm_ldw(in, c + nx.op, nx.wp)) + sm_ldw(in, c + ny.om, ny.wm)) +
                       sm_ldw(in, c + ny.op, ny.wp)) + sm_ldw(in, c + nzb.om, nzb.wm)) + sm_ldw(in, c + nzb.op, nzb.wp);
-        out[c] = cff1 * in[c] + om * (s - b[c]) * idg;
+        out[c] = cff1 * in[c] + (s - b[c]) * idg;
     });
     __syncthreads();
 }
@@ -682,7 +684,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_sweep(const MgGeom g
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
-    const T cff1 = T(1) - omega;
+    (void)omega;   // the tables hold omega/diag
     double s = 0.0;
     if (x < g.n[2] && y < g.n[1]) {
         const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
@@ -693,9 +695,10 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_sweep(const MgGeom g
             const T nsum = ((((mg_ldw(v, c + nx.om, nx.wm) + mg_ldw(v, c + nx.op, nx.wp)) + mg_ldw(v, c + ny.om, ny.wm)) +
                              mg_ldw(v, c + ny.op, ny.wp)) + zm) + zp;
             const T bv = b[c];
-            const double r = (double)((bv + T(dg) * x0) - nsum);
-            s += r * r;
-            y_out[c] = cff1 * x0 + omega * (nsum - bv) * mg_idiag<T>(g, dg);
+            const T r = (bv + T(dg) * x0) - nsum;
+            s += (double)r * (double)r;
+            // (1-omega)x + omega(nsum - b)/diag = x - (omega/diag) r
+            y_out[c] = x0 - mg_idiag<T>(g, dg) * r;
         };
         if (z0 + MG_ZC <= nz) {
             const MgNb lo = mg_nb(z0, nz, g.per[0], sz), hi = mg_nb(z0 + MG_ZC - 1, nz, g.per[0], sz);
@@ -1037,9 +1040,10 @@ static const dim3 kBlk(MG_BX, MG_BY, 1);
 static inline MgGeom mgg(const MgImpl* mg, int l) {
     MgGeom g;
     for (int k = 0; k < 3; ++k) { g.n[k] = mg->lev[l].n[k]; g.per[k] = mg->per[k]; }
-    // compute_diag (operators.f90:454-484): idiag = 1/diag where diag > 0
+    // compute_diag (operators.f90:454-484): idiag = 1/diag where diag > 0, times the
+    // smoother's damping omega (one multiplication less per cell and half-sweep)
     g.idiag[0] = 0.0;
-    for (int k = 1; k < 8; ++k) g.idiag[k] = 1.0 / (double)k;
+    for (int k = 1; k < 8; ++k) g.idiag[k] = mg->omega / (double)k;
     // compute_Pcoef (operators.f90:423-452): Pcoef = 1/(prolongation of the coarse mask)
     for (int bits = 0; bits < 8; ++bits) {
         const int W = (3 + (bits & 1)) * (3 + ((bits >> 1) & 1)) * (3 + ((bits >> 2) & 1));
