@@ -334,32 +334,36 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, 
     for (int q = 1; q < NP - 1; ++q) ld4(cb + (q - 1) * sz, true, v[q]);
     ld4(cb + (2 * MG_RZC - 1) * sz + zh.op, zh.wp, v[NP - 1]);
 #pragma unroll
+    // The 8 residuals b + diag*x - sum(x_nb) summed at once: each child's 6 neighbours
+    // are 3 siblings and 3 cells outside the 2 x 2 x 2 block, so the sum is
+    // sum(b) + sum(w_c x_c) - sum(24 outside cells) with w_c = diag_c - 3, the child's wet
+    // outside neighbours (dry ones are read as 0). Same value as the per-child sums up
+    // to rounding, with 2/3 of their FP64 instructions.
+    const T wxy[4] = {T(dxy[0] - 2), T(dxy[1] - 2), T(dxy[2] - 2), T(dxy[3] - 2)};
+#pragma unroll
     for (int zc = 0; zc < MG_RZC; ++zc) {
-        T s = T(0);
+        T sb = T(0), sx = T(0), so = T(0);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int q = 2 * zc + 1 + h;   // plane index in v
             const long long c = cb + (q - 1) * sz;
-            const int dz = (q == 1 ? (int)zl.wm : 1) + (q == NP - 2 ? (int)zh.wp : 1);
+            // the plane's z-neighbour outside the block: below for the lower plane, above
+            // for the upper one (dry at a closed wall)
+            const bool wz = (h == 0) ? (q == 1 ? zl.wm : true) : (q == NP - 2 ? zh.wp : true);
+            const T* zo = v[h == 0 ? q - 1 : q + 1];
             // x/y ring of the plane
             const T xm0 = mg_ldw(xf, c + xl.om, xl.wm), xm1 = mg_ldw(xf, c + sy + xl.om, xl.wm);
             const T xp0 = mg_ldw(xf, c + 1 + xh.op, xh.wp), xp1 = mg_ldw(xf, c + sy + 1 + xh.op, xh.wp);
             const T ym0 = mg_ldw(xf, c + yl.om, yl.wm), ym1 = mg_ldw(xf, c + 1 + yl.om, yl.wm);
             const T yp0 = mg_ldw(xf, c + sy + yh.op, yh.wp), yp1 = mg_ldw(xf, c + sy + 1 + yh.op, yh.wp);
             const T* p = v[q];
-            const T r00 = (bf[c] + T(dxy[0] + dz) * p[0]) - (((((xm0 + p[1]) + ym0) + p[2]) + v[q - 1][0]) + v[q + 1][0]);
-            const T r01 = (bf[c + 1] + T(dxy[1] + dz) * p[1]) -
-                          (((((p[0] + xp0) + ym1) + p[3]) + v[q - 1][1]) + v[q + 1][1]);
-            const T r10 = (bf[c + sy] + T(dxy[2] + dz) * p[2]) -
-                          (((((xm1 + p[3]) + p[0]) + yp0) + v[q - 1][2]) + v[q + 1][2]);
-            const T r11 = (bf[c + sy + 1] + T(dxy[3] + dz) * p[3]) -
-                          (((((p[2] + xp1) + p[1]) + yp1) + v[q - 1][3]) + v[q + 1][3]);
-            s = (h == 0) ? r00 : s + r00;
-            s = s + r01;
-            s = s + r10;
-            s = s + r11;
+            sb = sb + ((bf[c] + bf[c + 1]) + (bf[c + sy] + bf[c + sy + 1]));
+            const T pp = (p[0] + p[1]) + (p[2] + p[3]);
+            sx = sx + (wxy[0] * p[0] + wxy[1] * p[1] + wxy[2] * p[2] + wxy[3] * p[3]);
+            sx = wz ? sx + pp : sx;
+            so = so + ((((xm0 + xm1) + (xp0 + xp1)) + ((ym0 + ym1) + (yp0 + yp1))) + ((zo[0] + zo[1]) + (zo[2] + zo[3])));
         }
-        emit(z0 + zc, s);
+        emit(z0 + zc, (sb + sx) - so);
     }
 }
 
