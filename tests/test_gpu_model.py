@@ -121,6 +121,11 @@ MIXED_CASES = [
     dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30),
     dict(geometry="closed", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
          diff_coef={"u": 1e-3, "b": 2e-3, "t0": 1e-3}, tracer_diffusion=True),
+    # the linear tracer schemes in FP32 (k_tracer_linear<float>)
+    dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
+         tracer_scheme="linear", orderA=5),
+    dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
+         tracer_scheme="linear", orderA=3),
 ]
 
 
