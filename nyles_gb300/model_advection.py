@@ -14,8 +14,6 @@ calls ``Tracer_numerics`` without the `param` argument (TypeError), and
 (mgfor's multigrid, p = x*dx**2). ``update_stats`` records mean and standard deviation
 of b (the reference's version calls an undefined numpy name and keeps nothing).
 """
-import ctypes
-
 from . import _native as nat
 from .model_les import LES
 

@@ -12,7 +12,6 @@ reporting. Completion latency = time from arrival to the end of the run's last s
 
 The reference has no serving layer (one experiment per process, core/nyles.py).
 """
-import math
 import time
 from dataclasses import dataclass, field
 

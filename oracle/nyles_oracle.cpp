@@ -10,7 +10,11 @@
 // properties. The orchestration (views, halo fills, projection glue, time schemes)
 // is pinned against the reference's own Python modules, imported with this file's
 // kernels standing in for the f2py/ctypes libraries (tests/golden/make_golden.py).
-// Kernel-level parity is therefore "partially pinned".
+// Kernel-level parity is therefore "partially pinned". Two branches have no reference
+// output to pin against at all ("parity unpinned"): the linear tracer schemes
+// (upwind_linear, interpolate_tracer: the reference hard-codes WENO) and the advection
+// model (the reference's constructor cannot run); their restatements are checked by a
+// numpy restatement, convergence orders and conservation (tests/test_advection.py).
 //
 // Arithmetic follows the Fortran source operation by operation (association order,
 // REAL(4) literals and the implicitly REAL(4) `tau5` of weno5). Compile with

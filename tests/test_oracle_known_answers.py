@@ -120,7 +120,6 @@ def test_multigrid_hierarchy_sizes():
 
 def test_compute_dt_cases():
     """core/nyles.py:306-321: dt = cfl/|U| (or dt_max when U = 0)."""
-    from helpers import make_params  # noqa
     o = oracle.OracleModel(dict(nx=8, ny=8, nz=8, geometry="closed", dx=1.0, dy=1.0, dz=1.0,
                                 idx2=1.0, idy2=1.0, idz2=1.0))
     cfl, dt_max = 0.8, 1.5
