@@ -126,6 +126,9 @@ struct MgImpl {
     // search direction and its image under the operator, level-1 floats
     int krylov = 0;
     size_t off_fp = 0, off_fq = 0;
+    // 4-cell vector kernels where the level-1 extents allow (off with the environment
+    // variable NYLES_GB300_SCALAR_KERNELS=1, read when the solver is created)
+    bool vec4 = true;
     size_t off_partial = 0, off_partial2 = 0, off_scalars = 0;
     int npartial = 0;
     size_t bytes = 0;

@@ -16,6 +16,7 @@
 // neighbours all lie inside the level takes a fast path with direct strided loads;
 // only blocks touching the level's faces go through the ghost logic.
 #include "nyles_internal.h"
+#include <cstdlib>
 #include <vector>
 #include <cstring>
 
@@ -926,6 +927,97 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g,
     block_partial2((double)spq, (double)spr, ppq, ppr);
 }
 
+// The same with 4 consecutive x cells per thread (16-byte loads and stores: the kernel
+// is bound by the latency of its loads) and z-chunks of V4_ZC cells; needs nx and nz
+// divisible by 4 and V4_ZC. The x neighbours of a vector come from the adjacent lanes
+// of the warp (one warp = one row segment of 128 cells), and are loaded at the warp's
+// ends and at the level's x faces (periodic image or dry). Same per-cell arithmetic as
+// k_fcg_direction.
+constexpr int V4_ZC = 4;
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction_v4(const MgGeom g, const float* __restrict__ z,
+                                                                    const float* __restrict__ r, float* __restrict__ p,
+                                                                    float* __restrict__ q,
+                                                                    const double* __restrict__ sc,
+                                                                    double* __restrict__ ppq, double* __restrict__ ppr) {
+    const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
+    const int nx4 = nx >> 2;
+    const int lane = threadIdx.x;
+    const int xv = blockIdx.x * MG_BX + lane;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const float beta = reinterpret_cast<const float*>(sc + SC_BETA)[0];
+    const float zmean = reinterpret_cast<const float*>(sc + SC_ZMEAN)[0];
+    float spq = 0.f, spr = 0.f;
+    // idle lanes shadow the last vector of the row so that every lane takes part in the
+    // shuffles; only active lanes store and sum
+    const bool act = xv < nx4 && y < ny;
+    const int x0 = min(xv, nx4 - 1) * 4, ys = min(y, ny - 1);
+    const long long sy = nx, sz = (long long)ny * nx;
+    const MgNb nyb = mg_nb(ys, ny, g.per[1], sy);
+    // cells x0-1 and x0+4: offsets from cell x0 and wet flags
+    const bool wl = x0 > 0 || g.per[2], wr = x0 + 4 < nx || g.per[2];
+    const long long ol = x0 > 0 ? -1 : (g.per[2] ? (long long)(nx - 1) : 0);
+    const long long orr = x0 + 4 < nx ? 4 : (g.per[2] ? (long long)(4 - nx) : 0);
+    const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
+    // wet x neighbours of the four cells
+    int dgx[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int xx = x0 + e;
+        dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
+    }
+    const int zb = blockIdx.z * V4_ZC;
+    const long long c00 = (long long)ys * sy + x0;
+    auto ld4 = [&](long long c) { return *reinterpret_cast<const float4*>(z + c); };
+    auto zrow = [&](int zz) -> float4 {   // z value of the vector at level row zz (periodic image or dry)
+        const MgNb nzb = mg_nb(zz < 0 ? 0 : (zz >= nz ? nz - 1 : zz), nz, g.per[0], sz);
+        if (zz < 0) return nzb.wm ? ld4(c00 + (long long)(nz - 1) * sz) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (zz >= nz) return nzb.wp ? ld4(c00) : make_float4(0.f, 0.f, 0.f, 0.f);
+        return ld4(c00 + (long long)zz * sz);
+    };
+    float4 zm = zrow(zb - 1), zc = zrow(zb);
+#pragma unroll
+    for (int k = 0; k < V4_ZC; ++k) {
+        const int zz = zb + k;
+        const float4 zp = zrow(zz + 1);
+        const long long c = c00 + (long long)zz * sz;
+        const float4 ym = nyb.wm ? ld4(c + nyb.om) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 yp = nyb.wp ? ld4(c + nyb.op) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pv0 = *reinterpret_cast<const float4*>(p + c);
+        const float4 qv0 = *reinterpret_cast<const float4*>(q + c);
+        const float4 rv = *reinterpret_cast<const float4*>(r + c);
+        const float sl = __shfl_up_sync(0xffffffffu, zc.w, 1);
+        const float sr = __shfl_down_sync(0xffffffffu, zc.x, 1);
+        const float left = ownl ? mg_ldw(z, c + ol, wl) : sl;
+        const float right = ownr ? mg_ldw(z, c + orr, wr) : sr;
+        const int dzw = (int)(zz > 0 || g.per[0]) + (int)(zz < nz - 1 || g.per[0]);
+        const float zv[4] = {zc.x, zc.y, zc.z, zc.w};
+        const float xm[4] = {left, zc.x, zc.y, zc.z}, xp[4] = {zc.y, zc.z, zc.w, right};
+        const float yv[2][4] = {{ym.x, ym.y, ym.z, ym.w}, {yp.x, yp.y, yp.z, yp.w}};
+        const float zmv[4] = {zm.x, zm.y, zm.z, zm.w}, zpv[4] = {zp.x, zp.y, zp.z, zp.w};
+        const float p0[4] = {pv0.x, pv0.y, pv0.z, pv0.w}, q0[4] = {qv0.x, qv0.y, qv0.z, qv0.w};
+        const float rr[4] = {rv.x, rv.y, rv.z, rv.w};
+        float po[4], qo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float s = ((((xm[e] + xp[e]) + yv[0][e]) + yv[1][e]) + zmv[e]) + zpv[e];
+            const float az = __fmaf_rn(-(float)(dgx[e] + dzw), zv[e], s);
+            po[e] = __fmaf_rn(beta, p0[e], __fsub_rn(zv[e], zmean));
+            qo[e] = __fmaf_rn(beta, q0[e], az);
+            if (act) {
+                spq = __fmaf_rn(po[e], qo[e], spq);
+                spr = __fmaf_rn(po[e], rr[e], spr);
+            }
+        }
+        if (act) {
+            *reinterpret_cast<float4*>(p + c) = make_float4(po[0], po[1], po[2], po[3]);
+            *reinterpret_cast<float4*>(q + c) = make_float4(qo[0], qo[1], qo[2], qo[3]);
+        }
+        zm = zc;
+        zc = zp;
+    }
+    block_partial2((double)spq, (double)spr, ppq, ppr);
+}
+
 // sums of p.q and p.r, then alpha = (p.r)/(p.q) stored as a float pair
 __global__ void k_fcg_final_alpha(const double* __restrict__ ppq, const double* __restrict__ ppr, int n,
                                   double* __restrict__ sc) {
@@ -1149,6 +1241,10 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
     // one partial per block of the largest reduction grid (the float-pair residual's)
     const dim3 g0 = grid_zc(mg->lev[0].n, MG_DFZC < MG_ZC ? MG_DFZC : MG_ZC);
     mg->npartial = (int)(g0.x * g0.y * g0.z);
+    {
+        const char* e = getenv("NYLES_GB300_SCALAR_KERNELS");
+        mg->vec4 = !(e && e[0] == '1');
+    }
     mg->off_partial = take(mg->npartial * sizeof(double));
     mg->off_partial2 = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
@@ -1324,8 +1420,15 @@ static void enqueue_fcg_update(MgImpl* mg, cudaStream_t st, int k) {
     note_launch(4);
     // the partial sums of z.q and z were written by the V-cycle's last level-0 half-sweep
     k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, nb, (double)n, sc, k);
-    k_fcg_direction<<<grd, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
-    k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, nb, sc);
+    if (mg->vec4 && g.n[2] % 4 == 0 && g.n[0] % V4_ZC == 0) {
+        const dim3 gv((unsigned)((g.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((g.n[1] + MG_BY - 1) / MG_BY),
+                      (unsigned)(g.n[0] / V4_ZC));
+        k_fcg_direction_v4<<<gv, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
+        k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, (int)(gv.x * gv.y * gv.z), sc);
+    } else {
+        k_fcg_direction<<<grd, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
+        k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, nb, sc);
+    }
     k_fcg_xupdate<<<eb, 256, 0, st>>>(reinterpret_cast<float2*>(mg->ws + mg->off_pdf), P, n, sc);
 }
 

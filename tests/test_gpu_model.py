@@ -293,3 +293,38 @@ def test_mixed_krylov_graph_matches_eager():
     for s in runs[False][0]:
         np.testing.assert_array_equal(runs[True][0][s], runs[False][0][s])
     assert runs[True][1] == runs[False][1]
+
+
+def test_vector_kernels_match_scalar_kernels(tmp_path):
+    """The 4-cell vector kernels of the Krylov solve against the scalar ones (the same
+    per-cell arithmetic; block sums grouped differently): iteration counts within one and
+    the same solution to rounding, on every topology, in a fresh process each."""
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, sys\n"
+        "from nyles_gb300.multigrid import MG\n"
+        "out = []\n"
+        "for topo in ('closed', 'perio_x', 'perio_y', 'perio_xy', 'perio_xyz'):\n"
+        "    nx, ny, nz = (64, 32, 32) if topo != 'perio_xyz' else (32, 32, 32)\n"
+        "    rng = np.random.Generator(np.random.PCG64(31))\n"
+        "    b = rng.standard_normal((nz, ny, nx)); b -= b.mean()\n"
+        "    mg = MG(nx, ny, nz, topo, precision='mixed'); mg.set_params(1e-20, 80, 0.9); mg.set_krylov(True)\n"
+        "    x, st = mg.solve(b)\n"
+        "    x = x.double().cpu().numpy(); x -= x.mean()\n"
+        "    out.append((st['nite'], x))\n"
+        "np.savez(sys.argv[1], *[o[1] for o in out])\n"
+        "print(' '.join(str(o[0]) for o in out))\n")
+    root = os.path.dirname(helpers.HERE)
+    res = {}
+    for scalar in ("0", "1"):
+        env = dict(os.environ, NYLES_GB300_SCALAR_KERNELS=scalar, PYTHONPATH=root)
+        fn = str(tmp_path / ("vec_%s.npz" % scalar))
+        r = subprocess.run([sys.executable, "-c", code, fn], env=env, capture_output=True, text=True, cwd=root)
+        assert r.returncode == 0, r.stderr[-2000:]
+        with np.load(fn) as f:
+            res[scalar] = ([int(v) for v in r.stdout.split()], [f["arr_%d" % i] for i in range(len(f.files))])
+    assert all(abs(a - c) <= 1 for a, c in zip(res["0"][0], res["1"][0])), (res["0"][0], res["1"][0])
+    for a, c in zip(res["0"][1], res["1"][1]):
+        assert helpers.relerr(a, c) < 1e-6
