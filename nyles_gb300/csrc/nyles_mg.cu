@@ -279,6 +279,98 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
     if (MODE == 2) block_partial2((double)sdot, (double)ssum, partial, partial2);
 }
 
+// k_mg_jacobi for float levels with 4 consecutive x cells per thread (16-byte accesses;
+// the x neighbours of a vector from the adjacent lanes, loaded at the warp's ends and at
+// the level's x faces) and z-chunks of V4_ZC cells; needs nx and nz divisible by 4 and
+// V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
+constexpr int V4_ZC = 4;
+template <int MODE>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
+                                                               const float* __restrict__ b, float* __restrict__ out,
+                                                               float omega, float2* __restrict__ acc,
+                                                               const float* __restrict__ dot,
+                                                               double* __restrict__ partial,
+                                                               double* __restrict__ partial2) {
+    const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
+    const int nx4 = nx >> 2;
+    const int lane = threadIdx.x;
+    const int xv = blockIdx.x * MG_BX + lane;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    float sdot = 0.f, ssum = 0.f;
+    // idle lanes shadow the last vector of the row (every lane takes part in the
+    // shuffles); only active lanes store and sum
+    const bool act = xv < nx4 && y < ny;
+    const int x0 = min(xv, nx4 - 1) * 4, ys = min(y, ny - 1);
+    const long long sy = nx, sz = (long long)ny * nx;
+    const MgNb nyb = mg_nb(ys, ny, g.per[1], sy);
+    const bool wl = x0 > 0 || g.per[2], wr = x0 + 4 < nx || g.per[2];
+    const long long ol = x0 > 0 ? -1 : (g.per[2] ? (long long)(nx - 1) : 0);
+    const long long orr = x0 + 4 < nx ? 4 : (g.per[2] ? (long long)(4 - nx) : 0);
+    const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
+    int dgx[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int xx = x0 + e;
+        dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
+    }
+    const float cff1 = 1.f - omega;
+    const int zb = blockIdx.z * V4_ZC;
+    const long long c00 = (long long)ys * sy + x0;
+    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto zrow = [&](int zz) -> float4 {
+        if (zz < 0) return g.per[0] ? ld4(in, c00 + (long long)(nz - 1) * sz) : zero4;
+        if (zz >= nz) return g.per[0] ? ld4(in, c00) : zero4;
+        return ld4(in, c00 + (long long)zz * sz);
+    };
+    float4 zm = zrow(zb - 1), zc = zrow(zb);
+#pragma unroll
+    for (int k = 0; k < V4_ZC; ++k) {
+        const int zz = zb + k;
+        const float4 zp = zrow(zz + 1);
+        const long long c = c00 + (long long)zz * sz;
+        const float4 ym = nyb.wm ? ld4(in, c + nyb.om) : zero4;
+        const float4 yp = nyb.wp ? ld4(in, c + nyb.op) : zero4;
+        const float4 bv = ld4(b, c);
+        const float4 dv = (MODE == 2) ? ld4(dot, c) : zero4;
+        const float sl = __shfl_up_sync(0xffffffffu, zc.w, 1);
+        const float sr = __shfl_down_sync(0xffffffffu, zc.x, 1);
+        const float left = ownl ? mg_ldw(in, c + ol, wl) : sl;
+        const float right = ownr ? mg_ldw(in, c + orr, wr) : sr;
+        const int dzw = (int)(zz > 0 || g.per[0]) + (int)(zz < nz - 1 || g.per[0]);
+        const float xc[4] = {zc.x, zc.y, zc.z, zc.w};
+        const float xm[4] = {left, zc.x, zc.y, zc.z}, xp[4] = {zc.y, zc.z, zc.w, right};
+        const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
+        const float zmv[4] = {zm.x, zm.y, zm.z, zm.w}, zpv[4] = {zp.x, zp.y, zp.z, zp.w};
+        const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, dd[4] = {dv.x, dv.y, dv.z, dv.w};
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float s = ((((xm[e] + xp[e]) + ymv[e]) + ypv[e]) + zmv[e]) + zpv[e];
+            v[e] = cff1 * xc[e] + (s - bb[e]) * mg_idiag<float>(g, dgx[e] + dzw);
+            if (MODE == 2 && act) {
+                sdot = __fmaf_rn(v[e], dd[e], sdot);
+                ssum = __fadd_rn(ssum, v[e]);
+            }
+        }
+        if (act) {
+            if (MODE == 1) {
+                float4* a4 = reinterpret_cast<float4*>(acc + c);
+                float4 a01 = a4[0], a23 = a4[1];
+                float2 r0 = df_add_f(make_float2(a01.x, a01.y), v[0]), r1 = df_add_f(make_float2(a01.z, a01.w), v[1]);
+                float2 r2 = df_add_f(make_float2(a23.x, a23.y), v[2]), r3 = df_add_f(make_float2(a23.z, a23.w), v[3]);
+                a4[0] = make_float4(r0.x, r0.y, r1.x, r1.y);
+                a4[1] = make_float4(r2.x, r2.y, r3.x, r3.y);
+            } else {
+                *reinterpret_cast<float4*>(out + c) = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        zm = zc;
+        zc = zp;
+    }
+    if (MODE == 2) block_partial2((double)sdot, (double)ssum, partial, partial2);
+}
+
 // First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
 // depends on the cell's own b alone, so the kernel that produces b writes it.
 template <typename T>
@@ -933,7 +1025,6 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g,
 // of the warp (one warp = one row segment of 128 cells), and are loaded at the warp's
 // ends and at the level's x faces (periodic image or dry). Same per-cell arithmetic as
 // k_fcg_direction.
-constexpr int V4_ZC = 4;
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction_v4(const MgGeom g, const float* __restrict__ z,
                                                                     const float* __restrict__ r, float* __restrict__ p,
                                                                     float* __restrict__ q,
@@ -1133,6 +1224,13 @@ static inline dim3 grid_zc(const int n[3], int zc) {
 }
 static const dim3 kBlk(MG_BX, MG_BY, 1);
 
+// the 4-cell vector kernels apply to a level whose x and z extents allow them
+static inline bool use_v4(const MgImpl* mg, const int n[3]) { return mg->vec4 && n[2] % 4 == 0 && n[0] % V4_ZC == 0; }
+static inline dim3 grid_v4(const int n[3]) {
+    return dim3((unsigned)((n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((n[1] + MG_BY - 1) / MG_BY),
+                (unsigned)(n[0] / V4_ZC));
+}
+
 static inline MgGeom mgg(const MgImpl* mg, int l) {
     MgGeom g;
     for (int k = 0; k < 3; ++k) { g.n[k] = mg->lev[l].n[k]; g.per[k] = mg->per[k]; }
@@ -1267,6 +1365,23 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
     const T om = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch(from_y ? 1 : 2);
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (use_v4(mg, g.n)) {
+            const dim3 gv = grid_v4(g.n);
+            if (!from_y) k_mg_jacobi_v4<0><<<gv, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
+            if (last_mode == 1)
+                k_mg_jacobi_v4<1><<<gv, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf),
+                                                      nullptr, nullptr, nullptr);
+            else if (last_mode == 2)
+                k_mg_jacobi_v4<2><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr,
+                                                      reinterpret_cast<const float*>(mg->ws + mg->off_fq),
+                                                      reinterpret_cast<double*>(mg->ws + mg->off_partial),
+                                                      reinterpret_cast<double*>(mg->ws + mg->off_partial2));
+            else
+                k_mg_jacobi_v4<0><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr);
+            return;
+        }
+    }
     if (!from_y) k_mg_jacobi<T, 0><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
     if (last_mode == 1)
         k_mg_jacobi<T, 1><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf),
@@ -1419,10 +1534,10 @@ static void enqueue_fcg_update(MgImpl* mg, cudaStream_t st, int k) {
     ProfScope ps(mg->prof, 11, st);
     note_launch(4);
     // the partial sums of z.q and z were written by the V-cycle's last level-0 half-sweep
-    k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, nb, (double)n, sc, k);
-    if (mg->vec4 && g.n[2] % 4 == 0 && g.n[0] % V4_ZC == 0) {
-        const dim3 gv((unsigned)((g.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((g.n[1] + MG_BY - 1) / MG_BY),
-                      (unsigned)(g.n[0] / V4_ZC));
+    const dim3 gj = use_v4(mg, g.n) ? grid_v4(g.n) : grd;   // grid of the level-0 half-sweep that summed z.q
+    k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, (int)(gj.x * gj.y * gj.z), (double)n, sc, k);
+    if (use_v4(mg, g.n)) {
+        const dim3 gv = grid_v4(g.n);
         k_fcg_direction_v4<<<gv, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
         k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, (int)(gv.x * gv.y * gv.z), sc);
     } else {
