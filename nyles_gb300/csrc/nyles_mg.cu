@@ -910,6 +910,97 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
     block_partial((double)s * sc[SC_INVSCALE2], partial);
 }
 
+// k_mg_resid_df with 4 consecutive x cells per thread: each float-pair row segment is
+// two 16-byte loads, the x neighbours come from the adjacent lanes (loaded at the warp's
+// ends and at the level's x faces), r32 and y32 are stored 16 bytes at a time. Needs nx
+// and nz divisible by 4 and V4_ZC; same per-cell arithmetic as k_mg_resid_df.
+struct DfVec4 {
+    float2 v[4];
+};
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df_v4(const MgGeom g, const float2* __restrict__ p,
+                                                                    const float2* __restrict__ b,
+                                                                    float* __restrict__ r32, float* __restrict__ y32,
+                                                                    float omega, const double* __restrict__ sc,
+                                                                    double* __restrict__ partial) {
+    const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
+    const int nx4 = nx >> 2;
+    const int lane = threadIdx.x;
+    const int xv = blockIdx.x * MG_BX + lane;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const float scale = (float)sc[SC_SCALE];
+    float s = 0.f;
+    const bool act = xv < nx4 && y < ny;
+    const int x0 = min(xv, nx4 - 1) * 4, ys = min(y, ny - 1);
+    const long long sy = nx, sz = (long long)ny * nx;
+    const MgNb nyb = mg_nb(ys, ny, g.per[1], sy);
+    const bool wl = x0 > 0 || g.per[2], wr = x0 + 4 < nx || g.per[2];
+    const long long ol = x0 > 0 ? -1 : (g.per[2] ? (long long)(nx - 1) : 0);
+    const long long orr = x0 + 4 < nx ? 4 : (g.per[2] ? (long long)(4 - nx) : 0);
+    const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
+    int dgx[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int xx = x0 + e;
+        dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
+    }
+    const int zb = blockIdx.z * V4_ZC;
+    const long long c00 = (long long)ys * sy + x0;
+    auto ld = [&](const float2* a, long long c) -> DfVec4 {
+        const float4* q = reinterpret_cast<const float4*>(a + c);
+        const float4 u = q[0], w = q[1];
+        DfVec4 d;
+        d.v[0] = make_float2(u.x, u.y);
+        d.v[1] = make_float2(u.z, u.w);
+        d.v[2] = make_float2(w.x, w.y);
+        d.v[3] = make_float2(w.z, w.w);
+        return d;
+    };
+    DfVec4 zero;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) zero.v[e] = make_float2(0.f, 0.f);
+    auto zrow = [&](int zz) -> DfVec4 {
+        if (zz < 0) return g.per[0] ? ld(p, c00 + (long long)(nz - 1) * sz) : zero;
+        if (zz >= nz) return g.per[0] ? ld(p, c00) : zero;
+        return ld(p, c00 + (long long)zz * sz);
+    };
+    DfVec4 zm = zrow(zb - 1), zc = zrow(zb);
+#pragma unroll
+    for (int k = 0; k < V4_ZC; ++k) {
+        const int zz = zb + k;
+        const DfVec4 zp = zrow(zz + 1);
+        const long long c = c00 + (long long)zz * sz;
+        const DfVec4 ym = nyb.wm ? ld(p, c + nyb.om) : zero;
+        const DfVec4 yp = nyb.wp ? ld(p, c + nyb.op) : zero;
+        const DfVec4 bv = ld(b, c);
+        const float lx = __shfl_up_sync(0xffffffffu, zc.v[3].x, 1), ly = __shfl_up_sync(0xffffffffu, zc.v[3].y, 1);
+        const float rx = __shfl_down_sync(0xffffffffu, zc.v[0].x, 1), ry = __shfl_down_sync(0xffffffffu, zc.v[0].y, 1);
+        const float2 left = ownl ? mg_ldw_df(p, c + ol, wl) : make_float2(lx, ly);
+        const float2 right = ownr ? mg_ldw_df(p, c + orr, wr) : make_float2(rx, ry);
+        const int dzw = (int)(zz > 0 || g.per[0]) + (int)(zz < nz - 1 || g.per[0]);
+        float rv[4], yv[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int dg = dgx[e] + dzw;
+            const float2 nb[6] = {e == 0 ? left : zc.v[e - 1], e == 3 ? right : zc.v[e + 1], ym.v[e], yp.v[e],
+                                  zm.v[e], zp.v[e]};
+            const float r = df_resid(bv.v[e], zc.v[e], (float)dg, nb);
+            rv[e] = r;
+            yv[e] = mg_jacobi_from_zero(r, omega, mg_idiag<float>(g, dg));
+            if (act) {
+                const float rs = __fmul_rn(r, scale);
+                s = __fmaf_rn(rs, rs, s);
+            }
+        }
+        if (act) {
+            *reinterpret_cast<float4*>(r32 + c) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+            *reinterpret_cast<float4*>(y32 + c) = make_float4(yv[0], yv[1], yv[2], yv[3]);
+        }
+        zm = zc;
+        zc = zp;
+    }
+    block_partial((double)s * sc[SC_INVSCALE2], partial);
+}
+
 // ---------------------------------------------------------------- Krylov acceleration
 // Mixed precision with mg_krylov: flexible conjugate gradients FCG(1) on the level-0
 // equation, preconditioned by the FP32 V-cycle (zero initial guess), with the float-pair
@@ -1491,12 +1582,18 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     MgGeom g = mgg(mg, 0);
     double* part = reinterpret_cast<double*>(mg->ws + mg->off_partial);
     double* sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
-    const dim3 grd = grid_zc(g.n, MG_DFZC);
+    const bool v4 = use_v4(mg, g.n);
+    const dim3 grd = v4 ? grid_v4(g.n) : grid_zc(g.n, MG_DFZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(2);
-    k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
-                                        reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
-                                        lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
+    if (v4)
+        k_mg_resid_df_v4<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
+                                               reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
+                                               lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
+    else
+        k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
+                                            reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
+                                            lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
     k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
 }
 
