@@ -205,8 +205,13 @@ struct TracerMarch {
 // TR: buoyancy advection on; VF: vortex force on; BDIFF: buoyancy diffusion on (a
 // template flag so that the default instances carry none of its registers). ds[0..3]
 // are written.
+// blocks per SM asked of the register allocator: FP32 issue-bound march (more warps
+// hide its load latency), FP64 bound by the FP64 pipe
+template <typename T> struct RhsMinBlocks { static constexpr int n = 5; };
+template <> struct RhsMinBlocks<double> { static constexpr int n = 4; };
+
 template <typename T, bool TR, bool VF, bool BDIFF>
-__global__ void __launch_bounds__(RZ_BX * RZ_BY) k_rhs_march(const RhsArgs<T> a) {
+__global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march(const RhsArgs<T> a) {
     __shared__ T sfy[RZ_BY][RZ_BX];
     const Geom& g = a.g;
     const int x = a.lo[2] + blockIdx.x * RZ_BX + threadIdx.x;
