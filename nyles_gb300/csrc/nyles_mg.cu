@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
 template <int MODE>
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
+__global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
                                                                const float* __restrict__ b, float* __restrict__ out,
                                                                float omega, float2* __restrict__ acc,
                                                                const float* __restrict__ dot,
@@ -917,7 +917,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
 struct DfVec4 {
     float2 v[4];
 };
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df_v4(const MgGeom g, const float2* __restrict__ p,
+__global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeom g, const float2* __restrict__ p,
                                                                     const float2* __restrict__ b,
                                                                     float* __restrict__ r32, float* __restrict__ y32,
                                                                     float omega, const double* __restrict__ sc,
@@ -1116,7 +1116,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g,
 // of the warp (one warp = one row segment of 128 cells), and are loaded at the warp's
 // ends and at the level's x faces (periodic image or dry). Same per-cell arithmetic as
 // k_fcg_direction.
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction_v4(const MgGeom g, const float* __restrict__ z,
+__global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_fcg_direction_v4(const MgGeom g, const float* __restrict__ z,
                                                                     const float* __restrict__ r, float* __restrict__ p,
                                                                     float* __restrict__ q,
                                                                     const double* __restrict__ sc,
