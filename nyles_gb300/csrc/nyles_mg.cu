@@ -513,6 +513,191 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
     }
 }
 
+// Vector forms of the two transfers (FP32): a thread owns 4 consecutive fine x cells,
+// i.e. 2 coarse x cells, so that fine rows move as 16-byte and coarse pairs as 8-byte
+// accesses; x neighbours come from the adjacent lanes (loaded at the warp's ends and at
+// the level's x faces). Idle lanes shadow the last vector of their row so that every
+// lane takes part in the shuffles; only active lanes store. Both need the fine level
+// twice the coarse one in every direction and fine nx divisible by 4, and keep the
+// per-cell arithmetic of the full-chunk paths above.
+
+// k_mg_restrict: one coarse row pair of cells per thread, MG_RZC coarse planes (needs
+// coarse nz divisible by MG_RZC)
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom gf, const float* __restrict__ xf,
+                                                                 const float* __restrict__ bf, const MgGeom gc,
+                                                                 float* __restrict__ bc, float* __restrict__ yc,
+                                                                 float omega) {
+    const int nx = gf.n[2], ny = gf.n[1], nz = gf.n[0];
+    const int nx4 = nx >> 2;
+    const int lane = threadIdx.x;
+    const int xv = blockIdx.x * MG_BX + lane;
+    const int jc = blockIdx.y * MG_BY + threadIdx.y;   // coarse row
+    const bool act = xv < nx4 && jc < gc.n[1];
+    const int x0 = min(xv, nx4 - 1) * 4, j0 = 2 * min(jc, gc.n[1] - 1);
+    const long long sy = nx, sz = (long long)ny * nx;
+    const MgNb yl = mg_nb(j0, ny, gf.per[1], sy), yh = mg_nb(j0 + 1, ny, gf.per[1], sy);
+    const bool wl = x0 > 0 || gf.per[2], wr = x0 + 4 < nx || gf.per[2];
+    const long long ol = x0 > 0 ? -1 : (gf.per[2] ? (long long)(nx - 1) : 0);
+    const long long orr = x0 + 4 < nx ? 4 : (gf.per[2] ? (long long)(4 - nx) : 0);
+    const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
+    // w_c = wet outside x/y neighbours of each child (j0,i), (j0,i+1), (j0+1,i), (j0+1,i+1)
+    // of the coarse cells m = 0 (fine x0, x0+1) and m = 1 (x0+2, x0+3)
+    const int ylw = (int)yl.wm, yhw = (int)yh.wp;
+    const float wxy[2][4] = {{(float)((int)wl + ylw), (float)(1 + ylw), (float)((int)wl + yhw), (float)(1 + yhw)},
+                             {(float)(1 + ylw), (float)((int)wr + ylw), (float)(1 + yhw), (float)((int)wr + yhw)}};
+    const int zcb = blockIdx.z * MG_RZC, k0 = 2 * zcb;
+    const long long c00 = (long long)j0 * sy + x0;
+    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    struct Rows { float4 r0, r1; };
+    // rows j0 and j0 + 1 of fine plane k, one plane outside the level at most: periodic
+    // image, or 0 across a closed wall
+    auto plane = [&](int k) -> Rows {
+        Rows R;
+        if ((k < 0 || k >= nz) && !gf.per[0]) {
+            R.r0 = zero4;
+            R.r1 = zero4;
+            return R;
+        }
+        const int kk = k < 0 ? k + nz : (k >= nz ? k - nz : k);
+        const long long c = c00 + (long long)kk * sz;
+        R.r0 = ld4(xf, c);
+        R.r1 = ld4(xf, c + sy);
+        return R;
+    };
+    Rows below = plane(k0 - 1), cur = plane(k0);
+#pragma unroll
+    for (int zc = 0; zc < MG_RZC; ++zc) {
+        const int kz = k0 + 2 * zc;
+        const Rows up = plane(kz + 1), nxt = plane(kz + 2);
+        float sbv[2] = {0.f, 0.f}, sxv[2] = {0.f, 0.f}, sov[2] = {0.f, 0.f};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int kf = kz + h;
+            const Rows& P = h == 0 ? cur : up;
+            const Rows& O = h == 0 ? below : nxt;   // the plane's z-neighbour outside the block
+            const bool wz = h == 0 ? (kf > 0 || gf.per[0]) : (kf < nz - 1 || gf.per[0]);
+            const long long c = c00 + (long long)kf * sz;
+            const float4 ym = yl.wm ? ld4(xf, c + yl.om) : zero4;
+            const float4 yp = yh.wp ? ld4(xf, c + sy + yh.op) : zero4;
+            const float4 b0 = ld4(bf, c), b1 = ld4(bf, c + sy);
+            const float sl0 = __shfl_up_sync(0xffffffffu, P.r0.w, 1), sl1 = __shfl_up_sync(0xffffffffu, P.r1.w, 1);
+            const float sr0 = __shfl_down_sync(0xffffffffu, P.r0.x, 1), sr1 = __shfl_down_sync(0xffffffffu, P.r1.x, 1);
+            const float l0 = ownl ? mg_ldw(xf, c + ol, wl) : sl0, l1 = ownl ? mg_ldw(xf, c + sy + ol, wl) : sl1;
+            const float r0 = ownr ? mg_ldw(xf, c + orr, wr) : sr0, r1 = ownr ? mg_ldw(xf, c + sy + orr, wr) : sr1;
+            const float x0v[4] = {P.r0.x, P.r0.y, P.r0.z, P.r0.w}, x1v[4] = {P.r1.x, P.r1.y, P.r1.z, P.r1.w};
+            const float o0[4] = {O.r0.x, O.r0.y, O.r0.z, O.r0.w}, o1[4] = {O.r1.x, O.r1.y, O.r1.z, O.r1.w};
+            const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
+            const float b0v[4] = {b0.x, b0.y, b0.z, b0.w}, b1v[4] = {b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const int i = 2 * m;
+                const float p[4] = {x0v[i], x0v[i + 1], x1v[i], x1v[i + 1]};
+                const float xm0 = m == 0 ? l0 : x0v[1], xm1 = m == 0 ? l1 : x1v[1];
+                const float xp0 = m == 0 ? x0v[2] : r0, xp1 = m == 0 ? x1v[2] : r1;
+                sbv[m] = sbv[m] + ((b0v[i] + b0v[i + 1]) + (b1v[i] + b1v[i + 1]));
+                const float pp = (p[0] + p[1]) + (p[2] + p[3]);
+                sxv[m] = sxv[m] + (wxy[m][0] * p[0] + wxy[m][1] * p[1] + wxy[m][2] * p[2] + wxy[m][3] * p[3]);
+                sxv[m] = wz ? sxv[m] + pp : sxv[m];
+                sov[m] = sov[m] + ((((xm0 + xm1) + (xp0 + xp1)) + ((ymv[i] + ymv[i + 1]) + (ypv[i] + ypv[i + 1]))) +
+                                   ((o0[i] + o0[i + 1]) + (o1[i] + o1[i + 1])));
+            }
+        }
+        if (act) {
+            const int z = zcb + zc, xc0 = x0 >> 1;
+            const long long cc = mg_at(gc, z, jc, xc0);
+            float bv[2], yv[2];
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                bv[m] = 0.5f * ((sbv[m] + sxv[m]) - sov[m]);
+                yv[m] = mg_jacobi_from_zero(bv[m], omega, mg_idiag<float>(gc, mg_diag(gc, z, jc, xc0 + m)));
+            }
+            *reinterpret_cast<float2*>(bc + cc) = make_float2(bv[0], bv[1]);
+            *reinterpret_cast<float2*>(yc + cc) = make_float2(yv[0], yv[1]);
+        }
+        below = up;
+        cur = nxt;
+    }
+}
+
+// k_mg_prolong: one 4-cell fine row segment per thread, V4_ZC fine planes (needs fine
+// nz divisible by V4_ZC)
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf, float* __restrict__ xf,
+                                                                const MgGeom gc, const float* __restrict__ xc) {
+    const int nx = gf.n[2], ny = gf.n[1];
+    const int nx4 = nx >> 2;
+    const int lane = threadIdx.x;
+    const int xv = blockIdx.x * MG_BX + lane;
+    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const bool act = xv < nx4 && y < ny;
+    const int x0 = min(xv, nx4 - 1) * 4, ys = min(y, ny - 1);
+    const int ncx = gc.n[2], ic0 = x0 >> 1, jc = ys >> 1;
+    const long long csy = ncx, csz = (long long)gc.n[1] * ncx;
+    const MgNb cy = mg_nb(jc, gc.n[1], gc.per[1], csy);
+    const long long oy = (ys & 1) ? cy.op : cy.om;
+    const bool wy = (ys & 1) ? cy.wp : cy.wm;
+    // coarse x neighbours of the pair ic0, ic0 + 1: ic0 - 1 (fine x0) and ic0 + 2 (x0 + 3)
+    const bool cwl = ic0 > 0 || gc.per[2], cwr = ic0 + 2 < ncx || gc.per[2];
+    const long long col = ic0 > 0 ? -1 : (gc.per[2] ? (long long)(ncx - 1) : 0);
+    const long long cor = ic0 + 2 < ncx ? 2 : (gc.per[2] ? (long long)(2 - ncx) : 0);
+    const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
+    const int zb = blockIdx.z * V4_ZC, kc0 = zb >> 1;
+    const MgNb zl = mg_nb(kc0, gc.n[0], gc.per[0], csz), zh = mg_nb(kc0 + V4_ZC / 2 - 1, gc.n[0], gc.per[0], csz);
+    const long long cc = mg_at(gc, kc0, jc, ic0);
+    // in-plane 9-3-3-1 sums of the 4 fine cells from one coarse plane at c (0 when the
+    // plane is dry): fine x0 + e takes coarse ic0 + (e >> 1) and its x neighbour on the
+    // side of the fine cell
+    auto plane = [&](long long c, bool wet, float* out) {
+        const float2 a = wet ? *reinterpret_cast<const float2*>(xc + c) : make_float2(0.f, 0.f);
+        const float2 d = (wet && wy) ? *reinterpret_cast<const float2*>(xc + c + oy) : make_float2(0.f, 0.f);
+        const float sal = __shfl_up_sync(0xffffffffu, a.y, 1), sar = __shfl_down_sync(0xffffffffu, a.x, 1);
+        const float sdl = __shfl_up_sync(0xffffffffu, d.y, 1), sdr = __shfl_down_sync(0xffffffffu, d.x, 1);
+        const float al = ownl ? mg_ldw(xc, c + col, wet && cwl) : sal;
+        const float ar = ownr ? mg_ldw(xc, c + cor, wet && cwr) : sar;
+        const float dl = ownl ? mg_ldw(xc, c + oy + col, wet && cwl && wy) : sdl;
+        const float dr = ownr ? mg_ldw(xc, c + oy + cor, wet && cwr && wy) : sdr;
+        const float av[4] = {a.x, a.x, a.y, a.y}, bv[4] = {al, a.y, a.x, ar};
+        const float dv[4] = {d.x, d.x, d.y, d.y}, ev[4] = {dl, d.y, d.x, dr};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) out[e] = ((9.f * av[e] + 3.f * bv[e]) + 3.f * dv[e]) + ev[e];
+    };
+    const long long sz = (long long)ny * nx, c0 = (long long)zb * sz + (long long)ys * nx + x0;
+    float4 xv4[V4_ZC];   // the fine values, loaded together with the coarse ones
+#pragma unroll
+    for (int k = 0; k < V4_ZC; ++k) xv4[k] = *reinterpret_cast<const float4*>(xf + c0 + k * sz);
+    constexpr int NP = V4_ZC / 2 + 2;
+    float P[NP][4];
+    plane(cc + zl.om, zl.wm, P[0]);
+#pragma unroll
+    for (int q = 1; q < NP - 1; ++q) plane(cc + (q - 1) * csz, true, P[q]);
+    plane(cc + (V4_ZC / 2 - 1) * csz + zh.op, zh.wp, P[NP - 1]);
+    // 1/(Wx*Wy*Wz) of each fine cell: its coarse x neighbour is wet except beyond the
+    // level's x faces (cells x0 and x0 + 3)
+    float pc_wet[4], pc_lo[4], pc_hi[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const bool wx = e == 0 ? cwl : (e == 3 ? cwr : true);
+        const int bxy = (int)wx | ((int)wy << 1);
+        pc_wet[e] = mg_pcoef<float>(gf, bxy | 4);
+        pc_lo[e] = mg_pcoef<float>(gf, bxy | ((int)zl.wm << 2));
+        pc_hi[e] = mg_pcoef<float>(gf, bxy | ((int)zh.wp << 2));
+    }
+#pragma unroll
+    for (int k = 0; k < V4_ZC; ++k) {
+        const int m = (k >> 1) + 1;   // plane of z >> 1 in P
+        const float* bpl = P[m];
+        const float* opl = P[(k & 1) ? m + 1 : m - 1];
+        const float xo[4] = {xv4[k].x, xv4[k].y, xv4[k].z, xv4[k].w};
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float pc = (k == 0) ? pc_lo[e] : (k == V4_ZC - 1 ? pc_hi[e] : pc_wet[e]);
+            v[e] = xo[e] + pc * (3.f * bpl[e] + opl[e]);
+        }
+        if (act) *reinterpret_cast<float4*>(xf + c0 + k * sz) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
 // ---------------------------------------------------------------- coarse levels in one block
 // Levels l0..L-1 of a V-cycle (solvers.f90:35-55 from level l0 down and back up) run in
 // one thread block: the level arrays live in shared memory, and each half-sweep,
@@ -1321,6 +1506,20 @@ static inline dim3 grid_v4(const int n[3]) {
     return dim3((unsigned)((n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((n[1] + MG_BY - 1) / MG_BY),
                 (unsigned)(n[0] / V4_ZC));
 }
+// the vector transfers between levels l and l + 1: exact halving in every direction,
+// fine nx divisible by 4, and the z chunk of each kernel dividing its extent
+static inline bool v4_restrict(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc) {
+    if (!mg->vec4 || gf.n[2] % 4 != 0 || gc.n[0] % MG_RZC != 0) return false;
+    for (int k = 0; k < 3; ++k)
+        if (gf.n[k] != 2 * gc.n[k]) return false;
+    return true;
+}
+static inline bool v4_prolong(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc) {
+    if (!mg->vec4 || gf.n[2] % 4 != 0 || gf.n[0] % V4_ZC != 0) return false;
+    for (int k = 0; k < 3; ++k)
+        if (gf.n[k] != 2 * gc.n[k]) return false;
+    return true;
+}
 
 static inline MgGeom mgg(const MgImpl* mg, int l) {
     MgGeom g;
@@ -1522,9 +1721,21 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 9, st);
             note_launch();
-            k_mg_restrict<T><<<grid_zc(gc.n, MG_RZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
-                                                                    lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 3),
-                                                                    T(mg->omega));
+            bool done = false;
+            if constexpr (sizeof(T) == sizeof(float)) {
+                if (v4_restrict(mg, gf, gc)) {
+                    const dim3 gv((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
+                                  (unsigned)(gc.n[0] / MG_RZC));
+                    k_mg_restrict_v4<<<gv, kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
+                                                          lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3),
+                                                          (float)mg->omega);
+                    done = true;
+                }
+            }
+            if (!done)
+                k_mg_restrict<T><<<grid_zc(gc.n, MG_RZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
+                                                                        lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 3),
+                                                                        T(mg->omega));
         }
     }
     if (B < L)
@@ -1536,7 +1747,15 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 10, st);
             note_launch();
-            k_mg_prolong<T><<<grid_zc(gf.n, MG_ZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
+            bool done = false;
+            if constexpr (sizeof(T) == sizeof(float)) {
+                if (v4_prolong(mg, gf, gc)) {
+                    k_mg_prolong_v4<<<grid_v4(gf.n), kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), gc, lvp<float>(mg, l + 1, 1));
+                    done = true;
+                }
+            }
+            if (!done)
+                k_mg_prolong<T><<<grid_zc(gf.n, MG_ZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
         }
         smooth<T>(mg, l, st, l == 0 ? level0_last : 0);
     }

@@ -298,7 +298,9 @@ def test_mixed_krylov_graph_matches_eager():
 def test_vector_kernels_match_scalar_kernels(tmp_path):
     """The 4-cell vector kernels of the Krylov solve against the scalar ones (the same
     per-cell arithmetic; block sums grouped differently): iteration counts within one and
-    the same solution to rounding, on every topology, in a fresh process each."""
+    the same solution to rounding, on every topology, in a fresh process each; and the
+    iterate after a single stationary V-cycle (smoothing, restriction and prolongation on
+    every level), which a wrong transfer would change well above rounding."""
     import os
     import subprocess
     import sys
@@ -313,8 +315,11 @@ def test_vector_kernels_match_scalar_kernels(tmp_path):
         "    mg = MG(nx, ny, nz, topo, precision='mixed'); mg.set_params(1e-20, 80, 0.9); mg.set_krylov(True)\n"
         "    x, st = mg.solve(b)\n"
         "    x = x.double().cpu().numpy(); x -= x.mean()\n"
-        "    out.append((st['nite'], x))\n"
-        "np.savez(sys.argv[1], *[o[1] for o in out])\n"
+        "    mg1 = MG(nx, ny, nz, topo, precision='mixed'); mg1.set_params(1e-20, 1, 0.9); mg1.set_krylov(False)\n"
+        "    x1, st1 = mg1.solve(b)\n"
+        "    assert st1['nite'] == 1\n"
+        "    out.append((st['nite'], x, x1.double().cpu().numpy()))\n"
+        "np.savez(sys.argv[1], *[a for o in out for a in o[1:]])\n"
         "print(' '.join(str(o[0]) for o in out))\n")
     root = os.path.dirname(helpers.HERE)
     res = {}
@@ -326,5 +331,5 @@ def test_vector_kernels_match_scalar_kernels(tmp_path):
         with np.load(fn) as f:
             res[scalar] = ([int(v) for v in r.stdout.split()], [f["arr_%d" % i] for i in range(len(f.files))])
     assert all(abs(a - c) <= 1 for a, c in zip(res["0"][0], res["1"][0])), (res["0"][0], res["1"][0])
-    for a, c in zip(res["0"][1], res["1"][1]):
-        assert helpers.relerr(a, c) < 1e-6
+    for k, (a, c) in enumerate(zip(res["0"][1], res["1"][1])):
+        assert helpers.relerr(a, c) < (1e-6 if k % 2 == 0 else 1e-5), k
