@@ -208,6 +208,45 @@ __device__ __forceinline__ void block_partial2(double s, double t, double* __res
     }
 }
 
+// FP32 forms of block_partial and block_partial2 for kernels whose per-thread sums are
+// FP32: the warp and block stages add in float and only the block total is stored as a
+// double (times `scale`). On GB300 the FP64 pipe is narrow: the double shuffles, adds
+// and conversions of a 256-thread reduction took a visible share of a level-0 pass.
+__device__ __forceinline__ void block_partial_f(float s, double scale, double* __restrict__ partial) {
+    __shared__ float smf[MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
+    s = warp_sum(s);
+    if ((tid & 31) == 0) smf[tid >> 5] = s;
+    __syncthreads();
+    if (tid < 32) {
+        float t = (tid < MG_BX * MG_BY / 32) ? smf[tid] : 0.f;
+        t = warp_sum(t);
+        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = (double)t * scale;
+    }
+}
+__device__ __forceinline__ void block_partial2_f(float s, float t, double* __restrict__ ps, double* __restrict__ pt) {
+    __shared__ float smf[2][MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
+    s = warp_sum(s);
+    t = warp_sum(t);
+    if ((tid & 31) == 0) {
+        smf[0][tid >> 5] = s;
+        smf[1][tid >> 5] = t;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        float a = (tid < MG_BX * MG_BY / 32) ? smf[0][tid] : 0.f;
+        float b = (tid < MG_BX * MG_BY / 32) ? smf[1][tid] : 0.f;
+        a = warp_sum(a);
+        b = warp_sum(b);
+        if (tid == 0) {
+            const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            ps[blk] = (double)a;
+            pt[blk] = (double)b;
+        }
+    }
+}
+
 // one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
 // (basicoperators.f90:379-398). MODE 0 stores it; MODE 1 adds it to the float-pair
 // solution `acc` instead (mixed precision: the correction of iterative refinement,
@@ -276,7 +315,12 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
             }
         }
     }
-    if (MODE == 2) block_partial2((double)sdot, (double)ssum, partial, partial2);
+    if constexpr (MODE == 2) {
+        if constexpr (sizeof(T) == sizeof(float))
+            block_partial2_f(sdot, ssum, partial, partial2);
+        else
+            block_partial2((double)sdot, (double)ssum, partial, partial2);
+    }
 }
 
 // k_mg_jacobi for float levels with 4 consecutive x cells per thread (16-byte accesses;
@@ -368,7 +412,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         zm = zc;
         zc = zp;
     }
-    if (MODE == 2) block_partial2((double)sdot, (double)ssum, partial, partial2);
+    if (MODE == 2) block_partial2_f(sdot, ssum, partial, partial2);
 }
 
 // First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
@@ -1092,7 +1136,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
             }
         }
     }
-    block_partial((double)s * sc[SC_INVSCALE2], partial);
+    block_partial_f(s, sc[SC_INVSCALE2], partial);
 }
 
 // k_mg_resid_df with 4 consecutive x cells per thread: each float-pair row segment is
@@ -1183,7 +1227,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
         zm = zc;
         zc = zp;
     }
-    block_partial((double)s * sc[SC_INVSCALE2], partial);
+    block_partial_f(s, sc[SC_INVSCALE2], partial);
 }
 
 // ---------------------------------------------------------------- Krylov acceleration
@@ -1292,7 +1336,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g,
             }
         }
     }
-    block_partial2((double)spq, (double)spr, ppq, ppr);
+    block_partial2_f(spq, spr, ppq, ppr);
 }
 
 // The same with 4 consecutive x cells per thread (16-byte loads and stores: the kernel
@@ -1382,7 +1426,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_fcg_direction_v4(const MgG
         zm = zc;
         zc = zp;
     }
-    block_partial2((double)spq, (double)spr, ppq, ppr);
+    block_partial2_f(spq, spr, ppq, ppr);
 }
 
 // sums of p.q and p.r, then alpha = (p.r)/(p.q) stored as a float pair
