@@ -690,28 +690,42 @@ __global__ void __launch_bounds__(256) k_div(const Geom g, const T* __restrict__
 // mixed precision: the same divergence of the FP32 velocity carried as a float pair
 // (products by the metric factor and differences are exact to ~2^-48), written to the
 // multigrid right-hand side as (hi, lo); the model's div field gets hi + lo rounded.
-__global__ void __launch_bounds__(256) k_div_df(const Geom g, const float* __restrict__ ux,
-                                                const float* __restrict__ uy, const float* __restrict__ uz,
-                                                float2 idx2, float2 idy2, float2 idz2, float* __restrict__ div,
-                                                float2* __restrict__ mgb) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
-    const int zz = g.wrap(0, z), yy = g.wrap(1, y), xx = g.wrap(2, x);
-    const long long c = g.at(zz, yy, xx);
-    float2 acc = df_mul_f(ux[c], idx2);
-    if (xx != 0) acc = df_add(acc, df_neg(df_mul_f(ux[c - 1], idx2)));
-    float2 t = df_mul_f(uy[c], idy2);
-    if (yy != 0) t = df_add(t, df_neg(df_mul_f(uy[c - g.sy], idy2)));
-    acc = df_add(acc, t);
-    t = df_mul_f(uz[c], idz2);
-    if (zz != 0) t = df_add(t, df_neg(df_mul_f(uz[c - g.sz], idz2)));
-    acc = df_add(acc, t);
-    div[g.at(z, y, x)] = df_value(acc);
-    if (zz == z && yy == y && xx == x) {
-        const int iz = zz - (g.per[0] ? g.nh : 0), iy = yy - (g.per[1] ? g.nh : 0), ix = xx - (g.per[2] ? g.nh : 0);
-        mgb[((long long)iz * g.n[1] + iy) * g.n[2] + ix] = acc;
+// One thread per (y, x) column of the array and PJ_ZC cells in z: the column's wrapped
+// position and interior offset are computed once.
+constexpr int PJ_BX = 32, PJ_BY = 8, PJ_ZC = 8;
+static inline dim3 grid_pj(const Geom& g) {
+    return dim3((unsigned)((g.N[2] + PJ_BX - 1) / PJ_BX), (unsigned)((g.N[1] + PJ_BY - 1) / PJ_BY),
+                (unsigned)((g.N[0] + PJ_ZC - 1) / PJ_ZC));
+}
+
+__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const float* __restrict__ ux,
+                                                          const float* __restrict__ uy, const float* __restrict__ uz,
+                                                          float2 idx2, float2 idy2, float2 idz2,
+                                                          float* __restrict__ div, float2* __restrict__ mgb) {
+    const int x = blockIdx.x * PJ_BX + threadIdx.x;
+    const int y = blockIdx.y * PJ_BY + threadIdx.y;
+    if (x >= g.N[2] || y >= g.N[1]) return;
+    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const bool own_xy = yy == y && xx == x;
+    const long long cxy = (long long)yy * g.sy + xx;
+    const long long ixy = (long long)(yy - (g.per[1] ? g.nh : 0)) * g.n[2] + (xx - (g.per[2] ? g.nh : 0));
+    for (int z = z0; z < z1; ++z) {
+        const int zz = g.wrap(0, z);
+        const long long c = (long long)zz * g.sz + cxy;
+        float2 acc = df_mul_f(ux[c], idx2);
+        if (xx != 0) acc = df_add(acc, df_neg(df_mul_f(ux[c - 1], idx2)));
+        float2 t = df_mul_f(uy[c], idy2);
+        if (yy != 0) t = df_add(t, df_neg(df_mul_f(uy[c - g.sy], idy2)));
+        acc = df_add(acc, t);
+        t = df_mul_f(uz[c], idz2);
+        if (zz != 0) t = df_add(t, df_neg(df_mul_f(uz[c - g.sz], idz2)));
+        acc = df_add(acc, t);
+        div[g.at(z, y, x)] = df_value(acc);
+        if (own_xy && zz == z) {
+            const int iz = zz - (g.per[0] ? g.nh : 0);
+            mgb[(long long)iz * g.n[1] * g.n[2] + ixy] = acc;
+        }
     }
 }
 
@@ -725,8 +739,7 @@ int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* m
 }
 
 int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st) {
-    dim3 blk(32, 4, 2);
-    k_div_df<<<grid3(g, blk), blk, 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
+    k_div_df<<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
                                              df_split(d->idx2), df_split(d->idy2), df_split(d->idz2),
                                              s.f[NYLES_F_DIV], mg_b);
     note_launch();
@@ -797,30 +810,37 @@ struct CorrDfArgs {
     float2 dx2;
 };
 
-__device__ __forceinline__ float2 pres_df(const CorrDfArgs& a, int z, int y, int x) {
+// one thread per (y, x) column of the array, PJ_ZC cells in z (as k_div_df)
+__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a) {
     const Geom& g = a.g;
-    z = g.wrap(0, z); y = g.wrap(1, y); x = g.wrap(2, x);
-    const int iz = z - (g.per[0] ? g.nh : 0), iy = y - (g.per[1] ? g.nh : 0), ix = x - (g.per[2] ? g.nh : 0);
-    return a.x[((long long)iz * g.n[1] + iy) * g.n[2] + ix];
-}
-
-__global__ void __launch_bounds__(256) k_correct_df(const CorrDfArgs a) {
-    const Geom& g = a.g;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
-    const long long c = g.at(z, y, x);
-    const float2 p0 = pres_df(a, z, y, x);
-    a.p[c] = df_value(df_mul(p0, a.dx2));
-    if (g.wrap(0, z) != z || g.wrap(1, y) != y || g.wrap(2, x) != x) return;   // halo: filled later
-    const float2 np0 = df_neg(p0);
-    if (x < g.N[2] - 1)
-        a.u[0][c] = __fsub_rn(a.u[0][c], df_value(df_mul(df_add(pres_df(a, z, y, x + 1), np0), a.dx2)));
-    if (y < g.N[1] - 1)
-        a.u[1][c] = __fsub_rn(a.u[1][c], df_value(df_mul(df_add(pres_df(a, z, y + 1, x), np0), a.dx2)));
-    if (z < g.N[0] - 1)
-        a.u[2][c] = __fsub_rn(a.u[2][c], df_value(df_mul(df_add(pres_df(a, z + 1, y, x), np0), a.dx2)));
+    const int x = blockIdx.x * PJ_BX + threadIdx.x;
+    const int y = blockIdx.y * PJ_BY + threadIdx.y;
+    if (x >= g.N[2] || y >= g.N[1]) return;
+    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int oz = g.per[0] ? g.nh : 0, oy = g.per[1] ? g.nh : 0, ox = g.per[2] ? g.nh : 0;
+    const int yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const bool own_xy = yy == y && xx == x;
+    const long long n2 = g.n[2], sxy = (long long)g.n[1] * n2;
+    // interior index of the column's image and of its x + 1 and y + 1 neighbours' images
+    const long long ixy = (long long)(yy - oy) * n2 + (xx - ox);
+    const bool hx = x < g.N[2] - 1, hy = y < g.N[1] - 1;
+    const long long ixy_x = hx ? (long long)(yy - oy) * n2 + (g.wrap(2, x + 1) - ox) : ixy;
+    const long long ixy_y = hy ? (long long)(g.wrap(1, y + 1) - oy) * n2 + (xx - ox) : ixy;
+    for (int z = z0; z < z1; ++z) {
+        const long long c = g.at(z, y, x);
+        const int zz = g.wrap(0, z);
+        const long long iz = (long long)(zz - oz) * sxy;
+        const float2 p0 = a.x[iz + ixy];
+        a.p[c] = df_value(df_mul(p0, a.dx2));
+        if (!own_xy || zz != z) continue;   // halo: filled later
+        const float2 np0 = df_neg(p0);
+        if (hx) a.u[0][c] = __fsub_rn(a.u[0][c], df_value(df_mul(df_add(a.x[iz + ixy_x], np0), a.dx2)));
+        if (hy) a.u[1][c] = __fsub_rn(a.u[1][c], df_value(df_mul(df_add(a.x[iz + ixy_y], np0), a.dx2)));
+        if (z < g.N[0] - 1) {
+            const long long iz1 = (long long)(g.wrap(0, z + 1) - oz) * sxy;
+            a.u[2][c] = __fsub_rn(a.u[2][c], df_value(df_mul(df_add(a.x[iz1 + ixy], np0), a.dx2)));
+        }
+    }
 }
 
 int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st) {
@@ -830,8 +850,7 @@ int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* 
     a.x = mg_x;
     a.p = s.f[NYLES_F_P];
     a.dx2 = df_split(dx2);
-    dim3 blk(32, 4, 2);
-    k_correct_df<<<grid3(g, blk), blk, 0, st>>>(a);
+    k_correct_df<<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(a);
     note_launch();
     return cuda_status(cudaGetLastError(), "correct kernel");
 }
