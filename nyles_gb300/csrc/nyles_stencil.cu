@@ -657,46 +657,55 @@ int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st) {
 // core/projection.py:16-29 (fortran_bernoulli.f90:61-97) on U = u*ids2
 // (core/cov_to_contra.py:16-18), evaluated at the periodic image of each cell because
 // core/mgfordriver.py:70 fills the halo of div before the solve.
+// The divergence and the projection correction run one thread per (y, x) column of the
+// array and PJ_ZC cells in z: the column's wrapped position and interior offset are
+// computed once.
+constexpr int PJ_BX = 32, PJ_BY = 8, PJ_ZC = 8;
+static inline dim3 grid_pj(const Geom& g) {
+    return dim3((unsigned)((g.N[2] + PJ_BX - 1) / PJ_BX), (unsigned)((g.N[1] + PJ_BY - 1) / PJ_BY),
+                (unsigned)((g.N[0] + PJ_ZC - 1) / PJ_ZC));
+}
+
 template <typename T, typename TB>
-__global__ void __launch_bounds__(256) k_div(const Geom g, const T* __restrict__ ux, const T* __restrict__ uy,
-                                             const T* __restrict__ uz, TB idx2, TB idy2, TB idz2,
-                                             T* __restrict__ div, TB* __restrict__ mgb) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
-    const int zz = g.wrap(0, z), yy = g.wrap(1, y), xx = g.wrap(2, x);
-    const long long c = g.at(zz, yy, xx);
-    TB acc;
-    {
-        TB U0 = mul_rn(TB(ux[c]), idx2);
-        acc = (xx == 0) ? U0 : sub_rn(U0, mul_rn(TB(ux[c - 1]), idx2));
-    }
-    {
-        TB V0 = mul_rn(TB(uy[c]), idy2);
-        acc = (yy == 0) ? add_rn(acc, V0) : add_rn(acc, sub_rn(V0, mul_rn(TB(uy[c - g.sy]), idy2)));
-    }
-    {
-        TB W0 = mul_rn(TB(uz[c]), idz2);
-        acc = (zz == 0) ? add_rn(acc, W0) : add_rn(acc, sub_rn(W0, mul_rn(TB(uz[c - g.sz]), idz2)));
-    }
-    div[g.at(z, y, x)] = T(acc);
-    if (zz == z && yy == y && xx == x) {
-        const int iz = zz - (g.per[0] ? g.nh : 0), iy = yy - (g.per[1] ? g.nh : 0), ix = xx - (g.per[2] ? g.nh : 0);
-        mgb[((long long)iz * g.n[1] + iy) * g.n[2] + ix] = acc;
+__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div(const Geom g, const T* __restrict__ ux, const T* __restrict__ uy,
+                                                       const T* __restrict__ uz, TB idx2, TB idy2, TB idz2,
+                                                       T* __restrict__ div, TB* __restrict__ mgb) {
+    const int x = blockIdx.x * PJ_BX + threadIdx.x;
+    const int y = blockIdx.y * PJ_BY + threadIdx.y;
+    if (x >= g.N[2] || y >= g.N[1]) return;
+    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const bool own_xy = yy == y && xx == x;
+    const long long cxy = (long long)yy * g.sy + xx;
+    const long long ixy = (long long)(yy - (g.per[1] ? g.nh : 0)) * g.n[2] + (xx - (g.per[2] ? g.nh : 0));
+    for (int z = z0; z < z1; ++z) {
+        const int zz = g.wrap(0, z);
+        const long long c = (long long)zz * g.sz + cxy;
+        TB acc;
+        {
+            TB U0 = mul_rn(TB(ux[c]), idx2);
+            acc = (xx == 0) ? U0 : sub_rn(U0, mul_rn(TB(ux[c - 1]), idx2));
+        }
+        {
+            TB V0 = mul_rn(TB(uy[c]), idy2);
+            acc = (yy == 0) ? add_rn(acc, V0) : add_rn(acc, sub_rn(V0, mul_rn(TB(uy[c - g.sy]), idy2)));
+        }
+        {
+            TB W0 = mul_rn(TB(uz[c]), idz2);
+            acc = (zz == 0) ? add_rn(acc, W0) : add_rn(acc, sub_rn(W0, mul_rn(TB(uz[c - g.sz]), idz2)));
+        }
+        div[g.at(z, y, x)] = T(acc);
+        if (own_xy && zz == z) {
+            const int iz = zz - (g.per[0] ? g.nh : 0);
+            mgb[(long long)iz * g.n[1] * g.n[2] + ixy] = acc;
+        }
     }
 }
 
 // mixed precision: the same divergence of the FP32 velocity carried as a float pair
 // (products by the metric factor and differences are exact to ~2^-48), written to the
 // multigrid right-hand side as (hi, lo); the model's div field gets hi + lo rounded.
-// One thread per (y, x) column of the array and PJ_ZC cells in z: the column's wrapped
-// position and interior offset are computed once.
-constexpr int PJ_BX = 32, PJ_BY = 8, PJ_ZC = 8;
-static inline dim3 grid_pj(const Geom& g) {
-    return dim3((unsigned)((g.N[2] + PJ_BX - 1) / PJ_BX), (unsigned)((g.N[1] + PJ_BY - 1) / PJ_BY),
-                (unsigned)((g.N[0] + PJ_ZC - 1) / PJ_ZC));
-}
+// One column per thread, as k_div.
 
 __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const float* __restrict__ ux,
                                                           const float* __restrict__ uy, const float* __restrict__ uz,
@@ -731,8 +740,7 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const fl
 
 template <typename T, typename TB>
 int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* mg_b, cudaStream_t st) {
-    dim3 blk(32, 4, 2);
-    k_div<T, TB><<<grid3(g, blk), blk, 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
+    k_div<T, TB><<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
                                                  TB(d->idx2), TB(d->idy2), TB(d->idz2), s.f[NYLES_F_DIV], mg_b);
     note_launch();
     return cuda_status(cudaGetLastError(), "div kernel");
@@ -761,27 +769,36 @@ struct CorrArgs {
 };
 
 template <typename T, typename TP>
-__device__ __forceinline__ TP pres(const CorrArgs<T, TP>& a, int z, int y, int x) {
+__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct(const CorrArgs<T, TP> a) {
     const Geom& g = a.g;
-    z = g.wrap(0, z); y = g.wrap(1, y); x = g.wrap(2, x);
-    const int iz = z - (g.per[0] ? g.nh : 0), iy = y - (g.per[1] ? g.nh : 0), ix = x - (g.per[2] ? g.nh : 0);
-    return mul_rn(a.x[((long long)iz * g.n[1] + iy) * g.n[2] + ix], TP(a.dx2));
-}
-
-template <typename T, typename TP>
-__global__ void __launch_bounds__(256) k_correct(const CorrArgs<T, TP> a) {
-    const Geom& g = a.g;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z * blockDim.z + threadIdx.z;
-    if (x >= g.N[2] || y >= g.N[1] || z >= g.N[0]) return;
-    const long long c = g.at(z, y, x);
-    const TP p0 = pres(a, z, y, x);
-    a.p[c] = T(p0);
-    if (g.wrap(0, z) != z || g.wrap(1, y) != y || g.wrap(2, x) != x) return;   // halo: filled later
-    if (x < g.N[2] - 1) a.u[0][c] = T(sub_rn(TP(a.u[0][c]), sub_rn(pres(a, z, y, x + 1), p0)));
-    if (y < g.N[1] - 1) a.u[1][c] = T(sub_rn(TP(a.u[1][c]), sub_rn(pres(a, z, y + 1, x), p0)));
-    if (z < g.N[0] - 1) a.u[2][c] = T(sub_rn(TP(a.u[2][c]), sub_rn(pres(a, z + 1, y, x), p0)));
+    const int x = blockIdx.x * PJ_BX + threadIdx.x;
+    const int y = blockIdx.y * PJ_BY + threadIdx.y;
+    if (x >= g.N[2] || y >= g.N[1]) return;
+    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int oz = g.per[0] ? g.nh : 0, oy = g.per[1] ? g.nh : 0, ox = g.per[2] ? g.nh : 0;
+    const int yy = g.wrap(1, y), xx = g.wrap(2, x);
+    const bool own_xy = yy == y && xx == x;
+    const long long n2 = g.n[2], sxy = (long long)g.n[1] * n2;
+    // interior index of the column's image and of its x + 1 and y + 1 neighbours' images
+    const long long ixy = (long long)(yy - oy) * n2 + (xx - ox);
+    const bool hx = x < g.N[2] - 1, hy = y < g.N[1] - 1;
+    const long long ixy_x = hx ? (long long)(yy - oy) * n2 + (g.wrap(2, x + 1) - ox) : ixy;
+    const long long ixy_y = hy ? (long long)(g.wrap(1, y + 1) - oy) * n2 + (xx - ox) : ixy;
+    const TP dx2 = TP(a.dx2);
+    for (int z = z0; z < z1; ++z) {
+        const long long c = g.at(z, y, x);
+        const int zz = g.wrap(0, z);
+        const long long iz = (long long)(zz - oz) * sxy;
+        const TP p0 = mul_rn(a.x[iz + ixy], dx2);
+        a.p[c] = T(p0);
+        if (!own_xy || zz != z) continue;   // halo: filled later
+        if (hx) a.u[0][c] = T(sub_rn(TP(a.u[0][c]), sub_rn(mul_rn(a.x[iz + ixy_x], dx2), p0)));
+        if (hy) a.u[1][c] = T(sub_rn(TP(a.u[1][c]), sub_rn(mul_rn(a.x[iz + ixy_y], dx2), p0)));
+        if (z < g.N[0] - 1) {
+            const long long iz1 = (long long)(g.wrap(0, z + 1) - oz) * sxy;
+            a.u[2][c] = T(sub_rn(TP(a.u[2][c]), sub_rn(mul_rn(a.x[iz1 + ixy], dx2), p0)));
+        }
+    }
 }
 
 template <typename T, typename TP>
@@ -794,8 +811,7 @@ int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, c
     a.x = mg_x;
     a.p = s.f[NYLES_F_P];
     a.dx2 = dx2;
-    dim3 blk(32, 4, 2);
-    k_correct<T, TP><<<grid3(g, blk), blk, 0, st>>>(a);
+    k_correct<T, TP><<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(a);
     note_launch();
     return cuda_status(cudaGetLastError(), "correct kernel");
 }
