@@ -18,8 +18,8 @@ copy bandwidth; `roofline` = the dominant kernel alone.
 n in {32, 48, 64, 96, 128}, arriving as a seeded Poisson stream at 20 per second,
 mixed precision, served by continuous batching under a 120 GB HBM budget; p50/p99
 completion latency and aggregate cell-steps/s, against the same runs one at a time
-with the eager FP64 path. Each run lasts --serving-steps steps (30 by default, so that
-the default bench stays within a few minutes).
+with the eager FP64 path (each run's duration from the measured setup and step times
+of its case and grid). Each run lasts --serving-steps steps (300 by default).
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--n 256]
 """
