@@ -295,41 +295,52 @@ def test_mixed_krylov_graph_matches_eager():
     assert runs[True][1] == runs[False][1]
 
 
+_SOLVES_CODE = (
+    "import numpy as np, sys\n"
+    "from nyles_gb300.multigrid import MG\n"
+    "out = []\n"
+    "for topo in ('closed', 'perio_x', 'perio_y', 'perio_xy', 'perio_xyz'):\n"
+    "    nx, ny, nz = (64, 32, 32) if topo != 'perio_xyz' else (32, 32, 32)\n"
+    "    rng = np.random.Generator(np.random.PCG64(31))\n"
+    "    b = rng.standard_normal((nz, ny, nx)); b -= b.mean()\n"
+    "    mg = MG(nx, ny, nz, topo, precision='mixed'); mg.set_params(1e-20, 80, 0.9); mg.set_krylov(True)\n"
+    "    x, st = mg.solve(b)\n"
+    "    x = x.double().cpu().numpy(); x -= x.mean()\n"
+    "    mg1 = MG(nx, ny, nz, topo, precision='mixed'); mg1.set_params(1e-20, 1, 0.9); mg1.set_krylov(False)\n"
+    "    x1, st1 = mg1.solve(b)\n"
+    "    assert st1['nite'] == 1\n"
+    "    out.append((st['nite'], x, x1.double().cpu().numpy()))\n"
+    "np.savez(sys.argv[1], *[a for o in out for a in o[1:]])\n"
+    "print(' '.join(str(o[0]) for o in out))\n")
+
+
+def _mixed_solves(tmp_path, tag, **env_extra):
+    """FCG solves and single stationary V-cycles of a seeded right-hand side on every
+    topology, in a fresh process with the given environment (the kernel switches are
+    read when a solver is created): (iteration counts, [solution, one-cycle iterate] *
+    topologies)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(helpers.HERE)
+    env = dict(os.environ, PYTHONPATH=root, **env_extra)
+    fn = str(tmp_path / ("solves_%s.npz" % tag))
+    r = subprocess.run([sys.executable, "-c", _SOLVES_CODE, fn], env=env, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    with np.load(fn) as f:
+        return [int(v) for v in r.stdout.split()], [f["arr_%d" % i] for i in range(len(f.files))]
+
+
 def test_vector_kernels_match_scalar_kernels(tmp_path):
     """The 4-cell vector kernels of the Krylov solve against the scalar ones (the same
     per-cell arithmetic; block sums grouped differently): iteration counts within one and
     the same solution to rounding, on every topology, in a fresh process each; and the
     iterate after a single stationary V-cycle (smoothing, restriction and prolongation on
     every level), which a wrong transfer would change well above rounding."""
-    import os
-    import subprocess
-    import sys
-    code = (
-        "import numpy as np, sys\n"
-        "from nyles_gb300.multigrid import MG\n"
-        "out = []\n"
-        "for topo in ('closed', 'perio_x', 'perio_y', 'perio_xy', 'perio_xyz'):\n"
-        "    nx, ny, nz = (64, 32, 32) if topo != 'perio_xyz' else (32, 32, 32)\n"
-        "    rng = np.random.Generator(np.random.PCG64(31))\n"
-        "    b = rng.standard_normal((nz, ny, nx)); b -= b.mean()\n"
-        "    mg = MG(nx, ny, nz, topo, precision='mixed'); mg.set_params(1e-20, 80, 0.9); mg.set_krylov(True)\n"
-        "    x, st = mg.solve(b)\n"
-        "    x = x.double().cpu().numpy(); x -= x.mean()\n"
-        "    mg1 = MG(nx, ny, nz, topo, precision='mixed'); mg1.set_params(1e-20, 1, 0.9); mg1.set_krylov(False)\n"
-        "    x1, st1 = mg1.solve(b)\n"
-        "    assert st1['nite'] == 1\n"
-        "    out.append((st['nite'], x, x1.double().cpu().numpy()))\n"
-        "np.savez(sys.argv[1], *[a for o in out for a in o[1:]])\n"
-        "print(' '.join(str(o[0]) for o in out))\n")
-    root = os.path.dirname(helpers.HERE)
-    res = {}
-    for scalar in ("0", "1"):
-        env = dict(os.environ, NYLES_GB300_SCALAR_KERNELS=scalar, PYTHONPATH=root)
-        fn = str(tmp_path / ("vec_%s.npz" % scalar))
-        r = subprocess.run([sys.executable, "-c", code, fn], env=env, capture_output=True, text=True, cwd=root)
-        assert r.returncode == 0, r.stderr[-2000:]
-        with np.load(fn) as f:
-            res[scalar] = ([int(v) for v in r.stdout.split()], [f["arr_%d" % i] for i in range(len(f.files))])
-    assert all(abs(a - c) <= 1 for a, c in zip(res["0"][0], res["1"][0])), (res["0"][0], res["1"][0])
-    for k, (a, c) in enumerate(zip(res["0"][1], res["1"][1])):
+    vec = _mixed_solves(tmp_path, "vec", NYLES_GB300_SCALAR_KERNELS="0")
+    sca = _mixed_solves(tmp_path, "scalar", NYLES_GB300_SCALAR_KERNELS="1")
+    assert all(abs(a - c) <= 1 for a, c in zip(vec[0], sca[0])), (vec[0], sca[0])
+    for k, (a, c) in enumerate(zip(vec[1], sca[1])):
         assert helpers.relerr(a, c) < (1e-6 if k % 2 == 0 else 1e-5), k
+
+
