@@ -299,8 +299,9 @@ _SOLVES_CODE = (
     "import numpy as np, sys\n"
     "from nyles_gb300.multigrid import MG\n"
     "out = []\n"
-    "for topo in ('closed', 'perio_x', 'perio_y', 'perio_xy', 'perio_xyz'):\n"
-    "    nx, ny, nz = (64, 32, 32) if topo != 'perio_xyz' else (32, 32, 32)\n"
+    "cases = [(t, (64, 32, 32)) for t in ('closed', 'perio_x', 'perio_y', 'perio_xy')]\n"
+    "cases += [('perio_xyz', (32, 32, 32)), ('perio_xy', (48, 48, 48)), ('closed', (48, 48, 48))]\n"
+    "for topo, (nx, ny, nz) in cases:\n"
     "    rng = np.random.Generator(np.random.PCG64(31))\n"
     "    b = rng.standard_normal((nz, ny, nx)); b -= b.mean()\n"
     "    mg = MG(nx, ny, nz, topo, precision='mixed'); mg.set_params(1e-20, 80, 0.9); mg.set_krylov(True)\n"
@@ -316,9 +317,10 @@ _SOLVES_CODE = (
 
 def _mixed_solves(tmp_path, tag, **env_extra):
     """FCG solves and single stationary V-cycles of a seeded right-hand side on every
-    topology, in a fresh process with the given environment (the kernel switches are
-    read when a solver is created): (iteration counts, [solution, one-cycle iterate] *
-    topologies)."""
+    topology (and on 3·2^n grids, whose coarser levels leave the vector kernels' shapes
+    part-way down), in a fresh process with the given environment (the kernel switches
+    are read when a solver is created): (iteration counts, [solution, one-cycle
+    iterate] * cases)."""
     import os
     import subprocess
     import sys
