@@ -751,6 +751,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
 // that of the grid kernels' ghost paths.
 constexpr int MG_BOTTOM_MAXLEV = 12;
 constexpr size_t MG_BOTTOM_SMEM = 200 * 1024;
+constexpr long long MG_BOTTOM_MAXVOL_FP64 = 1024;   // largest level (cells) in the FP64 one-block kernel
 template <typename T> struct MgBottomThreads { static constexpr int n = 1024; };
 template <> struct MgBottomThreads<double> { static constexpr int n = 512; };   // register budget
 
@@ -1648,7 +1649,9 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         mg->off_fq = take(mg->lev[0].vol * sizeof(float));
     }
     // the coarsest levels whose arrays fit in one block's shared memory (two levels at
-    // least, never level 0) run as one k_mg_bottom launch per V-cycle
+    // least, never level 0) run as one k_mg_bottom launch per V-cycle. In FP64 the block's
+    // SM does the levels' FP64 work alone (~2 FP64 instructions per cycle): levels above
+    // MG_BOTTOM_MAXVOL_FP64 cells are faster as grid launches spread over every SM.
     mg->bottom = L;
     mg->bottom_smem = 0;
     {
@@ -1656,6 +1659,7 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         for (int l = L - 1; l >= 1 && L - l <= MG_BOTTOM_MAXLEV; --l) {
             bytes += 3 * (size_t)mg->lev[l].vol * es;
             if (bytes > MG_BOTTOM_SMEM) break;
+            if (precision != NYLES_MIXED && mg->lev[l].vol > MG_BOTTOM_MAXVOL_FP64) break;
             if (L - l >= 2) {
                 mg->bottom = l;
                 mg->bottom_smem = bytes;
