@@ -118,7 +118,7 @@ def parity_errors(get_a, get_b, names):
     """Relative max-norm error per variable. Scalars are normalised by their own
     max-norm; components of a vector field (u, U, vor) by the max-norm of the whole
     vector, so that a component that is only round-off noise (v in a 2-D flow) is
-    judged against the velocity scale, not against its own noise level."""
+    measured against the velocity scale, not against its own noise level."""
     out = {}
     scales = {}
     for vec, comps in VECTORS.items():

@@ -1,6 +1,6 @@
 """Whole time steps on the GPU against the oracle and the golden vectors.
 
-Bars (the benchmark spec): FP64 path within 1e-12 relative max-norm per step and 1e-9 after
+Bars: FP64 path within 1e-12 relative max-norm per step and 1e-9 after
 100 steps, equal multigrid V-cycle counts; mixed path within 1e-5 in u and b.
 """
 import numpy as np
