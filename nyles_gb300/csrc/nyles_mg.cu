@@ -470,7 +470,6 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, 
 #pragma unroll
     for (int q = 1; q < NP - 1; ++q) ld4(cb + (q - 1) * sz, true, v[q]);
     ld4(cb + (2 * MG_RZC - 1) * sz + zh.op, zh.wp, v[NP - 1]);
-#pragma unroll
     // The 8 residuals b + diag*x - sum(x_nb) summed at once: each child's 6 neighbours
     // are 3 siblings and 3 cells outside the 2 x 2 x 2 block, so the sum is
     // sum(b) + sum(w_c x_c) - sum(24 outside cells) with w_c = diag_c - 3, the child's wet
