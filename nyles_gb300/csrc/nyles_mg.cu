@@ -794,9 +794,24 @@ __device__ __forceinline__ void bottom_cells(const MgGeom& g, F f) {
     if (ncol == 0 || nz == 0) return;
     const int groups = max(1, (int)blockDim.x / ncol);
     const int zc = (nz + groups - 1) / groups;
+    // power-of-two extents (the usual coarse levels): masks and shifts instead of the
+    // integer divisions, which took a large share of a pass over a small level
+    const int n2 = g.n[2];
+    const bool p2 = ((ncol & (ncol - 1)) | (n2 & (n2 - 1))) == 0;
+    const int lc = __ffs(ncol) - 1, l2 = __ffs(n2) - 1;
     for (int t = threadIdx.x; t < ncol * groups; t += blockDim.x) {
-        const int col = t % ncol, grp = t / ncol;
-        const int x = col % g.n[2], y = col / g.n[2];
+        int col, grp, x, y;
+        if (p2) {
+            col = t & (ncol - 1);
+            grp = t >> lc;
+            x = col & (n2 - 1);
+            y = col >> l2;
+        } else {
+            col = t % ncol;
+            grp = t / ncol;
+            x = col % n2;
+            y = col / n2;
+        }
         const MgNbI nx = mg_nbi(x, g.n[2], g.per[2], 1), ny = mg_nbi(y, g.n[1], g.per[1], g.n[2]);
         const int ze = min(nz, (grp + 1) * zc);
         for (int z = grp * zc; z < ze; ++z) f(z, y, x, nx, ny);
