@@ -230,20 +230,23 @@ RHS_FP64_INSTR_PER_CELL = 699
 # DRAM bytes (read + write) per interior cell of one launch: ncu, FP64 at 128^3
 # (159.0 + 43.7 MB), mixed at 256^3 (607.6 + 255.1 MB)
 RHS_DRAM_BYTES_PER_CELL = {8: 202.72e6 / 128 ** 3, 4: 862.71e6 / 256 ** 3}
-# DRAM bytes of one level-0 Jacobi half-sweep launch at 256^3, mixed (ncu: 134.2 +
-# 41.6 MB; algorithmic 201.3 MB, the rest of the output still in L2 at the end)
-JACOBI_F32_L0_DRAM_BYTES_256 = 175.8e6
+# DRAM bytes of one level-0 Jacobi half-sweep launch at 256^3, mixed (ncu, vector form:
+# 134.3 + 40.9 MB; algorithmic 201.3 MB, the rest of the output still in L2 at the end)
+JACOBI_F32_L0_DRAM_BYTES_256 = 175.2e6
 
 
-def mg_bottom_level(levels, elem, smem=200 * 1024):
+def mg_bottom_level(levels, elem, smem=200 * 1024, maxvol_fp64=1024):
     """First level of the one-block coarse solve (the library's rule: the coarsest
-    levels whose x, b, y fit in `smem` bytes, two levels at least, never level 0)."""
+    levels whose x, b, y fit in `smem` bytes, two levels at least, never level 0; in
+    FP64 no level above `maxvol_fp64` cells)."""
     L = len(levels)
     bottom, total = L, 0
     for l in range(L - 1, 0, -1):
         z, y, x = levels[l]
         total += 3 * z * y * x * elem
         if total > smem:
+            break
+        if elem == 8 and z * y * x > maxvol_fp64:
             break
         if L - l >= 2:
             bottom = l
