@@ -38,6 +38,11 @@ def test_roofline_fractions_follow_the_phase_times():
     n2 = b.roofline("mg_norm", ph, 256, 4, 6778.0, "measured", None, nv=10.0, solves=6, krylov=True)
     assert n2["frac"] == pytest.approx(2 * n1["frac"])
     assert b.roofline("mg_smooth", ph, 256, 4, 6778.0, "measured", None) is None   # no such phase
+    # FP64 smoothing: 5 grid levels above the one-block 8^3 bottom, one bracketed call
+    # per smoothing and the coarse solve (2 x 5 + 1 per V-cycle)
+    sm = b.roofline("mg_smooth", {"mg_smooth": {"count": 11 * 4, "ms": 8.0}}, 256, 8, 6778.0, "measured", None)
+    assert sm["vcycles"] == pytest.approx(4.0)
+    assert sm["frac"] == pytest.approx(sm["bytes_per_vcycle"] * 4 / 8e-3 / 1e9 / 6778.0)
 
 
 def test_step_bytes_and_job_value():
