@@ -81,6 +81,13 @@ typedef struct NylesDesc {
      * from core/interpolate_tracer.f90 (odd: upwind-biased, even: centred), i.e.
      * param orderA. */
     int tracer_order;
+    /* Vortex-force reconstruction: 0 = WENO (core/fortran_vortex_force.f90:56-82 and
+     * :134-160, the only branch the reference runs: `linear` is hard-coded .false. at
+     * :28 and :106); 1..5 = the linear branch of :43-55 (direc) and :121-133 (flip)
+     * with core/interpolate.f90:3-112 of that order (odd: upwinded with the split
+     * velocity; even: the interpolated vorticity alone, as written there), i.e. param
+     * orderVF. */
+    int vf_order;
 } NylesDesc;
 
 typedef struct NylesMgStats {
@@ -88,7 +95,8 @@ typedef struct NylesMgStats {
     double res;        /* last squared residual ratio sum(r^2)/sum(b^2) (mgfor MG_Stats%res) */
     long long solves;  /* solves since creation */
     long long vcycles; /* V-cycles since creation */
-    int not_converged; /* solves that stopped at maxite */
+    int not_converged; /* solves that stopped at maxite above tol */
+    int nonfinite;     /* solves stopped by a non-finite norm of b or of a residual (blow-up) */
 } NylesMgStats;
 
 const char* nyles_last_error(void);
@@ -148,6 +156,8 @@ int nyles_mg_set_params(NylesMg* mg, double tol, int maxite, double omega);
  * whose iterates it no longer follows; 0 (default) keeps that iteration.
  * NYLES_UNSUPPORTED for an FP64 solver. */
 int nyles_mg_set_krylov(NylesMg* mg, int on);
+/* NYLES_NOT_CONVERGED when it stopped at maxite above tol; NYLES_BLOWUP, at once, when
+ * the norm of the right-hand side or of a residual is not finite */
 int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream);
 
 /* ---------------------------------------------------------------- whole model
@@ -168,7 +178,10 @@ int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omeg
 /* nyles_mg_set_krylov for the model's pressure solve (refused while a graph is captured) */
 int nyles_model_set_mg_krylov(NylesModel* m, int on);
 /* LES.forward: one time step, core/model_les.py:147-149 -> core/timescheme.py:113-221.
- * Returns NYLES_BLOWUP when the new state holds a non-finite value. */
+ * Returns NYLES_BLOWUP when a pressure solve of the step meets a non-finite divergence
+ * (a non-finite velocity, or a buoyancy that reached the velocity): the step stops at
+ * that stage and leaves the state as it is. Other non-finite values are caught by
+ * nyles_model_max_U2. */
 int nyles_model_forward(NylesModel* m, double t, double dt, void* stream);
 /* LES.diagnose_var, core/model_les.py:98-127 (core/model_les_euler.py:96-125) */
 int nyles_model_diagnose(NylesModel* m, void* stream);
@@ -238,9 +251,15 @@ long long nyles_launch_count(void);
  * The reduction's block partials live in a static device array of NYLES_STATIC_PARTIALS
  * doubles (8 KiB, held by every GPU that loads the library until the process exits).
  * n is limited to NYLES_STATIC_MAX_CELLS; larger n returns NYLES_BAD_ARG.
- * The first call on a device looks up the array's device address (once per device, with
- * that device current): make that first call before any stream capture. Calls share the
- * array, so calls that overlap on the GPU (different streams or threads) race. */
+ * The array's device address belongs to the current context: every call made outside
+ * stream capture looks it up afresh, with the calling device current, and records it for
+ * that device; a call made while `stream` is capturing reuses the address recorded by the
+ * last call outside capture on the device (NYLES_BAD_ARG when there was none). So make
+ * the first call on a device before any stream capture, and make one more outside
+ * capture after a cudaDeviceReset or any re-creation of the device's primary context,
+ * before capturing again. Every call writes the partials it reads, so nothing carries
+ * over from one call to the next; but calls share the array, so calls that overlap on
+ * the GPU (different streams or threads) race. */
 #define NYLES_STATIC_PARTIALS 1024
 #define NYLES_STATIC_MAX_CELLS (1LL << 28)
 int nyles_max_U2_static_f64(const double* U, const double* V, const double* W, long long n, double* out,

@@ -52,12 +52,12 @@ class NylesDesc(ctypes.Structure):
                 ("idx2", ctypes.c_double), ("idy2", ctypes.c_double), ("idz2", ctypes.c_double),
                 ("dx2", ctypes.c_double), ("fparam", ctypes.c_double), ("viscosity", ctypes.c_double),
                 ("tracer_diffusivity", ctypes.c_double * (MAX_TRACERS + 1)), ("tracer_diffusion", ctypes.c_int),
-                ("tracer_order", ctypes.c_int)]
+                ("tracer_order", ctypes.c_int), ("vf_order", ctypes.c_int)]
 
 
 class NylesMgStats(ctypes.Structure):
     _fields_ = [("nite", ctypes.c_int), ("res", ctypes.c_double), ("solves", ctypes.c_longlong),
-                ("vcycles", ctypes.c_longlong), ("not_converged", ctypes.c_int)]
+                ("vcycles", ctypes.c_longlong), ("not_converged", ctypes.c_int), ("nonfinite", ctypes.c_int)]
 
 
 # user forcing callback: fn(user, reg, t, stream)

@@ -157,7 +157,16 @@ struct GraphBuilder {
 // multigrid solve recorded into a graph: stop test on the device, V-cycles in a
 // conditional while-node (solvers.f90:8-33)
 int mg_solve_graph(MgImpl* mg, GraphBuilder& gb);
-// device-side statistics of graph-mode solves: last nite, last res, total V-cycles
-int mg_read_device_stats(MgImpl* mg, cudaStream_t st, int* nite, double* res, long long* vcycles);
+// device-side statistics of graph-mode solves: last nite, last res, and the totals of
+// V-cycles, of solves stopped at maxite above tol and of solves stopped by a
+// non-finite norm
+struct MgDeviceStats {
+    int nite = 0;
+    double res = 0.0;
+    long long vcycles = 0, not_converged = 0, nonfinite = 0;
+};
+int mg_read_device_stats(MgImpl* mg, cudaStream_t st, MgDeviceStats* out);
+// zero the solver's device scalars (synchronous; at workspace binding)
+int mg_zero_scalars(MgImpl* mg);
 
 }  // namespace nyles

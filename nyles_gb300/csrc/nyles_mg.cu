@@ -40,7 +40,11 @@ template <> __device__ __forceinline__ float mg_pcoef<float>(const MgGeom& g, in
 // Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
 // [3] nite of the current solve, [4] V-cycles since creation, [5] and [6] the scale of
 // the mixed-precision residual sums and its inverse square.
-enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE = 5, SC_INVSCALE2 = 6 };
+// device scalars of the solver (16 doubles, zeroed when the workspace is bound):
+// SC_NCONV counts graph-mode solves that stopped at maxite above tol, SC_NONFINITE
+// graph-mode solves stopped by a non-finite norm
+enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE = 5, SC_INVSCALE2 = 6,
+       SC_NCONV = 7, SC_NONFINITE = 8 };
 
 constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
 constexpr int MG_RZC = 2;                          // restriction (coarse z per thread)
@@ -1529,11 +1533,18 @@ __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __
 
 // ---------------------------------------------------------------- device-side stop test
 // before the loop: res = sum(r^2)/sum(b^2) (0 when b = 0), continue while res >= tol
+__device__ __forceinline__ bool finite_dev(double v) { return v == v && v <= 1.7976931348623157e308; }
+
 __global__ void k_mg_ctl_begin(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol) {
     const double normb = sc[SC_NORMB];
     const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
     sc[SC_RES] = res;
     sc[SC_NITE] = 0.0;
+    if (!finite_dev(normb) || !finite_dev(res)) {   // non-finite input: no V-cycle (host: NYLES_BLOWUP)
+        sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
+        cudaGraphSetConditional(h, 0u);
+        return;
+    }
     cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
 }
 
@@ -1544,12 +1555,18 @@ __global__ void k_mg_ctl_step(double* __restrict__ sc, cudaGraphConditionalHandl
     sc[SC_NITE] = nite;
     sc[SC_TOTAL] = sc[SC_TOTAL] + 1.0;
     if (nite >= (double)maxite) {
+        if (sc[SC_RES] >= tol) sc[SC_NCONV] = sc[SC_NCONV] + 1.0;   // as mg_solve's count
         cudaGraphSetConditional(h, 0u);
         return;
     }
     const double normb = sc[SC_NORMB];
     const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
     sc[SC_RES] = res;
+    if (!finite_dev(res)) {
+        sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
+        cudaGraphSetConditional(h, 0u);
+        return;
+    }
     cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
 }
 
@@ -1937,6 +1954,21 @@ static int read_slot(MgImpl* mg, int slot, double* host_out, cudaStream_t st) {
     return cuda_status(e, "multigrid norm");
 }
 
+// A non-finite norm means a non-finite right-hand side or solution: the solve stops
+// at once with NYLES_BLOWUP (the stop rule alone would either accept it, since a NaN
+// norm of b skips the iteration, or run to maxite on NaN residuals).
+static bool finite_norm(double v) { return v == v && v <= 1.7976931348623157e308; }
+
+static int blowup(MgImpl* mg, int nite, double res, const char* what) {
+    mg->stats.nite = nite;
+    mg->stats.res = res;
+    mg->stats.solves += 1;
+    mg->stats.vcycles += nite;
+    mg->stats.nonfinite += 1;
+    set_error(std::string("multigrid: non-finite ") + what + " (blow-up)");
+    return NYLES_BLOWUP;
+}
+
 // solvers.f90:8-33: stop when sum(r^2)/sum(b^2) < tol or after maxite V-cycles
 int mg_solve(MgImpl* mg, cudaStream_t st) {
     if (!mg->ws) { set_error("multigrid: workspace not bound"); return NYLES_BAD_ARG; }
@@ -1947,10 +1979,12 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
     if (mg->precision == NYLES_FP64) {
         double* b = lvp<double>(mg, 0, 2);
         if ((rc = sumsq<double, 0>(mg, g0, b, nullptr, &normb, st))) return rc;
+        if (!finite_norm(normb)) return blowup(mg, 0, normb, "right-hand side");
         if (normb > 0.0) {
             enqueue_resid_sweep(mg, st);
             if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
             res = rr / normb;
+            if (!finite_norm(res)) return blowup(mg, 0, res, "residual");
         }
         while (true) {
             if (res < mg->tol) break;
@@ -1961,6 +1995,7 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
                 enqueue_resid_sweep(mg, st);
                 if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
                 res = rr / normb;
+                if (!finite_norm(res)) return blowup(mg, nite, res, "residual");
             } else {
                 res = 0.0;
             }
@@ -1968,10 +2003,12 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
     } else {
         enqueue_normb_df(mg, st);
         if ((rc = read_slot(mg, SC_NORMB, &normb, st))) return rc;
+        if (!finite_norm(normb)) return blowup(mg, 0, normb, "right-hand side");
         if (normb > 0.0) {
             enqueue_resid_df(mg, st);
             if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
             res = rr / normb;
+            if (!finite_norm(res)) return blowup(mg, 0, res, "residual");
         }
         while (true) {
             if (res < mg->tol) break;
@@ -1987,6 +2024,7 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
                 enqueue_resid_df(mg, st);
                 if ((rc = read_slot(mg, SC_RR, &rr, st))) return rc;
                 res = rr / normb;
+                if (!finite_norm(res)) return blowup(mg, nite, res, "residual");
             } else {
                 res = 0.0;
             }
@@ -2080,15 +2118,22 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
     return gb.error;
 }
 
-int mg_read_device_stats(MgImpl* mg, cudaStream_t st, int* nite, double* res, long long* vcycles) {
-    double h[5];
+int mg_read_device_stats(MgImpl* mg, cudaStream_t st, MgDeviceStats* out) {
+    double h[SC_NONFINITE + 1];
     cudaError_t e = cudaMemcpyAsync(h, scalars(mg), sizeof(h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_status(e, "multigrid statistics read-back");
-    *nite = (int)h[SC_NITE];
-    *res = h[SC_RES];
-    *vcycles = (long long)h[SC_TOTAL];
+    out->nite = (int)h[SC_NITE];
+    out->res = h[SC_RES];
+    out->vcycles = (long long)h[SC_TOTAL];
+    out->not_converged = (long long)h[SC_NCONV];
+    out->nonfinite = (long long)h[SC_NONFINITE];
     return NYLES_OK;
+}
+
+int mg_zero_scalars(MgImpl* mg) {
+    cudaError_t e = cudaMemset(scalars(mg), 0, 16 * sizeof(double));
+    return cuda_status(e, "multigrid scalars reset");
 }
 
 }  // namespace nyles

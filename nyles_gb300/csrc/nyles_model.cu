@@ -72,6 +72,10 @@ static int check_desc(const NylesDesc* d, Geom* g) {
         set_error("tracer_order must be 0 (WENO) or an interpolation order 1..5");
         return NYLES_BAD_ARG;
     }
+    if (d->vf_order < 0 || d->vf_order > 5) {
+        set_error("vf_order must be 0 (WENO) or an interpolation order 1..5");
+        return NYLES_BAD_ARG;
+    }
     if (d->tracer_diffusion < 0 || (d->tracer_diffusion >> (d->n_tracers + 1)) != 0) {
         set_error("tracer_diffusion names a tracer beyond b, t0..t{n_tracers-1}");
         return NYLES_BAD_ARG;
@@ -257,7 +261,7 @@ int nyles_mg_bind(NylesMg* mg, void* workspace) {
     if (!mg || !workspace) { set_error("null argument"); return NYLES_BAD_ARG; }
     if (((uintptr_t)workspace) & 255) { set_error("workspace must be 256-byte aligned"); return NYLES_BAD_ARG; }
     mg->impl.ws = (char*)workspace;
-    return NYLES_OK;
+    return mg_zero_scalars(&mg->impl);
 }
 int nyles_mg_nlevels(const NylesMg* mg, int* nlevels) {
     if (!mg || !nlevels) { set_error("null argument"); return NYLES_BAD_ARG; }
@@ -365,7 +369,7 @@ int nyles_model_bind(NylesModel* m, void* const* fields, void* const* regs, void
     m->ws = (char*)workspace;
     m->mg.ws = m->ws + m->mg_off;
     m->bound = true;
-    return NYLES_OK;
+    return mg_zero_scalars(&m->mg);
 }
 
 int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omega) {
@@ -403,21 +407,22 @@ int nyles_model_mg_stats(const NylesModel* m, NylesMgStats* stats) {
     *stats = m->mg.stats;
     if (m->graph_launches > 0) {   // solves run inside graphs keep their statistics on the device
         NylesModel* mm = const_cast<NylesModel*>(m);
-        int nite = 0;
-        double res = 0.0;
-        long long vc = 0;
-        int rc = mg_read_device_stats(&mm->mg, mm->last_stream, &nite, &res, &vc);
+        MgDeviceStats ds;
+        int rc = mg_read_device_stats(&mm->mg, mm->last_stream, &ds);
         if (rc) return rc;
+        const long long vc = ds.vcycles;
         if (vc > mm->vcycles_counted) {
             note_launch((int)((vc - mm->vcycles_counted) * mm->graph_body_kernels));
             mm->vcycles_counted = vc;
         }
         if (m->last_solve_graph) {
-            stats->nite = nite;
-            stats->res = res;
+            stats->nite = ds.nite;
+            stats->res = ds.res;
         }
         stats->vcycles += vc;
         stats->solves += m->graph_launches * m->graph_solves;
+        stats->not_converged += (int)ds.not_converged;
+        stats->nonfinite += (int)ds.nonfinite;
     }
     return NYLES_OK;
 }

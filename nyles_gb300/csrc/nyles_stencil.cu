@@ -45,6 +45,21 @@ __device__ __forceinline__ T tr_flux(const T* __restrict__ Uf, const T* __restri
     return flux1d_at(i, n, __ldg(Uf + c), Q);
 }
 
+// REAL(4) literal coefficients of core/interpolate.f90:18-33 and
+// core/interpolate_tracer.f90 (the same values), widened
+template <typename T>
+struct LinK {
+    static __device__ __forceinline__ T c1() { return T(-1.0f / 6.0f); }
+    static __device__ __forceinline__ T c2() { return T(5.0f / 6.0f); }
+    static __device__ __forceinline__ T c3() { return T(2.0f / 6.0f); }
+    static __device__ __forceinline__ T e1() { return T(-1.0f / 12.0f); }
+    static __device__ __forceinline__ T e2() { return T(7.0f / 12.0f); }
+    static __device__ __forceinline__ T b1() { return T(2.0f / 60.0f); }
+    static __device__ __forceinline__ T b2() { return T(-13.0f / 60.0f); }
+    static __device__ __forceinline__ T b3() { return T(47.0f / 60.0f); }
+    static __device__ __forceinline__ T b4() { return T(27.0f / 60.0f); }
+    static __device__ __forceinline__ T b5() { return T(-3.0f / 60.0f); }
+};
 
 template <typename T>
 struct RhsArgs {
@@ -63,6 +78,7 @@ struct RhsArgs {
     T vcoef[3];       // viscosity*ids2 for directions x, y, z
     T kcoef[NYLES_MAX_TR + 1][3];   // tracer diffusivity*ids2 of b, t0.. for x, y, z
     int kmask;        // bit q: diffuse tracer q (b = 0) when TERM_TRDIFF is set
+    int vf_order;     // 0: WENO vortex force; 1..5: the linear branch of that order
     int lo[3], hi[3]; // k_rhs_march: index box (z, y, x) of the cells it computes
 };
 
@@ -97,6 +113,101 @@ __device__ __forceinline__ T tracer_rhs(const T* __restrict__ q, const T* const*
         if (diff) acc = acc + (pass == 0 ? kx : (pass == 1 ? ky : kz)) * lap1d(q, g, c, i, d);
     }
     return acc;
+}
+
+// ---------------------------------------------------------------- linear vortex force
+// The linear branch of core/fortran_vortex_force.f90 (direc :43-55, flip :121-133) with
+// core/interpolate.f90:3-112, which the reference never takes (`linear = .false.` at
+// :28 and :106); selected by NylesDesc.vf_order (param orderVF). Indices below are the
+// Fortran ones of a line of n values: vU(i) is the vorticity at 0-based position i - 1
+// (unshifted, unlike the WENO branch's q(i) = vort(i - 1)). core/interpolate.f90's top
+// end differs from the tracer version: identity at i = n - 1 and n, the third-order
+// stencil at n - 2.
+
+// qp(i) (plus) or qm(i) of an odd order, 1 <= i <= n
+template <typename T, typename VF>
+__device__ __forceinline__ T vf_interp_odd(int i, int n, int order, bool plus, VF V) {
+    using K = LinK<T>;
+    if (order == 1 || i == 1 || i >= n - 1) return V(i);
+    if (order == 3 || i == 2 || i == n - 2) {
+        const T wa = plus ? K::c1() : K::c3(), wc = plus ? K::c3() : K::c1();
+        return add_rn(add_rn(mul_rn(wa, V(i - 1)), mul_rn(K::c2(), V(i))), mul_rn(wc, V(i + 1)));
+    }
+    const T w0 = plus ? K::b1() : K::b5(), w1 = plus ? K::b2() : K::b4();
+    const T w3 = plus ? K::b4() : K::b2(), w4 = plus ? K::b5() : K::b1();
+    T v = mul_rn(w0, V(i - 2));
+    v = add_rn(v, mul_rn(w1, V(i - 1)));
+    v = add_rn(v, mul_rn(K::b3(), V(i)));
+    v = add_rn(v, mul_rn(w3, V(i + 1)));
+    return add_rn(v, mul_rn(w4, V(i + 2)));
+}
+
+// qm(i) of an even order (2: two-point mean; 4: the fourth-order centred stencil)
+template <typename T, typename VF>
+__device__ __forceinline__ T vf_interp_even(int i, int n, int order, VF V) {
+    using K = LinK<T>;
+    if (order == 2) return i == 1 ? mul_rn(T(0.5), V(1)) : mul_rn(T(0.5), add_rn(V(i - 1), V(i)));
+    if (i == 1) return add_rn(mul_rn(K::e2(), V(1)), mul_rn(K::e1(), V(2)));
+    if (i == 2) return add_rn(mul_rn(K::e2(), add_rn(V(1), V(2))), mul_rn(K::e1(), V(3)));
+    if (i == n) return add_rn(mul_rn(K::e2(), add_rn(V(n - 1), V(n))), mul_rn(K::e1(), V(n - 2)));
+    return add_rn(mul_rn(K::e2(), add_rn(V(i - 1), V(i))), mul_rn(K::e1(), add_rn(V(i - 2), V(i + 1))));
+}
+
+// The two products the reference subtracts (direc) or adds (flip) one after the other at
+// 0-based position k along fa: qp(k) up(k+1) and qm(k+1) um(k+1) in Fortran indices
+// (qp(0) = 0; up, um = positive and negative parts of the velocity averaged along aa,
+// then along fa, as the WENO branch); even orders give qm(k+1) and 0.
+template <typename T>
+struct VfTerms {
+    T a, b;
+};
+template <typename T>
+__device__ __forceinline__ VfTerms<T> vf_lin(const T* __restrict__ Uf, const T* __restrict__ Wf, const Geom& g,
+                                             long long c, int k, int fa, int aa, int order) {
+    const int n = g.N[fa];
+    const long long sf = g.stride(fa);
+    const long long base = c - (long long)k * sf;
+    auto V = [&](int i) -> T { return __ldg(Wf + base + (long long)(i - 1) * sf); };
+    if ((order & 1) == 0) return {vf_interp_even<T>(k + 1, n, order, V), T(0)};
+    const long long sa = g.stride(aa);
+    const T UU1 = mul_rn(T(0.5), add_rn(__ldg(Uf + c), __ldg(Uf + c + sa)));
+    const T UU0 = (k > 0) ? mul_rn(T(0.5), add_rn(__ldg(Uf + c - sf), __ldg(Uf + c - sf + sa))) : T(0);
+    const T u1 = mul_rn(T(0.5), add_rn(UU0, UU1));
+    const T uu = fabs(u1);
+    const T up = mul_rn(T(0.5), add_rn(u1, uu)), um = mul_rn(T(0.5), sub_rn(u1, uu));
+    const T qp = (k == 0) ? T(0) : vf_interp_odd<T>(k, n, order, true, V);
+    const T qm = vf_interp_odd<T>(k + 1, n, order, false, V);
+    return {mul_rn(qp, up), mul_rn(qm, um)};
+}
+template <typename T>
+__device__ __forceinline__ T vf_sub(T acc, VfTerms<T> r) { return sub_rn(sub_rn(acc, r.a), r.b); }
+template <typename T>
+__device__ __forceinline__ T vf_add(T acc, VfTerms<T> r) { return add_rn(add_rn(acc, r.a), r.b); }
+
+// The six vortex-force terms of one cell in the call order of core/vortex_force.py:69-81
+// (triplets "ikj", "jik", "kji": direc then flip). VF = 1: WENO; VF = 2: the linear
+// branch of order a.vf_order.
+template <typename T, int VF>
+__device__ __forceinline__ void vortex_force_cell(const RhsArgs<T>& a, long long c, int z, int y, int x, T& dux,
+                                                  T& duy, T& duz) {
+    const Geom& g = a.g;
+    const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
+    if (VF == 1) {
+        if (y < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, x, 2, 1);   // u_j -= U^i w_k, along i
+        if (x < Nx - 1) dux = dux + vf_flux(a.U[1], a.W[2], g, c, y, 1, 2);   // u_i += U^j w_k, along j
+        if (z < Nz - 1) duz = duz - vf_flux(a.U[1], a.W[0], g, c, y, 1, 0);   // u_k -= U^j w_i, along j
+        if (y < Ny - 1) duy = duy + vf_flux(a.U[2], a.W[0], g, c, z, 0, 1);   // u_j += U^k w_i, along k
+        if (x < Nx - 1) dux = dux - vf_flux(a.U[2], a.W[1], g, c, z, 0, 2);   // u_i -= U^k w_j, along k
+        if (z < Nz - 1) duz = duz + vf_flux(a.U[0], a.W[1], g, c, x, 2, 0);   // u_k += U^i w_j, along i
+    } else {
+        const int o = a.vf_order;
+        if (y < Ny - 1) duy = vf_sub(duy, vf_lin(a.U[0], a.W[2], g, c, x, 2, 1, o));
+        if (x < Nx - 1) dux = vf_add(dux, vf_lin(a.U[1], a.W[2], g, c, y, 1, 2, o));
+        if (z < Nz - 1) duz = vf_sub(duz, vf_lin(a.U[1], a.W[0], g, c, y, 1, 0, o));
+        if (y < Ny - 1) duy = vf_add(duy, vf_lin(a.U[2], a.W[0], g, c, z, 0, 1, o));
+        if (x < Nx - 1) dux = vf_sub(dux, vf_lin(a.U[2], a.W[1], g, c, z, 0, 2, o));
+        if (z < Nz - 1) duz = vf_add(duz, vf_lin(a.U[0], a.W[1], g, c, x, 2, 0, o));
+    }
 }
 
 template <typename T>
@@ -134,13 +245,8 @@ __global__ void __launch_bounds__(128) k_rhs(const RhsArgs<T> a) {
     T duz = acc ? a.ds[3][c] : T(0);
     const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
     if (a.terms & TERM_VF) {
-        // call order of core/vortex_force.py:69-81: triplets "ikj", "jik", "kji"
-        if (y < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, x, 2, 1);   // u_j -= U^i w_k, along i
-        if (x < Nx - 1) dux = dux + vf_flux(a.U[1], a.W[2], g, c, y, 1, 2);   // u_i += U^j w_k, along j
-        if (z < Nz - 1) duz = duz - vf_flux(a.U[1], a.W[0], g, c, y, 1, 0);   // u_k -= U^j w_i, along j
-        if (y < Ny - 1) duy = duy + vf_flux(a.U[2], a.W[0], g, c, z, 0, 1);   // u_j += U^k w_i, along k
-        if (x < Nx - 1) dux = dux - vf_flux(a.U[2], a.W[1], g, c, z, 0, 2);   // u_i -= U^k w_j, along k
-        if (z < Nz - 1) duz = duz + vf_flux(a.U[0], a.W[1], g, c, x, 2, 0);   // u_k += U^i w_j, along i
+        if (a.vf_order) vortex_force_cell<T, 2>(a, c, z, y, x, dux, duy, duz);
+        else vortex_force_cell<T, 1>(a, c, z, y, x, dux, duy, duz);
     }
     if (a.terms & TERM_BERNOULLI) {   // core/bernoulli.py:14-23
         const T* ke = a.ke;
@@ -202,15 +308,15 @@ struct TracerMarch {
     }
 };
 
-// TR: buoyancy advection on; VF: vortex force on; BDIFF: buoyancy diffusion on (a
-// template flag so that the default instances carry none of its registers). ds[0..3]
-// are written.
+// TR: buoyancy advection on; VF: vortex force off (0), WENO (1) or the linear branch
+// (2); BDIFF: buoyancy diffusion on (template flags, so that the default instances carry
+// none of the optional terms' registers). ds[0..3] are written.
 // blocks per SM asked of the register allocator: FP32 issue-bound march (more warps
 // hide its load latency), FP64 bound by the FP64 pipe
 template <typename T> struct RhsMinBlocks { static constexpr int n = 5; };
 template <> struct RhsMinBlocks<double> { static constexpr int n = 4; };
 
-template <typename T, bool TR, bool VF, bool BDIFF>
+template <typename T, bool TR, int VF, bool BDIFF>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march(const RhsArgs<T> a) {
     __shared__ T sfy[RZ_BY][RZ_BX];
     const Geom& g = a.g;
@@ -231,14 +337,7 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march
         T db = T(0);
         if (TR) db = tm.step(a.b, Uzyx, g, c, z, ys, xs, sfy, BDIFF, a.kcoef[0][0], a.kcoef[0][1], a.kcoef[0][2]);
         T dux = T(0), duy = T(0), duz = T(0);
-        if (VF) {
-            if (ys < Ny - 1) duy = duy - vf_flux(a.U[0], a.W[2], g, c, xs, 2, 1);
-            if (xs < Nx - 1) dux = dux + vf_flux(a.U[1], a.W[2], g, c, ys, 1, 2);
-            if (z < Nz - 1) duz = duz - vf_flux(a.U[1], a.W[0], g, c, ys, 1, 0);
-            if (ys < Ny - 1) duy = duy + vf_flux(a.U[2], a.W[0], g, c, z, 0, 1);
-            if (xs < Nx - 1) dux = dux - vf_flux(a.U[2], a.W[1], g, c, z, 0, 2);
-            if (z < Nz - 1) duz = duz + vf_flux(a.U[0], a.W[1], g, c, xs, 2, 0);
-        }
+        if (VF) vortex_force_cell<T, VF>(a, c, z, ys, xs, dux, duy, duz);
         {
             const T* ke = a.ke;
             if (xs < Nx - 1) dux = sub_rn(dux, sub_rn(__ldg(ke + c + 1), __ldg(ke + c)));
@@ -293,19 +392,6 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, co
 // core/interpolate_tracer.f90:3-116 (coefficients: REAL(4) literals widened) and the
 // linear branch of core/fortran_upwind.f90:32-61, which the reference never takes
 // (`linear = .false.`, :28): selected by NylesDesc.tracer_order (param orderA).
-template <typename T>
-struct LinK {
-    static __device__ __forceinline__ T c1() { return T(-1.0f / 6.0f); }
-    static __device__ __forceinline__ T c2() { return T(5.0f / 6.0f); }
-    static __device__ __forceinline__ T c3() { return T(2.0f / 6.0f); }
-    static __device__ __forceinline__ T e1() { return T(-1.0f / 12.0f); }
-    static __device__ __forceinline__ T e2() { return T(7.0f / 12.0f); }
-    static __device__ __forceinline__ T b1() { return T(2.0f / 60.0f); }
-    static __device__ __forceinline__ T b2() { return T(-13.0f / 60.0f); }
-    static __device__ __forceinline__ T b3() { return T(47.0f / 60.0f); }
-    static __device__ __forceinline__ T b4() { return T(27.0f / 60.0f); }
-    static __device__ __forceinline__ T b5() { return T(-3.0f / 60.0f); }
-};
 
 // interpolation qp(j) (plus) or qm(j) of an odd order at 0-based position j of a line
 // of n values
@@ -418,6 +504,7 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     a.vcoef[1] = T(d->viscosity * d->idy2);
     a.vcoef[2] = T(d->viscosity * d->idz2);
     a.kmask = d->tracer_diffusion;
+    a.vf_order = d->vf_order;
     for (int q = 0; q <= NYLES_MAX_TR; ++q) {   // diff_coef[name]*ids2[direction], core/tracer.py:75
         a.kcoef[q][0] = T(d->tracer_diffusivity[q] * d->idx2);
         a.kcoef[q][1] = T(d->tracer_diffusivity[q] * d->idy2);
@@ -463,12 +550,17 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     if (linear_tr) terms &= ~TERM_TRACER;   // b's tendency comes from k_tracer_linear after the march
     const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
     const bool bdiff = tr && (terms & TERM_TRDIFF) && (d->tracer_diffusion & 1);
-    if (tr && vf && bdiff) k_rhs_march<T, true, true, true><<<grd_box, blk, 0, st>>>(a);
-    else if (tr && vf) k_rhs_march<T, true, true, false><<<grd_box, blk, 0, st>>>(a);
-    else if (tr && bdiff) k_rhs_march<T, true, false, true><<<grd_box, blk, 0, st>>>(a);
-    else if (tr) k_rhs_march<T, true, false, false><<<grd_box, blk, 0, st>>>(a);
-    else if (vf) k_rhs_march<T, false, true, false><<<grd_box, blk, 0, st>>>(a);
-    else k_rhs_march<T, false, false, false><<<grd_box, blk, 0, st>>>(a);
+    const bool lin = vf && d->vf_order > 0;
+    if (lin) {   // the linear vortex force (opt-in)
+        if (tr && bdiff) k_rhs_march<T, true, 2, true><<<grd_box, blk, 0, st>>>(a);
+        else if (tr) k_rhs_march<T, true, 2, false><<<grd_box, blk, 0, st>>>(a);
+        else k_rhs_march<T, false, 2, false><<<grd_box, blk, 0, st>>>(a);
+    } else if (tr && vf && bdiff) k_rhs_march<T, true, 1, true><<<grd_box, blk, 0, st>>>(a);
+    else if (tr && vf) k_rhs_march<T, true, 1, false><<<grd_box, blk, 0, st>>>(a);
+    else if (tr && bdiff) k_rhs_march<T, true, 0, true><<<grd_box, blk, 0, st>>>(a);
+    else if (tr) k_rhs_march<T, true, 0, false><<<grd_box, blk, 0, st>>>(a);
+    else if (vf) k_rhs_march<T, false, 1, false><<<grd_box, blk, 0, st>>>(a);
+    else k_rhs_march<T, false, 0, false><<<grd_box, blk, 0, st>>>(a);
     note_launch();
     if (linear_tr) {
         tracer_linear(a.b, a.ds[0], 0);
@@ -1127,22 +1219,39 @@ template int launch_correct<double, double>(const NylesDesc*, const Geom&, const
 // workspace. Every GPU that loads the library holds it (8 KiB) until the process exits.
 static __device__ __align__(256) double g_static_partials[NYLES_STATIC_PARTIALS];
 
-// Device address of g_static_partials, looked up once per device with that device
-// current. In host code the array's name is only a host-side stand-in; handing it to a
-// kernel would make the kernel touch the wrong memory, so only this address is used.
-static double* static_partials_for_current_device(int* status) {
+// Device address of g_static_partials in the current device's context. In host code the
+// array's name is only a host-side stand-in; handing it to a kernel would make the
+// kernel touch the wrong memory, so only this address is used. The address belongs to
+// the context that loaded the module: after cudaDeviceReset (or a primary context that
+// a host framework released and re-created) the module loads again, possibly
+// elsewhere. So every call made outside stream capture looks the address up afresh
+// (a host-side table lookup, no device work) and records it for its device; a call
+// made while `st` is capturing uses the address recorded by the last call outside
+// capture on that device, and fails with NYLES_BAD_ARG when there is none.
+static double* static_partials_for_current_device(cudaStream_t st, int* status) {
     static std::mutex mtx;
     static double* addr[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) { *status = cuda_status(e, "cudaGetDevice"); return nullptr; }
     if (dev < 0 || dev >= 64) { set_error("device ordinal above 63"); *status = NYLES_UNSUPPORTED; return nullptr; }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();   // not sticky; treat the stream as capturing
+        cs = cudaStreamCaptureStatusActive;
+    }
     std::lock_guard<std::mutex> lock(mtx);
-    if (!addr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_static_partials);
         if (e != cudaSuccess) { *status = cuda_status(e, "cudaGetSymbolAddress(g_static_partials)"); return nullptr; }
         addr[dev] = static_cast<double*>(p);
+    } else if (!addr[dev]) {
+        set_error("max_U2_static: first call on this device made during stream capture; make one call outside "
+                  "capture first");
+        *status = NYLES_BAD_ARG;
+        return nullptr;
     }
     *status = NYLES_OK;
     return addr[dev];
@@ -1159,13 +1268,13 @@ extern "C" int nyles_max_U2_static_f64(const double* U, const double* V, const d
                   std::to_string((long long)NYLES_STATIC_MAX_CELLS) + " for the static scratch");
         return NYLES_BAD_ARG;
     }
+    cudaStream_t st = (cudaStream_t)stream;
     int status = NYLES_OK;
-    double* partial = static_partials_for_current_device(&status);
+    double* partial = static_partials_for_current_device(st, &status);
     if (!partial) return status;
     // one block per 2^18 cells (at least one), at most NYLES_STATIC_PARTIALS blocks
     long long blocks = (n + (1LL << 18) - 1) >> 18;
     if (blocks > NYLES_STATIC_PARTIALS) blocks = NYLES_STATIC_PARTIALS;
-    cudaStream_t st = (cudaStream_t)stream;
     k_max_U2<double><<<(unsigned)blocks, 256, 0, st>>>(n, U, V, W, partial);
     k_max_final<<<1, 1024, 0, st>>>(partial, (int)blocks, out);
     note_launch(2);

@@ -43,6 +43,10 @@ def make_desc(param, grid, modelname):
     # core/fortran_upwind.f90:32-61 instead of WENO (the reference hard-codes WENO)
     if gpu.get("tracer_scheme", "weno") == "linear":
         d.tracer_order = int(param.get("orderA", 5))
+    # vf_scheme "linear": the orderVF interpolation of the linear branch of
+    # core/fortran_vortex_force.f90:43-55,121-133 instead of WENO (hard-coded there)
+    if gpu.get("vf_scheme", "weno") == "linear":
+        d.vf_order = int(param.get("orderVF", 5))
     d.dx, d.dy, d.dz = grid.dx, grid.dy, grid.dz
     d.idx2, d.idy2, d.idz2 = grid.idx2, grid.idy2, grid.idz2
     d.dx2 = grid.dx ** 2
@@ -198,7 +202,7 @@ class LES(object):
         s = nat.NylesMgStats()
         nat.check(self.lib.nyles_model_mg_stats(self._h, ctypes.byref(s)))
         return {"nite": s.nite, "res": s.res, "solves": s.solves, "vcycles": s.vcycles,
-                "not_converged": s.not_converged}
+                "not_converged": s.not_converged, "nonfinite": s.nonfinite}
 
     def update_stats(self):
         """Append the multigrid statistics and max|div| of the state to `stats`
@@ -240,7 +244,10 @@ class LES(object):
             raise RuntimeError("the parameter `forced` is set but no forcing is attached (model.forcing = ...)")
 
     def forward(self, t, dt):
-        """One time step (core/model_les.py:147-149). Returns the blow-up flag.
+        """One time step (core/model_les.py:147-149). Returns the blow-up flag: True
+        when a pressure solve of an eagerly run step met a non-finite divergence (the
+        reference's flag is never set). Replayed steps return False; Nyles.run checks
+        them with the CFL reduction.
 
         With graphs on (gpu parameter `graphs`), the second consecutive call with the same
         dt captures the step into a CUDA graph, and every later call with that dt replays
@@ -260,8 +267,10 @@ class LES(object):
         self._last_dt = dt
         rc = self.lib.nyles_model_forward(self._h, float(t), dt, nat.stream_ptr())
         self._raise_forcing_error()
-        nat.check(rc)
         self._first_step_pending = False
+        if rc == nat.NYLES_BLOWUP:   # a projection met a non-finite divergence
+            return True
+        nat.check(rc)
         return False
 
     def profile(self, enable=True):

@@ -98,7 +98,11 @@ class Nyles(object):
         dt_hist = float(self.param.get("timestep_history", 0.0))
         t_next_hist = dt_hist
         self.kdiss = []
-        self.model.diagnose_var(self.model.state)   # core/nyles.py:122
+        blowup = False
+        try:
+            self.model.diagnose_var(self.model.state)   # core/nyles.py:122
+        except nat.BlowUp:
+            blowup = True
         if self.IO is not None:                      # core/nyles.py:131-139
             if verbose:
                 print("Creating output file:", self.IO.hist_path)
@@ -110,8 +114,8 @@ class Nyles(object):
                     print("Backing up script to:", self.IO.script_path)
                 self.IO.backup_scriptfile(script)
         realtime0 = time.time()
-        blowup = False
-        while True:
+        nonfinite_seen = self.model.mg_stats()["nonfinite"] if hasattr(self.model, "mg_stats") else 0
+        while not blowup:
             try:
                 dt = self.compute_dt()
             except nat.BlowUp:
@@ -120,9 +124,20 @@ class Nyles(object):
                     self.IO.t_next_hist = t
                     self.IO.write(self.model.state, t, n)
                 break
-            self.model.forward(t, dt)
+            blowup = self.model.forward(t, dt)
+            if not blowup and self.blowup_check and getattr(self.model, "graph", None) is not None:
+                # a replayed step returns no flag: its solves count non-finite norms on the
+                # device (one small read-back per step)
+                nonfinite = self.model.mg_stats()["nonfinite"]
+                blowup = nonfinite > nonfinite_seen
+                nonfinite_seen = nonfinite
             t += dt
             n += 1
+            if blowup:
+                if self.IO is not None:
+                    self.IO.t_next_hist = t
+                    self.IO.write(self.model.state, t, n)
+                break
             if t >= t_next_hist:                     # core/nyles.py:166-171
                 Kdiss = self.diag.compute()
                 self.kdiss.append((t, Kdiss))

@@ -56,10 +56,18 @@ class Result:
     done: float
     cells: int
     mg_vcycles: int = 0
+    # "ok"; "refused" (footprint above the whole budget, never admitted); "blowup" (a
+    # non-finite velocity or pressure solve); "not_converged" (finished, but some
+    # pressure solve stopped at mg_maxite above the tolerance)
+    status: str = "ok"
 
     @property
     def latency(self):
         return self.done - self.arrival
+
+    @property
+    def completed(self):
+        return self.status in ("ok", "not_converged")
 
 
 def make_requests(count=96, rate=20.0, seed=5, steps=300, sizes=(32, 48, 64, 96, 128)):
@@ -189,6 +197,25 @@ class Run:
     def vcycles(self):
         return self.nyl.model.mg_stats()["vcycles"]
 
+    def outcome(self):
+        """(status, V-cycles) of a finished run: "blowup" when a pressure solve met a
+        non-finite norm or the final velocity is not finite, "not_converged" when a
+        solve stopped at maxite above the tolerance, else "ok"."""
+        from . import _native as nat
+        m = self.nyl.model
+        s = m.mg_stats()
+        status = "ok"
+        if s["nonfinite"] > 0:
+            status = "blowup"
+        else:
+            try:
+                m.max_U2()
+            except nat.BlowUp:
+                status = "blowup"
+        if status == "ok" and s["not_converged"] > 0:
+            status = "not_converged"
+        return status, s["vcycles"]
+
     def final_state(self):
         st = self.nyl.model.state
         return {s: st.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k", "p")}
@@ -244,10 +271,17 @@ class ServingEngine:
             while nxt < len(pending) and (not realtime or pending[nxt].arrival <= now):
                 queue.append(pending[nxt])
                 nxt += 1
-            # admission: FIFO while the footprint fits
+            # admission: FIFO while the footprint fits; a request larger than the whole
+            # budget is refused at once (it could never fit) and the queue moves on
             while queue:
                 req = queue[0]
                 need = footprint_bytes(req.case, req.n, self.precision)
+                if need > self.budget:
+                    queue.pop(0)
+                    now = self.clock() - t0
+                    results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
+                                          now, now, req.n ** 3, 0, "refused"))
+                    continue
                 if self.used + need > self.budget and active:
                     break
                 queue.pop(0)
@@ -270,8 +304,9 @@ class ServingEngine:
                 if run.finished():
                     done = self.clock() - t0
                     req = run.req
+                    status, vcycles = run.outcome()
                     results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
-                                          run.admitted, done, req.n ** 3, run.vcycles()))
+                                          run.admitted, done, req.n ** 3, vcycles, status))
                     if keep_states:
                         states[req.rid] = run.final_state()
                     self.used -= run.need
@@ -374,8 +409,14 @@ def replay_queue(requests, duration):
 
 
 def summarize(results, makespan=None):
-    lat = np.array([r.latency for r in results])
-    cells = sum(r.cells * r.steps for r in results)
-    span = makespan if makespan is not None else (max(r.done for r in results) - min(r.arrival for r in results))
-    return {"runs": len(results), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "mean_s": float(lat.mean()), "makespan_s": float(span), "cell_steps_per_s": cells / span}
+    """Latency percentiles and throughput over the completed runs (status "ok" or
+    "not_converged"); refused and blown-up runs are counted, not timed."""
+    done = [r for r in results if r.completed]
+    counts = {k: sum(1 for r in results if r.status == k) for k in ("refused", "blowup", "not_converged")}
+    if not done:
+        return dict(runs=0, **counts)
+    lat = np.array([r.latency for r in done])
+    cells = sum(r.cells * r.steps for r in done)
+    span = makespan if makespan is not None else (max(r.done for r in done) - min(r.arrival for r in done))
+    return dict({"runs": len(done), "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                 "mean_s": float(lat.mean()), "makespan_s": float(span), "cell_steps_per_s": cells / span}, **counts)

@@ -1,6 +1,6 @@
 // CPU ORACLE — test infrastructure only.
 //
-// A single-threaded C++ restatement of the Nyles LES time step (pvthinker/Nyles),
+// A C++ restatement of the Nyles LES time step (pvthinker/Nyles),
 // used by the test-suite and by bench.py's CPU-baseline leg as the checker of the
 // CUDA path. It is never linked into, called by, or shipped with the product library.
 //
@@ -23,6 +23,13 @@
 // Layout: every model field is a C-order array of shape (Nz, Ny, Nx) — the
 // reference's `view('i')` — including halos in periodic directions. The reference's
 // transposed views are expressed as strided views of that one array.
+//
+// Threads: the outer loop of each stencil and multigrid sweep may be split into
+// contiguous chunks run on several host threads (orc_set_threads; the environment
+// variable NYLES_ORACLE_THREADS, default 1). Every element is still computed by the
+// same expression from the same inputs and no two chunks write the same element; the
+// sums (multigrid norms, VFwork) stay sequential. Results are therefore identical for
+// every thread count.
 
 #include <cmath>
 #include <cstdint>
@@ -30,8 +37,54 @@
 #include <vector>
 #include <string>
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
+#include <thread>
 
 namespace {
+
+// ---------------------------------------------------------------- host threads
+std::atomic<int> g_threads{0};   // 0: not read yet
+
+int oracle_threads() {
+    int n = g_threads.load();
+    if (n == 0) {
+        const char* e = std::getenv("NYLES_ORACLE_THREADS");
+        n = e ? std::atoi(e) : 1;
+        if (n <= 0) n = (int)std::thread::hardware_concurrency();
+        n = std::max(1, std::min(n, 256));
+        g_threads.store(n);
+    }
+    return n;
+}
+
+// f(lo, hi) over [0, n) in contiguous chunks, one per thread, when the loop does at
+// least 2^16 elements of work in total (`work` per index); inline otherwise
+template <class F>
+void pfor(int n, long work, F&& f) {
+    int nt = std::min(oracle_threads(), n);
+    if (nt <= 1 || (long)n * work < (1L << 16)) {
+        if (n > 0) f(0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    th.reserve(nt - 1);
+    for (int t = 1; t < nt; ++t)
+        th.emplace_back([&f, n, nt, t] { f((int)((long)n * t / nt), (int)((long)n * (t + 1) / nt)); });
+    f(0, (int)((long)n / nt));
+    for (auto& x : th) x.join();
+}
+
+// elementwise loops over [0, vol) in 4096-element blocks
+template <class F>
+void pfor_elems(long vol, F&& f) {
+    const long blk = 4096;
+    const int nb = (int)((vol + blk - 1) / blk);
+    pfor(nb, blk, [&](int b0, int b1) {
+        const long c0 = (long)b0 * blk, c1 = std::min(vol, (long)b1 * blk);
+        for (long c = c0; c < c1; ++c) f(c);
+    });
+}
 
 // ---------------------------------------------------------------- strided views
 struct V3 {
@@ -128,8 +181,9 @@ void flux1d(const double* u, const double* q, double* flux, int n) {
 // arrays in (j, i, k) convention, dims (m, n, l)
 void vortex_force_direc(const V3& U, const V3& vort, const V3& res) {
     const int m = U.n0, n = U.n1, l = U.n2;
+    pfor(m, (long)n * l, [&](int j0, int j1) {
     std::vector<double> u1d(l), q(l), flux(l);
-    for (int j = 0; j < m; ++j) {
+    for (int j = j0; j < j1; ++j) {
         for (int i = 0; i < n - 1; ++i) {
             double UU_0 = 0.0;
             for (int k = 0; k < l; ++k) {
@@ -143,13 +197,15 @@ void vortex_force_direc(const V3& U, const V3& vort, const V3& res) {
             for (int k = 0; k < l; ++k) res(j, i, k) = res(j, i, k) - flux[k];
         }
     }
+    });
 }
 
 // core/fortran_vortex_force.f90:87-165 (WENO branch)
 void vortex_force_flip(const V3& U, const V3& vort, const V3& res) {
     const int m = U.n0, n = U.n1, l = U.n2;
+    pfor(m, (long)n * l, [&](int j0, int j1) {
     std::vector<double> u1d(n), q(n), flux(n);
-    for (int j = 0; j < m; ++j) {
+    for (int j = j0; j < j1; ++j) {
         for (int k = 0; k < l - 1; ++k) {
             double UU_0 = 0.0;
             for (int i = 0; i < n; ++i) {
@@ -163,20 +219,121 @@ void vortex_force_flip(const V3& U, const V3& vort, const V3& res) {
             for (int i = 0; i < n; ++i) res(j, i, k) = res(j, i, k) + flux[i];
         }
     }
+    });
+}
+
+// core/interpolate.f90:3-112 (the vortex-force interpolation) in its own 1-based
+// indexing: vU[1..n], qp[0..n-1], qm[1..n] (index 0 of vU and qm unused). The
+// coefficients are REAL(4) literals widened to double. Entries the Fortran leaves
+// unset are left as they are (never read by the callers).
+void interpolate_vf(const double* vU, double* qp, double* qm, int order, int n) {
+    const double c1 = (double)(-1.0f / 6.0f), c2 = (double)(5.0f / 6.0f), c3 = (double)(2.0f / 6.0f);
+    const double e1 = (double)(-1.0f / 12.0f), e2 = (double)(7.0f / 12.0f);
+    const double b1 = (double)(2.0f / 60.0f), b2 = (double)(-13.0f / 60.0f), b3 = (double)(47.0f / 60.0f),
+                 b4 = (double)(27.0f / 60.0f), b5 = (double)(-3.0f / 60.0f);
+    int i;
+    if (order == 5) {
+        qp[0] = 0.0;
+        i = 1; qp[i] = vU[i]; qm[i] = vU[i];
+        i = 2;
+        qp[i] = c1 * vU[i - 1] + c2 * vU[i] + c3 * vU[i + 1];
+        qm[i] = c3 * vU[i - 1] + c2 * vU[i] + c1 * vU[i + 1];
+        for (i = 3; i <= n - 3; ++i) {
+            qp[i] = b1 * vU[i - 2] + b2 * vU[i - 1] + b3 * vU[i] + b4 * vU[i + 1] + b5 * vU[i + 2];
+            qm[i] = b5 * vU[i - 2] + b4 * vU[i - 1] + b3 * vU[i] + b2 * vU[i + 1] + b1 * vU[i + 2];
+        }
+        i = n - 2;
+        qp[i] = c1 * vU[i - 1] + c2 * vU[i] + c3 * vU[i + 1];
+        qm[i] = c3 * vU[i - 1] + c2 * vU[i] + c1 * vU[i + 1];
+        i = n - 1; qp[i] = vU[i]; qm[i] = vU[i];
+        qm[n] = vU[n];
+    } else if (order == 3) {
+        qp[0] = 0.0;
+        i = 1; qp[i] = vU[i]; qm[i] = vU[i];
+        for (i = 2; i <= n - 2; ++i) {
+            qp[i] = c1 * vU[i - 1] + c2 * vU[i] + c3 * vU[i + 1];
+            qm[i] = c3 * vU[i - 1] + c2 * vU[i] + c1 * vU[i + 1];
+        }
+        i = n - 1; qp[i] = vU[i]; qm[i] = vU[i];
+        qm[n] = vU[n];
+    } else if (order == 1) {
+        qp[0] = 0.0;
+        for (i = 1; i <= n - 1; ++i) { qp[i] = vU[i]; qm[i] = vU[i]; }
+        qm[n] = vU[n];
+    } else if (order == 2) {
+        qm[1] = 0.5 * vU[1];
+        for (i = 2; i <= n; ++i) qm[i] = 0.5 * (vU[i - 1] + vU[i]);
+    } else if (order == 4) {
+        i = 1; qm[i] = e2 * (vU[i]) + e1 * (vU[i + 1]);
+        i = 2; qm[i] = e2 * (vU[i - 1] + vU[i]) + e1 * (vU[i + 1]);
+        for (i = 3; i <= n - 1; ++i) qm[i] = e2 * (vU[i - 1] + vU[i]) + e1 * (vU[i - 2] + vU[i + 1]);
+        i = n; qm[i] = e2 * (vU[i - 1] + vU[i]) + e1 * (vU[i - 2]);
+    }
+}
+
+// core/fortran_vortex_force.f90:43-55 (direc) and :121-133 (flip), the linear branch the
+// reference never takes (`linear = .false.`): the vorticity of the line, unshifted, is
+// interpolated with core/interpolate.f90 of order `order`; odd orders upwind qp/qm with
+// the positive/negative parts of the doubly averaged velocity, even orders add the
+// interpolated vorticity alone (as written there). `sign` = -1 for direc, +1 for flip;
+// the two products are applied one after the other, in the Fortran statement order.
+void vf_linear_line(const double* U0, const double* U1, long su, const double* vort, long sv, double* res, long sr,
+                    int len, int order, int sign, std::vector<double>& vU, std::vector<double>& qp,
+                    std::vector<double>& qm, std::vector<double>& up, std::vector<double>& um) {
+    double UU_0 = 0.0;
+    for (int k = 1; k <= len; ++k) {
+        double UU_1 = 0.5 * (U0[(k - 1) * su] + U1[(k - 1) * su]);
+        vU[k] = vort[(k - 1) * sv];
+        double Ui = 0.5 * (UU_0 + UU_1);
+        double UU = std::fabs(Ui);
+        up[k] = 0.5 * (Ui + UU);
+        um[k] = 0.5 * (Ui - UU);
+        UU_0 = UU_1;
+    }
+    interpolate_vf(vU.data(), qp.data(), qm.data(), order, len);
+    for (int k = 1; k <= len; ++k) {
+        double& r = res[(k - 1) * sr];
+        if (order % 2 == 0) r = (sign < 0) ? r - qm[k] : r + qm[k];
+        else r = (sign < 0) ? r - qp[k - 1] * up[k] - qm[k] * um[k] : r + qp[k - 1] * up[k] + qm[k] * um[k];
+    }
+}
+
+void vortex_force_direc_linear(const V3& U, const V3& vort, const V3& res, int order) {
+    const int m = U.n0, n = U.n1, l = U.n2;
+    pfor(m, (long)n * l, [&](int j0, int j1) {
+    std::vector<double> vU(l + 1), qp(l + 1, 0.0), qm(l + 1, 0.0), up(l + 1), um(l + 1);
+    for (int j = j0; j < j1; ++j)
+        for (int i = 0; i < n - 1; ++i)
+            vf_linear_line(&U(j, i, 0), &U(j, i + 1, 0), U.s2, &vort(j, i, 0), vort.s2, &res(j, i, 0), res.s2, l,
+                           order, -1, vU, qp, qm, up, um);
+    });
+}
+
+void vortex_force_flip_linear(const V3& U, const V3& vort, const V3& res, int order) {
+    const int m = U.n0, n = U.n1, l = U.n2;
+    pfor(m, (long)n * l, [&](int j0, int j1) {
+    std::vector<double> vU(n + 1), qp(n + 1, 0.0), qm(n + 1, 0.0), up(n + 1), um(n + 1);
+    for (int j = j0; j < j1; ++j)
+        for (int k = 0; k < l - 1; ++k)
+            vf_linear_line(&U(j, 0, k), &U(j, 0, k + 1), U.s1, &vort(j, 0, k), vort.s1, &res(j, 0, k), res.s1, n,
+                           order, +1, vU, qp, qm, up, um);
+    });
 }
 
 // ---------------------------------------------------------------- tracer flux
 // core/fortran_upwind.f90:3-87 (WENO branch), dims (l, m, n), direction = last index
 void upwind(const V3& trac, const V3& u, const V3& dtrac) {
     const int l = trac.n0, m = trac.n1, n = trac.n2;
+    pfor(l, (long)m * n, [&](int k0, int k1) {
     std::vector<double> up(n), phi(n), flux(n);
-    for (int k = 0; k < l; ++k)
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j) {
             for (int i = 0; i < n; ++i) { up[i] = u(k, j, i); phi[i] = trac(k, j, i); }
             flux1d(up.data(), phi.data(), flux.data(), n);
             dtrac(k, j, 0) = dtrac(k, j, 0) - flux[0];
             for (int i = 1; i < n; ++i) dtrac(k, j, i) = dtrac(k, j, i) + flux[i - 1] - flux[i];
         }
+    });
 }
 
 // core/interpolate_tracer.f90:3-116 on one line of n values (0-based here; the source is
@@ -220,8 +377,9 @@ void interpolate_tracer(const double* q, double* qp, double* qm, int order, int 
 // qp(i); the last face carries no flux.
 void upwind_linear(const V3& trac, const V3& u, const V3& dtrac, int order) {
     const int l = trac.n0, m = trac.n1, n = trac.n2;
+    pfor(l, (long)m * n, [&](int k0, int k1) {
     std::vector<double> up(n), um(n), phi(n), qp(n, 0.0), qm(n, 0.0);
-    for (int k = 0; k < l; ++k)
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j) {
             for (int i = 0; i < n; ++i) {
                 double uu = std::fabs(u(k, j, i));
@@ -239,18 +397,21 @@ void upwind_linear(const V3& trac, const V3& u, const V3& dtrac, int order) {
             fx = 0.0;
             dtrac(k, j, n - 1) = dtrac(k, j, n - 1) + fxm - fx;
         }
+    });
 }
 
 // ---------------------------------------------------------------- vorticity
 // core/fortran_vorticity.f90:2-28
 void vorticity_k(const V3& ui, const V3& uj, const V3& wk) {
     const int l = ui.n0, m = ui.n1, n = ui.n2;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m - 1; ++j) {
             for (int i = 0; i < n - 1; ++i)
                 wk(k, j, i) = uj(k, j, i + 1) - uj(k, j, i) - ui(k, j + 1, i) + ui(k, j, i);
             wk(k, j, n - 1) = 0.0;
         }
+    });
 }
 
 // ---------------------------------------------------------------- kinetic energy
@@ -258,36 +419,43 @@ void vorticity_k(const V3& ui, const V3& uj, const V3& wk) {
 void kin(const V3& u, const V3& ke, double ds2) {
     const int l = u.n0, m = u.n1, n = u.n2;
     double cff2 = 0.5 * ds2;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j)
             for (int i = 1; i < n; ++i) {
                 double a = u(k, j, i), b = u(k, j, i - 1);
                 ke(k, j, i) = ke(k, j, i) + cff2 * 0.5 * (a * a + b * b);
             }
+    });
 }
 
 // ---------------------------------------------------------------- Bernoulli / div
 // core/fortran_bernoulli.f90:2-26
 void gradke(const V3& ke, const V3& du) {
     const int l = ke.n0, m = ke.n1, n = ke.n2;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j)
             for (int i = 0; i < n - 1; ++i)
                 du(k, j, i) = du(k, j, i) - (ke(k, j, i + 1) - ke(k, j, i));
+    });
 }
 // core/fortran_bernoulli.f90:29-58
 void gradkeandb(const V3& ke, const V3& b, const V3& du, double dz) {
     const int l = ke.n0, m = ke.n1, n = ke.n2;
     double cff = 0.5 * dz;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j)
             for (int i = 0; i < n - 1; ++i)
                 du(k, j, i) = du(k, j, i) - (ke(k, j, i + 1) - ke(k, j, i)) + cff * (b(k, j, i + 1) + b(k, j, i));
+    });
 }
 // core/fortran_bernoulli.f90:61-97
 void divop(const V3& d, const V3& u, int iflag) {
     const int l = d.n0, m = d.n1, n = d.n2;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j) {
             if (iflag > 0) {
                 d(k, j, 0) = d(k, j, 0) + u(k, j, 0);
@@ -297,11 +465,13 @@ void divop(const V3& d, const V3& u, int iflag) {
                 for (int i = 1; i < n; ++i) d(k, j, i) = (u(k, j, i) - u(k, j, i - 1));
             }
         }
+    });
 }
 // core/fortran_dissipation.f90:2-35
 void add_laplacian(const V3& phi, const V3& dphi, double coef) {
     const int l = phi.n0, m = phi.n1, n = phi.n2;
-    for (int k = 0; k < l; ++k)
+    pfor(l, (long)m * n, [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < m; ++j) {
             double fxm = 0.0, fx;
             for (int i = 0; i < n - 1; ++i) {
@@ -312,6 +482,7 @@ void add_laplacian(const V3& phi, const V3& dphi, double coef) {
             fx = 0.0;
             dphi(k, j, n - 1) = dphi(k, j, n - 1) + coef * (fx - fxm);
         }
+    });
 }
 
 V3 contig(double* p, int l, int m, int n) { return V3{p, l, m, n, (long)m * n, n, 1}; }
@@ -353,12 +524,15 @@ void mg_fill(const Mg& mg, const MgLevel& g, double* a) {
     auto copyblock = [&](int di0, int di1, int dj0, int dj1, int dk0, int dk1, int si0, int sj0, int sk0) {
         int ni = di1 - di0 + 1, nj = dj1 - dj0 + 1, nk = dk1 - dk0 + 1;
         tmp.resize((size_t)ni * nj * nk);
-        size_t c = 0;
-        for (int k = 0; k < nk; ++k) for (int j = 0; j < nj; ++j) for (int i = 0; i < ni; ++i)
-            tmp[c++] = A(si0 + i, sj0 + j, sk0 + k);
-        c = 0;
-        for (int k = 0; k < nk; ++k) for (int j = 0; j < nj; ++j) for (int i = 0; i < ni; ++i)
-            A(di0 + i, dj0 + j, dk0 + k) = tmp[c++];
+        const long plane = (long)ni * nj;
+        pfor(nk, plane, [&](int k0, int k1) {
+            for (int k = k0; k < k1; ++k) { size_t c = (size_t)k * plane;
+                for (int j = 0; j < nj; ++j) for (int i = 0; i < ni; ++i) tmp[c++] = A(si0 + i, sj0 + j, sk0 + k); }
+        });
+        pfor(nk, plane, [&](int k0, int k1) {
+            for (int k = k0; k < k1; ++k) { size_t c = (size_t)k * plane;
+                for (int j = 0; j < nj; ++j) for (int i = 0; i < ni; ++i) A(di0 + i, dj0 + j, dk0 + k) = tmp[c++]; }
+        });
     };
     bool ex = mg.xper, ey = mg.yper;
     // neighbour ranks (mod_tiles.f90:59-106): for one rank a neighbour exists (== myrank)
@@ -386,18 +560,22 @@ void fsmoother3d(const Mg& mg, MgLevel& g) {
     const double* b = g.b.data(); const double* idiag = g.idiag.data();
     const double omega = mg.omega, cff1 = 1.0 - omega;
     const long pi = g.pi, pj = g.pj;
-    for (int k = nh; k <= nz + 1 - nh; ++k)
+    pfor(nz + 2 - 2 * nh, (long)(nx + 2) * (ny + 2), [&](int k0, int k1) {
+    for (int k = nh + k0; k < nh + k1; ++k)
         for (int j = 0; j <= ny + 1; ++j)
             for (int i = 0; i <= nx + 1; ++i) {
                 long c = g.at(i, j, k);
                 y[c] = (cff1 * x[c] + omega * ((x[c - 1] + x[c + 1] + x[c - pi] + x[c + pi] + x[c - pj] + x[c + pj]) - b[c]) * idiag[c]);
             }
-    for (int k = nh + 1; k <= nz - nh; ++k)
+    });
+    pfor(nz - 2 * nh, (long)nx * ny, [&](int k0, int k1) {
+    for (int k = nh + 1 + k0; k < nh + 1 + k1; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx; ++i) {
                 long c = g.at(i, j, k);
                 x[c] = (cff1 * y[c] + omega * ((y[c - 1] + y[c + 1] + y[c - pi] + y[c + pi] + y[c - pj] + y[c + pj]) - b[c]) * idiag[c]);
             }
+    });
 }
 
 // basicoperators.f90:300-323
@@ -406,18 +584,21 @@ void fresidual3d(MgLevel& g) {
     const double* x = g.x.data(); const double* b = g.b.data(); const double* diag = g.diag.data();
     double* r = g.r.data(); const int* msk = g.msk.data();
     const long pi = g.pi, pj = g.pj;
-    for (int k = 1 + nh; k <= nz - nh; ++k)
+    pfor(nz - 2 * nh, (long)nx * ny, [&](int k0, int k1) {
+    for (int k = 1 + nh + k0; k < 1 + nh + k1; ++k)
         for (int j = 1; j <= ny; ++j)
             for (int i = 1; i <= nx; ++i) {
                 long c = g.at(i, j, k);
                 r[c] = (double)msk[c] * (b[c] + diag[c] * x[c] - (x[c - 1] + x[c + 1] + x[c - pi] + x[c + pi] + x[c - pj] + x[c + pj]));
             }
+    });
 }
 
 // basicoperators.f90:32-60
 void frestrict3d(const MgLevel& f, const double* xf, MgLevel& c, double* xc, const double* coef) {
     const int nh = f.nh;
-    for (int kc = 1 + nh; kc <= c.nz - nh; ++kc) {
+    pfor(c.nz - 2 * nh, 8L * c.nx * c.ny, [&](int q0, int q1) {
+    for (int kc = 1 + nh + q0; kc < 1 + nh + q1; ++kc) {
         int k = 1 + nh + (kc - 1 - nh) * 2;
         for (int jc = 1; jc <= c.ny; ++jc) {
             int j = 1 + (jc - 1) * 2;
@@ -430,13 +611,16 @@ void frestrict3d(const MgLevel& f, const double* xf, MgLevel& c, double* xc, con
             }
         }
     }
+    });
 }
 
 // basicoperators.f90:173-231
 void fprolong3d(MgLevel& f, double* xf, const double* coef, const MgLevel& c, const double* xcp) {
     const int nh = f.nh;
     auto XC = [&](int a, int bb, int cc) { return xcp[c.at(a, bb, cc)]; };
-    for (int k = 1 + nh; k <= f.nz - nh; k += 2) {
+    const int npairs = (f.nz - 2 * nh + 1) / 2;   // k = 1 + nh + 2q, q < npairs
+    pfor(npairs, 2L * f.nx * f.ny, [&](int q0, int q1) {
+    for (int k = 1 + nh + 2 * q0; k < 1 + nh + 2 * q1; k += 2) {
         int kc = nh + (k + 1 - nh) / 2;
         for (int j = 1; j <= f.ny - 1; j += 2) {
             int jc = (j + 1) / 2;
@@ -474,6 +658,7 @@ void fprolong3d(MgLevel& f, double* xf, const double* coef, const MgLevel& c, co
             }
         }
     }
+    });
 }
 
 // basicoperators.f90:422-440
@@ -673,6 +858,7 @@ struct Model {
     // set (q = 0 for b): the reference's rhs never passes `last` to rhstrac
     double kappa[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}; int trdiff_mask = 0;
     int tr_order = 0;     // 0 WENO (the reference); 1..5 the linear branch of order orderA
+    int vf_order = 0;     // vortex force: 0 WENO (the reference); 1..5 the linear branch (orderVF)
     bool lfam3_first = true;
     long vol;
     std::vector<std::vector<double>> f;    // state fields (14 + ntr)
@@ -701,7 +887,9 @@ void model_fill(const Model& M, double* a) {
         if (c >= nh + n) return c - n;
         return c;
     };
-    for (int k = 0; k < N[0]; ++k)
+    // halo cells only are written, interior cells only are read
+    pfor(N[0], (long)N[1] * N[2], [&](int k0, int k1) {
+    for (int k = k0; k < k1; ++k)
         for (int j = 0; j < N[1]; ++j)
             for (int i = 0; i < N[2]; ++i) {
                 bool inside = (k >= lo[0] && k < hi[0]) && (j >= lo[1] && j < hi[1]) && (i >= lo[2] && i < hi[2]);
@@ -710,6 +898,7 @@ void model_fill(const Model& M, double* a) {
                 long s = ((long)src(0, k) * N[1] + src(1, j)) * N[2] + src(2, i);
                 a[dst] = a[s];
             }
+    });
 }
 
 V3 fv(Model& M, int fld, char d) { return view(M.f[fld].data(), M.N, d); }
@@ -734,8 +923,13 @@ void model_vortex_force(Model& M, std::vector<std::vector<double>>& ds) {
         V3 U_i = ffv(M, CX + dirn(i), j);
         V3 U_k = ffv(M, CX + dirn(k), j);
         V3 w_j = ffv(M, WX + dirn(j), j);
-        vortex_force_direc(U_k, w_j, u_i);
-        vortex_force_flip(U_i, w_j, u_k);
+        if (M.vf_order > 0) {
+            vortex_force_direc_linear(U_k, w_j, u_i, M.vf_order);
+            vortex_force_flip_linear(U_i, w_j, u_k, M.vf_order);
+        } else {
+            vortex_force_direc(U_k, w_j, u_i);
+            vortex_force_flip(U_i, w_j, u_k);
+        }
     }
 }
 
@@ -798,7 +992,8 @@ void model_U_from_u(Model& M) {
     const double c[3] = {M.idx2, M.idy2, M.idz2};
     for (int d = 0; d < 3; ++d) {
         const double* u = M.f[UX + d].data(); double* U = M.f[CX + d].data();
-        for (long q = 0; q < M.vol; ++q) U[q] = u[q] * c[d];
+        const double cd = c[d];
+        pfor_elems(M.vol, [&](long q) { U[q] = u[q] * cd; });
     }
 }
 
@@ -916,17 +1111,17 @@ void model_forward(Model& M, double t, double dt) {
         auto& ds0 = M.reg[0]; auto& ds1 = M.reg[1]; auto& ds2 = M.reg[2];
         model_rhs_at(M, 0, false, t);
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data();
-            for (long c = 0; c < M.vol; ++c) s[c] = s[c] + dt * a[c]; }
+            pfor_elems(M.vol, [&](long c) { s[c] = s[c] + dt * a[c]; }); }
         model_diagnose(M);
         model_rhs_at(M, 1, false, t + dt);
         const double c2 = dt / 4.0;
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data(); const double* b = ds1[q].data();
-            for (long c = 0; c < M.vol; ++c) s[c] = s[c] + c2 * (b[c] - 3.0 * a[c]); }
+            pfor_elems(M.vol, [&](long c) { s[c] = s[c] + c2 * (b[c] - 3.0 * a[c]); }); }
         model_diagnose(M);
         model_rhs_at(M, 2, true, t + dt * 0.5);
         const double c3 = dt / 12.0;
         for (int q = 0; q < np; ++q) { double* s = S(q); const double* a = ds0[q].data(); const double* b = ds1[q].data(); const double* e = ds2[q].data();
-            for (long c = 0; c < M.vol; ++c) s[c] = s[c] + c3 * (8.0 * e[c] - a[c] - b[c]); }
+            pfor_elems(M.vol, [&](long c) { s[c] = s[c] + c3 * (8.0 * e[c] - a[c] - b[c]); }); }
         model_diagnose(M);
     } else if (M.scheme == 0) {   // EF
         auto& ds = M.reg[0];
@@ -966,6 +1161,13 @@ void model_forward(Model& M, double t, double dt) {
 extern "C" {
 
 // --- f2py-signature kernels on contiguous arrays (dims = numpy shape) -------------
+// host threads of the parallel loops (n <= 0: all hardware threads); returns the count
+int orc_set_threads(int n) {
+    if (n <= 0) n = (int)std::thread::hardware_concurrency();
+    g_threads.store(std::max(1, std::min(n, 256)));
+    return g_threads.load();
+}
+int orc_get_threads(void) { return oracle_threads(); }
 double orc_weno3(double a, double b, double c) { return weno3(a, b, c); }
 double orc_weno5(double a, double b, double c, double d, double e) { return weno5(a, b, c, d, e); }
 void orc_flux1d(const double* u, const double* q, double* flux, int n) { flux1d(u, q, flux, n); }
@@ -1056,6 +1258,16 @@ void orc_model_vortex_force(void* h, int reg) {
     Model* M = (Model*)h; for (auto& a : M->reg[reg]) std::fill(a.begin(), a.end(), 0.0); model_vortex_force(*M, M->reg[reg]); }
 void orc_model_project(void* h) { model_project(*(Model*)h); }
 void orc_model_set_tracer_order(void* h, int order) { ((Model*)h)->tr_order = order; }
+void orc_model_set_vf_order(void* h, int order) { ((Model*)h)->vf_order = order; }
+// the f2py kernels with their `order` argument honoured (0 = WENO)
+void orc_vortex_force_direc_order(double* U, double* vort, double* res, int order, int m, int n, int l) {
+    V3 a = contig(U, m, n, l), b = contig(vort, m, n, l), c = contig(res, m, n, l);
+    if (order > 0) vortex_force_direc_linear(a, b, c, order); else vortex_force_direc(a, b, c);
+}
+void orc_vortex_force_flip_order(double* U, double* vort, double* res, int order, int m, int n, int l) {
+    V3 a = contig(U, m, n, l), b = contig(vort, m, n, l), c = contig(res, m, n, l);
+    if (order > 0) vortex_force_flip_linear(a, b, c, order); else vortex_force_flip(a, b, c);
+}
 void orc_upwind_linear(double* trac, double* u, double* dtrac, int order, int l, int m, int n) {
     upwind_linear(contig(trac, l, m, n), contig(u, l, m, n), contig(dtrac, l, m, n), order); }
 void orc_model_set_tracer_diffusion(void* h, const double* kappa, int mask) {

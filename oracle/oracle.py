@@ -1,8 +1,9 @@
 """CPU oracle for the Nyles LES time step — TEST INFRASTRUCTURE ONLY.
 
-ctypes wrapper around ``oracle/_build/libnyles_oracle.so`` (a single-threaded C++
-restatement of the reference's Fortran kernels, of mgfor, and of the Python
-orchestration in core/model_les.py, core/timescheme.py, core/projection.py).
+ctypes wrapper around ``oracle/_build/libnyles_oracle.so`` (a C++ restatement of the
+reference's Fortran kernels, of mgfor, and of the Python orchestration in
+core/model_les.py, core/timescheme.py, core/projection.py; its loops may run on several
+host threads with identical results).
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg
 import this module, and only as the checker. The product path never does.
 
@@ -46,6 +47,8 @@ def lib():
         d, i, p, v = ctypes.c_double, ctypes.c_int, ctypes.c_void_p, None
         dp = ctypes.POINTER(ctypes.c_double)
         sig = {
+            "orc_set_threads": (i, [i]),
+            "orc_get_threads": (i, []),
             "orc_weno3": (d, [d, d, d]),
             "orc_weno5": (d, [d, d, d, d, d]),
             "orc_flux1d": (v, [p, p, p, i]),
@@ -90,6 +93,9 @@ def lib():
             "orc_model_set_forcing": (v, [p, p, p]),
             "orc_model_set_tracer_diffusion": (v, [p, p, i]),
             "orc_model_set_tracer_order": (v, [p, i]),
+            "orc_model_set_vf_order": (v, [p, i]),
+            "orc_vortex_force_direc_order": (v, [p, p, p, i, i, i, i]),
+            "orc_vortex_force_flip_order": (v, [p, p, p, i, i, i, i]),
             "orc_model_project": (v, [p]),
         }
         for name, (res, args) in sig.items():
@@ -98,6 +104,17 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+def set_threads(n):
+    """Host threads of the oracle's parallel loops (n <= 0: all hardware threads).
+    Results do not depend on it: the loops split into chunks that write disjoint
+    elements, and the sums stay sequential."""
+    return lib().orc_set_threads(int(n))
+
+
+def threads():
+    return lib().orc_get_threads()
 
 
 def _ptr(a):
@@ -128,6 +145,16 @@ def vortex_force_direc(U, vort, res):
 
 def vortex_force_flip(U, vort, res):
     lib().orc_vortex_force_flip(_ptr(U), _ptr(vort), _ptr(res), *res.shape)
+
+
+def vortex_force_direc_order(U, vort, res, order):
+    """core/fortran_vortex_force.f90 vortex_force_direc with `order` honoured: 0 = the
+    WENO branch (the reference's), 1..5 = its linear branch with core/interpolate.f90"""
+    lib().orc_vortex_force_direc_order(_ptr(U), _ptr(vort), _ptr(res), int(order), *res.shape)
+
+
+def vortex_force_flip_order(U, vort, res, order):
+    lib().orc_vortex_force_flip_order(_ptr(U), _ptr(vort), _ptr(res), int(order), *res.shape)
 
 
 def upwind(trac, u, dtrac):
@@ -209,7 +236,8 @@ class OracleModel:
     dx, dy, dz, idx2, idy2, idz2, fparam, visc (None = off), and optionally
     tracer_diffusion = {"b": kappa, "t0": kappa, ...} for the opt-in tracer diffusion
     on the last stage (core/tracer.py:74-76; never applied by the reference's rhs), and
-    tracer_order = 1..5 for the linear advection branch (0 = WENO, the reference).
+    tracer_order = 1..5 for the linear advection branch (0 = WENO, the reference),
+    vf_order = 1..5 for the linear vortex-force branch (0 = WENO, the reference).
     modelname "advection" is core/model_advection.py.
     """
 
@@ -242,6 +270,8 @@ class OracleModel:
             lib().orc_model_set_tracer_diffusion(self.h, kappa, mask)
         if desc.get("tracer_order", 0):
             lib().orc_model_set_tracer_order(self.h, int(desc["tracer_order"]))
+        if desc.get("vf_order", 0):
+            lib().orc_model_set_vf_order(self.h, int(desc["vf_order"]))
 
     def __del__(self):
         if getattr(self, "h", None):

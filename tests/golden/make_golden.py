@@ -1,9 +1,10 @@
 """Generate golden vectors by running the REFERENCE's own Python orchestration.
 
-Run in the development container only (it imports the reference from
-``/root/reference``; that tree does not exist where the tests run):
+Run where a checkout of the reference exists (the tests themselves never need it).
+The path of the reference's ``core`` directory comes from the first argument or from the
+environment variable NYLES_REFERENCE_CORE:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py <reference checkout>/core
 
 The reference's Python modules (core/nyles.py, core/model_les.py,
 core/timescheme.py, core/projection.py, core/mgfordriver.py, core/mpi/halo.py,
@@ -35,7 +36,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference/core"
+REF = None   # the reference's core/ directory, set by main()
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 import oracle  # noqa: E402
 
@@ -373,4 +374,7 @@ def main():
 
 
 if __name__ == "__main__":
+    REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NYLES_REFERENCE_CORE")
+    if not REF or not os.path.isfile(os.path.join(REF, "nyles.py")):
+        sys.exit("usage: make_golden.py <reference core/ directory> (or set NYLES_REFERENCE_CORE)")
     main()

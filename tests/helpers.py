@@ -15,7 +15,7 @@ DIAG = ["p", "ke", "U_i", "U_j", "U_k", "vor_i", "vor_j", "vor_k", "div"]
 def make_params(geometry="closed", modelname="LES", timestepping="RK3_SSP", n=(16, 8, 8), L=(1.0, 1.0, 1.0),
                 n_tracers=0, auto_dt=False, dt=1e-3, cfl=0.8, dt_max=1.0, rotating=False, coriolis=1.0,
                 diff_coef=None, precision="fp64", mg_tol=1e-6, mg_maxite=20, forced=False, tracer_diffusion=False,
-                tracer_scheme="weno", orderA=5):
+                tracer_scheme="weno", orderA=5, vf_scheme="weno", orderVF=5):
     from nyles_gb300 import parameters
     parameters.InextensibleDict.unfreeze()
     p = parameters.UserParameters()
@@ -40,6 +40,8 @@ def make_params(geometry="closed", modelname="LES", timestepping="RK3_SSP", n=(1
     p.gpu["tracer_diffusion"] = tracer_diffusion
     p.gpu["tracer_scheme"] = tracer_scheme
     p.discretization["orderA"] = orderA
+    p.gpu["vf_scheme"] = vf_scheme
+    p.discretization["orderVF"] = orderVF
     return p
 
 
@@ -53,11 +55,12 @@ def oracle_for(nyl):
     live = prm["gpu"].get("tracer_diffusion") or prm["modelname"] == "advection"
     trd = {k: v for k, v in prm["diff_coef"].items() if k != "u"} if live and prm["diff_coef"] else None
     order = prm["orderA"] if prm["gpu"].get("tracer_scheme") == "linear" else 0
+    vf_order = prm["orderVF"] if prm["gpu"].get("vf_scheme") == "linear" else 0
     o = oracle.OracleModel(dict(nx=prm["nx"], ny=prm["ny"], nz=prm["nz"], nh=prm["nh"], geometry=prm["geometry"],
                                 n_tracers=prm["n_tracers"], modelname=prm["modelname"],
                                 timestepping=prm["timestepping"], dx=g.dx, dy=g.dy, dz=g.dz, idx2=g.idx2,
                                 idy2=g.idy2, idz2=g.idz2, fparam=float(m.fparameter), visc=visc,
-                                tracer_diffusion=trd, tracer_order=order))
+                                tracer_diffusion=trd, tracer_order=order, vf_order=vf_order))
     o.mg_params(prm["gpu"]["mg_tol"], prm["gpu"]["mg_maxite"], prm["gpu"]["mg_omega"])
     return o
 

@@ -1,0 +1,213 @@
+"""The FP64 GPU path against the oracle on the workload configurations as specified.
+
+* Lock exchange: 64 x 32 x 32 cells in the 4 x 1 x 1 box, free-slip walls, RK3,
+  dt = 2e-3, seed 1. With dx = 2 dy = 2 dz the reference's projection (p = x dx^2,
+  core/mgfordriver.py:78) over-corrects the transverse velocity, so divergence modes grow
+  about threefold per projection and the run blows up at step 6. Steps 1-5 are compared
+  with equal V-cycle counts, and both sides must report the blow-up at the same step
+  (the GPU through NYLES_BLOWUP / the flag of forward, the oracle through its state
+  turning non-finite).
+* Taylor-Green: 64^3 for 200 steps (<= 1e-9 at the end) and 128^3 for 10 steps
+  (<= 1e-12 per step), WENO5, RK3, dt = 5e-3, relative residual 1e-10.
+* Rayleigh-Taylor at its full 256 x 256 x 512 (box 1 x 1 x 2, interface at z = 1):
+  the initial projection and one step.
+* The stratified shear case shaped as specified (L = 4 x 2 x 1, one tracer, adaptive
+  CFL 0.8) at 128 x 64 x 64, 20 steps.
+
+Per-step bar: max|GPU - oracle| / max|oracle| <= 1e-12 x steps for b, u (normalised by
+the velocity vector), p and tracers, with equal V-cycle counts. The lock-exchange and
+shear boxes are anisotropic (dx = 2 dz), where the reference's own step amplifies round-
+off: in the shear case an oracle whose initial state differs from another's by one
+unit in the last place in every cell differs from it by ~1e-11 in b and t0 after one
+step. For those two the bar is the larger of 1e-12 x steps and ten times that measured
+round-off sensitivity (two oracle runs, one perturbed), which the GPU must not exceed.
+"""
+import numpy as np
+import pytest
+
+import helpers
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TWO_PI = 6.283185307179586
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _oracle_threads():
+    import oracle
+    old = oracle.threads()
+    oracle.set_threads(0)          # every host core: results do not depend on it
+    yield
+    oracle.set_threads(old)
+
+
+def _gpu(nyl, name):
+    return nyl.model.state.get(name).view("i").double().cpu().numpy()
+
+
+def _names(ntr):
+    return helpers.PROG + ["t%d" % i for i in range(ntr)] + ["p"]
+
+
+def _perturbed_copy(nyl, fields, seed):
+    """An oracle with the same descriptor whose prognostic fields differ from `fields`
+    by one unit in the last place, up or down at random, in every cell."""
+    o = helpers.oracle_for(nyl)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    for k, v in fields.items():
+        up = rng.integers(2, size=v.shape).astype(bool)
+        o.field(k)[...] = np.where(up, np.nextafter(v, np.inf), np.nextafter(v, -np.inf))
+    return o
+
+
+def _load(nyl, o, fields):
+    helpers.load_state(nyl, o, fields)
+
+
+def _step_compare(nyl, o, oref2, steps, dt_fn, bar_per_step, sensitivity_factor=None, blowup_by=None):
+    """Advance the GPU model, the oracle and (optionally) a perturbed oracle together.
+    Returns the list of per-step errors. Stops at the first non-finite step."""
+    m = nyl.model
+    names = _names(nyl.param["n_tracers"])
+    t = 0.0
+    history = []
+    for n in range(1, steps + 1):
+        dt = dt_fn(nyl, o)
+        blow_gpu = m.forward(t, dt)
+        o.forward(t, dt)
+        if oref2 is not None:
+            oref2.forward(t, dt_fn(nyl, oref2) if blowup_by is None else dt)
+        t += dt
+        finite_o = all(np.isfinite(o.field(s)).all() for s in names)
+        finite_g = (not blow_gpu) and all(np.isfinite(_gpu(nyl, s)).all() for s in names)
+        if blowup_by is not None and not finite_o:
+            assert not finite_g, "oracle blew up at step %d, the GPU did not" % n
+            history.append((n, None))
+            return history
+        assert finite_o and finite_g, (n, finite_o, finite_g)
+        assert m.mg_stats()["nite"] == o.mg_stats()[0], n
+        errs = helpers.parity_errors(lambda s: _gpu(nyl, s), o.field, names)
+        bar = {s: bar_per_step * n for s in names}
+        if oref2 is not None:
+            sens = helpers.parity_errors(oref2.field, o.field, names)
+            for s in names:
+                bar[s] = max(bar[s], sensitivity_factor * sens[s])
+        for s in names:
+            assert errs[s] <= bar[s], (n, s, errs[s], bar[s])
+        history.append((n, errs))
+    return history
+
+
+def test_lock_exchange_as_specified_steps_and_blowup():
+    """64 x 32 x 32 in 4 x 1 x 1: steps 1-5 match, both blow up at step 6."""
+    from nyles_gb300.nyles import Nyles
+    nyl = Nyles(helpers.make_params(geometry="closed", n=(64, 32, 32), L=(4.0, 1.0, 1.0), dt=2e-3))
+    o = helpers.oracle_for(nyl)
+    fields = helpers.seeded_state(nyl, "lock", 1)
+    _load(nyl, o, fields)
+    o2 = _perturbed_copy(nyl, fields, 101)
+    nyl.model.diagnose_var(nyl.model.state)
+    o.diagnose()
+    o2.diagnose()
+    assert nyl.model.mg_stats()["nite"] == o.mg_stats()[0]
+    hist = _step_compare(nyl, o, o2, 8, lambda ny, oo: 2e-3, 1e-12, sensitivity_factor=10.0, blowup_by=True)
+    assert [n for n, e in hist if e is None] == [6]
+    assert len(hist) == 6
+    # the first steps hold the strict bar by themselves
+    for n, e in hist[:3]:
+        for s, v in e.items():
+            assert v <= 1e-12 * n, (n, s, v)
+
+
+def test_taylor_green_64_200_steps():
+    from nyles_gb300.nyles import Nyles
+    cfg = dict(geometry="perio_xyz", n=(64, 64, 64), L=(TWO_PI,) * 3, dt=5e-3, mg_tol=1e-20, mg_maxite=40)
+    nyl = Nyles(helpers.make_params(**cfg))
+    o = helpers.oracle_for(nyl)
+    _load(nyl, o, helpers.seeded_state(nyl, "tgv", 2))
+    m = nyl.model
+    m.diagnose_var(m.state)
+    o.diagnose()
+    nites_g, nites_o = [], []
+    for n in range(200):
+        m.forward(0.0, 5e-3)
+        o.forward(0.0, 5e-3)
+        nites_g.append(m.mg_stats()["nite"])
+        nites_o.append(o.mg_stats()[0])
+    assert nites_g == nites_o
+    names = _names(0)
+    errs = helpers.parity_errors(lambda s: _gpu(nyl, s), o.field, names)
+    for s in names:
+        assert errs[s] < 1e-9, (s, errs[s])
+
+
+def test_taylor_green_128_ten_steps():
+    from nyles_gb300.nyles import Nyles
+    cfg = dict(geometry="perio_xyz", n=(128, 128, 128), L=(TWO_PI,) * 3, dt=5e-3, mg_tol=1e-20, mg_maxite=40)
+    nyl = Nyles(helpers.make_params(**cfg))
+    o = helpers.oracle_for(nyl)
+    _load(nyl, o, helpers.seeded_state(nyl, "tgv", 2))
+    nyl.model.diagnose_var(nyl.model.state)
+    o.diagnose()
+    assert nyl.model.mg_stats()["nite"] == o.mg_stats()[0]
+    _step_compare(nyl, o, None, 10, lambda ny, oo: 5e-3, 1e-12)
+
+
+def test_rayleigh_taylor_full_size_one_step():
+    """256 x 256 x 512, box 1 x 1 x 2, b = +0.5 above z = 1 + eta (Fourier modes k <= 8,
+    amplitude 1e-2, seed 3), RK3, dt = 1e-3, relative residual 1e-10."""
+    import bench
+    from nyles_gb300.nyles import Nyles
+    p = bench.rt_params(256, "fp64")
+    p.discretization["global_nz"] = 512
+    p.model["Lz"] = 2.0
+    nyl = Nyles(p)
+    bench.rt_init(nyl)
+    o = helpers.oracle_for(nyl)
+    o.field("b")[...] = _gpu(nyl, "b")
+    nyl.model.diagnose_var(nyl.model.state)
+    o.diagnose()
+    assert nyl.model.mg_stats()["nite"] == o.mg_stats()[0]
+    errs = helpers.parity_errors(lambda s: _gpu(nyl, s), o.field, ["p", "u_i", "u_j", "u_k"])
+    for s, v in errs.items():
+        assert v <= 1e-12, ("initial projection", s, v)
+    _step_compare(nyl, o, None, 1, lambda ny, oo: 1e-3, 1e-12)
+
+
+def test_shear_shape_adaptive_cfl_20_steps():
+    """L = 4 x 2 x 1 at 128 x 64 x 64, one tracer, u = U0 tanh((z - 0.5)/0.05) with
+    U0 = 0.05 sqrt(5) (minimum Richardson number 0.2 at N^2 = 1), b = z, t0 = the tanh
+    profile, v and w noise of std 1e-3 (seed 4), RK3 with adaptive CFL 0.8."""
+    from nyles_gb300.nyles import Nyles
+    cfg = dict(geometry="perio_xy", n=(128, 64, 64), L=(4.0, 2.0, 1.0), n_tracers=1, auto_dt=True, cfl=0.8,
+               dt_max=1.0)
+    nyl = Nyles(helpers.make_params(**cfg))
+    g = nyl.grid
+    shape = tuple(nyl.model.state.b.view("i").shape)
+    rng = np.random.Generator(np.random.PCG64(4))
+    zb = np.broadcast_to(g.z_b.view("i").numpy(), shape)
+    zu = np.broadcast_to(g.z_vel["i"].view("i").numpy(), shape)
+    U0 = 0.05 * np.sqrt(5.0)
+    w = 1e-3 * rng.standard_normal(shape) * g.dz
+    w[-1, :, :] = 0.0
+    fields = {"u_i": U0 * np.tanh((zu - 0.5) / 0.05) * g.dx, "b": zb.copy(),
+              "t0": np.tanh((zb - 0.5) / 0.05), "u_j": 1e-3 * rng.standard_normal(shape) * g.dy, "u_k": w}
+    o = helpers.oracle_for(nyl)
+    _load(nyl, o, fields)
+    o2 = _perturbed_copy(nyl, fields, 104)
+    nyl.model.diagnose_var(nyl.model.state)
+    o.diagnose()
+    o2.diagnose()
+    dts = []
+
+    def dt_fn(ny, oo):
+        if oo is o:
+            d = ny.compute_dt()
+            assert d == pytest.approx(oo.compute_dt(True, 1.0, 0.8, 1.0), rel=1e-12)
+            dts.append(d)
+            return d
+        return oo.compute_dt(True, 1.0, 0.8, 1.0)
+
+    _step_compare(nyl, o, o2, 20, dt_fn, 1e-12, sensitivity_factor=10.0)
+    assert len(dts) == 20 and dts[0] > 10 * dts[-1]     # the CFL step follows the growing velocity

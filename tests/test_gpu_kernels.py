@@ -117,6 +117,57 @@ def test_vortex_force_f64_matches_oracle(k):
         assert helpers.relerr(got, ref) < TOL64, name
 
 
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_vortex_force_linear_matches_oracle(k, order):
+    """The linear branch of core/fortran_vortex_force.f90 (vf_order = orderVF), FP64 at
+    the kernel bar and FP32 within 1e-5 of the FP64 oracle."""
+    nat = _lib()
+    for prec in ("fp64", "mixed"):
+        cfg = dict(CONFIGS[k], vf_scheme="linear", orderVF=order, precision=prec)
+        nyl, o = _setup(cfg, 50 + k)
+        _fill_random_diagnostics(nyl, o, 60 + k)
+        m = nyl.model
+        assert m.desc.vf_order == order
+        ds = m.timescheme.registers[0]
+        ds.storage.zero_()
+        fields = nat.ptr_array([s.data_ptr() for s in m.state.scalars()])
+        dsp = nat.ptr_array([s.data_ptr() for s in ds.scalars()])
+        fn = nat.lib().nyles_vortex_force_f64 if prec == "fp64" else nat.lib().nyles_vortex_force_f32
+        nat.check(fn(ctypes.byref(m.desc), fields, dsp, nat.stream_ptr()))
+        torch.cuda.synchronize()
+        o.vortex_force(0)
+        for q, name in enumerate(["u_i", "u_j", "u_k"]):
+            got = ds.get(name).view("i").double().cpu().numpy()
+            ref = o.register(0, 1 + q)
+            assert helpers.relerr(got, ref) < (TOL64 if prec == "fp64" else 1e-5), (prec, name)
+
+
+@pytest.mark.parametrize("order", [2, 5])
+@pytest.mark.parametrize("k", [0, 1])
+def test_rhs_with_linear_vortex_force_matches_oracle(k, order):
+    nyl, o = _setup(dict(CONFIGS[k], vf_scheme="linear", orderVF=order), 70 + k)
+    _fill_random_diagnostics(nyl, o, 80 + k)
+    m = nyl.model
+    ds = m.timescheme.registers[1]
+    ds.storage.fill_(123.0)
+    m.rhs(m.state, 0.0, ds, last=True)
+    torch.cuda.synchronize()
+    o.rhs(1, True)
+    for q, name in enumerate(["b", "u_i", "u_j", "u_k"] + ["t%d" % t for t in range(nyl.param["n_tracers"])]):
+        got = ds.get(name).view("i").cpu().numpy()
+        assert helpers.relerr(got, o.register(1, q)) < TOL64, name
+
+
+def test_vf_order_out_of_range_is_refused():
+    nat = _lib()
+    nyl, o = _setup(CONFIGS[0], 1)
+    d = nat.NylesDesc.from_buffer_copy(nyl.model.desc)
+    d.vf_order = 6
+    rc = nat.lib().nyles_vortex_force_f64(ctypes.byref(d), nat.ptr_array([0] * 14), nat.ptr_array([0] * 4), None)
+    assert rc == nat.NYLES_BAD_ARG and b"vf_order" in nat.lib().nyles_last_error()
+
+
 @pytest.mark.parametrize("last", [False, True])
 @pytest.mark.parametrize("k", range(len(CONFIGS)))
 def test_rhs_f64_matches_oracle(k, last):

@@ -70,6 +70,11 @@ STEP_CASES = [
           tracer_diffusion=True), "noise"),
     (dict(geometry="closed", n=(16, 16, 16), n_tracers=1, timestepping="LFAM3", dt=1e-3,
           diff_coef={"b": 5e-3, "t0": 1e-3}, tracer_diffusion=True), "noise"),
+    # opt-in linear vortex force (core/fortran_vortex_force.f90:43-55,121-133)
+    (dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, vf_scheme="linear", orderVF=5), "noise"),
+    (dict(geometry="closed", n=(32, 16, 16), L=(2.0, 1.0, 1.0), dt=2e-3, vf_scheme="linear", orderVF=3), "lock"),
+    (dict(geometry="perio_xyz", n=(16, 16, 16), L=(6.283185307179586,) * 3, dt=5e-3, mg_tol=1e-20,
+          vf_scheme="linear", orderVF=1), "tgv"),
 ]
 
 
@@ -126,6 +131,11 @@ MIXED_CASES = [
          tracer_scheme="linear", orderA=5),
     dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
          tracer_scheme="linear", orderA=3),
+    # the linear vortex force in FP32 (k_rhs_march<float, ..., 2, ...>)
+    dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30,
+         vf_scheme="linear", orderVF=5),
+    dict(geometry="perio_xy", n=(16, 16, 32), L=(1.0, 1.0, 2.0), dt=1e-3, mg_tol=1e-20, mg_maxite=30, n_tracers=1,
+         vf_scheme="linear", orderVF=4),
 ]
 
 

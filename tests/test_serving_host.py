@@ -54,8 +54,11 @@ class FakeRun:
             FakeRun.live -= 1
         return done
 
-    def vcycles(self):
-        return 0
+    # rid -> status reported at completion (default "ok")
+    outcomes = {}
+
+    def outcome(self):
+        return FakeRun.outcomes.get(self.req.rid, "ok"), 0
 
     def final_state(self):
         return {}
@@ -108,3 +111,25 @@ def test_window_serves_shortest_remaining_work_first():
     order = [r.rid for r in sorted(results, key=lambda r: r.done)]
     assert order == sorted(range(5), key=lambda i: sizes[i])
     assert FakeRun.live == 0
+
+
+def test_oversize_request_refused_while_the_others_finish():
+    """A request whose footprint exceeds the whole budget is refused at once (it could
+    never be admitted); the others are served and release their memory; a run that blew
+    up is counted, not timed."""
+    FakeRun.live = FakeRun.peak = 0
+    FakeRun.outcomes = {3: "blowup"}
+    try:
+        reqs = [S.Request(i, "lock", 64, i, 20, 0.01 * i) for i in range(6)]
+        reqs[2] = S.Request(2, "tgv", 128, 2, 20, 0.02)
+        budget = 2.5 * S.footprint_bytes("lock", 64, "mixed")
+        assert S.footprint_bytes("tgv", 128, "mixed") > budget
+        eng = S.ServingEngine(hbm_budget_bytes=budget, device="cpu", run_factory=FakeRun)
+        results, _ = eng.serve(reqs, realtime=False)
+    finally:
+        FakeRun.outcomes = {}
+    status = {r.rid: r.status for r in results}
+    assert status == {0: "ok", 1: "ok", 2: "refused", 3: "blowup", 4: "ok", 5: "ok"}
+    assert eng.used == 0 and FakeRun.live == 0 and eng.peak_used <= budget
+    summary = S.summarize(results)
+    assert summary["runs"] == 4 and summary["refused"] == 1 and summary["blowup"] == 1
