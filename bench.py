@@ -63,6 +63,9 @@ def parse():
     ap.add_argument("--no-eager", action="store_true", help="skip the eager (no graph) timing beside the headline")
     ap.add_argument("--accuracy-steps", type=int, default=100,
                     help="steps of the mixed-vs-FP64 error check (0 skips it)")
+    ap.add_argument("--configs", action="store_true",
+                    help="instead of the headline: FP64 and mixed throughput, V-cycles and mixed-vs-FP64 error of "
+                         "each workload configuration (lock exchange, Taylor-Green, Rayleigh-Taylor, shear)")
     return ap.parse_args()
 
 
@@ -436,11 +439,13 @@ def time_serving(a):
     return out
 
 
-def oracle_rt(n):
-    """The CPU oracle (single-threaded C++ restatement of the reference's numerics) set
-    up with the Rayleigh-Taylor workload at n^3 and projected once."""
+def oracle_rt(n, threads=1):
+    """The CPU oracle (C++ restatement of the reference's numerics, its loops on
+    `threads` host threads; 0 = all) set up with the Rayleigh-Taylor workload at n^3 and
+    projected once."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
+    oracle.set_threads(threads)
     import numpy as np
     from nyles_gb300 import grid as grid_module
     from nyles_gb300 import topology as topo
@@ -457,52 +462,56 @@ def oracle_rt(n):
     return o
 
 
-def cpu_baseline(nsample=128, steps=3):
-    """The oracle on one host core: `steps` RK3 steps of the workload at nsample^3."""
-    o = oracle_rt(nsample)
+def cpu_baseline(nsample=256, steps=1):
+    """The oracle on one host core (the reference runs one thread per subdomain):
+    `steps` RK3 steps of the workload at nsample^3 after its initial projection."""
+    o = oracle_rt(nsample, threads=1)
     t0 = time.perf_counter()
     for _ in range(steps):
         o.forward(0.0, 1e-3)
     el = time.perf_counter() - t0
     return {"value": nsample ** 3 * steps / el, "unit": "cell-steps/s", "cores": 1, "kind": "port",
             "sample": "oracle (C++ restatement of the reference numerics, 1 thread) on the same Rayleigh-Taylor "
-                      "setup at %d^3, %d RK3 steps, %.1f s" % (nsample, steps, el)}
+                      "setup at %d^3, %d RK3 step(s), %.1f s" % (nsample, steps, el)}
 
 
 # ------------------------------------------------------------------ reference arm
-def _ref_worker(args):
-    n, warmup, steps = args
-    o = oracle_rt(n)
-    for _ in range(warmup):
-        o.forward(0.0, 1e-3)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        o.forward(0.0, 1e-3)
-    return n ** 3 * steps, time.perf_counter() - t0
+REFERENCE_BUDGET_S = 150.0   # bound of the timed steps of the reference arm
 
 
 def run_reference(a, rank, world):
-    """The reference's numerics on the host cores: one single-threaded oracle per core
-    (the reference runs one thread per subdomain), each on the workload at 64^3, W
-    untimed and K timed RK3 steps; value = all cells x K / the slowest worker's time."""
+    """The reference's numerics on the host cores, on this arm's workload (the same
+    grid, setup and solver tolerance): the oracle, its stencil and multigrid sweeps split
+    over every host thread (the reference would run one MPI rank per core on as many
+    subdomains; one subdomain on all cores is the same machine's CPU throughput for this
+    grid). One untimed step, then up to K timed RK3 steps, stopped early once
+    REFERENCE_BUDGET_S seconds have passed (each step of the 256^3 grid takes seconds);
+    value = cells x timed steps / their time."""
     if rank != 0:
         return
-    import multiprocessing as mp
-    ncores = os.cpu_count() or 1
-    n = 64 if a.n >= 64 else a.n
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(ncores) as pool:
-        res = pool.map(_ref_worker, [(n, a.warmup, a.steps)] * ncores)
-    el = max(r[1] for r in res)
-    value = float(sum(r[0] for r in res) / el)
+    threads = os.cpu_count() or 1
+    n = a.n
+    o = oracle_rt(n, threads=0)
+    for _ in range(min(a.warmup, 1)):
+        o.forward(0.0, 1e-3)
+    t0 = time.perf_counter()
+    done = 0
+    while done < a.steps:
+        o.forward(0.0, 1e-3)
+        done += 1
+        if time.perf_counter() - t0 > REFERENCE_BUDGET_S:
+            break
+    el = time.perf_counter() - t0
+    value = float(n ** 3 * done / el)
+    sample = ("the oracle (C++ restatement of the reference numerics; the reference's Fortran path cannot be built "
+              "here) on this arm's Rayleigh-Taylor workload at %d^3, loops on %d host threads, %d timed RK3 step(s) "
+              "of the %d requested after %d untimed, %.1f s" % (n, threads, done, a.steps, min(a.warmup, 1), el))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": el * 1e3 / a.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": make_config(a.n, world),
-            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": ncores, "kind": "port",
-                             "sample": "%d concurrent single-thread oracle runs (one per host core) of the same "
-                                       "Rayleigh-Taylor setup at %d^3, %d timed RK3 steps each, %.1f s; the "
-                                       "reference's Fortran path cannot be built here" % (ncores, n, a.steps, el)},
+            "steps": a.steps, "timed_steps": done, "warmup": a.warmup, "ms_per_step": el * 1e3 / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": make_config(n, world),
+            "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -571,6 +580,176 @@ def step_bytes(prec, nv, n_vcycles, refine=True, krylov=False):
     return q
 
 
+# ------------------------------------------------------------------ configuration table
+TWO_PI = 6.283185307179586
+
+
+def config_params(name, precision):
+    """Parameters of a workload configuration: lock exchange 64x32x32 in 4x1x1 (closed,
+    RK3, dt 2e-3, reference tolerances), Taylor-Green 128^3 (triply periodic box 2 pi, RK3,
+    dt 5e-3, relative residual 1e-10), Rayleigh-Taylor 256x256x512 (box 1x1x2, perio_xy,
+    dt 1e-3, relative residual 1e-10), stratified shear 512x256x256 with a tracer (box
+    4x2x1, perio_xy, adaptive CFL 0.8)."""
+    from nyles_gb300 import parameters
+    parameters.InextensibleDict.unfreeze()
+    p = parameters.UserParameters()
+    c = {"lock": dict(geometry="closed", n=(64, 32, 32), L=(4.0, 1.0, 1.0), dt=2e-3, tol=1e-6, maxite=20),
+         "tgv": dict(geometry="perio_xyz", n=(128, 128, 128), L=(TWO_PI,) * 3, dt=5e-3, tol=1e-20, maxite=40),
+         "rt": dict(geometry="perio_xy", n=(256, 256, 512), L=(1.0, 1.0, 2.0), dt=1e-3, tol=1e-20, maxite=40),
+         "shear": dict(geometry="perio_xy", n=(512, 256, 256), L=(4.0, 2.0, 1.0), dt=None, tol=1e-6, maxite=20,
+                       ntr=1)}[name]
+    p.model["modelname"] = "LES"
+    p.model["geometry"] = c["geometry"]
+    p.model["Lx"], p.model["Ly"], p.model["Lz"] = c["L"]
+    p.model["n_tracers"] = c.get("ntr", 0)
+    p.time["timestepping"] = "RK3_SSP"
+    p.time["auto_dt"] = c["dt"] is None
+    p.time["dt"] = c["dt"] or 1.0
+    p.time["cfl"] = 0.8
+    p.time["dt_max"] = 1.0
+    p.discretization["global_nx"], p.discretization["global_ny"], p.discretization["global_nz"] = c["n"]
+    p.gpu["precision"] = precision
+    p.gpu["mg_tol"] = c["tol"]
+    p.gpu["mg_maxite"] = c["maxite"]
+    p.gpu["history"] = False
+    return p
+
+
+def config_init(name, nyl):
+    """Seeded initial state of a configuration (covariant velocities, walls at rest)."""
+    import numpy as np
+    import torch
+    from nyles_gb300 import serving
+    if name == "lock":
+        serving.initial_state(nyl, "lock", 1)
+    elif name == "tgv":
+        serving.initial_state(nyl, "tgv", 2)
+    elif name == "rt":
+        rt_init(nyl)
+    else:
+        g = nyl.grid
+        st = nyl.model.state
+        rng = np.random.Generator(np.random.PCG64(4))
+        zb = g.z_b.view("i").numpy()
+        zu = g.z_vel["i"].view("i").numpy()
+        U0 = 0.05 * np.sqrt(5.0)    # minimum Richardson number 0.2 at N^2 = 1
+        st.get("u_i").view("i")[...] = torch.from_numpy(U0 * np.tanh((zu - 0.5) / 0.05) * g.dx)
+        st.get("b").view("i")[...] = torch.from_numpy(zb.copy())
+        st.get("t0").view("i")[...] = torch.from_numpy(np.tanh((zb - 0.5) / 0.05))
+        v = 1e-3 * rng.standard_normal(zb.shape) * g.dy
+        w = 1e-3 * rng.standard_normal(zb.shape) * g.dz
+        w[-1, :, :] = 0.0
+        st.get("u_j").view("i")[...] = torch.from_numpy(v)
+        st.get("u_k").view("i")[...] = torch.from_numpy(w)
+
+
+def run_config(name, precision, steps, warmup, err_steps):
+    """Timed steps of one configuration (graph replay; adaptive dt: eager steps with the
+    CFL reduction, as Nyles.run takes them), then err_steps steps from the initial state
+    whose final fields are returned for the mixed-vs-FP64 comparison. Stops at a blow-up
+    (NYLES_BLOWUP or a non-finite CFL reduction) and reports its step."""
+    import numpy as np
+    import torch
+    from nyles_gb300 import _native as nat
+    from nyles_gb300.nyles import Nyles
+    nyl = Nyles(config_params(name, precision))
+    config_init(name, nyl)
+    m = nyl.model
+    m.diagnose_var(m.state)
+    cells = nyl.param["nx"] * nyl.param["ny"] * nyl.param["nz"]
+    out = {"cells": cells}
+
+    def step(t):
+        try:
+            dt = nyl.compute_dt()
+        except nat.BlowUp:
+            return None
+        return dt if not m.forward(t, dt) else None
+
+    # error trajectory from the initial state (the timed steps come after it)
+    t, blow = 0.0, None
+    s0 = m.mg_stats()
+    for k in range(err_steps):
+        dt = step(t)
+        if dt is None:
+            blow = k + 1
+            break
+        t += dt
+    torch.cuda.synchronize()
+    s1 = m.mg_stats()
+    out["mean_vcycles_per_solve"] = (s1["vcycles"] - s0["vcycles"]) / max(1, s1["solves"] - s0["solves"])
+    names = ["b", "u_i", "u_j", "u_k", "p"] + ["t%d" % i for i in range(nyl.param["n_tracers"])]
+    fields = {s: m.state.get(s).view("i").double().cpu().numpy() for s in names}
+    out["err_steps"] = err_steps if blow is None else blow
+    if blow is not None:
+        out["blowup_step"] = blow
+        del nyl, m
+        torch.cuda.empty_cache()
+        return out, fields
+    if name != "shear":
+        fields_ok = all(np.isfinite(v).all() for v in fields.values())
+        out["finite"] = bool(fields_ok)
+    # timed steps (continuing the trajectory)
+    stream = torch.cuda.current_stream()
+    if nyl.auto_dt:
+        for _ in range(warmup):
+            t += step(t) or 0.0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        done = 0
+        for _ in range(steps):
+            dt = step(t)
+            if dt is None:
+                break
+            t += dt
+            done += 1
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3
+        out["path"] = "eager steps, adaptive dt (CFL reduction read back every step)"
+    else:
+        ms, _, _ = time_steps(nyl, steps, warmup, stream)
+        done = steps
+        out["path"] = "graph replay"
+    out["timed_steps"] = done
+    if done:
+        out["ms_per_step"] = ms / done
+        out["cell_steps_per_s"] = cells * done / (ms * 1e-3)
+    del nyl, m
+    torch.cuda.empty_cache()
+    return out, fields
+
+
+def config_table(a):
+    """FP64 and mixed throughput of each configuration and the mixed path's relative
+    max-norm error in b, u (velocity vector) and p (means removed) against the FP64
+    path after the same number of steps from the same state."""
+    import numpy as np
+    plan = {"lock": (4, 1, 5), "tgv": (20, 3, 200), "rt": (10, 3, 100), "shear": (10, 2, 200)}
+    table = {}
+    for name, (steps, warmup, err_steps) in plan.items():
+        row = {}
+        runs = {}
+        for prec in ("fp64", "mixed"):
+            row[prec], runs[prec] = run_config(name, prec, steps, warmup, err_steps)
+        f, g = runs["mixed"], runs["fp64"]
+        if all(np.isfinite(v).all() for v in list(f.values()) + list(g.values())):
+            err = {}
+            for s in ("b", "p") + tuple(k for k in f if k.startswith("t")):
+                x, y = f[s], g[s]
+                if s == "p":
+                    x, y = x - x.mean(), y - y.mean()
+                err[s] = float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+            us = max(np.abs(g[c]).max() for c in ("u_i", "u_j", "u_k"))
+            err["u"] = float(max(np.abs(f[c] - g[c]).max() for c in ("u_i", "u_j", "u_k")) / max(us, 1e-300))
+            row["mixed_vs_fp64"] = {"steps": min(row["fp64"]["err_steps"], row["mixed"]["err_steps"]),
+                                    "rel_err": err}
+        if "cell_steps_per_s" in row["fp64"] and "cell_steps_per_s" in row["mixed"]:
+            row["mixed_speedup"] = row["mixed"]["cell_steps_per_s"] / row["fp64"]["cell_steps_per_s"]
+        table[name] = row
+        print(json.dumps({name: row}), flush=True)
+    return table
+
+
 # ------------------------------------------------------------------ main
 def main():
     a = parse()
@@ -582,6 +761,9 @@ def main():
         return
     import torch
     torch.cuda.set_device(local)
+    if a.configs:
+        print(json.dumps({"configs": config_table(a)}))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -676,7 +858,7 @@ def main():
     if a.accuracy_steps > 0 and len(results) == 2:
         out["mixed"]["accuracy"] = accuracy(n, a.accuracy_steps)
     if rank == 0 and not a.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(128 if n >= 128 else n, 3)
+        out["cpu_baseline"] = cpu_baseline(n, 1)
     if dist:
         dist.barrier()
         dist.destroy_process_group()

@@ -40,11 +40,14 @@ template <> __device__ __forceinline__ float mg_pcoef<float>(const MgGeom& g, in
 // Scalars of the solve in the workspace: [0] last sum(r^2), [1] sum(b^2), [2] res,
 // [3] nite of the current solve, [4] V-cycles since creation, [5] and [6] the scale of
 // the mixed-precision residual sums and its inverse square.
-// device scalars of the solver (16 doubles, zeroed when the workspace is bound):
-// SC_NCONV counts graph-mode solves that stopped at maxite above tol, SC_NONFINITE
-// graph-mode solves stopped by a non-finite norm
+// device scalars of the solver (SC_COUNT <= 16 doubles, zeroed when the workspace is
+// bound): slots 7-12 belong to the Krylov solve; SC_NCONV counts graph-mode solves
+// that stopped at maxite above tol, SC_NONFINITE graph-mode solves stopped by a
+// non-finite norm
 enum { SC_RR = 0, SC_NORMB = 1, SC_RES = 2, SC_NITE = 3, SC_TOTAL = 4, SC_SCALE = 5, SC_INVSCALE2 = 6,
-       SC_NCONV = 7, SC_NONFINITE = 8 };
+       SC_ZQ = 7, SC_PQ = 8, SC_PR = 9, SC_BETA = 10, SC_ALPHA = 11, SC_ZMEAN = 12,
+       SC_NCONV = 13, SC_NONFINITE = 14, SC_COUNT = 15 };
+static_assert(SC_COUNT <= 16, "multigrid scalars exceed their 16-double slot");
 
 constexpr int MG_BX = 32, MG_BY = 8, MG_ZC = 8;    // stencil kernels
 constexpr int MG_RZC = 2;                          // restriction (coarse z per thread)
@@ -1262,7 +1265,6 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
 // hence the flexible beta. Scalars live in the solve's slots: SC_ZQ, SC_PQ, SC_PR as
 // doubles, beta as a float and alpha as a float pair (so that the elementwise kernels
 // do no FP64 work).
-constexpr int SC_ZQ = 7, SC_PQ = 8, SC_PR = 9, SC_BETA = 10, SC_ALPHA = 11, SC_ZMEAN = 12;
 
 
 // sums of the partials of z.q and of z, then beta = -(z.q)/(p.q) of the previous

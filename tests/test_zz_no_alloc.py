@@ -35,7 +35,7 @@ def _call_static(nat, U, V, W, out, n=None):
 def test_static_scratch_reduction_matches_workspace_reduction():
     from nyles_gb300 import _native as nat
     from nyles_gb300.nyles import Nyles
-    nyl = Nyles(helpers.make_params(geometry="perio_xy", n=(64, 64, 72)))
+    nyl = Nyles(helpers.make_params(geometry="perio_xy", n=(64, 64, 96)))
     m = nyl.model
     st = m.state
     U, V, W = st.U["i"].data, st.U["j"].data, st.U["k"].data
