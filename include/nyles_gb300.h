@@ -227,6 +227,38 @@ int nyles_model_capture(NylesModel* m, double dt, int nsteps);
 int nyles_model_graph_launch(NylesModel* m, void* stream);
 int nyles_model_graph_release(NylesModel* m);
 
+/* ---------------------------------------------------------------- batched steps
+ * No counterpart in the reference (one experiment per process, core/nyles.py:44-117).
+ * A bucket of runs with the same grid, precision and parameters advances with one
+ * graph launch: every kernel of the recorded steps covers up to nrun runs. Each run's
+ * memory (its fields, registers and workspace, in one allocation laid out as the
+ * model's own) lies delta[r] bytes from the memory the model was bound to; slot r is
+ * advanced when active[r] is nonzero, and its pressure solves stop on their own
+ * (live[r], written on the device), so a run's result does not depend on the others.
+ * The caller writes delta and active into the device table before each launch;
+ * loop_iterations counts the multigrid loop-body iterations run (device-side). */
+#define NYLES_BATCH_RUNS 32
+typedef struct NylesBatchTable {
+    long long delta[NYLES_BATCH_RUNS];  /* byte distance of run r's memory from the model's */
+    int active[NYLES_BATCH_RUNS];       /* 1: slot r holds a run that the launch advances */
+    int live[NYLES_BATCH_RUNS];         /* device-side: run r's current solve still iterates */
+    long long loop_iterations;          /* device-side: multigrid loop-body iterations run */
+} NylesBatchTable;
+/* Record nsteps steps with a fixed dt for nrun (<= NYLES_BATCH_RUNS) runs whose table is
+ * the device memory `table`. Mixed-precision LES with the stationary pressure solve, no
+ * tracers, the reference's schemes; NYLES_UNSUPPORTED otherwise. */
+int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table);
+int nyles_model_batch_launch(NylesModel* m, void* stream);
+int nyles_model_batch_release(NylesModel* m);
+/* adds the kernels of `iterations` multigrid loop-body iterations (read from the table)
+ * to nyles_launch_count */
+int nyles_model_batch_note_iterations(NylesModel* m, long long iterations);
+/* The counters the pressure solves of recorded (graph or batched) steps keep on the
+ * device, read from the model's workspace: last nite and res, V-cycles, solves stopped
+ * at maxite above tol, solves stopped by a non-finite norm (solves = 0). Synchronises
+ * `stream`. */
+int nyles_model_device_stats(NylesModel* m, NylesMgStats* stats, void* stream);
+
 /* ---------------------------------------------------------------- instrumentation
  * No counterpart in the reference (its timing is core/timing.py's wall-clock decorator).
  * Phases: 0 right-hand side, 1 time-scheme update, 2 halo fill, 3 divergence,

@@ -60,6 +60,14 @@ class NylesMgStats(ctypes.Structure):
                 ("vcycles", ctypes.c_longlong), ("not_converged", ctypes.c_int), ("nonfinite", ctypes.c_int)]
 
 
+BATCH_RUNS = 32   # NYLES_BATCH_RUNS
+
+
+class NylesBatchTable(ctypes.Structure):
+    _fields_ = [("delta", ctypes.c_longlong * BATCH_RUNS), ("active", ctypes.c_int * BATCH_RUNS),
+                ("live", ctypes.c_int * BATCH_RUNS), ("loop_iterations", ctypes.c_longlong)]
+
+
 # user forcing callback: fn(user, reg, t, stream)
 FORCING_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_void_p)
 
@@ -109,6 +117,11 @@ SIGNATURES = {
     "nyles_model_graph_release": (_I, [_P]),
     "nyles_model_profile": (_I, [_P, _I]),
     "nyles_model_profile_read": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _I]),
+    "nyles_model_batch_capture": (_I, [_P, _D, _I, _I, _P]),
+    "nyles_model_batch_launch": (_I, [_P, _P]),
+    "nyles_model_batch_release": (_I, [_P]),
+    "nyles_model_batch_note_iterations": (_I, [_P, ctypes.c_longlong]),
+    "nyles_model_device_stats": (_I, [_P, ctypes.POINTER(NylesMgStats), _P]),
     "nyles_launch_count": (ctypes.c_longlong, []),
     "nyles_max_U2_static_f64": (_I, [_P, _P, _P, ctypes.c_longlong, _P, _P]),
 }

@@ -8,8 +8,56 @@
 #define NYLES_MAX_TR 8
 #endif
 #define NYLES_MAX_PROG (4 + NYLES_MAX_TR)
+#ifndef NYLES_MAX_BATCH
+#define NYLES_MAX_BATCH 32
+#endif
 
 namespace nyles {
+
+// ---------------------------------------------------------------- batched launches
+// One launch can advance several runs of one bucket (the same grid, precision and
+// parameters; each run's fields, registers and workspace in one allocation of the same
+// layout). The memory of run r lies `delta[r]` bytes from the memory the kernel's
+// arguments point to. A batched kernel's grid repeats the one-run grid along z, once
+// per run: the block finds its run from blockIdx.z, shifts every pointer it uses by that
+// run's delta and returns at once when the run's gate is closed (the slot holds no run,
+// or, inside a multigrid loop, the run's solve has stopped). The table is device
+// memory written by the host before each launch (delta, active) and by the multigrid
+// control kernels (live, loop_iterations); its layout is NylesBatchTable of the public
+// header.
+struct BatchTab {
+    long long delta[NYLES_MAX_BATCH];
+    int active[NYLES_MAX_BATCH];
+    int live[NYLES_MAX_BATCH];
+    long long loop_iterations;
+};
+enum { GATE_ACTIVE = 0, GATE_LIVE = 1 };
+struct Bat {
+    BatchTab* tab = nullptr;   // null: one run, no shift
+    int nrun = 1;
+    int gate = GATE_ACTIVE;
+};
+
+// Run of this block. zb = z-blocks of one run's grid. Returns false when the run is gated
+// off; sets bz (the block's z index within its run's grid) and dlt (the byte shift).
+__device__ __forceinline__ bool batch_enter(const Bat& b, int& bz, long long& dlt) {
+    if (!b.tab) {
+        bz = blockIdx.z;
+        dlt = 0;
+        return true;
+    }
+    const int zb = gridDim.z / b.nrun;
+    const int run = blockIdx.z / zb;
+    bz = blockIdx.z - run * zb;
+    const int open = b.gate == GATE_LIVE ? b.tab->live[run] : b.tab->active[run];
+    dlt = b.tab->delta[run];
+    return open != 0;
+}
+// p shifted by dlt bytes (a null pointer stays null: it marks an unused argument)
+template <typename P>
+__device__ __forceinline__ P* bshift(P* p, long long dlt) {
+    return p ? (P*)((uintptr_t)p + (uintptr_t)dlt) : p;
+}
 
 // Model array geometry. Every field is a row-major (z, y, x) array — the layout of the
 // reference's `Scalar.view('i')` (core/variables.py:146-151) — with a halo of `nh`

@@ -57,18 +57,20 @@ enum { TERM_TRACER = 1, TERM_VF = 2, TERM_BERNOULLI = 4, TERM_VISC = 8, TERM_ACC
 
 // interior = true skips the b and u tendencies of periodic halo cells (the time step
 // refills those halos before it reads them); false covers every stored cell
+// `bat` (every launch_* below): a batched launch over the runs of its table (default:
+// one run)
 template <typename T>
 int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
-               cudaStream_t st, bool interior = false);
+               cudaStream_t st, bool interior = false, const Bat& bat = Bat());
 
 // time-scheme elementwise updates (core/timescheme.py:113-221)
 enum { UPD_EULER = 0, UPD_RK3_2 = 1, UPD_RK3_3 = 2, UPD_LF_PRED = 3, UPD_LF_FIRST = 4, UPD_LF_CORR = 5 };
 template <typename T>
 int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs<T>& a, const ProgPtrs<T>& b,
-                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st);
+                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st, const Bat& bat = Bat());
 
 template <typename T>
-int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st);
+int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st, const Bat& bat = Bat());
 
 // divergence of the contravariant velocity: writes state div (every cell, halo as its
 // periodic image) and the interior right-hand side of the pressure solve
@@ -81,12 +83,15 @@ int launch_correct(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, c
                    cudaStream_t st);
 // mixed precision: divergence into a float-pair right-hand side, correction from a
 // float-pair solution
-int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st);
-int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st);
+int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st,
+                  const Bat& bat = Bat());
+int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st,
+                      const Bat& bat = Bat());
 
 // contravariant velocity, vorticity and kinetic energy from the filled velocity
 template <typename T>
-int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st);
+int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st,
+                const Bat& bat = Bat());
 
 template <typename T>
 int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream_t st);
@@ -135,6 +140,7 @@ struct MgImpl {
     char* ws = nullptr;
     NylesMgStats stats{};
     Prof* prof = nullptr;             // phase timing (owned by the model)
+    Bat bat;                          // batched launches (set while a batched step is captured)
 };
 
 int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision);

@@ -176,8 +176,9 @@ __device__ __forceinline__ T mg_ldw(const T* __restrict__ a, long long c, bool w
     return wet ? v : T(0);
 }
 
-// per-block partial sum (one double per block, block index order)
-__device__ __forceinline__ void block_partial(double s, double* __restrict__ partial) {
+// per-block partial sum (one double per block, block index order); bz = the block's z
+// index within its run's grid (blockIdx.z outside batched launches)
+__device__ __forceinline__ void block_partial(double s, double* __restrict__ partial, int bz) {
     __shared__ double sm[MG_BX * MG_BY / 32];
     const int tid = threadIdx.y * MG_BX + threadIdx.x;
     s = warp_sum(s);
@@ -186,13 +187,13 @@ __device__ __forceinline__ void block_partial(double s, double* __restrict__ par
     if (tid < 32) {
         double t = (tid < MG_BX * MG_BY / 32) ? sm[tid] : 0.0;
         t = warp_sum(t);
-        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
+        if (tid == 0) partial[(bz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
     }
 }
 
 // two per-block partial sums at once
 __device__ __forceinline__ void block_partial2(double s, double t, double* __restrict__ ps,
-                                               double* __restrict__ pt) {
+                                               double* __restrict__ pt, int bz) {
     __shared__ double sm[2][MG_BX * MG_BY / 32];
     const int tid = threadIdx.y * MG_BX + threadIdx.x;
     s = warp_sum(s);
@@ -208,7 +209,7 @@ __device__ __forceinline__ void block_partial2(double s, double t, double* __res
         a = warp_sum(a);
         b = warp_sum(b);
         if (tid == 0) {
-            const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            const int blk = (bz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
             ps[blk] = a;
             pt[blk] = b;
         }
@@ -219,7 +220,7 @@ __device__ __forceinline__ void block_partial2(double s, double t, double* __res
 // FP32: the warp and block stages add in float and only the block total is stored as a
 // double (times `scale`). On GB300 the FP64 pipe is narrow: the double shuffles, adds
 // and conversions of a 256-thread reduction took a visible share of a level-0 pass.
-__device__ __forceinline__ void block_partial_f(float s, double scale, double* __restrict__ partial) {
+__device__ __forceinline__ void block_partial_f(float s, double scale, double* __restrict__ partial, int bz) {
     __shared__ float smf[MG_BX * MG_BY / 32];
     const int tid = threadIdx.y * MG_BX + threadIdx.x;
     s = warp_sum(s);
@@ -228,10 +229,11 @@ __device__ __forceinline__ void block_partial_f(float s, double scale, double* _
     if (tid < 32) {
         float t = (tid < MG_BX * MG_BY / 32) ? smf[tid] : 0.f;
         t = warp_sum(t);
-        if (tid == 0) partial[(blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = (double)t * scale;
+        if (tid == 0) partial[(bz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = (double)t * scale;
     }
 }
-__device__ __forceinline__ void block_partial2_f(float s, float t, double* __restrict__ ps, double* __restrict__ pt) {
+__device__ __forceinline__ void block_partial2_f(float s, float t, double* __restrict__ ps, double* __restrict__ pt,
+                                                 int bz) {
     __shared__ float smf[2][MG_BX * MG_BY / 32];
     const int tid = threadIdx.y * MG_BX + threadIdx.x;
     s = warp_sum(s);
@@ -247,7 +249,7 @@ __device__ __forceinline__ void block_partial2_f(float s, float t, double* __res
         a = warp_sum(a);
         b = warp_sum(b);
         if (tid == 0) {
-            const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            const int blk = (bz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
             ps[blk] = (double)a;
             pt[blk] = (double)b;
         }
@@ -260,17 +262,30 @@ __device__ __forceinline__ void block_partial2_f(float s, float t, double* __res
 // fused into the last half-sweep of the V-cycle); MODE 2 stores it and sums out*dot
 // and out per block into `partial` and `partial2` (the Krylov solve: z.q of the new
 // preconditioned residual against the previous direction's image, and the sum of z).
-template <typename T, int MODE>
+// BAT: batched launch over the runs of `bat` (pointers shifted to each run's memory)
+template <typename T, int MODE, bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, const T* __restrict__ in,
                                                             const T* __restrict__ b, T* __restrict__ out, T omega,
                                                             float2* __restrict__ acc, const T* __restrict__ dot,
                                                             double* __restrict__ partial,
-                                                            double* __restrict__ partial2) {
+                                                            double* __restrict__ partial2, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        in = bshift(in, dlt);
+        b = bshift(b, dlt);
+        out = bshift(out, dlt);
+        acc = bshift(acc, dlt);
+        dot = bshift(dot, dlt);
+        partial = bshift(partial, dlt);
+        partial2 = bshift(partial2, dlt);
+    }
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     float sdot = 0.f, ssum = 0.f;
     if (x < g.n[2] && y < g.n[1]) {
-        const int nz = g.n[0], z0 = blockIdx.z * MG_ZC;
+        const int nz = g.n[0], z0 = bz * MG_ZC;
         const long long sy = g.n[2], sz = (long long)g.n[1] * g.n[2];
         const MgNb nx = mg_nb(x, g.n[2], g.per[2], 1), ny = mg_nb(y, g.n[1], g.per[1], sy);
         const int dxy = (int)nx.wm + (int)nx.wp + (int)ny.wm + (int)ny.wp;
@@ -324,9 +339,9 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
     }
     if constexpr (MODE == 2) {
         if constexpr (sizeof(T) == sizeof(float))
-            block_partial2_f(sdot, ssum, partial, partial2);
+            block_partial2_f(sdot, ssum, partial, partial2, bz);
         else
-            block_partial2((double)sdot, (double)ssum, partial, partial2);
+            block_partial2((double)sdot, (double)ssum, partial, partial2, bz);
     }
 }
 
@@ -335,13 +350,25 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // the level's x faces) and z-chunks of V4_ZC cells; needs nx and nz divisible by 4 and
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
-template <int MODE>
+template <int MODE, bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
                                                                const float* __restrict__ b, float* __restrict__ out,
                                                                float omega, float2* __restrict__ acc,
                                                                const float* __restrict__ dot,
                                                                double* __restrict__ partial,
-                                                               double* __restrict__ partial2) {
+                                                               double* __restrict__ partial2, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        in = bshift(in, dlt);
+        b = bshift(b, dlt);
+        out = bshift(out, dlt);
+        acc = bshift(acc, dlt);
+        dot = bshift(dot, dlt);
+        partial = bshift(partial, dlt);
+        partial2 = bshift(partial2, dlt);
+    }
     const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
@@ -365,7 +392,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
     }
     const float cff1 = 1.f - omega;
-    const int zb = blockIdx.z * V4_ZC;
+    const int zb = bz * V4_ZC;
     const long long c00 = (long long)ys * sy + x0;
     auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -419,7 +446,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         zm = zc;
         zc = zp;
     }
-    if (MODE == 2) block_partial2_f(sdot, ssum, partial, partial2);
+    if (MODE == 2) block_partial2_f(sdot, ssum, partial, partial2, bz);
 }
 
 // First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
@@ -434,14 +461,24 @@ __device__ __forceinline__ T mg_jacobi_from_zero(T b, T omega, T idg) {
 // bc = Rcoef*(sum of the 8 children) with Rcoef = 1/2 (basicoperators.f90:32-60,
 // operators.f90:172-213). The coarse solution is zero at this point (operators.f90:209),
 // so the first half-sweep of the coarse smoothing is written here, into yc.
-template <typename T>
+template <typename T, bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, const T* __restrict__ xf,
                                                               const T* __restrict__ bf, const MgGeom gc,
-                                                              T* __restrict__ bc, T* __restrict__ yc, T omega) {
+                                                              T* __restrict__ bc, T* __restrict__ yc, T omega,
+                                                              const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        xf = bshift(xf, dlt);
+        bf = bshift(bf, dlt);
+        bc = bshift(bc, dlt);
+        yc = bshift(yc, dlt);
+    }
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     if (x >= gc.n[2] || y >= gc.n[1]) return;
-    const int nzc = gc.n[0], z0 = blockIdx.z * MG_RZC;
+    const int nzc = gc.n[0], z0 = bz * MG_RZC;
     auto emit = [&](int z, T s) {
         const long long c = mg_at(gc, z, y, x);
         const T bv = T(0.5) * s;
@@ -511,13 +548,20 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict(const MgGeom gf, 
 }
 
 // trilinear 9-3-3-1 prolongation added to the fine solution (basicoperators.f90:173-231)
-template <typename T>
+template <typename T, bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T* __restrict__ xf, const MgGeom gc,
-                                                             const T* __restrict__ xc) {
+                                                             const T* __restrict__ xc, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        xf = bshift(xf, dlt);
+        xc = bshift(xc, dlt);
+    }
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
     if (x >= gf.n[2] || y >= gf.n[1]) return;
-    const int nzf = gf.n[0], z0 = blockIdx.z * MG_ZC;   // z0 even
+    const int nzf = gf.n[0], z0 = bz * MG_ZC;   // z0 even
     if (z0 + MG_ZC > nzf) {   // last, partial chunk
         for (int z = z0; z < nzf; ++z) {
             const long long c = mg_at(gf, z, y, x);
@@ -573,10 +617,20 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
 
 // k_mg_restrict: one coarse row pair of cells per thread, MG_RZC coarse planes (needs
 // coarse nz divisible by MG_RZC)
+template <bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom gf, const float* __restrict__ xf,
                                                                  const float* __restrict__ bf, const MgGeom gc,
                                                                  float* __restrict__ bc, float* __restrict__ yc,
-                                                                 float omega) {
+                                                                 float omega, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        xf = bshift(xf, dlt);
+        bf = bshift(bf, dlt);
+        bc = bshift(bc, dlt);
+        yc = bshift(yc, dlt);
+    }
     const int nx = gf.n[2], ny = gf.n[1], nz = gf.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
@@ -595,7 +649,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
     const int ylw = (int)yl.wm, yhw = (int)yh.wp;
     const float wxy[2][4] = {{(float)((int)wl + ylw), (float)(1 + ylw), (float)((int)wl + yhw), (float)(1 + yhw)},
                              {(float)(1 + ylw), (float)((int)wr + ylw), (float)(1 + yhw), (float)((int)wr + yhw)}};
-    const int zcb = blockIdx.z * MG_RZC, k0 = 2 * zcb;
+    const int zcb = bz * MG_RZC, k0 = 2 * zcb;
     const long long c00 = (long long)j0 * sy + x0;
     auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -672,8 +726,17 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
 
 // k_mg_prolong: one 4-cell fine row segment per thread, V4_ZC fine planes (needs fine
 // nz divisible by V4_ZC)
+template <bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf, float* __restrict__ xf,
-                                                                const MgGeom gc, const float* __restrict__ xc) {
+                                                                const MgGeom gc, const float* __restrict__ xc,
+                                                                const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        xf = bshift(xf, dlt);
+        xc = bshift(xc, dlt);
+    }
     const int nx = gf.n[2], ny = gf.n[1];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
@@ -691,7 +754,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
     const long long col = ic0 > 0 ? -1 : (gc.per[2] ? (long long)(ncx - 1) : 0);
     const long long cor = ic0 + 2 < ncx ? 2 : (gc.per[2] ? (long long)(2 - ncx) : 0);
     const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
-    const int zb = blockIdx.z * V4_ZC, kc0 = zb >> 1;
+    const int zb = bz * V4_ZC, kc0 = zb >> 1;
     const MgNb zl = mg_nb(kc0, gc.n[0], gc.per[0], csz), zh = mg_nb(kc0 + V4_ZC / 2 - 1, gc.n[0], gc.per[0], csz);
     const long long cc = mg_at(gc, kc0, jc, ic0);
     // in-plane 9-3-3-1 sums of the 4 fine cells from one coarse plane at c (0 when the
@@ -918,8 +981,14 @@ __device__ __forceinline__ T bottom_prolong(const MgGeom& gf, const MgGeom& gc, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const MgBottom<T> a) {
+__global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const MgBottom<T> a0, const Bat bat = Bat()) {
     extern __shared__ __align__(16) unsigned char mg_smem[];
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    MgBottom<T> a = a0;
+    a.xg = bshift(a.xg, dlt);
+    a.bg = bshift(a.bg, dlt);
     T* sm = reinterpret_cast<T*>(mg_smem);
     const T om = a.omega, cff1 = T(1) - om;
     const int L = a.nlev;
@@ -1018,7 +1087,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq(const MgGeom g, cons
             }
         }
     }
-    block_partial(s, partial);
+    block_partial(s, partial, blockIdx.z);
 }
 
 // Stop-test residual of the level-1 solution together with the first half-sweep of the
@@ -1068,7 +1137,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_sweep(const MgGeom g
             }
         }
     }
-    block_partial(s, partial);
+    block_partial(s, partial, blockIdx.z);
 }
 
 // ---------------------------------------------------------------- mixed precision
@@ -1109,15 +1178,27 @@ __device__ __forceinline__ float2 mg_ldw_df(const float2* __restrict__ a, long l
 // float per thread on r * scale, scale = sc[SC_SCALE] a power of two near 1/rms(b)
 // (k_mg_scale), so that they neither underflow nor overflow; each block partial is
 // unscaled in double.
+template <bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, const float2* __restrict__ p,
                                                                  const float2* __restrict__ b, float* __restrict__ r32,
                                                                  float* __restrict__ y32, float omega,
                                                                  const double* __restrict__ sc,
-                                                                 double* __restrict__ partial) {
+                                                                 double* __restrict__ partial, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        p = bshift(p, dlt);
+        b = bshift(b, dlt);
+        r32 = bshift(r32, dlt);
+        y32 = bshift(y32, dlt);
+        sc = bshift(sc, dlt);
+        partial = bshift(partial, dlt);
+    }
     constexpr int ZC = MG_DFZC;
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int nz = g.n[0], z0 = blockIdx.z * ZC;
+    const int nz = g.n[0], z0 = bz * ZC;
     const float scale = (float)sc[SC_SCALE];
     float s = 0.f;
     if (x < g.n[2] && y < g.n[1]) {
@@ -1158,7 +1239,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
             }
         }
     }
-    block_partial_f(s, sc[SC_INVSCALE2], partial);
+    block_partial_f(s, sc[SC_INVSCALE2], partial, bz);
 }
 
 // k_mg_resid_df with 4 consecutive x cells per thread: each float-pair row segment is
@@ -1168,11 +1249,24 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_resid_df(const MgGeom g, c
 struct DfVec4 {
     float2 v[4];
 };
+template <bool BAT = false>
 __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeom g, const float2* __restrict__ p,
                                                                     const float2* __restrict__ b,
                                                                     float* __restrict__ r32, float* __restrict__ y32,
                                                                     float omega, const double* __restrict__ sc,
-                                                                    double* __restrict__ partial) {
+                                                                    double* __restrict__ partial,
+                                                                    const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        p = bshift(p, dlt);
+        b = bshift(b, dlt);
+        r32 = bshift(r32, dlt);
+        y32 = bshift(y32, dlt);
+        sc = bshift(sc, dlt);
+        partial = bshift(partial, dlt);
+    }
     const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
@@ -1194,7 +1288,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
         const int xx = x0 + e;
         dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
     }
-    const int zb = blockIdx.z * V4_ZC;
+    const int zb = bz * V4_ZC;
     const long long c00 = (long long)ys * sy + x0;
     auto ld = [&](const float2* a, long long c) -> DfVec4 {
         const float4* q = reinterpret_cast<const float4*>(a + c);
@@ -1249,7 +1343,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
         zm = zc;
         zc = zp;
     }
-    block_partial_f(s, sc[SC_INVSCALE2], partial);
+    block_partial_f(s, sc[SC_INVSCALE2], partial, bz);
 }
 
 // ---------------------------------------------------------------- Krylov acceleration
@@ -1357,7 +1451,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_fcg_direction(const MgGeom g,
             }
         }
     }
-    block_partial2_f(spq, spr, ppq, ppr);
+    block_partial2_f(spq, spr, ppq, ppr, blockIdx.z);
 }
 
 // The same with 4 consecutive x cells per thread (16-byte loads and stores: the kernel
@@ -1447,7 +1541,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_fcg_direction_v4(const MgG
         zm = zc;
         zc = zp;
     }
-    block_partial2_f(spq, spr, ppq, ppr);
+    block_partial2_f(spq, spr, ppq, ppr, blockIdx.z);
 }
 
 // sums of p.q and p.r, then alpha = (p.r)/(p.q) stored as a float pair
@@ -1494,10 +1588,15 @@ __global__ void __launch_bounds__(256) k_fcg_xupdate(float2* __restrict__ xdf, c
 
 // sum of squares of a float-pair array (high parts, squared and summed in double)
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq_df(const MgGeom g, const float2* __restrict__ v,
-                                                              double* __restrict__ partial) {
+                                                              double* __restrict__ partial, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    v = bshift(v, dlt);
+    partial = bshift(partial, dlt);
     const int x = blockIdx.x * MG_BX + threadIdx.x;
     const int y = blockIdx.y * MG_BY + threadIdx.y;
-    const int z0 = blockIdx.z * MG_ZC;
+    const int z0 = bz * MG_ZC;
     const int z1 = min(z0 + MG_ZC, g.n[0]) - 1;
     double s = 0.0;
     if (x < g.n[2] && y < g.n[1])
@@ -1505,12 +1604,16 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq_df(const MgGeom g, c
             const double h = (double)v[mg_at(g, z, y, x)].x;
             s += h * h;
         }
-    block_partial(s, partial);
+    block_partial(s, partial, bz);
 }
 
 // scale of the float sums of squares: 2^-e with 2^e near rms(b) = sqrt(sum(b^2)/vol),
 // and its inverse square (both exact powers of two)
-__global__ void k_mg_scale(double* __restrict__ sc, double vol) {
+__global__ void k_mg_scale(double* __restrict__ sc, double vol, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    sc = bshift(sc, dlt);
     const double nb = sc[SC_NORMB];
     int e = 0;
     if (nb > 0.0) frexp(sqrt(nb / vol), &e);
@@ -1519,7 +1622,13 @@ __global__ void k_mg_scale(double* __restrict__ sc, double vol) {
     sc[SC_INVSCALE2] = ldexp(1.0, 2 * e);
 }
 
-__global__ void k_mg_final(const double* __restrict__ partial, int n, double* __restrict__ out) {
+__global__ void k_mg_final(const double* __restrict__ partial, int n, double* __restrict__ out,
+                           const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    partial = bshift(partial, dlt);
+    out = bshift(out, dlt);
     double s = 0.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
     __shared__ double sm[32];
@@ -1537,39 +1646,57 @@ __global__ void k_mg_final(const double* __restrict__ partial, int n, double* __
 // before the loop: res = sum(r^2)/sum(b^2) (0 when b = 0), continue while res >= tol
 __device__ __forceinline__ bool finite_dev(double v) { return v == v && v <= 1.7976931348623157e308; }
 
-__global__ void k_mg_ctl_begin(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol) {
-    const double normb = sc[SC_NORMB];
-    const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
-    sc[SC_RES] = res;
-    sc[SC_NITE] = 0.0;
-    if (!finite_dev(normb) || !finite_dev(res)) {   // non-finite input: no V-cycle (host: NYLES_BLOWUP)
-        sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
-        cudaGraphSetConditional(h, 0u);
-        return;
+// One thread per run (a single thread for one run): each run's stop test, its `live`
+// flag in a batched launch, and the loop condition = any run still iterating.
+__global__ void k_mg_ctl_begin(double* __restrict__ sc0, cudaGraphConditionalHandle h, double tol,
+                               const Bat bat = Bat()) {
+    const int r = threadIdx.x;
+    bool go = false;
+    if (r < bat.nrun && (!bat.tab || bat.tab->active[r])) {
+        double* sc = bat.tab ? bshift(sc0, bat.tab->delta[r]) : sc0;
+        const double normb = sc[SC_NORMB];
+        const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
+        sc[SC_RES] = res;
+        sc[SC_NITE] = 0.0;
+        if (!finite_dev(normb) || !finite_dev(res))   // non-finite input: no V-cycle (host: NYLES_BLOWUP)
+            sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
+        else
+            go = !(res < tol);
     }
-    cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
+    if (bat.tab && r < NYLES_MAX_BATCH) bat.tab->live[r] = go ? 1 : 0;
+    const int any = __syncthreads_or(go ? 1 : 0);
+    if (r == 0) cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
 // after each V-cycle: nite += 1; stop at maxite (res keeps its previous value, as
 // solvers.f90:24-26 leaves the loop before recomputing it), else recompute res
-__global__ void k_mg_ctl_step(double* __restrict__ sc, cudaGraphConditionalHandle h, double tol, int maxite) {
-    const double nite = sc[SC_NITE] + 1.0;
-    sc[SC_NITE] = nite;
-    sc[SC_TOTAL] = sc[SC_TOTAL] + 1.0;
-    if (nite >= (double)maxite) {
-        if (sc[SC_RES] >= tol) sc[SC_NCONV] = sc[SC_NCONV] + 1.0;   // as mg_solve's count
-        cudaGraphSetConditional(h, 0u);
-        return;
+__global__ void k_mg_ctl_step(double* __restrict__ sc0, cudaGraphConditionalHandle h, double tol, int maxite,
+                              const Bat bat = Bat()) {
+    const int r = threadIdx.x;
+    bool go = false;
+    if (r < bat.nrun && (!bat.tab || bat.tab->live[r])) {   // runs whose solve stopped keep their counters
+        double* sc = bat.tab ? bshift(sc0, bat.tab->delta[r]) : sc0;
+        const double nite = sc[SC_NITE] + 1.0;
+        sc[SC_NITE] = nite;
+        sc[SC_TOTAL] = sc[SC_TOTAL] + 1.0;
+        if (nite >= (double)maxite) {
+            if (sc[SC_RES] >= tol) sc[SC_NCONV] = sc[SC_NCONV] + 1.0;   // as mg_solve's count
+        } else {
+            const double normb = sc[SC_NORMB];
+            const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
+            sc[SC_RES] = res;
+            if (!finite_dev(res))
+                sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
+            else
+                go = !(res < tol);
+        }
+        if (bat.tab) bat.tab->live[r] = go ? 1 : 0;
     }
-    const double normb = sc[SC_NORMB];
-    const double res = normb > 0.0 ? sc[SC_RR] / normb : 0.0;
-    sc[SC_RES] = res;
-    if (!finite_dev(res)) {
-        sc[SC_NONFINITE] = sc[SC_NONFINITE] + 1.0;
-        cudaGraphSetConditional(h, 0u);
-        return;
+    const int any = __syncthreads_or(go ? 1 : 0);
+    if (r == 0) {
+        if (bat.tab) bat.tab->loop_iterations += 1;
+        cudaGraphSetConditional(h, any ? 1u : 0u);
     }
-    cudaGraphSetConditional(h, (res < tol) ? 0u : 1u);
 }
 
 // ---------------------------------------------------------------- host side
@@ -1577,6 +1704,11 @@ static inline dim3 grid_zc(const int n[3], int zc) {
     return dim3((n[2] + MG_BX - 1) / MG_BX, (n[1] + MG_BY - 1) / MG_BY, (n[0] + zc - 1) / zc);
 }
 static const dim3 kBlk(MG_BX, MG_BY, 1);
+// the grid of a batched launch repeats the one-run grid along z once per run
+static inline dim3 bgrid(const MgImpl* mg, dim3 g) {
+    if (mg->bat.tab) g.z *= mg->bat.nrun;
+    return g;
+}
 
 // the 4-cell vector kernels apply to a level whose x and z extents allow them
 static inline bool use_v4(const MgImpl* mg, const int n[3]) { return mg->vec4 && n[2] % 4 == 0 && n[0] % V4_ZC == 0; }
@@ -1736,6 +1868,28 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
     const T om = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch(from_y ? 1 : 2);
+    if (mg->bat.tab) {   // batched (stationary mixed refinement): modes 0 and 1
+        const Bat& bt = mg->bat;
+        float2* pdf = last_mode == 1 ? reinterpret_cast<float2*>(mg->ws + mg->off_pdf) : nullptr;
+        if constexpr (sizeof(T) == sizeof(float)) {
+            if (use_v4(mg, g.n)) {
+                const dim3 gv = bgrid(mg, grid_v4(g.n));
+                if (!from_y) k_mg_jacobi_v4<0, true><<<gv, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr, bt);
+                if (last_mode == 1)
+                    k_mg_jacobi_v4<1, true><<<gv, kBlk, 0, st>>>(g, y, b, x, om, pdf, nullptr, nullptr, nullptr, bt);
+                else
+                    k_mg_jacobi_v4<0, true><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr, bt);
+                return;
+            }
+        }
+        const dim3 gb = bgrid(mg, grd);
+        if (!from_y) k_mg_jacobi<T, 0, true><<<gb, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr, bt);
+        if (last_mode == 1)
+            k_mg_jacobi<T, 1, true><<<gb, kBlk, 0, st>>>(g, y, b, x, om, pdf, nullptr, nullptr, nullptr, bt);
+        else
+            k_mg_jacobi<T, 0, true><<<gb, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr, bt);
+        return;
+    }
     if constexpr (sizeof(T) == sizeof(float)) {
         if (use_v4(mg, g.n)) {
             const dim3 gv = grid_v4(g.n);
@@ -1785,7 +1939,7 @@ static void bottom(MgImpl* mg, cudaStream_t st) {
     a.omega = T(mg->omega);
     ProfScope ps(mg->prof, 8, st);
     note_launch();
-    k_mg_bottom<T><<<1, MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a);
+    k_mg_bottom<T><<<bgrid(mg, dim3(1, 1, 1)), MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a, mg->bat);
 }
 
 // level0_last: mode of the last level-0 half-sweep (see smooth)
@@ -1807,13 +1961,22 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
                 if (v4_restrict(mg, gf, gc)) {
                     const dim3 gv((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
                                   (unsigned)(gc.n[0] / MG_RZC));
-                    k_mg_restrict_v4<<<gv, kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
-                                                          lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3),
-                                                          (float)mg->omega);
+                    if (mg->bat.tab)
+                        k_mg_restrict_v4<true><<<bgrid(mg, gv), kBlk, 0, st>>>(
+                            gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc, lvp<float>(mg, l + 1, 2),
+                            lvp<float>(mg, l + 1, 3), (float)mg->omega, mg->bat);
+                    else
+                        k_mg_restrict_v4<<<gv, kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
+                                                              lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3),
+                                                              (float)mg->omega);
                     done = true;
                 }
             }
-            if (!done)
+            if (!done && mg->bat.tab)
+                k_mg_restrict<T, true><<<bgrid(mg, grid_zc(gc.n, MG_RZC)), kBlk, 0, st>>>(
+                    gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc, lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 3),
+                    T(mg->omega), mg->bat);
+            else if (!done)
                 k_mg_restrict<T><<<grid_zc(gc.n, MG_RZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), lvp<T>(mg, l, 2), gc,
                                                                         lvp<T>(mg, l + 1, 2), lvp<T>(mg, l + 1, 3),
                                                                         T(mg->omega));
@@ -1831,11 +1994,19 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
             bool done = false;
             if constexpr (sizeof(T) == sizeof(float)) {
                 if (v4_prolong(mg, gf, gc)) {
-                    k_mg_prolong_v4<<<grid_v4(gf.n), kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), gc, lvp<float>(mg, l + 1, 1));
+                    if (mg->bat.tab)
+                        k_mg_prolong_v4<true><<<bgrid(mg, grid_v4(gf.n)), kBlk, 0, st>>>(
+                            gf, lvp<float>(mg, l, 1), gc, lvp<float>(mg, l + 1, 1), mg->bat);
+                    else
+                        k_mg_prolong_v4<<<grid_v4(gf.n), kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), gc,
+                                                                        lvp<float>(mg, l + 1, 1));
                     done = true;
                 }
             }
-            if (!done)
+            if (!done && mg->bat.tab)
+                k_mg_prolong<T, true><<<bgrid(mg, grid_zc(gf.n, MG_ZC)), kBlk, 0, st>>>(
+                    gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1), mg->bat);
+            else if (!done)
                 k_mg_prolong<T><<<grid_zc(gf.n, MG_ZC), kBlk, 0, st>>>(gf, lvp<T>(mg, l, 1), gc, lvp<T>(mg, l + 1, 1));
         }
         smooth<T>(mg, l, st, l == 0 ? level0_last : 0);
@@ -1871,9 +2042,10 @@ static void enqueue_normb_df(MgImpl* mg, cudaStream_t st) {
     const dim3 grd = grid_zc(g.n, MG_ZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(3);
-    k_mg_sumsq_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_bdf), part);
-    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_NORMB);
-    k_mg_scale<<<1, 1, 0, st>>>(sc, (double)mg->lev[0].vol);
+    k_mg_sumsq_df<<<bgrid(mg, grd), kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_bdf), part,
+                                                   mg->bat);
+    k_mg_final<<<bgrid(mg, dim3(1, 1, 1)), 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_NORMB, mg->bat);
+    k_mg_scale<<<bgrid(mg, dim3(1, 1, 1)), 1, 0, st>>>(sc, (double)mg->lev[0].vol, mg->bat);
 }
 
 // mixed precision: enqueue the float-pair residual (also the next correction's rhs)
@@ -1886,15 +2058,23 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     const dim3 grd = v4 ? grid_v4(g.n) : grid_zc(g.n, MG_DFZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(2);
-    if (v4)
-        k_mg_resid_df_v4<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
-                                               reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
-                                               lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
-    else
-        k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, reinterpret_cast<const float2*>(mg->ws + mg->off_pdf),
-                                            reinterpret_cast<const float2*>(mg->ws + mg->off_bdf),
-                                            lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega, sc, part);
-    k_mg_final<<<1, 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR);
+    const float2* pdf = reinterpret_cast<const float2*>(mg->ws + mg->off_pdf);
+    const float2* bdf = reinterpret_cast<const float2*>(mg->ws + mg->off_bdf);
+    if (mg->bat.tab) {
+        if (v4)
+            k_mg_resid_df_v4<true><<<bgrid(mg, grd), kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
+                                                                    (float)mg->omega, sc, part, mg->bat);
+        else
+            k_mg_resid_df<true><<<bgrid(mg, grd), kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
+                                                                 (float)mg->omega, sc, part, mg->bat);
+    } else if (v4) {
+        k_mg_resid_df_v4<<<grd, kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
+                                               (float)mg->omega, sc, part);
+    } else {
+        k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega,
+                                            sc, part);
+    }
+    k_mg_final<<<bgrid(mg, dim3(1, 1, 1)), 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR, mg->bat);
 }
 
 // FP64: enqueue the stop-test sum(r^2) into sc[SC_RR] together with the next V-cycle's
@@ -2082,7 +2262,8 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         enqueue_normb_df(mg, st);
         enqueue_resid_df(mg, st);
     }
-    k_mg_ctl_begin<<<1, 1, 0, st>>>(sc, h, mg->tol);
+    const unsigned nctl = mg->bat.tab ? NYLES_MAX_BATCH : 1;   // one thread per run
+    k_mg_ctl_begin<<<1, nctl, 0, st>>>(sc, h, mg->tol, mg->bat);
     note_launch();
     gb.end_segment();
     if (gb.error) return gb.error;
@@ -2098,6 +2279,8 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
     e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
     if (e != cudaSuccess) return gb.error = cuda_status(e, "capture of the multigrid loop body");
     const long long l0 = nyles_launch_count();
+    const int gate0 = mg->bat.gate;
+    mg->bat.gate = GATE_LIVE;   // batched: runs whose solve has stopped skip the loop body
     if (!mixed) {
         vcycle<double>(mg, st, 0);
         enqueue_resid_sweep(mg, st);
@@ -2109,7 +2292,8 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         vcycle<float>(mg, st, 1);
         enqueue_resid_df(mg, st);
     }
-    k_mg_ctl_step<<<1, 1, 0, st>>>(sc, h, mg->tol, mg->maxite);
+    mg->bat.gate = gate0;
+    k_mg_ctl_step<<<1, nctl, 0, st>>>(sc, h, mg->tol, mg->maxite, mg->bat);
     note_launch();
     gb.body_kernels = nyles_launch_count() - l0;
     cudaGraph_t g = nullptr;

@@ -3,11 +3,18 @@
 // core/mgfordriver.py restated as a sequence of kernel launches on one stream).
 #include "nyles_internal.h"
 #include <atomic>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <new>
 
 namespace nyles {
+
+static_assert(sizeof(BatchTab) == sizeof(NylesBatchTable) && offsetof(BatchTab, active) == offsetof(NylesBatchTable, active) &&
+                  offsetof(BatchTab, live) == offsetof(NylesBatchTable, live) &&
+                  offsetof(BatchTab, loop_iterations) == offsetof(NylesBatchTable, loop_iterations) &&
+                  NYLES_MAX_BATCH == NYLES_BATCH_RUNS,
+              "the device batch table and NylesBatchTable of the public header differ");
 
 static thread_local std::string g_last_error;
 
@@ -161,15 +168,27 @@ struct NylesModel {
     cudaStream_t last_stream = nullptr;  // stream of the latest graph launch
     nyles_forcing_fn forcing = nullptr;  // user forcing called after each right-hand side
     void* forcing_user = nullptr;
+    // batched graph: the same steps for up to NYLES_MAX_BATCH runs of one bucket
+    Bat bat;                             // set while the batched graph is captured
+    cudaGraph_t bgraph = nullptr;
+    cudaGraphExec_t bgexec = nullptr;
+    long long bgraph_kernels = 0, bgraph_body_kernels = 0;
     void release_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         gexec = nullptr;
         graph = nullptr;
     }
+    void release_batch() {
+        if (bgexec) cudaGraphExecDestroy(bgexec);
+        if (bgraph) cudaGraphDestroy(bgraph);
+        bgexec = nullptr;
+        bgraph = nullptr;
+    }
     ~NylesModel() {
         prof.release();
         release_graph();
+        release_batch();
         if (cap_stream) cudaStreamDestroy(cap_stream);
     }
 };
@@ -440,7 +459,7 @@ static int model_rhs(NylesModel* m, int reg, int last, double t, cudaStream_t st
     // divergence next to the halo reads updated halo velocities, so their tendencies count
     if (m->d.model == NYLES_MODEL_EULER3D) interior = false;
     ProfScope ps(&m->prof, 0, st);
-    int rc = launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st, interior);
+    int rc = launch_rhs<T>(&m->d, m->g, s, ds, rhs_terms(&m->d, last), st, interior, m->bat);
     // user forcing, core/model_les.py:143-144: called with the stage's register set and
     // time; it enqueues its own work on `st`
     if (!rc && m->forcing) m->forcing(m->forcing_user, reg, t, (void*)st);
@@ -462,7 +481,7 @@ static int model_pressure_projection(NylesModel* m, cudaStream_t st) {
             rc = launch_div<T, double>(&m->d, m->g, s, reinterpret_cast<double*>(mgb), st);
         else
             rc = launch_div_df(&m->d, m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)),
-                               reinterpret_cast<float2*>(mgb), st);
+                               reinterpret_cast<float2*>(mgb), st, m->bat);
         if (rc) return rc;
     }
     {
@@ -482,11 +501,11 @@ static int model_pressure_projection(NylesModel* m, cudaStream_t st) {
             rc = launch_correct<T, double>(&m->d, m->g, s, reinterpret_cast<const double*>(mgx), m->d.dx2, st);
         else
             rc = launch_correct_df(m->g, field_ptrs<float>(&m->d, reinterpret_cast<float* const*>(m->fields)),
-                                   reinterpret_cast<const float2*>(mgx), m->d.dx2, st);
+                                   reinterpret_cast<const float2*>(mgx), m->d.dx2, st, m->bat);
         if (rc) return rc;
     }
     ProfScope ps(&m->prof, 2, st);
-    return launch_fill<T>(m->g, uf, 3, st);
+    return launch_fill<T>(m->g, uf, 3, st, m->bat);
 }
 
 // core/model_les.py:98-127 ; core/model_les_euler.py:96-125 ; the advection model fills
@@ -502,11 +521,11 @@ static int model_diagnose(NylesModel* m, cudaStream_t st) {
     }
     if (m->d.model != NYLES_MODEL_EULER3D) {
         ProfScope ps(&m->prof, 2, st);
-        if ((rc = launch_fill<T>(m->g, uf, 4, st))) return rc;
+        if ((rc = launch_fill<T>(m->g, uf, 4, st, m->bat))) return rc;
     }
     if ((rc = model_pressure_projection<T>(m, st))) return rc;
     ProfScope ps(&m->prof, 6, st);
-    return launch_diag<T>(&m->d, m->g, s, m->d.model != NYLES_MODEL_LINEAR, st);
+    return launch_diag<T>(&m->d, m->g, s, m->d.model != NYLES_MODEL_LINEAR, st, m->bat);
 }
 
 // Advection.make_u_divergentfree (core/model_advection.py:38-53) with the projection of
@@ -534,7 +553,7 @@ static int model_update(NylesModel* m, int kind, int ra, int rb, int rc_, double
     ProgPtrs<T> sp = state_prog<T>(&m->d, s);
     auto reg = [&](int r) { return prog_ptrs<T>(&m->d, r >= 0 ? reinterpret_cast<T* const*>(m->regs[r]) : nullptr); };
     ProfScope ps(&m->prof, 1, st);
-    return launch_update<T>(m->g, m->nprog, sp, reg(ra), reg(rb), reg(rc_), kind, dt, st);
+    return launch_update<T>(m->g, m->nprog, sp, reg(ra), reg(rb), reg(rc_), kind, dt, st, m->bat);
 }
 
 // core/timescheme.py:113-221
@@ -685,8 +704,12 @@ int nyles_model_profile_read(NylesModel* m, double* ms, long long* count, int np
 
 long long nyles_launch_count(void) { return g_launches.load(); }
 
-int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
-    if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
+}  // extern "C"
+
+// Record nsteps steps of m into a new graph (multigrid stop tests on the device); the
+// kernels outside the multigrid loops and those of one loop iteration are counted.
+static int record_steps(NylesModel* m, double dt, int nsteps, cudaGraph_t* graph, cudaGraphExec_t* exec,
+                        long long* kernels, long long* body_kernels) {
     if (m->scheme == NYLES_SCHEME_LFAM3 && m->lf_first) {
         set_error("LFAM3: run the first (Euler) step before capturing the steady step");
         return NYLES_BAD_ARG;
@@ -700,11 +723,10 @@ int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
         e = cudaStreamCreateWithFlags(&m->cap_stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cuda_status(e, "capture stream");
     }
-    m->release_graph();
-    e = cudaGraphCreate(&m->graph, 0);
+    e = cudaGraphCreate(graph, 0);
     if (e != cudaSuccess) return cuda_status(e, "cudaGraphCreate");
     GraphBuilder gb;
-    gb.graph = m->graph;
+    gb.graph = *graph;
     gb.st = m->cap_stream;
     const bool prof_on = m->prof.on;
     m->prof.on = false;   // event records are not allowed inside loop bodies
@@ -722,11 +744,85 @@ int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
     const long long captured = g_launches.load() - l0;
     g_launches.fetch_sub(captured);   // nothing ran yet: launches are counted at replay
     if (!rc) rc = gb.error;
-    if (rc) { m->release_graph(); return rc; }
-    m->graph_body_kernels = gb.body_kernels;
-    m->graph_kernels = captured - (long long)m->graph_solves * gb.body_kernels;
-    e = cudaGraphInstantiate(&m->gexec, m->graph, 0);
-    if (e != cudaSuccess) { m->release_graph(); return cuda_status(e, "cudaGraphInstantiate"); }
+    if (!rc) {
+        *body_kernels = gb.body_kernels;
+        *kernels = captured - (long long)m->graph_solves * gb.body_kernels;
+        e = cudaGraphInstantiate(exec, *graph, 0);
+        if (e != cudaSuccess) rc = cuda_status(e, "cudaGraphInstantiate");
+    }
+    if (rc) {
+        if (*graph) cudaGraphDestroy(*graph);
+        *graph = nullptr;
+        *exec = nullptr;
+    }
+    return rc;
+}
+
+extern "C" {
+
+int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
+    if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
+    m->release_graph();
+    return record_steps(m, dt, nsteps, &m->graph, &m->gexec, &m->graph_kernels, &m->graph_body_kernels);
+}
+
+int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table) {
+    if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
+    if (nrun < 1 || nrun > NYLES_MAX_BATCH || !table || (((uintptr_t)table) & 7)) {
+        set_error("batched capture: 1 <= nrun <= NYLES_MAX_BATCH and an 8-byte aligned device table required");
+        return NYLES_BAD_ARG;
+    }
+    const NylesDesc& d = m->d;
+    if (m->precision != NYLES_MIXED || m->mg.krylov || d.model != NYLES_MODEL_LES || d.n_tracers != 0 ||
+        d.tracer_diffusion != 0 || d.tracer_order != 0 || d.vf_order != 0) {
+        set_error("batched steps cover the mixed-precision LES model with the stationary pressure solve, "
+                  "no tracers and the reference's schemes");
+        return NYLES_UNSUPPORTED;
+    }
+    m->release_batch();
+    m->bat.tab = reinterpret_cast<BatchTab*>(table);
+    m->bat.nrun = nrun;
+    m->bat.gate = GATE_ACTIVE;
+    m->mg.bat = m->bat;
+    const int solves = m->graph_solves;   // of the one-run graph, if any
+    int rc = record_steps(m, dt, nsteps, &m->bgraph, &m->bgexec, &m->bgraph_kernels, &m->bgraph_body_kernels);
+    m->graph_solves = solves;
+    m->bat = Bat();
+    m->mg.bat = Bat();
+    return rc;
+}
+
+int nyles_model_batch_launch(NylesModel* m, void* stream) {
+    if (!m || !m->bgexec) { set_error("no captured batched graph"); return NYLES_BAD_ARG; }
+    cudaError_t e = cudaGraphLaunch(m->bgexec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGraphLaunch");
+    note_launch((int)m->bgraph_kernels);
+    return NYLES_OK;
+}
+
+int nyles_model_batch_release(NylesModel* m) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    m->release_batch();
+    return NYLES_OK;
+}
+
+int nyles_model_batch_note_iterations(NylesModel* m, long long iterations) {
+    if (!m || iterations < 0) { set_error("null model or negative count"); return NYLES_BAD_ARG; }
+    note_launch((int)(iterations * m->bgraph_body_kernels));
+    return NYLES_OK;
+}
+
+int nyles_model_device_stats(NylesModel* m, NylesMgStats* stats, void* stream) {
+    if (!m || !m->bound || !stats) { set_error("model not bound or null output"); return NYLES_BAD_ARG; }
+    MgDeviceStats ds;
+    int rc = mg_read_device_stats(&m->mg, (cudaStream_t)stream, &ds);
+    if (rc) return rc;
+    *stats = NylesMgStats{};
+    stats->nite = ds.nite;
+    stats->res = ds.res;
+    stats->vcycles = ds.vcycles;
+    stats->not_converged = (int)ds.not_converged;
+    stats->nonfinite = (int)ds.nonfinite;
     return NYLES_OK;
 }
 

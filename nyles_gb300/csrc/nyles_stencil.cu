@@ -82,6 +82,21 @@ struct RhsArgs {
     int lo[3], hi[3]; // k_rhs_march: index box (z, y, x) of the cells it computes
 };
 
+// every pointer of the arguments shifted by dlt bytes (batched launches)
+template <typename T>
+__device__ __forceinline__ void shift_rhs_args(RhsArgs<T>& a, long long dlt) {
+    a.b = bshift(a.b, dlt);
+    a.ke = bshift(a.ke, dlt);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        a.U[i] = bshift(a.U[i], dlt);
+        a.W[i] = bshift(a.W[i], dlt);
+        a.u[i] = bshift(a.u[i], dlt);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a.ds[q] = bshift(a.ds[q], dlt);
+}
+
 // viscosity along direction d of component field u at c, core/fortran_dissipation.f90:18-33
 template <typename T>
 __device__ __forceinline__ T lap1d(const T* __restrict__ u, const Geom& g, long long c, int i, int d) {
@@ -316,13 +331,23 @@ struct TracerMarch {
 template <typename T> struct RhsMinBlocks { static constexpr int n = 5; };
 template <> struct RhsMinBlocks<double> { static constexpr int n = 4; };
 
-template <typename T, bool TR, int VF, bool BDIFF>
-__global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march(const RhsArgs<T> a) {
+// BAT: batched launch (bat names the runs; ds[0..3] and the fields of each run are
+// shifted to its memory; a batched instance exists for the buoyancy-and-WENO form only)
+template <typename T, bool TR, int VF, bool BDIFF, bool BAT = false>
+__global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march(const RhsArgs<T> a0,
+                                                                               const Bat bat = Bat()) {
     __shared__ T sfy[RZ_BY][RZ_BX];
+    int bz = blockIdx.z;
+    RhsArgs<T> a = a0;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        shift_rhs_args(a, dlt);
+    }
     const Geom& g = a.g;
     const int x = a.lo[2] + blockIdx.x * RZ_BX + threadIdx.x;
     const int y = a.lo[1] + blockIdx.y * RZ_BY + threadIdx.y;
-    const int z0 = a.lo[0] + blockIdx.z * RZ_ZC;
+    const int z0 = a.lo[0] + bz * RZ_ZC;
     const int z1 = min(z0 + RZ_ZC, a.hi[0]) - 1;
     const int Nz = g.N[0], Ny = g.N[1], Nx = g.N[2];
     const bool valid = x < a.hi[2] && y < a.hi[1];
@@ -478,7 +503,7 @@ static dim3 grid3(const Geom& g, dim3 blk) {
 
 template <typename T>
 int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const ProgPtrs<T>& ds, int terms,
-               cudaStream_t st, bool interior) {
+               cudaStream_t st, bool interior, const Bat& bat) {
     RhsArgs<T> a;
     a.g = g;
     // interior: the b and u tendencies of the periodic halo are not computed (the time
@@ -551,6 +576,16 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
     const bool tr = (terms & TERM_TRACER) != 0, vf = (terms & TERM_VF) != 0;
     const bool bdiff = tr && (terms & TERM_TRDIFF) && (d->tracer_diffusion & 1);
     const bool lin = vf && d->vf_order > 0;
+    if (bat.tab) {   // batched: buoyancy advection, WENO vortex force, no buoyancy diffusion
+        if (!(tr && vf && !bdiff && !lin && !linear_tr && d->n_tracers == 0 && d->model != NYLES_MODEL_ADVECTION)) {
+            set_error("batched right-hand side: only buoyancy advection with the WENO vortex force and no tracers");
+            return NYLES_UNSUPPORTED;
+        }
+        const dim3 gb(grd_box.x, grd_box.y, grd_box.z * bat.nrun);
+        k_rhs_march<T, true, 1, false, true><<<gb, blk, 0, st>>>(a, bat);
+        note_launch();
+        return cuda_status(cudaGetLastError(), "rhs kernel");
+    }
     if (lin) {   // the linear vortex force (opt-in)
         if (tr && bdiff) k_rhs_march<T, true, 2, true><<<grd_box, blk, 0, st>>>(a);
         else if (tr) k_rhs_march<T, true, 2, false><<<grd_box, blk, 0, st>>>(a);
@@ -599,7 +634,19 @@ struct UpdArgs {
 
 // numpy's evaluation order of core/timescheme.py:113-221, one rounding per operation
 template <typename T>
-__global__ void k_update(const UpdArgs<T> p) {
+__global__ void k_update(const UpdArgs<T> p0, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    UpdArgs<T> p = p0;
+    if (dlt) {
+        for (int q = 0; q < NYLES_MAX_PROG; ++q) {
+            p.s[q] = bshift(p.s[q], dlt);
+            p.a[q] = bshift(p.a[q], dlt);
+            p.b[q] = bshift(p.b[q], dlt);
+            p.c[q] = bshift(p.c[q], dlt);
+        }
+    }
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.vol; i += stride) {
         for (int q = 0; q < p.nprog; ++q) {
@@ -654,7 +701,7 @@ __global__ void k_update(const UpdArgs<T> p) {
 
 template <typename T>
 int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs<T>& a, const ProgPtrs<T>& b,
-                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st) {
+                  const ProgPtrs<T>& c, int kind, double dt, cudaStream_t st, const Bat& bat) {
     UpdArgs<T> p;
     p.vol = g.vol;
     p.nprog = nprog;
@@ -665,7 +712,7 @@ int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs
     }
     long long blocks = (g.vol + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_update<T><<<(unsigned)blocks, 256, 0, st>>>(p);
+    k_update<T><<<dim3((unsigned)blocks, 1, bat.tab ? bat.nrun : 1), 256, 0, st>>>(p, bat);
     note_launch();
     return cuda_status(cudaGetLastError(), "update kernel");
 }
@@ -689,7 +736,10 @@ struct FillArgs {
 };
 
 template <typename T>
-__global__ void k_fill(const FillArgs<T> a) {
+__global__ void k_fill(const FillArgs<T> a, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
     const int s = blockIdx.y;
     if (s >= a.sl.nslab) return;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -701,7 +751,10 @@ __global__ void k_fill(const FillArgs<T> a) {
     const Geom& g = a.g;
     const long long dst = g.at(z, y, x);
     const long long src = g.at(g.wrap(0, z), g.wrap(1, y), g.wrap(2, x));
-    for (int k = 0; k < a.nf; ++k) a.f[k][dst] = a.f[k][src];
+    for (int k = 0; k < a.nf; ++k) {
+        T* f = bshift(a.f[k], dlt);
+        f[dst] = f[src];
+    }
 }
 
 static FillSlabs make_slabs(const Geom& g) {
@@ -728,7 +781,7 @@ static FillSlabs make_slabs(const Geom& g) {
 }
 
 template <typename T>
-int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st) {
+int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st, const Bat& bat) {
     FillArgs<T> a;
     a.g = g;
     a.sl = make_slabs(g);
@@ -738,8 +791,8 @@ int launch_fill(const Geom& g, T* const* fields, int nf, cudaStream_t st) {
     for (int base = 0; base < nf; base += 8) {
         a.nf = (nf - base) < 8 ? (nf - base) : 8;
         for (int k = 0; k < a.nf; ++k) a.f[k] = fields[base + k];
-        dim3 grd((unsigned)((mx + 255) / 256), a.sl.nslab);
-        k_fill<T><<<grd, 256, 0, st>>>(a);
+        dim3 grd((unsigned)((mx + 255) / 256), a.sl.nslab, bat.tab ? bat.nrun : 1);
+        k_fill<T><<<grd, 256, 0, st>>>(a, bat);
         note_launch();
     }
     return cuda_status(cudaGetLastError(), "fill kernel");
@@ -802,11 +855,20 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div(const Geom g, const T* __
 __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const float* __restrict__ ux,
                                                           const float* __restrict__ uy, const float* __restrict__ uz,
                                                           float2 idx2, float2 idy2, float2 idz2,
-                                                          float* __restrict__ div, float2* __restrict__ mgb) {
+                                                          float* __restrict__ div, float2* __restrict__ mgb,
+                                                          const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    ux = bshift(ux, dlt);
+    uy = bshift(uy, dlt);
+    uz = bshift(uz, dlt);
+    div = bshift(div, dlt);
+    mgb = bshift(mgb, dlt);
     const int x = blockIdx.x * PJ_BX + threadIdx.x;
     const int y = blockIdx.y * PJ_BY + threadIdx.y;
     if (x >= g.N[2] || y >= g.N[1]) return;
-    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int z0 = bz * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
     const int yy = g.wrap(1, y), xx = g.wrap(2, x);
     const bool own_xy = yy == y && xx == x;
     const long long cxy = (long long)yy * g.sy + xx;
@@ -838,10 +900,13 @@ int launch_div(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, TB* m
     return cuda_status(cudaGetLastError(), "div kernel");
 }
 
-int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st) {
-    k_div_df<<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
-                                             df_split(d->idx2), df_split(d->idy2), df_split(d->idz2),
-                                             s.f[NYLES_F_DIV], mg_b);
+int launch_div_df(const NylesDesc* d, const Geom& g, const StencilPtrs<float>& s, float2* mg_b, cudaStream_t st,
+                  const Bat& bat) {
+    dim3 grd = grid_pj(g);
+    if (bat.tab) grd.z *= bat.nrun;
+    k_div_df<<<grd, dim3(PJ_BX, PJ_BY), 0, st>>>(g, s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K],
+                                                 df_split(d->idx2), df_split(d->idy2), df_split(d->idz2),
+                                                 s.f[NYLES_F_DIV], mg_b, bat);
     note_launch();
     return cuda_status(cudaGetLastError(), "div kernel");
 }
@@ -919,12 +984,21 @@ struct CorrDfArgs {
 };
 
 // one thread per (y, x) column of the array, PJ_ZC cells in z (as k_div_df)
-__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a) {
+__global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a0, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    CorrDfArgs a = a0;
+    if (dlt) {
+        for (int i = 0; i < 3; ++i) a.u[i] = bshift(a.u[i], dlt);
+        a.x = bshift(a.x, dlt);
+        a.p = bshift(a.p, dlt);
+    }
     const Geom& g = a.g;
     const int x = blockIdx.x * PJ_BX + threadIdx.x;
     const int y = blockIdx.y * PJ_BY + threadIdx.y;
     if (x >= g.N[2] || y >= g.N[1]) return;
-    const int z0 = blockIdx.z * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
+    const int z0 = bz * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
     const int oz = g.per[0] ? g.nh : 0, oy = g.per[1] ? g.nh : 0, ox = g.per[2] ? g.nh : 0;
     const int yy = g.wrap(1, y), xx = g.wrap(2, x);
     const bool own_xy = yy == y && xx == x;
@@ -951,14 +1025,17 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a
     }
 }
 
-int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st) {
+int launch_correct_df(const Geom& g, const StencilPtrs<float>& s, const float2* mg_x, double dx2, cudaStream_t st,
+                      const Bat& bat) {
     CorrDfArgs a;
     a.g = g;
     for (int i = 0; i < 3; ++i) a.u[i] = s.f[NYLES_F_U_I + i];
     a.x = mg_x;
     a.p = s.f[NYLES_F_P];
     a.dx2 = df_split(dx2);
-    k_correct_df<<<grid_pj(g), dim3(PJ_BX, PJ_BY), 0, st>>>(a);
+    dim3 grd = grid_pj(g);
+    if (bat.tab) grd.z *= bat.nrun;
+    k_correct_df<<<grd, dim3(PJ_BX, PJ_BY), 0, st>>>(a, bat);
     note_launch();
     return cuda_status(cudaGetLastError(), "correct kernel");
 }
@@ -983,11 +1060,23 @@ struct DiagArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_diag(const DiagArgs<T> a) {
+__global__ void __launch_bounds__(256) k_diag(const DiagArgs<T> a0, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    DiagArgs<T> a = a0;
+    if (dlt) {
+        for (int i = 0; i < 3; ++i) {
+            a.u[i] = bshift(a.u[i], dlt);
+            a.U[i] = bshift(a.U[i], dlt);
+            a.W[i] = bshift(a.W[i], dlt);
+        }
+        a.ke = bshift(a.ke, dlt);
+    }
     const Geom& g = a.g;
     const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int y0 = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z0 = blockIdx.z * blockDim.z + threadIdx.z;
+    const int z0 = bz * blockDim.z + threadIdx.z;
     if (x0 >= g.N[2] || y0 >= g.N[1] || z0 >= g.N[0]) return;
     const long long c0 = g.at(z0, y0, x0);
     const T* __restrict__ ux = a.u[0];
@@ -1017,7 +1106,8 @@ __global__ void __launch_bounds__(256) k_diag(const DiagArgs<T> a) {
 }
 
 template <typename T>
-int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st) {
+int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int nonlinear, cudaStream_t st,
+                const Bat& bat) {
     DiagArgs<T> a;
     a.g = g;
     for (int i = 0; i < 3; ++i) {
@@ -1034,7 +1124,9 @@ int launch_diag(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, int 
     a.fparam = T(d->fparam);
     a.nonlinear = nonlinear;
     dim3 blk(32, 4, 2);
-    k_diag<T><<<grid3(g, blk), blk, 0, st>>>(a);
+    dim3 grd = grid3(g, blk);
+    if (bat.tab) grd.z *= bat.nrun;
+    k_diag<T><<<grd, blk, 0, st>>>(a, bat);
     note_launch();
     return cuda_status(cudaGetLastError(), "diag kernel");
 }
@@ -1199,11 +1291,12 @@ int launch_flux1d(const T* u, const T* q, T* flux, int nlines, int n, cudaStream
 // ---------------------------------------------------------------- instantiations
 #define NYLES_INST(T)                                                                                          \
     template int launch_rhs<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, const ProgPtrs<T>&, int, \
-                               cudaStream_t, bool);                                                            \
+                               cudaStream_t, bool, const Bat&);                                                \
     template int launch_update<T>(const Geom&, int, const ProgPtrs<T>&, const ProgPtrs<T>&, const ProgPtrs<T>&, \
-                                  const ProgPtrs<T>&, int, double, cudaStream_t);                              \
-    template int launch_fill<T>(const Geom&, T* const*, int, cudaStream_t);                                    \
-    template int launch_diag<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, int, cudaStream_t);      \
+                                  const ProgPtrs<T>&, int, double, cudaStream_t, const Bat&);                  \
+    template int launch_fill<T>(const Geom&, T* const*, int, cudaStream_t, const Bat&);                        \
+    template int launch_diag<T>(const NylesDesc*, const Geom&, const StencilPtrs<T>&, int, cudaStream_t,       \
+                                const Bat&);                                                                   \
     template int launch_max_U2<T>(const Geom&, const StencilPtrs<T>&, double*, int, double*, cudaStream_t);   \
     template int launch_vfwork<T>(const Geom&, const StencilPtrs<T>&, const ProgPtrs<T>&, const VfBox&, double*, \
                                   int, double*, cudaStream_t);                                                 \

@@ -65,7 +65,7 @@ class LES(object):
 
     modelname = "LES"
 
-    def __init__(self, param, grid, linear=False, device=None):
+    def __init__(self, param, grid, linear=False, device=None, arena=None):
         if not torch.cuda.is_available():
             raise RuntimeError("nyles_gb300 needs a CUDA GPU: the model runs only through libnyles_gb300.so")
         self.lib = nat.lib()
@@ -82,7 +82,7 @@ class LES(object):
         if ntr > nat.MAX_TRACERS:
             raise ValueError("at most %d tracers" % nat.MAX_TRACERS)
         self.traclist = ["b"] + var.tracer_names(ntr) if self.modelname != "Euler3d" else [""] + var.tracer_names(ntr)
-        self.state = var.get_state(param, dtype=self.dtype, device=self.device)
+        self.state = var.get_state(param, dtype=self.dtype, device=self.device, arena=arena)
         self.neighbours = param["neighbours"]
         self.orderA = param.get("orderA", 5)
         self.orderVF = param.get("orderVF", 5)
@@ -95,7 +95,7 @@ class LES(object):
             self.viscosity = self.diff_coef["u"]
         self.fparameter = param["coriolis"] * grid.dx * grid.dy if self.rotating else 0.0
         self.desc = make_desc(param, grid, self.modelname)
-        self.timescheme = ts.Timescheme(param, self.state, model=self)
+        self.timescheme = ts.Timescheme(param, self.state, model=self, arena=arena)
         self.timescheme.set(self.rhs, self.diagnose_var)
         # native model: arrays owned here, pointers bound once
         h = ctypes.c_void_p()
@@ -104,10 +104,14 @@ class LES(object):
         self._h = h
         nbytes = ctypes.c_size_t()
         nat.check(self.lib.nyles_model_workspace_bytes(h, ctypes.byref(nbytes)))
-        self.workspace = torch.zeros(nbytes.value + 256, dtype=torch.uint8, device=self.device)
-        ws = self.workspace.data_ptr()
-        ws = (ws + 255) & ~255
-        off = ws - self.workspace.data_ptr()
+        if arena is not None:
+            self.workspace = arena.take((nbytes.value,), torch.uint8)
+            ws, off = self.workspace.data_ptr(), 0
+        else:
+            self.workspace = torch.zeros(nbytes.value + 256, dtype=torch.uint8, device=self.device)
+            ws = self.workspace.data_ptr()
+            ws = (ws + 255) & ~255
+            off = ws - self.workspace.data_ptr()
         self._ws_used = self.workspace[off:off + nbytes.value]   # the aligned bytes the library uses
         self._fields = nat.ptr_array([s.data_ptr() for s in self.state.scalars()])
         self._regs = nat.ptr_array(self.timescheme.register_pointers())
@@ -333,8 +337,8 @@ class Euler3d(LES):
 
     modelname = "Euler3d"
 
-    def __init__(self, param, grid, device=None):
+    def __init__(self, param, grid, device=None, arena=None):
         if param["geometry"] not in ("closed", "perio_xyz"):
             # core/model_les_euler.py:80-90 maps only closed and perio_xyz to a multigrid topology
             raise ValueError("Euler3d supports the geometries closed and perio_xyz")
-        super().__init__(param, grid, linear=False, device=device)
+        super().__init__(param, grid, linear=False, device=device, arena=arena)

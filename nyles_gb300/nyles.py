@@ -24,39 +24,73 @@ from . import online_diag
 from . import topology as topo
 
 
-class Nyles(object):
-    def __init__(self, user_param, device=None):
-        user_param.check()
-        user_param.freeze()
-        param = dict(user_param.view_parameters())
-        param["gpu"] = dict(user_param.gpu)
-        self.param = param
-        npx, npy, npz = param["npx"], param["npy"], param["npz"]
-        if (npx, npy, npz) != (1, 1, 1):
-            raise NotImplementedError("one subdomain per GPU: npx = npy = npz = 1 (no MPI in this build)")
-        param["nx"] = param["global_nx"] // npx
-        param["ny"] = param["global_ny"] // npy
-        param["nz"] = param["global_nz"] // npz
-        procs = [npz, npy, npx]
-        myrank = 0
-        loc = topo.rank2loc(myrank, procs)
-        neighbours = topo.get_neighbours(loc, procs, param["geometry"])
-        param["procs"] = procs
-        param["myrank"] = myrank
-        param["neighbours"] = neighbours
-        param["loc"] = loc
-        self.myrank = myrank
-        self.grid = grid_module.Grid(param)
-        self.initiate(param, device)
+def prepare_parameters(user_param):
+    """Checked parameter dictionary of one subdomain (core/nyles.py:44-76): nx/ny/nz,
+    the processor layout, neighbours and location, and the gpu category."""
+    user_param.check()
+    user_param.freeze()
+    param = dict(user_param.view_parameters())
+    param["gpu"] = dict(user_param.gpu)
+    npx, npy, npz = param["npx"], param["npy"], param["npz"]
+    if (npx, npy, npz) != (1, 1, 1):
+        raise NotImplementedError("one subdomain per GPU: npx = npy = npz = 1 (no MPI in this build)")
+    param["nx"] = param["global_nx"] // npx
+    param["ny"] = param["global_ny"] // npy
+    param["nz"] = param["global_nz"] // npz
+    procs = [npz, npy, npx]
+    loc = topo.rank2loc(0, procs)
+    param["procs"] = procs
+    param["myrank"] = 0
+    param["neighbours"] = topo.get_neighbours(loc, procs, param["geometry"])
+    param["loc"] = loc
+    return param
 
-    def initiate(self, param, device=None):
+
+def arena_bytes(user_param):
+    """Bytes of the Arena (variables.Arena) that a Nyles model of these parameters
+    carves its arrays from: the state, the time-scheme registers and the library's
+    workspace, each 256-byte aligned."""
+    import ctypes
+    from . import _native as nat
+    from . import variables as var
+    param = prepare_parameters(user_param)
+    grid = grid_module.Grid(param)
+    size, _ = var.variable_shape(param)
+    vol = int(size[0]) * int(size[1]) * int(size[2])
+    prec = param["gpu"].get("precision", "fp64")
+    es = 8 if prec == "fp64" else 4
+    ntr = param.get("n_tracers", 0)
+    desc = model_les.make_desc(param, grid, param["modelname"])
+    h = ctypes.c_void_p()
+    nat.check(nat.lib().nyles_model_create(ctypes.byref(desc), nat.SCHEME[param["timestepping"]],
+                                           nat.PRECISION[prec], ctypes.byref(h)))
+    try:
+        nb = ctypes.c_size_t()
+        nat.check(nat.lib().nyles_model_workspace_bytes(h, ctypes.byref(nb)))
+    finally:
+        nat.lib().nyles_model_destroy(h)
+    A = var.Arena.aligned
+    return A((14 + ntr) * vol * es) + A(3 * (4 + ntr) * vol * es) + A(nb.value)
+
+
+class Nyles(object):
+    def __init__(self, user_param, device=None, arena=None):
+        param = prepare_parameters(user_param)
+        self.param = param
+        self.myrank = param["myrank"]
+        self.grid = grid_module.Grid(param)
+        self.initiate(param, device, arena)
+
+    def initiate(self, param, device=None, arena=None):
+        """The model of `modelname` (core/nyles.py:92-100). `arena` (variables.Arena):
+        carve the model's arrays from one buffer (batched serving)."""
         name = param["modelname"]
         if name == "LES":
-            self.model = model_les.LES(param, self.grid, device=device)
+            self.model = model_les.LES(param, self.grid, device=device, arena=arena)
         elif name == "Euler3d":
-            self.model = model_les.Euler3d(param, self.grid, device=device)
+            self.model = model_les.Euler3d(param, self.grid, device=device, arena=arena)
         elif name == "linear":
-            self.model = model_les.LES(param, self.grid, linear=True, device=device)
+            self.model = model_les.LES(param, self.grid, linear=True, device=device, arena=arena)
         elif name == "advection":
             self.model = model_advection.Advection(param, self.grid, device=device)
         else:

@@ -1,14 +1,14 @@
 """Serving engine: continuous batching of independent Nyles runs on one GPU.
 
 Requests (a lock exchange or a Taylor-Green case on an n^3 grid, a number of steps, a
-noise seed) arrive over time. The engine admits a request as soon as its device
-footprint fits the HBM budget, builds the run (state, multigrid, initial projection)
-and captures a CUDA graph of k time steps; from then on the run is resident and is
-advanced by replaying that graph on its own stream. Every engine tick keeps up to two
-graph launches in flight per run, so runs of every size overlap on the device while new
-ones are admitted and finished ones release their memory. Runs are grouped into size
-buckets (same case and grid: same graph shape and footprint) for admission and
-reporting. Completion latency = time from arrival to the end of the run's last step.
+noise seed) arrive over time. Runs of the same case and grid form a bucket: its runs
+live in the slots of one device buffer, and one batched CUDA graph of k time steps,
+whose every kernel covers all slots of the bucket, advances all of them with a single
+launch (nyles_model_batch_capture). A request is admitted as soon as its bucket has a
+free slot (or a new bucket fits the HBM budget); it joins the bucket's next launch
+after its initial projection, and frees its slot when its last launch completes.
+Buckets run on their own streams, so every size overlaps on the device.
+Completion latency = time from arrival to the end of the run's last step.
 
 The reference has no serving layer (one experiment per process, core/nyles.py).
 """
@@ -156,99 +156,230 @@ def steps_per_graph(steps, kmax=10):
     return 1
 
 
-class Run:
-    """One admitted request: resident state, its stream (of CUDA priority `priority`,
-    lower = scheduled first) and its captured graph."""
+class Slot:
+    """One place of a bucket: a model whose arrays are carved from the slot's part of
+    the bucket buffer, and the request it currently serves (None: free)."""
 
-    def __init__(self, req, precision, device, mg_tol, priority=0):
-        self.req = req
-        self.nyl = Nyles(build_params(req.case, req.n, precision, mg_tol), device=device)
-        initial_state(self.nyl, req.case, req.seed)
-        m = self.nyl.model
-        m.diagnose_var(m.state)                       # core/nyles.py:122
-        self.k = steps_per_graph(req.steps)
-        m.capture_graph(CASES[req.case]["dt"], self.k)
-        self.stream = torch.cuda.Stream(device=device, priority=priority)
-        self.stream.wait_stream(torch.cuda.current_stream(device))
+    def __init__(self, index, nyl):
+        self.index = index
+        self.nyl = nyl
+        self.req = None
+        self.ready = None          # event: the run's setup (zeroing, initial state, projection) done
+        self.setup_pending = False
         self.launched = 0
-        self.inflight = []                            # events of launches not yet seen complete
-        self.last_event = None
+        self.last_event = None     # event of the latest launch that advanced this run
+        self.admitted = 0.0
+        self.failed = None         # status when the setup already failed
 
-    def launch(self):
-        self.nyl.model.replay(stream=self.stream)
-        ev = torch.cuda.Event()
-        ev.record(self.stream)
-        self.inflight.append(ev)
-        self.last_event = ev
-        self.launched += self.k
+    @property
+    def active(self):
+        return self.req is not None and self.failed is None and self.launched < self.req.steps
 
+    def finished(self):
+        if self.req is None:
+            return False
+        if self.failed is not None:
+            return True
+        return self.launched >= self.req.steps and (self.last_event is None or self.last_event.query())
+
+
+class Bucket:
+    """The resident runs of one (case, grid, steps per launch) on `capacity` slots of one
+    device buffer. Every slot's model is built in an Arena of the same size, so its
+    arrays sit at the same offsets: run r's memory is slot 0's shifted by r x slot_bytes.
+    One batched graph of k time steps (captured on slot 0's model, every kernel covering
+    all slots) advances every active slot; a slot whose run is done, or free, is skipped
+    by all kernels (its table entry is inactive), and each run's pressure solves stop on
+    their own, so a run's result is the same whatever else shares the launch. Runs join
+    at launch boundaries: a new run's state is zeroed, initialised and projected on a
+    setup stream while the bucket's launches go on."""
+
+    def __init__(self, key, precision, mg_tol, device, capacity, priority=0):
+        import ctypes
+        from . import _native as nat
+        from .nyles import arena_bytes
+        from .variables import Arena
+        case, n, k = key
+        self.key, self.case, self.n, self.k = key, case, n, k
+        self.capacity = capacity
+        self.slot_bytes = Arena.aligned(arena_bytes(build_params(case, n, precision, mg_tol)))
+        self.bytes = self.slot_bytes * capacity
+        self.buf = torch.zeros(self.bytes, dtype=torch.uint8, device=device)
+        self.slots = []
+        for r in range(capacity):
+            arena = Arena(self.buf[r * self.slot_bytes:(r + 1) * self.slot_bytes])
+            self.slots.append(Slot(r, Nyles(build_params(case, n, precision, mg_tol), device=device, arena=arena)))
+        self.lib = nat.lib()
+        self.nat = nat
+        tb = ctypes.sizeof(nat.NylesBatchTable)
+        self.table = torch.zeros(tb, dtype=torch.uint8, device=device)
+        # the host writes delta and active (the leading fields); live and loop_iterations
+        # belong to the device
+        self.host_bytes = nat.NylesBatchTable.live.offset
+        self.ring = [torch.zeros(tb, dtype=torch.uint8).pin_memory() for _ in range(4)]
+        self.ring_events = [None] * len(self.ring)
+        self.ring_pos = 0
+        for buf in self.ring:
+            t = nat.NylesBatchTable.from_address(buf.data_ptr())
+            for r in range(capacity):
+                t.delta[r] = r * self.slot_bytes
+        self.stream = torch.cuda.Stream(device=device, priority=priority)
+        self.setup_stream = torch.cuda.Stream(device=device, priority=priority)
+        self.read_stream = torch.cuda.Stream(device=device, priority=priority)
+        self.inflight = []
+        self.launches = 0
+        self.template = self.slots[0].nyl.model
+        nat.check(self.lib.nyles_model_batch_capture(self.template._h, CASES[case]["dt"], k, capacity,
+                                                     ctypes.c_void_p(self.table.data_ptr())))
+
+    # ---- slots
+    def free_slot(self):
+        return next((sl for sl in self.slots if sl.req is None), None)
+
+    def resident(self):
+        return [sl for sl in self.slots if sl.req is not None]
+
+    def admit(self, slot, req, now):
+        """Zero the slot (a fresh allocation's contents), write the request's initial
+        state and project it (core/nyles.py:122) on the setup stream."""
+        from . import _native as nat
+        slot.req, slot.launched, slot.last_event, slot.failed = req, 0, None, None
+        slot.admitted = now
+        lo = slot.index * self.slot_bytes
+        with torch.cuda.stream(self.setup_stream):
+            self.buf[lo:lo + self.slot_bytes].zero_()
+            initial_state(slot.nyl, req.case, req.seed)
+            try:
+                slot.nyl.model.diagnose_var(slot.nyl.model.state)
+            except nat.BlowUp:
+                slot.failed = "blowup"
+            slot.ready = torch.cuda.Event()
+            slot.ready.record(self.setup_stream)
+        slot.setup_pending = True
+
+    # ---- launches
     def poll(self):
         while self.inflight and self.inflight[0].query():
             self.inflight.pop(0)
         return len(self.inflight)
 
-    @property
-    def all_launched(self):
-        return self.launched >= self.req.steps
+    def launch(self):
+        """Advance every active slot by k steps with one graph launch."""
+        act = [sl for sl in self.slots if sl.active]
+        if not act:
+            return False
+        i = self.ring_pos
+        self.ring_pos = (i + 1) % len(self.ring)
+        if self.ring_events[i] is not None:
+            self.ring_events[i].synchronize()          # the pinned buffer's previous copy is done
+        t = self.nat.NylesBatchTable.from_address(self.ring[i].data_ptr())
+        for r in range(self.capacity):
+            t.active[r] = 0
+        for sl in act:
+            t.active[sl.index] = 1
+            if sl.setup_pending:
+                self.stream.wait_event(sl.ready)
+                sl.setup_pending = False
+        with torch.cuda.stream(self.stream):
+            self.table[:self.host_bytes].copy_(self.ring[i][:self.host_bytes], non_blocking=True)
+        ev_tab = torch.cuda.Event()
+        ev_tab.record(self.stream)
+        self.ring_events[i] = ev_tab
+        self.nat.check(self.lib.nyles_model_batch_launch(self.template._h, self.nat.stream_ptr(self.stream)))
+        ev = torch.cuda.Event()
+        ev.record(self.stream)
+        self.inflight.append(ev)
+        self.launches += 1
+        for sl in act:
+            sl.launched += self.k
+            sl.last_event = ev
+        return True
 
-    def finished(self):
-        return self.all_launched and self.poll() == 0
-
-    def vcycles(self):
-        return self.nyl.model.mg_stats()["vcycles"]
-
-    def outcome(self):
-        """(status, V-cycles) of a finished run: "blowup" when a pressure solve met a
+    # ---- completion
+    def outcome(self, slot, keep_state=False):
+        """(status, V-cycles, final fields or None) of a finished run, read on the read
+        stream once its last launch is complete: "blowup" when a pressure solve met a
         non-finite norm or the final velocity is not finite, "not_converged" when a
         solve stopped at maxite above the tolerance, else "ok"."""
-        from . import _native as nat
-        m = self.nyl.model
-        s = m.mg_stats()
-        status = "ok"
-        if s["nonfinite"] > 0:
-            status = "blowup"
-        else:
-            try:
-                m.max_U2()
-            except nat.BlowUp:
+        import ctypes
+        nat = self.nat
+        if slot.failed is not None:
+            return slot.failed, 0, None
+        m = slot.nyl.model
+        st = nat.NylesMgStats()
+        with torch.cuda.stream(self.read_stream):
+            if slot.last_event is not None:
+                self.read_stream.wait_event(slot.last_event)
+            nat.check(self.lib.nyles_model_device_stats(m._h, ctypes.byref(st), nat.stream_ptr(self.read_stream)))
+            status = "ok"
+            if st.nonfinite > 0:
                 status = "blowup"
-        if status == "ok" and s["not_converged"] > 0:
-            status = "not_converged"
-        return status, s["vcycles"]
+            else:
+                try:
+                    m.max_U2()
+                except nat.BlowUp:
+                    status = "blowup"
+            if status == "ok" and st.not_converged > 0:
+                status = "not_converged"
+            fields = None
+            if keep_state:
+                fields = {s: m.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k", "p")}
+        return status, st.vcycles, fields
 
-    def final_state(self):
-        st = self.nyl.model.state
-        return {s: st.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k", "p")}
+    def release(self, slot):
+        slot.req = None
+        slot.failed = None
+        slot.last_event = None
+
+    def loop_iterations(self):
+        """multigrid loop-body iterations the batched launches ran (device counter)"""
+        import ctypes
+        t = self.nat.NylesBatchTable()
+        torch.cuda.synchronize(self.table.device)
+        ctypes.memmove(ctypes.addressof(t), self.table.cpu().numpy().ctypes.data, ctypes.sizeof(t))
+        return t.loop_iterations
+
+    def close(self):
+        """Count the loop kernels, release the graph and the memory."""
+        self.stream.synchronize()
+        self.nat.check(self.lib.nyles_model_batch_note_iterations(self.template._h, self.loop_iterations()))
+        self.nat.check(self.lib.nyles_model_batch_release(self.template._h))
+        self.slots = []
+        self.template = None
+        self.buf = None
 
 
-def remaining_work(run):
-    """cells x steps not yet launched"""
-    return run.req.n ** 3 * max(0, run.req.steps - run.launched)
+def remaining_work(bucket):
+    """cells x steps not yet launched in a bucket"""
+    return sum(bucket.n ** 3 * max(0, sl.req.steps - sl.launched) for sl in bucket.slots if sl.req is not None)
 
 
 class ServingEngine:
-    """Admission against an HBM budget, resident runs, overlapping graph replays.
+    """Continuous batching: admission against an HBM budget, resident runs grouped into
+    size buckets, one batched graph launch per bucket advancing all of its runs.
 
-    priority "work" (default) gives each run's stream a CUDA priority by its total work
-    (cells x steps): the GPU schedules the blocks of small runs first; "none" gives every
-    stream the same priority. `window` = W advances only the W runs with the least
-    remaining work at each tick (shortest remaining work first): small runs complete
-    soon after they arrive, the large ones, which set the makespan, fill the device once
-    the small ones are done; None advances every resident run."""
+    A request is admitted as soon as its bucket (case, grid and steps per launch) has a
+    free slot, or a new bucket fits the budget; a request larger than the whole budget
+    is refused at once. Each bucket keeps up to `inflight` launches queued on its own
+    stream (CUDA priority by the per-run work n^3 x steps, smallest first, with
+    priority "work"; equal with "none"), so buckets of every size overlap on the device.
+    `capacity` = slots per bucket (at most NYLES_BATCH_RUNS); a bucket with no run left
+    and none waiting is released. Completion latency = arrival to the end of the run's
+    last launch."""
 
     def __init__(self, hbm_budget_bytes=120e9, precision="mixed", mg_tol=1e-6, device=None, inflight=2,
-                 clock=time.perf_counter, run_factory=None, priority="work", window=None):
+                 clock=time.perf_counter, bucket_factory=None, priority="work", capacity=16):
         if priority not in ("work", "none"):
             raise ValueError("priority must be 'work' or 'none'")
-        if window is not None and window < 1:
-            raise ValueError("window must be None or >= 1")
+        if not 1 <= capacity <= 32:
+            raise ValueError("capacity must be 1..32 (NYLES_BATCH_RUNS)")
         self.priority = priority
-        self.window = window
+        self.capacity = capacity
         self.budget = float(hbm_budget_bytes)
         self.precision = precision
         self.mg_tol = mg_tol
-        self.run_factory = run_factory or Run
-        if device is None and run_factory is None:
+        self.bucket_factory = bucket_factory or Bucket
+        if device is None and bucket_factory is None:
             device = torch.device("cuda", torch.cuda.current_device())
         self.device = torch.device(device) if device is not None else None
         self.inflight = inflight
@@ -256,6 +387,8 @@ class ServingEngine:
         self.used = 0
         self.peak_used = 0
         self.max_active = 0
+        self.buckets_made = 0
+        self.launches = 0
 
     def serve(self, requests, realtime=True, keep_states=False):
         """Serve `requests` (arrival times relative to now when `realtime`, else all at
@@ -263,62 +396,71 @@ class ServingEngine:
         prognostic fields when keep_states."""
         pending = sorted(requests, key=lambda r: r.arrival)
         prio = self.stream_priorities(requests)
-        queue, active, results, states = [], [], [], {}
+        queue, buckets, results, states = [], {}, [], {}
         t0 = self.clock()
         nxt = 0
-        while nxt < len(pending) or queue or active:
+        while nxt < len(pending) or queue or buckets:
             now = self.clock() - t0
             while nxt < len(pending) and (not realtime or pending[nxt].arrival <= now):
                 queue.append(pending[nxt])
                 nxt += 1
-            # admission: FIFO while the footprint fits; a request larger than the whole
-            # budget is refused at once (it could never fit) and the queue moves on
-            while queue:
-                req = queue[0]
+            # admission, in arrival order; a request whose bucket is full waits without
+            # blocking the others
+            waiting = []
+            for req in queue:
                 need = footprint_bytes(req.case, req.n, self.precision)
                 if need > self.budget:
-                    queue.pop(0)
-                    now = self.clock() - t0
                     results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
                                           now, now, req.n ** 3, 0, "refused"))
                     continue
-                if self.used + need > self.budget and active:
-                    break
-                queue.pop(0)
-                run = self.run_factory(req, self.precision, self.device, self.mg_tol, priority=prio[req.rid])
-                run.admitted = self.clock() - t0
-                run.need = need
-                self.used += need
-                self.peak_used = max(self.peak_used, self.used)
-                active.append(run)
-            self.max_active = max(self.max_active, len(active))
-            # advance: keep up to `inflight` graph launches queued per run, for the
-            # `window` runs with the least remaining work (all runs without a window)
-            order = active if self.window is None else sorted(active, key=remaining_work)[:self.window]
-            for run in order:
-                if not run.all_launched and run.poll() < self.inflight:
-                    run.launch()
+                key = (req.case, req.n, steps_per_graph(req.steps))
+                b = buckets.get(key)
+                if b is None:
+                    cap = min(self.capacity, int((self.budget - self.used) // need))
+                    if cap < 1:
+                        waiting.append(req)
+                        continue
+                    b = self.bucket_factory(key, self.precision, self.mg_tol, self.device, cap,
+                                            priority=prio[req.rid])
+                    buckets[key] = b
+                    self.buckets_made += 1
+                    self.used += b.bytes
+                    self.peak_used = max(self.peak_used, self.used)
+                slot = b.free_slot()
+                if slot is None:
+                    waiting.append(req)
+                    continue
+                b.admit(slot, req, self.clock() - t0)
+            queue = waiting
+            self.max_active = max(self.max_active, sum(len(b.resident()) for b in buckets.values()))
+            # launches
+            busy = False
+            for b in buckets.values():
+                if b.poll() < self.inflight:
+                    busy |= b.launch()
             # completion
-            still = []
-            for run in active:
-                if run.finished():
-                    done = self.clock() - t0
-                    req = run.req
-                    status, vcycles = run.outcome()
-                    results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
-                                          run.admitted, done, req.n ** 3, vcycles, status))
-                    if keep_states:
-                        states[req.rid] = run.final_state()
-                    self.used -= run.need
-                    del run
-                else:
-                    still.append(run)
-            active = still
-            waiting = order if self.window is None else [r for r in order if r in active]
-            if waiting and all(r.all_launched or r.poll() >= self.inflight for r in waiting):
-                time.sleep(2e-4)
-            elif not active and not queue and nxt < len(pending):
-                time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
+            for key in list(buckets):
+                b = buckets[key]
+                for sl in b.slots:
+                    if sl.finished():
+                        req = sl.req
+                        status, vcycles, fields = b.outcome(sl, keep_states)
+                        done = self.clock() - t0
+                        results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
+                                              sl.admitted, done, req.n ** 3, vcycles, status))
+                        if keep_states and fields is not None:
+                            states[req.rid] = fields
+                        b.release(sl)
+                if not b.resident() and not any((r.case, r.n, steps_per_graph(r.steps)) == key for r in queue):
+                    self.launches += b.launches
+                    b.close()
+                    self.used -= b.bytes
+                    del buckets[key]
+            if not busy:
+                if buckets:
+                    time.sleep(2e-4)
+                elif not queue and nxt < len(pending):
+                    time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
         if self.device is not None and self.device.type == "cuda":
             torch.cuda.synchronize(self.device)
         return sorted(results, key=lambda r: r.rid), states

@@ -11,7 +11,7 @@ SCHEMES = ("EF", "LFAM3", "RK3_SSP")
 
 
 class Timescheme(object):
-    def __init__(self, param, state, model=None):
+    def __init__(self, param, state, model=None, arena=None):
         timestepping = param["timestepping"]
         if timestepping not in SCHEMES:
             raise ValueError("unknown time scheme " + repr(timestepping))
@@ -19,7 +19,8 @@ class Timescheme(object):
         self.prognostic_scalars = state.get_prognostic_scalars()
         dtype = state.storage.dtype if state.storage is not None else None
         device = state.storage.device if state.storage is not None else "cpu"
-        self.registers, self.storage = var.get_prognostic_registers(param, 3, dtype=dtype, device=device)
+        self.registers, self.storage = var.get_prognostic_registers(param, 3, dtype=dtype, device=device,
+                                                                    arena=arena)
         self.dstate = self.registers[0]
         if timestepping == "LFAM3":
             self.stateb = self.registers[1]

@@ -165,13 +165,17 @@ def tracer_names(n_tracers):
     return ["t{}".format(i) for i in range(n_tracers)]
 
 
-def get_state(param, dtype=torch.float64, device="cpu"):
+def get_state(param, dtype=torch.float64, device="cpu", arena=None):
     """Full model state in one (nfields, nz, ny, nx) tensor; tracers t0.. come last
-    (core/model_les.py:36-44, core/variables.py:414-437)."""
+    (core/model_les.py:36-44, core/variables.py:414-437). With `arena` (an Arena) the
+    tensor is carved from its buffer instead of allocated."""
     ntr = param.get("n_tracers", 0)
     size, _ = variable_shape(param)
     nf = 14 + ntr
-    storage = torch.zeros((nf,) + tuple(size), dtype=dtype, device=device)
+    if arena is not None:
+        storage = arena.take((nf,) + tuple(size), dtype)
+    else:
+        storage = torch.zeros((nf,) + tuple(size), dtype=dtype, device=device)
     listvar, k = [], 0
     for nickname, var in modelvar.items():
         if var.type == "scalar":
@@ -187,13 +191,16 @@ def get_state(param, dtype=torch.float64, device="cpu"):
     return State(listvar, storage=storage)
 
 
-def get_prognostic_registers(param, nreg, dtype=torch.float64, device="cpu"):
+def get_prognostic_registers(param, nreg, dtype=torch.float64, device="cpu", arena=None):
     """`nreg` States of the prognostic variables (b, u, t0..) in one tensor
     (nreg, nprog, nz, ny, nx) — the time-scheme registers (core/timescheme.py:92-101)."""
     ntr = param.get("n_tracers", 0)
     size, _ = variable_shape(param)
     nprog = 4 + ntr
-    storage = torch.zeros((nreg, nprog) + tuple(size), dtype=dtype, device=device)
+    if arena is not None:
+        storage = arena.take((nreg, nprog) + tuple(size), dtype)
+    else:
+        storage = torch.zeros((nreg, nprog) + tuple(size), dtype=dtype, device=device)
     states = []
     for r in range(nreg):
         lv = [Scalar(param, "buoyancy", "b", "L.T^-2", True, data=storage[r, 0]),
@@ -202,3 +209,34 @@ def get_prognostic_registers(param, nreg, dtype=torch.float64, device="cpu"):
             lv.append(Scalar(param, "tracer{}".format(i), t, "", True, data=storage[r, 4 + i]))
         states.append(State(lv, storage=storage[r]))
     return states, storage
+
+
+class Arena(object):
+    """Sub-allocations from one uint8 device buffer, each 256-byte aligned, handed out in
+    call order. Models built in arenas of the same size from the same parameters get the
+    same layout (each array at the same offset), which batched launches rely on: one
+    run's memory is another's shifted by the distance between their buffers. The buffer
+    must start zeroed, as fresh allocations are."""
+
+    ALIGN = 256
+
+    def __init__(self, buf):
+        if buf.dtype != torch.uint8 or buf.dim() != 1:
+            raise ValueError("an Arena takes a 1-D uint8 tensor")
+        self.buf = buf
+        self.used = 0
+
+    @staticmethod
+    def aligned(nbytes):
+        return (int(nbytes) + Arena.ALIGN - 1) // Arena.ALIGN * Arena.ALIGN
+
+    def take(self, shape, dtype):
+        esize = torch.empty(0, dtype=dtype).element_size()
+        n = esize
+        for d in shape:
+            n *= int(d)
+        start = self.aligned(self.buf.data_ptr() + self.used) - self.buf.data_ptr()
+        if start + n > self.buf.numel():
+            raise MemoryError("arena of %d bytes exhausted (%d more needed)" % (self.buf.numel(), start + n))
+        self.used = start + n
+        return self.buf[start:start + n].view(dtype).view(tuple(shape))

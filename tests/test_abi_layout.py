@@ -81,3 +81,10 @@ def test_mg_stats_layout_matches_header(tmp_path):
     assert fields == ["nite", "res", "solves", "vcycles", "not_converged", "nonfinite"]
     layout = _c_layout(tmp_path, "NylesMgStats", fields)
     _check("NylesMgStats", nat.NylesMgStats, fields, layout)
+
+
+def test_batch_table_layout_matches_header(tmp_path):
+    fields = _struct_fields("NylesBatchTable")
+    assert fields == ["delta", "active", "live", "loop_iterations"]
+    layout = _c_layout(tmp_path, "NylesBatchTable", fields)
+    _check("NylesBatchTable", nat.NylesBatchTable, fields, layout)

@@ -1,10 +1,12 @@
 """Continuous batching on the GPU: every run's result is the same alone and in the mix.
 
-A handful of requests of different cases and sizes are served together (admitted
-while others are in flight, advanced by overlapping graph replays on their own
-streams); each is then run alone with eager stepping. The final fields must be
-identical: runs share no data, reductions are deterministic, and graph replay equals
-eager stepping bit for bit.
+Requests of different cases and sizes are served together: runs of one case and grid
+share a bucket and advance with one batched graph launch per k steps (every kernel
+covering all of the bucket's runs), buckets overlap on their own streams, and new runs
+join while others are in flight. Each run is then stepped alone, eagerly, through the
+one-run path. The final fields must be identical: runs share no data, each run's
+pressure solves stop on their own, reductions are deterministic, and graph replay
+equals eager stepping bit for bit.
 """
 import numpy as np
 import pytest
@@ -22,6 +24,13 @@ def test_results_identical_alone_and_in_the_mix():
     eng = S.ServingEngine(precision="mixed")
     results, mixed_states = eng.serve(reqs, realtime=False, keep_states=True)
     assert eng.max_active == len(reqs)
+    assert eng.buckets_made == 4                       # the two lock 32^3 runs share a bucket
+    assert all(r.status == "ok" for r in results)
+    # the same run alone in its bucket
+    alone = S.ServingEngine(precision="mixed")
+    _, alone_states = alone.serve([reqs[0]], realtime=False, keep_states=True)
+    for s, arr in alone_states[0].items():
+        np.testing.assert_array_equal(mixed_states[0][s], arr, err_msg="alone vs mix, field %s" % s)
     for req in reqs:
         nyl = Nyles(S.build_params(req.case, req.n, "mixed"))
         S.initial_state(nyl, req.case, req.seed)
@@ -47,17 +56,43 @@ def test_realtime_stream_latencies():
 
 @pytest.mark.parametrize("case,n,precision", [("lock", 32, "mixed"), ("tgv", 48, "mixed"), ("lock", 32, "fp64")])
 def test_footprint_model_covers_the_allocation(case, n, precision):
+    """The admission footprint covers the arena of one run (state, registers, workspace)
+    with at most 50% to spare, and a one-slot mixed bucket allocates about that much."""
     import gc
     from nyles_gb300 import serving as S
-    gc.collect()
-    torch.cuda.synchronize()
-    before = torch.cuda.memory_allocated()
-    run = S.Run(S.Request(0, case, n, 1, 10, 0.0), precision, torch.device("cuda", 0), 1e-6)
-    torch.cuda.synchronize()
-    used = torch.cuda.memory_allocated() - before
+    from nyles_gb300.nyles import arena_bytes
+    exact = arena_bytes(S.build_params(case, n, precision))
     need = S.footprint_bytes(case, n, precision)
-    assert used <= need <= 1.5 * used, (used, need)
-    del run
+    assert exact <= need <= 1.5 * exact, (exact, need)
+    if precision == "mixed":
+        gc.collect()
+        torch.cuda.synchronize()
+        before = torch.cuda.memory_allocated()
+        b = S.Bucket((case, n, 10), precision, 1e-6, torch.device("cuda", torch.cuda.current_device()), 1)
+        torch.cuda.synchronize()
+        used = torch.cuda.memory_allocated() - before
+        assert used <= need + (1 << 20), (used, need)
+        b.close()
+        del b
+
+
+def test_batched_launches_are_fewer_than_per_run_launches():
+    """A bucket of 6 runs of 32^3 advances with one launch per 10 steps: the library's
+    kernel count for the ensemble is about one run's, not six."""
+    from nyles_gb300 import _native as nat
+    from nyles_gb300 import serving as S
+    reqs = [S.Request(i, "tgv", 32, 20 + i, 30, 0.0) for i in range(6)]
+    l0 = nat.lib().nyles_launch_count()
+    eng = S.ServingEngine(precision="mixed")
+    results, _ = eng.serve(reqs, realtime=False)
+    batched = nat.lib().nyles_launch_count() - l0
+    assert eng.launches == 3 and all(r.status == "ok" for r in results)
+    l0 = nat.lib().nyles_launch_count()
+    one = S.ServingEngine(precision="mixed")
+    one.serve(reqs[:1], realtime=False)
+    single = nat.lib().nyles_launch_count() - l0
+    # the setup (initial projection per run) is per run; the stepping is shared
+    assert batched < 2.5 * single, (batched, single)
 
 
 def test_sequential_estimate_tracks_the_sequential_run():

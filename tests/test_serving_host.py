@@ -1,5 +1,6 @@
 """Host logic of the serving engine on the CPU: request stream, footprint model,
-admission against the HBM budget, completion bookkeeping (fake runs, no GPU)."""
+admission against the HBM budget, buckets and completion bookkeeping (fake buckets, no
+GPU)."""
 import numpy as np
 
 from nyles_gb300 import serving as S
@@ -21,60 +22,106 @@ def test_footprint_grows_with_size_and_precision():
     assert S.steps_per_graph(300) == 10 and S.steps_per_graph(7) == 7 and S.steps_per_graph(13) == 1
 
 
-class FakeRun:
-    """Stands in for a resident run: each launch completes on the next poll."""
-    live = 0
-    peak = 0
-
-    def __init__(self, req, precision, device, mg_tol, priority=0):
-        self.req = req
-        self.priority = priority
-        self.k = S.steps_per_graph(req.steps)
+class FakeSlot:
+    def __init__(self, index):
+        self.index = index
+        self.req = None
         self.launched = 0
+        self.admitted = 0.0
         self.pending = 0
-        FakeRun.live += 1
-        FakeRun.peak = max(FakeRun.peak, FakeRun.live)
-
-    def launch(self):
-        self.launched += self.k
-        self.pending += 1
-
-    def poll(self):
-        n = self.pending
-        self.pending = 0
-        return n
 
     @property
-    def all_launched(self):
-        return self.launched >= self.req.steps
+    def active(self):
+        return self.req is not None and self.launched < self.req.steps
 
     def finished(self):
-        done = self.all_launched and self.poll() == 0
-        if done:
-            FakeRun.live -= 1
-        return done
+        return self.req is not None and self.launched >= self.req.steps and self.pending == 0
 
+
+class FakeBucket:
+    """Stands in for a bucket of resident runs: each launch advances every active slot
+    by k steps and completes on the next poll."""
+    live = 0
+    peak = 0
+    made = []
     # rid -> status reported at completion (default "ok")
     outcomes = {}
 
-    def outcome(self):
-        return FakeRun.outcomes.get(self.req.rid, "ok"), 0
+    def __init__(self, key, precision, mg_tol, device, capacity, priority=0):
+        self.key = key
+        self.case, self.n, self.k = key
+        self.capacity = capacity
+        self.bytes = capacity * S.footprint_bytes(self.case, self.n, precision)
+        self.slots = [FakeSlot(r) for r in range(capacity)]
+        self.launches = 0
+        self.priority = priority
+        FakeBucket.made.append(self)
 
-    def final_state(self):
-        return {}
+    def free_slot(self):
+        return next((sl for sl in self.slots if sl.req is None), None)
+
+    def resident(self):
+        return [sl for sl in self.slots if sl.req is not None]
+
+    def admit(self, slot, req, now):
+        slot.req, slot.launched, slot.admitted, slot.pending = req, 0, now, 0
+        FakeBucket.live += 1
+        FakeBucket.peak = max(FakeBucket.peak, FakeBucket.live)
+
+    def poll(self):
+        for sl in self.slots:
+            sl.pending = 0
+        return 0
+
+    def launch(self):
+        act = [sl for sl in self.slots if sl.active]
+        for sl in act:
+            sl.launched += self.k
+            sl.pending = 1
+        self.launches += bool(act)
+        return bool(act)
+
+    def outcome(self, slot, keep_state=False):
+        return FakeBucket.outcomes.get(slot.req.rid, "ok"), 0, None
+
+    def release(self, slot):
+        slot.req = None
+        FakeBucket.live -= 1
+
+    def close(self):
+        pass
+
+
+def _reset():
+    FakeBucket.live = FakeBucket.peak = 0
+    FakeBucket.made = []
+    FakeBucket.outcomes = {}
 
 
 def test_admission_respects_the_budget_and_serves_everything():
-    FakeRun.live = FakeRun.peak = 0
+    _reset()
     reqs = S.make_requests(20, 20.0, seed=1, steps=30, sizes=(64,))
     one = S.footprint_bytes("lock", 64, "mixed")
-    eng = S.ServingEngine(hbm_budget_bytes=3.5 * one, device="cpu", run_factory=FakeRun)
+    eng = S.ServingEngine(hbm_budget_bytes=3.5 * one, device="cpu", bucket_factory=FakeBucket)
     results, _ = eng.serve(reqs, realtime=False)
     assert [r.rid for r in results] == list(range(20))
+    assert all(r.status == "ok" for r in results)
     assert eng.max_active <= 3 and eng.peak_used <= 3.5 * one
-    assert FakeRun.live == 0
+    assert FakeBucket.live == 0
     summary = S.summarize(results)
     assert summary["runs"] == 20 and summary["p99_s"] >= summary["p50_s"]
+
+
+def test_runs_of_a_bucket_share_its_launches():
+    """Runs of the same case and grid sit in one bucket and advance together: the
+    launches are far fewer than one per run and step group."""
+    _reset()
+    reqs = [S.Request(i, "tgv", 32, i, 30, 0.0) for i in range(8)] + [S.Request(8, "lock", 32, 8, 30, 0.0)]
+    eng = S.ServingEngine(device="cpu", bucket_factory=FakeBucket, capacity=16)
+    results, _ = eng.serve(reqs, realtime=False)
+    assert len(results) == 9 and eng.buckets_made == 2
+    assert eng.launches == 2 * 3           # 30 steps in launches of 10, once per bucket
+    assert eng.max_active == 9
 
 
 def test_replay_queue_one_at_a_time():
@@ -92,44 +139,27 @@ def test_stream_priorities_by_work():
     priority; "none" leaves every stream at 0."""
     from nyles_gb300 import serving as S
     reqs = [S.Request(i, "lock", n, i, 300, 0.0) for i, n in enumerate((32, 48, 64, 96, 128, 32))]
-    eng = S.ServingEngine(device="cpu", run_factory=FakeRun)
+    eng = S.ServingEngine(device="cpu", bucket_factory=FakeBucket)
     pr = eng.stream_priorities(reqs, levels=(0, -5))
     assert pr[0] == pr[5] == -5 and pr[4] > pr[3] > pr[2] > pr[1] > pr[0] and pr[4] <= 0
-    assert set(S.ServingEngine(device="cpu", run_factory=FakeRun, priority="none")
+    assert set(S.ServingEngine(device="cpu", bucket_factory=FakeBucket, priority="none")
                .stream_priorities(reqs).values()) == {0}
-
-
-def test_window_serves_shortest_remaining_work_first():
-    """With a window of one run and every request available at once, runs complete in
-    the order of their work; every run completes."""
-    from nyles_gb300 import serving as S
-    sizes = [96, 32, 128, 48, 64]
-    reqs = [S.Request(i, "lock", n, i, 20, 0.0) for i, n in enumerate(sizes)]
-    ticks = iter(range(10 ** 6))
-    eng = S.ServingEngine(device="cpu", run_factory=FakeRun, window=1, clock=lambda: float(next(ticks)))
-    results, _ = eng.serve(reqs, realtime=False)
-    order = [r.rid for r in sorted(results, key=lambda r: r.done)]
-    assert order == sorted(range(5), key=lambda i: sizes[i])
-    assert FakeRun.live == 0
 
 
 def test_oversize_request_refused_while_the_others_finish():
     """A request whose footprint exceeds the whole budget is refused at once (it could
     never be admitted); the others are served and release their memory; a run that blew
     up is counted, not timed."""
-    FakeRun.live = FakeRun.peak = 0
-    FakeRun.outcomes = {3: "blowup"}
-    try:
-        reqs = [S.Request(i, "lock", 64, i, 20, 0.01 * i) for i in range(6)]
-        reqs[2] = S.Request(2, "tgv", 128, 2, 20, 0.02)
-        budget = 2.5 * S.footprint_bytes("lock", 64, "mixed")
-        assert S.footprint_bytes("tgv", 128, "mixed") > budget
-        eng = S.ServingEngine(hbm_budget_bytes=budget, device="cpu", run_factory=FakeRun)
-        results, _ = eng.serve(reqs, realtime=False)
-    finally:
-        FakeRun.outcomes = {}
+    _reset()
+    FakeBucket.outcomes = {3: "blowup"}
+    reqs = [S.Request(i, "lock", 64, i, 20, 0.01 * i) for i in range(6)]
+    reqs[2] = S.Request(2, "tgv", 128, 2, 20, 0.02)
+    budget = 2.5 * S.footprint_bytes("lock", 64, "mixed")
+    assert S.footprint_bytes("tgv", 128, "mixed") > budget
+    eng = S.ServingEngine(hbm_budget_bytes=budget, device="cpu", bucket_factory=FakeBucket)
+    results, _ = eng.serve(reqs, realtime=False)
     status = {r.rid: r.status for r in results}
     assert status == {0: "ok", 1: "ok", 2: "refused", 3: "blowup", 4: "ok", 5: "ok"}
-    assert eng.used == 0 and FakeRun.live == 0 and eng.peak_used <= budget
+    assert eng.used == 0 and FakeBucket.live == 0 and eng.peak_used <= budget
     summary = S.summarize(results)
     assert summary["runs"] == 4 and summary["refused"] == 1 and summary["blowup"] == 1
