@@ -244,15 +244,20 @@ typedef struct NylesBatchTable {
     int live[NYLES_BATCH_RUNS];         /* device-side: run r's current solve still iterates */
     long long loop_iterations;          /* device-side: multigrid loop-body iterations run */
 } NylesBatchTable;
-/* Record nsteps steps with a fixed dt for nrun (<= NYLES_BATCH_RUNS) runs whose table is
- * the device memory `table`. Mixed-precision LES with the stationary pressure solve, no
- * tracers, the reference's schemes; NYLES_UNSUPPORTED otherwise. */
-int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table);
-int nyles_model_batch_launch(NylesModel* m, void* stream);
-int nyles_model_batch_release(NylesModel* m);
+/* Record nsteps steps with a fixed dt (nsteps = 0: one LES.diagnose_var, the initial
+ * projection of a run, core/model_les.py:98-127) for nrun (<= NYLES_BATCH_RUNS) runs
+ * whose table is the device memory `table`, into a new batched graph. The graph refers
+ * to m's memory (shifted per run by the table); m must stay bound while it is launched.
+ * Mixed-precision LES with the stationary pressure solve, no tracers, the reference's
+ * schemes; NYLES_UNSUPPORTED otherwise. */
+typedef struct NylesBatchGraph NylesBatchGraph;
+int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table,
+                              NylesBatchGraph** out);
+int nyles_batch_launch(NylesBatchGraph* g, void* stream);
 /* adds the kernels of `iterations` multigrid loop-body iterations (read from the table)
  * to nyles_launch_count */
-int nyles_model_batch_note_iterations(NylesModel* m, long long iterations);
+int nyles_batch_note_iterations(const NylesBatchGraph* g, long long iterations);
+int nyles_batch_destroy(NylesBatchGraph* g);
 /* The counters the pressure solves of recorded (graph or batched) steps keep on the
  * device, read from the model's workspace: last nite and res, V-cycles, solves stopped
  * at maxite above tol, solves stopped by a non-finite norm (solves = 0). Synchronises

@@ -117,10 +117,10 @@ SIGNATURES = {
     "nyles_model_graph_release": (_I, [_P]),
     "nyles_model_profile": (_I, [_P, _I]),
     "nyles_model_profile_read": (_I, [_P, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong), _I]),
-    "nyles_model_batch_capture": (_I, [_P, _D, _I, _I, _P]),
-    "nyles_model_batch_launch": (_I, [_P, _P]),
-    "nyles_model_batch_release": (_I, [_P]),
-    "nyles_model_batch_note_iterations": (_I, [_P, ctypes.c_longlong]),
+    "nyles_model_batch_capture": (_I, [_P, _D, _I, _I, _P, _PP]),
+    "nyles_batch_launch": (_I, [_P, _P]),
+    "nyles_batch_note_iterations": (_I, [_P, ctypes.c_longlong]),
+    "nyles_batch_destroy": (_I, [_P]),
     "nyles_model_device_stats": (_I, [_P, ctypes.POINTER(NylesMgStats), _P]),
     "nyles_launch_count": (ctypes.c_longlong, []),
     "nyles_max_U2_static_f64": (_I, [_P, _P, _P, ctypes.c_longlong, _P, _P]),

@@ -139,6 +139,19 @@ struct NylesMg {
     MgImpl impl;
 };
 
+// A recorded batched graph: its executable and its kernel counts. It refers to the
+// memory of the model it was recorded on, shifted per run through the table.
+struct NylesBatchGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;        // per launch, outside the multigrid loops
+    long long body_kernels = 0;   // per loop-body iteration
+    ~NylesBatchGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
 struct NylesModel {
     NylesDesc d;
     Geom g;
@@ -168,27 +181,16 @@ struct NylesModel {
     cudaStream_t last_stream = nullptr;  // stream of the latest graph launch
     nyles_forcing_fn forcing = nullptr;  // user forcing called after each right-hand side
     void* forcing_user = nullptr;
-    // batched graph: the same steps for up to NYLES_MAX_BATCH runs of one bucket
-    Bat bat;                             // set while the batched graph is captured
-    cudaGraph_t bgraph = nullptr;
-    cudaGraphExec_t bgexec = nullptr;
-    long long bgraph_kernels = 0, bgraph_body_kernels = 0;
+    Bat bat;                             // set while a batched graph is recorded
     void release_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         gexec = nullptr;
         graph = nullptr;
     }
-    void release_batch() {
-        if (bgexec) cudaGraphExecDestroy(bgexec);
-        if (bgraph) cudaGraphDestroy(bgraph);
-        bgexec = nullptr;
-        bgraph = nullptr;
-    }
     ~NylesModel() {
         prof.release();
         release_graph();
-        release_batch();
         if (cap_stream) cudaStreamDestroy(cap_stream);
     }
 };
@@ -706,11 +708,12 @@ long long nyles_launch_count(void) { return g_launches.load(); }
 
 }  // extern "C"
 
-// Record nsteps steps of m into a new graph (multigrid stop tests on the device); the
-// kernels outside the multigrid loops and those of one loop iteration are counted.
+// Record nsteps steps of m (nsteps = 0: one diagnose_var) into a new graph (multigrid
+// stop tests on the device); the kernels outside the multigrid loops and those of one
+// loop iteration are counted.
 static int record_steps(NylesModel* m, double dt, int nsteps, cudaGraph_t* graph, cudaGraphExec_t* exec,
                         long long* kernels, long long* body_kernels) {
-    if (m->scheme == NYLES_SCHEME_LFAM3 && m->lf_first) {
+    if (nsteps > 0 && m->scheme == NYLES_SCHEME_LFAM3 && m->lf_first) {
         set_error("LFAM3: run the first (Euler) step before capturing the steady step");
         return NYLES_BAD_ARG;
     }
@@ -738,6 +741,8 @@ static int record_steps(NylesModel* m, double dt, int nsteps, cudaGraph_t* graph
     for (int s = 0; s < nsteps && !rc && !gb.error; ++s)
         rc = m->precision == NYLES_FP64 ? model_forward<double>(m, 0.0, dt, gb.st)
                                         : model_forward<float>(m, 0.0, dt, gb.st);
+    if (nsteps == 0)
+        rc = m->precision == NYLES_FP64 ? model_diagnose<double>(m, gb.st) : model_diagnose<float>(m, gb.st);
     gb.end_segment();
     m->gb = nullptr;
     m->prof.on = prof_on;
@@ -766,10 +771,12 @@ int nyles_model_capture(NylesModel* m, double dt, int nsteps) {
     return record_steps(m, dt, nsteps, &m->graph, &m->gexec, &m->graph_kernels, &m->graph_body_kernels);
 }
 
-int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table) {
-    if (!m || !m->bound || nsteps < 1) { set_error("model not bound or nsteps < 1"); return NYLES_BAD_ARG; }
+int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, NylesBatchTable* table,
+                              NylesBatchGraph** out) {
+    if (!m || !m->bound || nsteps < 0 || !out) { set_error("model not bound, nsteps < 0 or null output"); return NYLES_BAD_ARG; }
+    *out = nullptr;
     if (nrun < 1 || nrun > NYLES_MAX_BATCH || !table || (((uintptr_t)table) & 7)) {
-        set_error("batched capture: 1 <= nrun <= NYLES_MAX_BATCH and an 8-byte aligned device table required");
+        set_error("batched capture: 1 <= nrun <= NYLES_BATCH_RUNS and an 8-byte aligned device table required");
         return NYLES_BAD_ARG;
     }
     const NylesDesc& d = m->d;
@@ -779,36 +786,38 @@ int nyles_model_batch_capture(NylesModel* m, double dt, int nsteps, int nrun, Ny
                   "no tracers and the reference's schemes");
         return NYLES_UNSUPPORTED;
     }
-    m->release_batch();
+    NylesBatchGraph* g = new (std::nothrow) NylesBatchGraph;
+    if (!g) { set_error("out of host memory"); return NYLES_CUDA_ERROR; }
     m->bat.tab = reinterpret_cast<BatchTab*>(table);
     m->bat.nrun = nrun;
     m->bat.gate = GATE_ACTIVE;
     m->mg.bat = m->bat;
     const int solves = m->graph_solves;   // of the one-run graph, if any
-    int rc = record_steps(m, dt, nsteps, &m->bgraph, &m->bgexec, &m->bgraph_kernels, &m->bgraph_body_kernels);
+    int rc = record_steps(m, dt, nsteps, &g->graph, &g->exec, &g->kernels, &g->body_kernels);
     m->graph_solves = solves;
     m->bat = Bat();
     m->mg.bat = Bat();
-    return rc;
+    if (rc) { delete g; return rc; }
+    *out = g;
+    return NYLES_OK;
 }
 
-int nyles_model_batch_launch(NylesModel* m, void* stream) {
-    if (!m || !m->bgexec) { set_error("no captured batched graph"); return NYLES_BAD_ARG; }
-    cudaError_t e = cudaGraphLaunch(m->bgexec, (cudaStream_t)stream);
+int nyles_batch_launch(NylesBatchGraph* g, void* stream) {
+    if (!g || !g->exec) { set_error("no batched graph"); return NYLES_BAD_ARG; }
+    cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_status(e, "cudaGraphLaunch");
-    note_launch((int)m->bgraph_kernels);
+    note_launch((int)g->kernels);
     return NYLES_OK;
 }
 
-int nyles_model_batch_release(NylesModel* m) {
-    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
-    m->release_batch();
+int nyles_batch_note_iterations(const NylesBatchGraph* g, long long iterations) {
+    if (!g || iterations < 0) { set_error("null graph or negative count"); return NYLES_BAD_ARG; }
+    note_launch((int)(iterations * g->body_kernels));
     return NYLES_OK;
 }
 
-int nyles_model_batch_note_iterations(NylesModel* m, long long iterations) {
-    if (!m || iterations < 0) { set_error("null model or negative count"); return NYLES_BAD_ARG; }
-    note_launch((int)(iterations * m->bgraph_body_kernels));
+int nyles_batch_destroy(NylesBatchGraph* g) {
+    delete g;
     return NYLES_OK;
 }
 

@@ -103,27 +103,30 @@ def build_params(case, n, precision="mixed", mg_tol=1e-6):
     return p
 
 
-def initial_state(nyl, case, seed):
-    """Seeded initial fields written through view('i'): lock exchange (b = -0.5 | +0.5
-    across x = L/2 plus uniform noise 1e-3) or Taylor-Green (u = sin x cos y cos z,
-    v = -cos x sin y cos z plus Gaussian noise 1e-4, covariant: times the spacing)."""
+def initial_fields(nyl, case, seed):
+    """Seeded initial fields (numpy, the (z, y, x) arrays of view('i')): lock exchange
+    (b = -0.5 | +0.5 across x = L/2 plus uniform noise 1e-3) or Taylor-Green (u = sin x
+    cos y cos z, v = -cos x sin y cos z plus Gaussian noise 1e-4, covariant: times the
+    spacing)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     g = nyl.grid
-    st = nyl.model.state
     if case == "lock":
         xb = g.x_b.view("i").numpy()
-        b = np.where(xb < 0.5 * g.Lx, -0.5, 0.5) + 1e-3 * rng.uniform(-1, 1, size=xb.shape)
-        st.b.view("i")[...] = torch.from_numpy(b)
-    else:
-        xu, yu, zu = (g.x_vel["i"].view("i").numpy(), g.y_vel["i"].view("i").numpy(), g.z_vel["i"].view("i").numpy())
-        xv, yv, zv = (g.x_vel["j"].view("i").numpy(), g.y_vel["j"].view("i").numpy(), g.z_vel["j"].view("i").numpy())
-        shape = xu.shape
-        u = (np.sin(xu) * np.cos(yu) * np.cos(zu) + 1e-4 * rng.standard_normal(shape)) * g.dx
-        v = (-np.cos(xv) * np.sin(yv) * np.cos(zv) + 1e-4 * rng.standard_normal(shape)) * g.dy
-        w = 1e-4 * rng.standard_normal(shape) * g.dz
-        st.u["i"].view("i")[...] = torch.from_numpy(u)
-        st.u["j"].view("i")[...] = torch.from_numpy(v)
-        st.u["k"].view("i")[...] = torch.from_numpy(w)
+        return {"b": np.where(xb < 0.5 * g.Lx, -0.5, 0.5) + 1e-3 * rng.uniform(-1, 1, size=xb.shape)}
+    xu, yu, zu = (g.x_vel["i"].view("i").numpy(), g.y_vel["i"].view("i").numpy(), g.z_vel["i"].view("i").numpy())
+    xv, yv, zv = (g.x_vel["j"].view("i").numpy(), g.y_vel["j"].view("i").numpy(), g.z_vel["j"].view("i").numpy())
+    shape = xu.shape
+    u = (np.sin(xu) * np.cos(yu) * np.cos(zu) + 1e-4 * rng.standard_normal(shape)) * g.dx
+    v = (-np.cos(xv) * np.sin(yv) * np.cos(zv) + 1e-4 * rng.standard_normal(shape)) * g.dy
+    w = 1e-4 * rng.standard_normal(shape) * g.dz
+    return {"u_i": u, "u_j": v, "u_k": w}
+
+
+def initial_state(nyl, case, seed):
+    """Write the seeded initial fields of `initial_fields` through view('i')."""
+    st = nyl.model.state
+    for name, arr in initial_fields(nyl, case, seed).items():
+        st.get(name).view("i")[...] = torch.from_numpy(arr)
 
 
 def footprint_bytes(case, n, precision="mixed"):
@@ -164,35 +167,35 @@ class Slot:
         self.index = index
         self.nyl = nyl
         self.req = None
-        self.ready = None          # event: the run's setup (zeroing, initial state, projection) done
-        self.setup_pending = False
+        self.projected = False     # the initial projection has been launched
         self.launched = 0
         self.last_event = None     # event of the latest launch that advanced this run
         self.admitted = 0.0
-        self.failed = None         # status when the setup already failed
+        self.staging = None        # pinned host copies of the initial state, kept until used
 
     @property
     def active(self):
-        return self.req is not None and self.failed is None and self.launched < self.req.steps
+        return self.req is not None and self.projected and self.launched < self.req.steps
 
     def finished(self):
-        if self.req is None:
+        if self.req is None or not self.projected:
             return False
-        if self.failed is not None:
-            return True
         return self.launched >= self.req.steps and (self.last_event is None or self.last_event.query())
 
 
 class Bucket:
     """The resident runs of one (case, grid, steps per launch) on `capacity` slots of one
     device buffer. Every slot's model is built in an Arena of the same size, so its
-    arrays sit at the same offsets: run r's memory is slot 0's shifted by r x slot_bytes.
-    One batched graph of k time steps (captured on slot 0's model, every kernel covering
-    all slots) advances every active slot; a slot whose run is done, or free, is skipped
-    by all kernels (its table entry is inactive), and each run's pressure solves stop on
-    their own, so a run's result is the same whatever else shares the launch. Runs join
-    at launch boundaries: a new run's state is zeroed, initialised and projected on a
-    setup stream while the bucket's launches go on."""
+    arrays sit at the same offsets: slot r's memory is slot 0's shifted by r x slot_bytes.
+    Batched graphs recorded on slot 0's model (nyles_model_batch_capture), one per
+    batch size (powers of two up to the capacity, recorded when first needed), advance a
+    list of runs: the table of a launch lists the slots' offsets first, so a launch
+    covers only as many slots as it advances, and the runs are processed in the smallest
+    batch size that holds them. Each run's pressure solves stop on their own, so its
+    result is the same whatever else shares the launch. A new run's slot is zeroed, its
+    initial state copied from pinned host memory and its initial projection recorded as
+    a batched graph too, all queued on the bucket's stream: admission never waits for
+    the device."""
 
     def __init__(self, key, precision, mg_tol, device, capacity, priority=0):
         import ctypes
@@ -216,21 +219,37 @@ class Bucket:
         # the host writes delta and active (the leading fields); live and loop_iterations
         # belong to the device
         self.host_bytes = nat.NylesBatchTable.live.offset
-        self.ring = [torch.zeros(tb, dtype=torch.uint8).pin_memory() for _ in range(4)]
+        self.ring = [torch.zeros(tb, dtype=torch.uint8).pin_memory() for _ in range(8)]
         self.ring_events = [None] * len(self.ring)
         self.ring_pos = 0
-        for buf in self.ring:
-            t = nat.NylesBatchTable.from_address(buf.data_ptr())
-            for r in range(capacity):
-                t.delta[r] = r * self.slot_bytes
         self.stream = torch.cuda.Stream(device=device, priority=priority)
-        self.setup_stream = torch.cuda.Stream(device=device, priority=priority)
         self.read_stream = torch.cuda.Stream(device=device, priority=priority)
         self.inflight = []
         self.launches = 0
         self.template = self.slots[0].nyl.model
-        nat.check(self.lib.nyles_model_batch_capture(self.template._h, CASES[case]["dt"], k, capacity,
-                                                     ctypes.c_void_p(self.table.data_ptr())))
+        self.graphs = {}          # (kind, batch size) -> NylesBatchGraph handle
+        self.dt = CASES[case]["dt"]
+
+    # ---- graphs
+    def sizes(self):
+        out, b = [], 1
+        while b < self.capacity:
+            out.append(b)
+            b *= 2
+        return out + [self.capacity]
+
+    def graph(self, kind, nact):
+        import ctypes
+        size = next(b for b in self.sizes() if b >= nact)
+        g = self.graphs.get((kind, size))
+        if g is None:
+            h = ctypes.c_void_p()
+            steps = self.k if kind == "step" else 0
+            self.nat.check(self.lib.nyles_model_batch_capture(self.template._h, self.dt, steps, size,
+                                                              ctypes.c_void_p(self.table.data_ptr()),
+                                                              ctypes.byref(h)))
+            g = self.graphs[(kind, size)] = h
+        return g, size
 
     # ---- slots
     def free_slot(self):
@@ -240,22 +259,23 @@ class Bucket:
         return [sl for sl in self.slots if sl.req is not None]
 
     def admit(self, slot, req, now):
-        """Zero the slot (a fresh allocation's contents), write the request's initial
-        state and project it (core/nyles.py:122) on the setup stream."""
-        from . import _native as nat
-        slot.req, slot.launched, slot.last_event, slot.failed = req, 0, None, None
+        """Queue on the bucket stream: zero the slot (a fresh allocation's contents) and
+        copy the request's initial state in from pinned host memory; the projection
+        follows in the next launch (`launch`)."""
+        slot.req, slot.launched, slot.last_event, slot.projected = req, 0, None, False
         slot.admitted = now
+        fields = initial_fields(slot.nyl, req.case, req.seed)
         lo = slot.index * self.slot_bytes
-        with torch.cuda.stream(self.setup_stream):
+        staging = []
+        with torch.cuda.stream(self.stream):
             self.buf[lo:lo + self.slot_bytes].zero_()
-            initial_state(slot.nyl, req.case, req.seed)
-            try:
-                slot.nyl.model.diagnose_var(slot.nyl.model.state)
-            except nat.BlowUp:
-                slot.failed = "blowup"
-            slot.ready = torch.cuda.Event()
-            slot.ready.record(self.setup_stream)
-        slot.setup_pending = True
+            st = slot.nyl.model.state
+            for name, arr in fields.items():
+                dst = st.get(name).view("i")
+                h = torch.from_numpy(arr).to(dst.dtype).pin_memory()
+                dst.copy_(h, non_blocking=True)
+                staging.append(h)
+        slot.staging = staging
 
     # ---- launches
     def poll(self):
@@ -263,35 +283,43 @@ class Bucket:
             self.inflight.pop(0)
         return len(self.inflight)
 
-    def launch(self):
-        """Advance every active slot by k steps with one graph launch."""
-        act = [sl for sl in self.slots if sl.active]
-        if not act:
-            return False
+    def _launch(self, kind, slots):
+        g, size = self.graph(kind, len(slots))
         i = self.ring_pos
         self.ring_pos = (i + 1) % len(self.ring)
         if self.ring_events[i] is not None:
             self.ring_events[i].synchronize()          # the pinned buffer's previous copy is done
         t = self.nat.NylesBatchTable.from_address(self.ring[i].data_ptr())
-        for r in range(self.capacity):
-            t.active[r] = 0
-        for sl in act:
-            t.active[sl.index] = 1
-            if sl.setup_pending:
-                self.stream.wait_event(sl.ready)
-                sl.setup_pending = False
+        for r in range(size):
+            t.active[r] = 1 if r < len(slots) else 0
+            t.delta[r] = slots[r].index * self.slot_bytes if r < len(slots) else 0
         with torch.cuda.stream(self.stream):
             self.table[:self.host_bytes].copy_(self.ring[i][:self.host_bytes], non_blocking=True)
         ev_tab = torch.cuda.Event()
         ev_tab.record(self.stream)
         self.ring_events[i] = ev_tab
-        self.nat.check(self.lib.nyles_model_batch_launch(self.template._h, self.nat.stream_ptr(self.stream)))
+        self.nat.check(self.lib.nyles_batch_launch(g, self.nat.stream_ptr(self.stream)))
+        self.launches += 1
+
+    def launch(self):
+        """Project the newly admitted runs, then advance every active run by k steps,
+        each group with one graph launch; returns False when there was nothing to do."""
+        new = [sl for sl in self.slots if sl.req is not None and not sl.projected]
+        if new:
+            self._launch("diag", new)
+            for sl in new:
+                sl.projected = True
+        act = [sl for sl in self.slots if sl.active]
+        if act:
+            self._launch("step", act)
+            for sl in act:
+                sl.launched += self.k
+        if not (new or act):
+            return False
         ev = torch.cuda.Event()
         ev.record(self.stream)
         self.inflight.append(ev)
-        self.launches += 1
-        for sl in act:
-            sl.launched += self.k
+        for sl in new + act:
             sl.last_event = ev
         return True
 
@@ -299,28 +327,17 @@ class Bucket:
     def outcome(self, slot, keep_state=False):
         """(status, V-cycles, final fields or None) of a finished run, read on the read
         stream once its last launch is complete: "blowup" when a pressure solve met a
-        non-finite norm or the final velocity is not finite, "not_converged" when a
-        solve stopped at maxite above the tolerance, else "ok"."""
+        non-finite norm (a non-finite velocity reaches every projection), "not_converged"
+        when a solve stopped at maxite above the tolerance, else "ok"."""
         import ctypes
         nat = self.nat
-        if slot.failed is not None:
-            return slot.failed, 0, None
         m = slot.nyl.model
         st = nat.NylesMgStats()
         with torch.cuda.stream(self.read_stream):
             if slot.last_event is not None:
                 self.read_stream.wait_event(slot.last_event)
             nat.check(self.lib.nyles_model_device_stats(m._h, ctypes.byref(st), nat.stream_ptr(self.read_stream)))
-            status = "ok"
-            if st.nonfinite > 0:
-                status = "blowup"
-            else:
-                try:
-                    m.max_U2()
-                except nat.BlowUp:
-                    status = "blowup"
-            if status == "ok" and st.not_converged > 0:
-                status = "not_converged"
+            status = "blowup" if st.nonfinite > 0 else ("not_converged" if st.not_converged > 0 else "ok")
             fields = None
             if keep_state:
                 fields = {s: m.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k", "p")}
@@ -328,22 +345,26 @@ class Bucket:
 
     def release(self, slot):
         slot.req = None
-        slot.failed = None
         slot.last_event = None
+        slot.staging = None
 
     def loop_iterations(self):
         """multigrid loop-body iterations the batched launches ran (device counter)"""
         import ctypes
         t = self.nat.NylesBatchTable()
-        torch.cuda.synchronize(self.table.device)
-        ctypes.memmove(ctypes.addressof(t), self.table.cpu().numpy().ctypes.data, ctypes.sizeof(t))
+        host = self.table.cpu()
+        ctypes.memmove(ctypes.addressof(t), host.data_ptr(), ctypes.sizeof(t))
         return t.loop_iterations
 
     def close(self):
-        """Count the loop kernels, release the graph and the memory."""
+        """Count the loop kernels, release the graphs and the memory."""
         self.stream.synchronize()
-        self.nat.check(self.lib.nyles_model_batch_note_iterations(self.template._h, self.loop_iterations()))
-        self.nat.check(self.lib.nyles_model_batch_release(self.template._h))
+        if self.graphs:
+            g = next(iter(self.graphs.values()))
+            self.nat.check(self.lib.nyles_batch_note_iterations(g, self.loop_iterations()))
+        for g in self.graphs.values():
+            self.lib.nyles_batch_destroy(g)
+        self.graphs = {}
         self.slots = []
         self.template = None
         self.buf = None

@@ -77,8 +77,9 @@ def test_footprint_model_covers_the_allocation(case, n, precision):
 
 
 def test_batched_launches_are_fewer_than_per_run_launches():
-    """A bucket of 6 runs of 32^3 advances with one launch per 10 steps: the library's
-    kernel count for the ensemble is about one run's, not six."""
+    """A bucket of 6 runs of 32^3 is projected with one launch and advances with one
+    launch per 10 steps: the library's kernel count for the ensemble is about one run's,
+    not six."""
     from nyles_gb300 import _native as nat
     from nyles_gb300 import serving as S
     reqs = [S.Request(i, "tgv", 32, 20 + i, 30, 0.0) for i in range(6)]
@@ -86,13 +87,12 @@ def test_batched_launches_are_fewer_than_per_run_launches():
     eng = S.ServingEngine(precision="mixed")
     results, _ = eng.serve(reqs, realtime=False)
     batched = nat.lib().nyles_launch_count() - l0
-    assert eng.launches == 3 and all(r.status == "ok" for r in results)
+    assert eng.launches == 4 and all(r.status == "ok" for r in results)   # one projection, 3 x 10 steps
     l0 = nat.lib().nyles_launch_count()
     one = S.ServingEngine(precision="mixed")
     one.serve(reqs[:1], realtime=False)
     single = nat.lib().nyles_launch_count() - l0
-    # the setup (initial projection per run) is per run; the stepping is shared
-    assert batched < 2.5 * single, (batched, single)
+    assert batched < 1.5 * single, (batched, single)
 
 
 def test_sequential_estimate_tracks_the_sequential_run():
