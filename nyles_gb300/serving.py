@@ -385,11 +385,17 @@ class ServingEngine:
     stream (CUDA priority by the per-run work n^3 x steps, smallest first, with
     priority "work"; equal with "none"), so buckets of every size overlap on the device.
     `capacity` = slots per bucket (at most NYLES_BATCH_RUNS); a bucket with no run left
-    and none waiting is released. Completion latency = arrival to the end of the run's
-    last launch."""
+    and none waiting is released. `window` = W launches only the W buckets with the least
+    remaining work (cells x steps not yet launched) at each tick, so that small runs
+    finish soon after they arrive and the large ones, which set the makespan, fill the
+    device afterwards; None launches every bucket. Completion latency = arrival to the
+    end of the run's last launch."""
 
     def __init__(self, hbm_budget_bytes=120e9, precision="mixed", mg_tol=1e-6, device=None, inflight=2,
-                 clock=time.perf_counter, bucket_factory=None, priority="work", capacity=16):
+                 clock=time.perf_counter, bucket_factory=None, priority="work", capacity=16, window=None):
+        if window is not None and window < 1:
+            raise ValueError("window must be None or >= 1")
+        self.window = window
         if priority not in ("work", "none"):
             raise ValueError("priority must be 'work' or 'none'")
         if not 1 <= capacity <= 32:
@@ -454,9 +460,12 @@ class ServingEngine:
                 b.admit(slot, req, self.clock() - t0)
             queue = waiting
             self.max_active = max(self.max_active, sum(len(b.resident()) for b in buckets.values()))
-            # launches
+            # launches: every bucket, or the `window` with the least remaining work
             busy = False
-            for b in buckets.values():
+            order = list(buckets.values())
+            if self.window is not None:
+                order = sorted(order, key=remaining_work)[:self.window]
+            for b in order:
                 if b.poll() < self.inflight:
                     busy |= b.launch()
             # completion
