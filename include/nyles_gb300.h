@@ -177,6 +177,15 @@ int nyles_model_bind(NylesModel* m, void* const* fields, void* const* regs, void
 int nyles_model_set_mg_params(NylesModel* m, double tol, int maxite, double omega);
 /* nyles_mg_set_krylov for the model's pressure solve (refused while a graph is captured) */
 int nyles_model_set_mg_krylov(NylesModel* m, int on);
+/* Warm start of the pressure solves. 0 (default): every solve starts from the last
+ * solve's solution, as the reference's single mgfor x does (core/mgfordriver.py:66-78).
+ * 1, mixed precision only: the k-th projection of a step starts from the solution of
+ * the k-th projection of the previous step (one float-pair solution per projection of
+ * the time scheme). The stages of a step project divergences of different tendency
+ * combinations, so the same stage one step earlier is the nearer start; the solution
+ * is the same to the solve's tolerance, in fewer V-cycles. No counterpart in the
+ * reference. NYLES_UNSUPPORTED for an FP64 model (its parity keeps the reference's). */
+int nyles_model_set_mg_warm_start(NylesModel* m, int per_stage);
 /* LES.forward: one time step, core/model_les.py:147-149 -> core/timescheme.py:113-221.
  * Returns NYLES_BLOWUP when a pressure solve of the step meets a non-finite divergence
  * (a non-finite velocity, or a buoyancy that reached the velocity): the step stops at

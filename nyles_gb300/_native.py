@@ -101,6 +101,7 @@ SIGNATURES = {
     "nyles_model_bind": (_I, [_P, _PP, _PP, _P]),
     "nyles_model_set_mg_params": (_I, [_P, _D, _I, _D]),
     "nyles_model_set_mg_krylov": (_I, [_P, _I]),
+    "nyles_model_set_mg_warm_start": (_I, [_P, _I]),
     "nyles_model_forward": (_I, [_P, _D, _D, _P]),
     "nyles_model_diagnose": (_I, [_P, _P]),
     "nyles_model_rhs": (_I, [_P, _I, _D, _I, _P]),

@@ -125,8 +125,12 @@ struct MgImpl {
     MgLevelDesc lev[32];
     int bottom = 0;                   // first level of the one-block coarse solve (nlevels: none)
     size_t bottom_smem = 0;           // its shared memory bytes
-    // mixed precision: level-1 solution and right-hand side as float pairs (hi, lo)
+    // mixed precision: level-1 solution and right-hand side as float pairs (hi, lo);
+    // `nsol` solution arrays one after the other (sol_bytes apart), `cur_sol` the one the
+    // next solve starts from and updates (a model keeps one per stage of its time scheme)
     size_t off_pdf = 0, off_bdf = 0;
+    int nsol = 1, cur_sol = 0;
+    size_t sol_bytes = 0;
     // mixed precision, Krylov acceleration (FCG(1) preconditioned by the V-cycle): the
     // search direction and its image under the operator, level-1 floats
     int krylov = 0;
@@ -143,7 +147,9 @@ struct MgImpl {
     Bat bat;                          // batched launches (set while a batched step is captured)
 };
 
-int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision);
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol = 1);
+// the float-pair level-1 solution the next mixed-precision solve works on
+float2* mg_pdf(MgImpl* mg);
 int mg_solve(MgImpl* mg, cudaStream_t st);
 void* mg_level_ptr(MgImpl* mg, int lev, int var);
 

@@ -1760,7 +1760,7 @@ static T* lvp(MgImpl* mg, int l, int var) {
 void* mg_level_ptr(MgImpl* mg, int lev, int var) {
     if (!mg->ws || lev < 1 || lev > mg->nlevels) return nullptr;
     if (lev == 1 && mg->precision == NYLES_MIXED) {
-        if (var == 1) return mg->ws + mg->off_pdf;
+        if (var == 1) return reinterpret_cast<char*>(mg_pdf(mg));
         if (var == 2) return mg->ws + mg->off_bdf;
     }
     size_t off = var == 1 ? mg->lev[lev - 1].off_x : (var == 2 ? mg->lev[lev - 1].off_b : mg->lev[lev - 1].off_y);
@@ -1770,7 +1770,11 @@ void* mg_level_ptr(MgImpl* mg, int lev, int var) {
 // mg_setup.f90:225-307 (create_hierarchy) for one rank. The reference leaves the loop
 // only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
 // 3*2^n sizes terminate (the reference does not terminate on them).
-int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
+float2* mg_pdf(MgImpl* mg) {
+    return reinterpret_cast<float2*>(mg->ws + mg->off_pdf + (size_t)mg->cur_sol * mg->sol_bytes);
+}
+
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol) {
     if (nx < 2 || ny < 2 || nz < 1) { set_error("multigrid: grid too small"); return NYLES_BAD_ARG; }
     if (topology < 1 || topology > 6) { set_error("multigrid: bad topology"); return NYLES_BAD_ARG; }
     mg->precision = precision;
@@ -1808,7 +1812,10 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision) {
         d.off_y = take(d.vol * es);
     }
     if (precision == NYLES_MIXED) {
-        mg->off_pdf = take(mg->lev[0].vol * sizeof(float2));
+        mg->nsol = nsol < 1 ? 1 : nsol;
+        mg->cur_sol = 0;
+        mg->sol_bytes = (mg->lev[0].vol * sizeof(float2) + 255) & ~(size_t)255;
+        mg->off_pdf = take(mg->sol_bytes * mg->nsol);
         mg->off_bdf = take(mg->lev[0].vol * sizeof(float2));
         mg->off_fp = take(mg->lev[0].vol * sizeof(float));
         mg->off_fq = take(mg->lev[0].vol * sizeof(float));
@@ -1870,7 +1877,7 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
     note_launch(from_y ? 1 : 2);
     if (mg->bat.tab) {   // batched (stationary mixed refinement): modes 0 and 1
         const Bat& bt = mg->bat;
-        float2* pdf = last_mode == 1 ? reinterpret_cast<float2*>(mg->ws + mg->off_pdf) : nullptr;
+        float2* pdf = last_mode == 1 ? mg_pdf(mg) : nullptr;
         if constexpr (sizeof(T) == sizeof(float)) {
             if (use_v4(mg, g.n)) {
                 const dim3 gv = bgrid(mg, grid_v4(g.n));
@@ -1895,7 +1902,7 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
             const dim3 gv = grid_v4(g.n);
             if (!from_y) k_mg_jacobi_v4<0><<<gv, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
             if (last_mode == 1)
-                k_mg_jacobi_v4<1><<<gv, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf),
+                k_mg_jacobi_v4<1><<<gv, kBlk, 0, st>>>(g, y, b, x, om, mg_pdf(mg),
                                                       nullptr, nullptr, nullptr);
             else if (last_mode == 2)
                 k_mg_jacobi_v4<2><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr,
@@ -1909,7 +1916,7 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
     }
     if (!from_y) k_mg_jacobi<T, 0><<<grd, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
     if (last_mode == 1)
-        k_mg_jacobi<T, 1><<<grd, kBlk, 0, st>>>(g, y, b, x, om, reinterpret_cast<float2*>(mg->ws + mg->off_pdf),
+        k_mg_jacobi<T, 1><<<grd, kBlk, 0, st>>>(g, y, b, x, om, mg_pdf(mg),
                                                 nullptr, nullptr, nullptr);
     else if (last_mode == 2)
         k_mg_jacobi<T, 2><<<grd, kBlk, 0, st>>>(g, y, b, x, om, nullptr,
@@ -2058,7 +2065,7 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     const dim3 grd = v4 ? grid_v4(g.n) : grid_zc(g.n, MG_DFZC);
     ProfScope ps(mg->prof, 11, st);
     note_launch(2);
-    const float2* pdf = reinterpret_cast<const float2*>(mg->ws + mg->off_pdf);
+    const float2* pdf = mg_pdf(mg);
     const float2* bdf = reinterpret_cast<const float2*>(mg->ws + mg->off_bdf);
     if (mg->bat.tab) {
         if (v4)
@@ -2121,7 +2128,7 @@ static void enqueue_fcg_update(MgImpl* mg, cudaStream_t st, int k) {
         k_fcg_direction<<<grd, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
         k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, nb, sc);
     }
-    k_fcg_xupdate<<<eb, 256, 0, st>>>(reinterpret_cast<float2*>(mg->ws + mg->off_pdf), P, n, sc);
+    k_fcg_xupdate<<<eb, 256, 0, st>>>(mg_pdf(mg), P, n, sc);
 }
 
 template <typename T, int MODE>

@@ -182,6 +182,9 @@ struct NylesModel {
     nyles_forcing_fn forcing = nullptr;  // user forcing called after each right-hand side
     void* forcing_user = nullptr;
     Bat bat;                             // set while a batched graph is recorded
+    // mixed precision: each stage's pressure solve starts from the solution of the same
+    // stage of the previous step (1) or, as the reference, from the last solve's (0)
+    int warm_per_stage = 0;
     void release_graph() {
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
@@ -354,7 +357,10 @@ int nyles_model_create(const NylesDesc* d, int scheme, int precision, NylesModel
         set_error("z-periodic geometry needs x and y periodic (perio_xyz)");
         return NYLES_UNSUPPORTED;
     }
-    rc = mg_init(&m->mg, d->nx, d->ny, d->nz, topo, precision);
+    // mixed precision: one float-pair solution per projection of a step (RK3: 3, LFAM3:
+    // 2, EF: 1), the per-stage warm starts of nyles_model_set_mg_warm_start
+    const int nstage = scheme == NYLES_SCHEME_RK3_SSP ? 3 : (scheme == NYLES_SCHEME_LFAM3 ? 2 : 1);
+    rc = mg_init(&m->mg, d->nx, d->ny, d->nz, topo, precision, precision == NYLES_MIXED ? nstage : 1);
     if (rc) { delete m; return rc; }
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
@@ -403,6 +409,19 @@ int nyles_model_set_mg_krylov(NylesModel* m, int on) {
     if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
     if (m->gexec) { set_error("release the captured graph before changing the solver"); return NYLES_BAD_ARG; }
     return set_krylov(&m->mg, on);
+}
+
+int nyles_model_set_mg_warm_start(NylesModel* m, int per_stage) {
+    if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    if (m->gexec) { set_error("release the captured graph before changing the warm start"); return NYLES_BAD_ARG; }
+    if (per_stage && m->precision != NYLES_MIXED) {
+        set_error("per-stage warm starts are provided for the mixed-precision solve only (the FP64 solve keeps "
+                  "the reference's warm start)");
+        return NYLES_UNSUPPORTED;
+    }
+    m->warm_per_stage = per_stage ? 1 : 0;
+    m->mg.cur_sol = 0;
+    return NYLES_OK;
 }
 
 int nyles_model_reset_scheme(NylesModel* m) {
@@ -512,8 +531,11 @@ static int model_pressure_projection(NylesModel* m, cudaStream_t st) {
 
 // core/model_les.py:98-127 ; core/model_les_euler.py:96-125 ; the advection model fills
 // b only (core/model_advection.py:33-35)
+// `stage`: index of the projection within the time step (selects the per-stage warm
+// start of a mixed-precision model that keeps them)
 template <typename T>
-static int model_diagnose(NylesModel* m, cudaStream_t st) {
+static int model_diagnose(NylesModel* m, cudaStream_t st, int stage = 0) {
+    m->mg.cur_sol = (m->warm_per_stage && stage < m->mg.nsol) ? stage : 0;
     StencilPtrs<T> s = field_ptrs<T>(&m->d, reinterpret_cast<T* const*>(m->fields));
     int rc;
     T* uf[4] = {s.f[NYLES_F_B], s.f[NYLES_F_U_I], s.f[NYLES_F_U_J], s.f[NYLES_F_U_K]};
@@ -565,13 +587,13 @@ static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
     if (m->scheme == NYLES_SCHEME_RK3_SSP) {
         if ((rc = model_rhs<T>(m, 0, 0, t, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_EULER, 0, -1, -1, dt, st))) return rc;
-        if ((rc = model_diagnose<T>(m, st))) return rc;
+        if ((rc = model_diagnose<T>(m, st, 0))) return rc;
         if ((rc = model_rhs<T>(m, 1, 0, t + dt, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_2, 0, 1, -1, dt, st))) return rc;
-        if ((rc = model_diagnose<T>(m, st))) return rc;
+        if ((rc = model_diagnose<T>(m, st, 1))) return rc;
         if ((rc = model_rhs<T>(m, 2, 1, t + dt * 0.5, st, true))) return rc;
         if ((rc = model_update<T>(m, UPD_RK3_3, 0, 1, 2, dt, st))) return rc;
-        return model_diagnose<T>(m, st);
+        return model_diagnose<T>(m, st, 2);
     }
     if (m->scheme == NYLES_SCHEME_EF) {
         if ((rc = model_rhs<T>(m, 0, 1, t, st, true))) return rc;
@@ -586,10 +608,10 @@ static int model_forward(NylesModel* m, double t, double dt, cudaStream_t st) {
         return model_diagnose<T>(m, st);
     }
     if ((rc = model_update<T>(m, UPD_LF_PRED, 0, 1, 2, dt, st))) return rc;
-    if ((rc = model_diagnose<T>(m, st))) return rc;
+    if ((rc = model_diagnose<T>(m, st, 0))) return rc;
     if ((rc = model_rhs<T>(m, 0, 1, t + dt * 0.5, st, true))) return rc;
     if ((rc = model_update<T>(m, UPD_LF_CORR, 0, 1, 2, dt, st))) return rc;
-    return model_diagnose<T>(m, st);
+    return model_diagnose<T>(m, st, 1);
 }
 
 }  // namespace nyles

@@ -117,7 +117,7 @@ class LES(object):
         self._regs = nat.ptr_array(self.timescheme.register_pointers())
         nat.check(self.lib.nyles_model_bind(h, self._fields, self._regs, ctypes.c_void_p(ws)))
         self.set_mg_params(gpu.get("mg_tol", 1e-6), gpu.get("mg_maxite", 20), gpu.get("mg_omega", 0.9),
-                           krylov=gpu.get("mg_krylov", "auto"))
+                           krylov=gpu.get("mg_krylov", "auto"), warm_start=gpu.get("mg_warm_start", "auto"))
         self.stats = []
         # graph replay of fixed-dt steps (see forward)
         self.use_graphs = bool(gpu.get("graphs", True))
@@ -176,14 +176,18 @@ class LES(object):
             self._h = None
 
     # ------------------------------------------------------------------ settings
-    def set_mg_params(self, tol=1e-6, maxite=20, omega=0.9, krylov=None):
+    def set_mg_params(self, tol=1e-6, maxite=20, omega=0.9, krylov=None, warm_start=None):
         """Multigrid stop rule: sum(r^2)/sum(b^2) < tol or maxite V-cycles. `krylov`
         ("auto", "on", "off"; None keeps the current mode) selects the mixed-precision
         solver: FCG(1) preconditioned by the V-cycle, or the reference's stationary
         iteration; "auto" takes FCG when tol <= KRYLOV_AUTO_TOL, where both solvers land
         within the tolerance of the exact solution (at looser tolerances the stationary
-        iterates are the ones that track the FP64 solve). A captured graph holds the
-        solver and its parameters, so it is released first."""
+        iterates are the ones that track the FP64 solve). `warm_start` ("auto", "stage",
+        "last"; None keeps the current mode) picks the start of each solve: the previous
+        solve's solution (the reference's), or, mixed precision only, the solution of the
+        same stage one step earlier; "auto" takes "stage" exactly when FCG runs, for the
+        same reason. A captured graph holds the solver and its parameters, so it is
+        released first."""
         if getattr(self, "graph", None) is not None:
             self.release_graph()
         if krylov is not None:
@@ -201,6 +205,17 @@ class LES(object):
             use = mode == "on" or (mode == "auto" and float(tol) <= KRYLOV_AUTO_TOL)
         nat.check(self.lib.nyles_model_set_mg_krylov(self._h, 1 if use else 0))
         self.krylov = use
+        if warm_start is not None:
+            if warm_start not in ("auto", "stage", "last"):
+                raise ValueError("mg_warm_start must be 'auto', 'stage' or 'last'")
+            self.mg_warm_start = warm_start
+        wmode = getattr(self, "mg_warm_start", "auto")
+        if wmode == "stage" and self.precision == "fp64":
+            raise ValueError("mg_warm_start = 'stage' needs the mixed precision (the FP64 solve keeps the "
+                             "reference's warm start)")
+        per_stage = wmode == "stage" or (wmode == "auto" and use)
+        nat.check(self.lib.nyles_model_set_mg_warm_start(self._h, 1 if per_stage else 0))
+        self.warm_per_stage = per_stage
 
     def mg_stats(self):
         s = nat.NylesMgStats()

@@ -132,8 +132,9 @@ def initial_state(nyl, case, seed):
 def footprint_bytes(case, n, precision="mixed"):
     """Device bytes of one run: 14 state fields, 3 x 4 time-scheme registers, and the
     multigrid workspace (x, b, y per level; in mixed precision also the float-pair
-    solution and rhs of level 1 and the two float vectors of the Krylov solver), plus
-    3% and 256 KiB for partial sums, scalars and allocator rounding."""
+    solutions of level 1, one per RK3 stage, its float-pair rhs and the two float
+    vectors of the Krylov solver), plus 3% and 256 KiB for partial sums, scalars and
+    allocator rounding."""
     per = CASES[case]["geometry"]
     e = 8 if precision == "fp64" else 4
     dims = [n + (6 if ax in per else 0) for ax in ("z", "y", "x")]
@@ -147,7 +148,7 @@ def footprint_bytes(case, n, precision="mixed"):
         x //= 2
         z //= 2
     if precision == "mixed":
-        mg += 2 * 8 * n ** 3 + 2 * 4 * n ** 3
+        mg += (3 + 1) * 8 * n ** 3 + 2 * 4 * n ** 3
     return int(1.03 * (fields + mg)) + (1 << 18)
 
 

@@ -305,6 +305,48 @@ def test_mixed_krylov_graph_matches_eager():
     assert runs[True][1] == runs[False][1]
 
 
+
+@pytest.mark.parametrize("scheme", ["RK3_SSP", "LFAM3"])
+def test_mixed_per_stage_warm_start(scheme):
+    """Each stage's solve warm-started from the same stage one step earlier: the state
+    stays within the mixed bar of the FP64 run and of the reference's warm start, in
+    fewer V-cycles; graph replay equals eager stepping bit for bit; the FP64 model
+    refuses the mode."""
+    from nyles_gb300 import _native as nat
+    from nyles_gb300.nyles import Nyles
+    runs = {}
+    for tag, prec, warm, graphs in (("fp64", "fp64", "last", False), ("last", "mixed", "last", False),
+                                    ("stage", "mixed", "stage", False), ("stage_graph", "mixed", "stage", True)):
+        p = helpers.make_params(geometry="perio_xy", n=(32, 32, 32), dt=1e-3, precision=prec, mg_tol=1e-20,
+                                mg_maxite=40, timestepping=scheme)
+        p.gpu["graphs"] = graphs
+        p.gpu["mg_warm_start"] = warm
+        nyl = Nyles(p)
+        m = nyl.model
+        assert m.warm_per_stage == (warm == "stage")
+        for k, v in helpers.seeded_state(nyl, "noise", 9).items():
+            m.state.get(k).view("i")[...] = torch.from_numpy(v)
+        m.diagnose_var(m.state)
+        v0 = m.mg_stats()["vcycles"]
+        for n in range(10):
+            m.forward(n * 1e-3, 1e-3)
+        torch.cuda.synchronize()
+        runs[tag] = ({s: m.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k")},
+                     m.mg_stats()["vcycles"] - v0)
+    for s in runs["fp64"][0]:
+        assert helpers.relerr(runs["stage"][0][s], runs["fp64"][0][s]) < 1e-5, s
+        assert helpers.relerr(runs["stage"][0][s], runs["last"][0][s]) < 1e-5, s
+        np.testing.assert_array_equal(runs["stage_graph"][0][s], runs["stage"][0][s])
+    assert runs["stage"][1] < runs["last"][1], (runs["stage"][1], runs["last"][1])
+    assert runs["stage_graph"][1] == runs["stage"][1]
+    p = helpers.make_params(geometry="perio_xy", n=(16, 16, 16), precision="fp64")
+    p.gpu["mg_warm_start"] = "stage"
+    with pytest.raises(ValueError):
+        Nyles(p)
+    nyl = Nyles(helpers.make_params(geometry="perio_xy", n=(16, 16, 16), precision="fp64"))
+    assert nat.lib().nyles_model_set_mg_warm_start(nyl.model._h, 1) == nat.NYLES_UNSUPPORTED
+
+
 _SOLVES_CODE = (
     "import numpy as np, sys\n"
     "from nyles_gb300.multigrid import MG\n"

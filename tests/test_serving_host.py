@@ -18,7 +18,7 @@ def test_request_stream_is_seeded_poisson():
 def test_footprint_grows_with_size_and_precision():
     f = [S.footprint_bytes("tgv", n, "mixed") for n in (32, 48, 64, 96, 128)]
     assert all(x < y for x, y in zip(f, f[1:]))
-    assert S.footprint_bytes("lock", 64, "fp64") > 1.5 * S.footprint_bytes("lock", 64, "mixed")
+    assert S.footprint_bytes("lock", 64, "fp64") > 1.4 * S.footprint_bytes("lock", 64, "mixed")
     assert S.steps_per_graph(300) == 10 and S.steps_per_graph(7) == 7 and S.steps_per_graph(13) == 1
 
 
