@@ -58,8 +58,9 @@ def parse():
     ap.add_argument("--no-serving-baseline", action="store_true")
     ap.add_argument("--serving-priority", default="work", choices=["work", "none"],
                     help="CUDA stream priority of each run by its total work, or none")
-    ap.add_argument("--serving-capacity", type=int, default=16,
-                    help="slots per size bucket (runs advanced by one batched launch), at most 32")
+    ap.add_argument("--serving-capacity", default="auto",
+                    help="slots per size bucket (runs advanced by one batched launch): 1..32, or auto (as many "
+                         "n^3 runs as 2^23 cells hold)")
     ap.add_argument("--serving-sequential", default="estimate", choices=["estimate", "measured"],
                     help="sequential FP64 baseline: bucket timings replayed over the queue, or every run executed")
     ap.add_argument("--no-eager", action="store_true", help="skip the eager (no graph) timing beside the headline")
@@ -418,8 +419,8 @@ def time_serving(a):
     warm = [S.Request(i, c, n, i, 4, 0.0) for i, (c, n) in enumerate((("lock", 32), ("tgv", 32)))]
     S.ServingEngine(precision="mixed").serve(warm, realtime=False)
     reqs = S.make_requests(a.serving_requests, a.serving_rate, seed=5, steps=a.serving_steps)
-    eng = S.ServingEngine(hbm_budget_bytes=120e9, precision="mixed", priority=a.serving_priority,
-                          capacity=a.serving_capacity)
+    cap = a.serving_capacity if a.serving_capacity == "auto" else int(a.serving_capacity)
+    eng = S.ServingEngine(hbm_budget_bytes=120e9, precision="mixed", priority=a.serving_priority, capacity=cap)
     from nyles_gb300 import _native
     l0 = _native.lib().nyles_launch_count()
     torch.cuda.synchronize()
@@ -427,7 +428,8 @@ def time_serving(a):
     launches = _native.lib().nyles_launch_count() - l0
     out = {"requests": len(reqs), "steps_per_run": a.serving_steps, "rate_per_s": a.serving_rate,
            "stream_seed": 5, "sizes": [32, 48, 64, 96, 128], "precision": "mixed", "mg_tol_sq_ratio": 1e-6,
-           "hbm_budget_gb": 120, "stream_priority": a.serving_priority, "bucket_capacity": a.serving_capacity,
+           "hbm_budget_gb": 120, "stream_priority": a.serving_priority,
+           "bucket_capacity": ({str(n): S.auto_capacity(n) for n in (32, 48, 64, 96, 128)} if cap == "auto" else cap),
            "buckets": eng.buckets_made, "batched_launches": eng.launches,
            "max_resident_runs": eng.max_active, "peak_footprint_gb": eng.peak_used / 1e9,
            "kernel_launches": launches}

@@ -12,7 +12,9 @@ Completion latency = time from arrival to the end of the run's last step.
 
 The reference has no serving layer (one experiment per process, core/nyles.py).
 """
+import functools
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -103,13 +105,21 @@ def build_params(case, n, precision="mixed", mg_tol=1e-6):
     return p
 
 
+@functools.lru_cache(maxsize=64)
+def case_grid(case, n):
+    """The grid of a case on n^3 cells (the coordinates that initial_fields reads)"""
+    from . import grid as grid_module
+    from .nyles import prepare_parameters
+    return grid_module.Grid(prepare_parameters(build_params(case, n)))
+
+
 def initial_fields(nyl, case, seed):
     """Seeded initial fields (numpy, the (z, y, x) arrays of view('i')): lock exchange
     (b = -0.5 | +0.5 across x = L/2 plus uniform noise 1e-3) or Taylor-Green (u = sin x
     cos y cos z, v = -cos x sin y cos z plus Gaussian noise 1e-4, covariant: times the
-    spacing)."""
+    spacing). `nyl`: a Nyles of the case, or its grid."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    g = nyl.grid
+    g = getattr(nyl, "grid", nyl)
     if case == "lock":
         xb = g.x_b.view("i").numpy()
         return {"b": np.where(xb < 0.5 * g.Lx, -0.5, 0.5) + 1e-3 * rng.uniform(-1, 1, size=xb.shape)}
@@ -152,6 +162,17 @@ def footprint_bytes(case, n, precision="mixed"):
     return int(1.03 * (fields + mg)) + (1 << 18)
 
 
+# cells that the batched launches of one bucket cover at most (capacity "auto"): a run of
+# 128^3 cells fills the device alone, so its bucket batches few runs, while runs of 32^3
+# to 64^3 are bound by launch latency and batch up to NYLES_BATCH_RUNS
+CELLS_PER_BUCKET = 1 << 23
+
+
+def auto_capacity(n, cap_max=32):
+    """slots of a bucket of n^3-cell runs under capacity 'auto'"""
+    return max(1, min(cap_max, CELLS_PER_BUCKET // n ** 3))
+
+
 def steps_per_graph(steps, kmax=10):
     """largest divisor of `steps` not above kmax: graph launches land exactly on `steps`"""
     for k in range(min(kmax, steps), 0, -1):
@@ -162,17 +183,26 @@ def steps_per_graph(steps, kmax=10):
 
 class Slot:
     """One place of a bucket: a model whose arrays are carved from the slot's part of
-    the bucket buffer, and the request it currently serves (None: free)."""
+    the bucket buffer, and the request it currently serves (None: free). The model is
+    built when the slot is first used (`make` returns it): the batched graphs address
+    every slot through slot 0's model and the slot's byte offset."""
 
-    def __init__(self, index, nyl):
+    def __init__(self, index, make):
         self.index = index
-        self.nyl = nyl
+        self._make = make
+        self._nyl = None
         self.req = None
         self.projected = False     # the initial projection has been launched
         self.launched = 0
         self.last_event = None     # event of the latest launch that advanced this run
         self.admitted = 0.0
         self.staging = None        # pinned host copies of the initial state, kept until used
+
+    @property
+    def nyl(self):
+        if self._nyl is None:
+            self._nyl = self._make()
+        return self._nyl
 
     @property
     def active(self):
@@ -209,10 +239,11 @@ class Bucket:
         self.slot_bytes = Arena.aligned(arena_bytes(build_params(case, n, precision, mg_tol)))
         self.bytes = self.slot_bytes * capacity
         self.buf = torch.zeros(self.bytes, dtype=torch.uint8, device=device)
-        self.slots = []
-        for r in range(capacity):
+        def make(r):
             arena = Arena(self.buf[r * self.slot_bytes:(r + 1) * self.slot_bytes])
-            self.slots.append(Slot(r, Nyles(build_params(case, n, precision, mg_tol), device=device, arena=arena)))
+            return Nyles(build_params(case, n, precision, mg_tol), device=device, arena=arena)
+
+        self.slots = [Slot(r, functools.partial(make, r)) for r in range(capacity)]
         self.lib = nat.lib()
         self.nat = nat
         tb = ctypes.sizeof(nat.NylesBatchTable)
@@ -259,24 +290,22 @@ class Bucket:
     def resident(self):
         return [sl for sl in self.slots if sl.req is not None]
 
-    def admit(self, slot, req, now):
+    def admit(self, slot, req, now, staged=None):
         """Queue on the bucket stream: zero the slot (a fresh allocation's contents) and
-        copy the request's initial state in from pinned host memory; the projection
-        follows in the next launch (`launch`)."""
+        copy the request's initial state in from pinned host memory (`staged`, from
+        stage_initial_state, or made here); the projection follows in the next launch
+        (`launch`)."""
         slot.req, slot.launched, slot.last_event, slot.projected = req, 0, None, False
         slot.admitted = now
-        fields = initial_fields(slot.nyl, req.case, req.seed)
+        if staged is None:
+            staged = stage_initial_state(req, self.template.state.b.dtype)
         lo = slot.index * self.slot_bytes
-        staging = []
         with torch.cuda.stream(self.stream):
             self.buf[lo:lo + self.slot_bytes].zero_()
             st = slot.nyl.model.state
-            for name, arr in fields.items():
-                dst = st.get(name).view("i")
-                h = torch.from_numpy(arr).to(dst.dtype).pin_memory()
-                dst.copy_(h, non_blocking=True)
-                staging.append(h)
-        slot.staging = staging
+            for name, h in staged.items():
+                st.get(name).view("i").copy_(h, non_blocking=True)
+        slot.staging = staged
 
     # ---- launches
     def poll(self):
@@ -371,6 +400,14 @@ class Bucket:
         self.buf = None
 
 
+def stage_initial_state(req, dtype, grid=None):
+    """{field: pinned host tensor} of a request's initial state in the model's dtype
+    (host work only: the engine runs it on worker threads ahead of admission, with the
+    grid built beforehand on the engine's thread, which alone touches the parameters)"""
+    fields = initial_fields(grid if grid is not None else case_grid(req.case, req.n), req.case, req.seed)
+    return {name: torch.from_numpy(arr).to(dtype).pin_memory() for name, arr in fields.items()}
+
+
 def remaining_work(bucket):
     """cells x steps not yet launched in a bucket"""
     return sum(bucket.n ** 3 * max(0, sl.req.steps - sl.launched) for sl in bucket.slots if sl.req is not None)
@@ -385,22 +422,27 @@ class ServingEngine:
     is refused at once. Each bucket keeps up to `inflight` launches queued on its own
     stream (CUDA priority by the per-run work n^3 x steps, smallest first, with
     priority "work"; equal with "none"), so buckets of every size overlap on the device.
-    `capacity` = slots per bucket (at most NYLES_BATCH_RUNS); a bucket with no run left
-    and none waiting is released. `window` = W launches only the W buckets with the least
+    `capacity` = slots per bucket (at most NYLES_BATCH_RUNS), or "auto": as many runs as
+    CELLS_PER_BUCKET cells hold (auto_capacity); a bucket with no run left and none
+    waiting is released. The initial states of queued requests are built on
+    `prep_threads` host threads while the loop keeps launching. `window` = W launches only the W buckets with the least
     remaining work (cells x steps not yet launched) at each tick, so that small runs
     finish soon after they arrive and the large ones, which set the makespan, fill the
     device afterwards; None launches every bucket. Completion latency = arrival to the
     end of the run's last launch."""
 
     def __init__(self, hbm_budget_bytes=120e9, precision="mixed", mg_tol=1e-6, device=None, inflight=2,
-                 clock=time.perf_counter, bucket_factory=None, priority="work", capacity=16, window=None):
+                 clock=time.perf_counter, bucket_factory=None, priority="work", capacity="auto", window=None,
+                 prep_threads=4, prep_ahead=16):
         if window is not None and window < 1:
             raise ValueError("window must be None or >= 1")
         self.window = window
         if priority not in ("work", "none"):
             raise ValueError("priority must be 'work' or 'none'")
-        if not 1 <= capacity <= 32:
-            raise ValueError("capacity must be 1..32 (NYLES_BATCH_RUNS)")
+        if capacity != "auto" and not 1 <= capacity <= 32:
+            raise ValueError("capacity must be 'auto' or 1..32 (NYLES_BATCH_RUNS)")
+        self.prep_threads = prep_threads
+        self.prep_ahead = prep_ahead
         self.priority = priority
         self.capacity = capacity
         self.budget = float(hbm_budget_bytes)
@@ -418,6 +460,9 @@ class ServingEngine:
         self.buckets_made = 0
         self.launches = 0
 
+    def capacity_for(self, n):
+        return auto_capacity(n) if self.capacity == "auto" else self.capacity
+
     def serve(self, requests, realtime=True, keep_states=False):
         """Serve `requests` (arrival times relative to now when `realtime`, else all at
         once). Returns (results, final_states) with final_states[rid] = dict of numpy
@@ -425,76 +470,101 @@ class ServingEngine:
         pending = sorted(requests, key=lambda r: r.arrival)
         prio = self.stream_priorities(requests)
         queue, buckets, results, states = [], {}, [], {}
+        # initial states built on host threads ahead of admission (real device only)
+        pool = (ThreadPoolExecutor(self.prep_threads) if self.prep_threads > 0 and self.device is not None
+                and self.device.type == "cuda" else None)
+        dtype = torch.float64 if self.precision == "fp64" else torch.float32
+        staging = {}
         t0 = self.clock()
         nxt = 0
-        while nxt < len(pending) or queue or buckets:
-            now = self.clock() - t0
-            while nxt < len(pending) and (not realtime or pending[nxt].arrival <= now):
-                queue.append(pending[nxt])
-                nxt += 1
-            # admission, in arrival order; a request whose bucket is full waits without
-            # blocking the others
-            waiting = []
-            for req in queue:
-                need = footprint_bytes(req.case, req.n, self.precision)
-                if need > self.budget:
-                    results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
-                                          now, now, req.n ** 3, 0, "refused"))
-                    continue
-                key = (req.case, req.n, steps_per_graph(req.steps))
-                b = buckets.get(key)
-                if b is None:
-                    cap = min(self.capacity, int((self.budget - self.used) // need))
-                    if cap < 1:
-                        waiting.append(req)
-                        continue
-                    b = self.bucket_factory(key, self.precision, self.mg_tol, self.device, cap,
-                                            priority=prio[req.rid])
-                    buckets[key] = b
-                    self.buckets_made += 1
-                    self.used += b.bytes
-                    self.peak_used = max(self.peak_used, self.used)
-                slot = b.free_slot()
-                if slot is None:
-                    waiting.append(req)
-                    continue
-                b.admit(slot, req, self.clock() - t0)
-            queue = waiting
-            self.max_active = max(self.max_active, sum(len(b.resident()) for b in buckets.values()))
-            # launches: every bucket, or the `window` with the least remaining work
-            busy = False
-            order = list(buckets.values())
-            if self.window is not None:
-                order = sorted(order, key=remaining_work)[:self.window]
-            for b in order:
-                if b.poll() < self.inflight:
-                    busy |= b.launch()
-            # completion
-            for key in list(buckets):
-                b = buckets[key]
-                for sl in b.slots:
-                    if sl.finished():
-                        req = sl.req
-                        status, vcycles, fields = b.outcome(sl, keep_states)
-                        done = self.clock() - t0
-                        results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
-                                              sl.admitted, done, req.n ** 3, vcycles, status))
-                        if keep_states and fields is not None:
-                            states[req.rid] = fields
-                        b.release(sl)
-                if not b.resident() and not any((r.case, r.n, steps_per_graph(r.steps)) == key for r in queue):
-                    self.launches += b.launches
-                    b.close()
-                    self.used -= b.bytes
-                    del buckets[key]
-            if not busy:
-                if buckets:
-                    time.sleep(2e-4)
-                elif not queue and nxt < len(pending):
-                    time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
+        try:
+            while nxt < len(pending) or queue or buckets:
+                nxt, queue = self._tick(pending, nxt, queue, buckets, results, states, prio, realtime,
+                                        keep_states, t0, pool, staging, dtype)
+        finally:
+            if pool is not None:
+                pool.shutdown(wait=True, cancel_futures=True)
         if self.device is not None and self.device.type == "cuda":
             torch.cuda.synchronize(self.device)
         return sorted(results, key=lambda r: r.rid), states
+
+    def _tick(self, pending, nxt, queue, buckets, results, states, prio, realtime, keep_states, t0, pool,
+              staging, dtype):
+        """one pass of the serving loop: arrivals, admission, launches, completions"""
+        now = self.clock() - t0
+        while nxt < len(pending) and (not realtime or pending[nxt].arrival <= now):
+            queue.append(pending[nxt])
+            nxt += 1
+        if pool is not None:
+            for req in queue[:self.prep_ahead]:
+                if req.rid not in staging and footprint_bytes(req.case, req.n, self.precision) <= self.budget:
+                    staging[req.rid] = pool.submit(stage_initial_state, req, dtype, case_grid(req.case, req.n))
+        # admission, in arrival order; a request whose bucket is full, or whose
+        # initial state is still being built, waits without blocking the others
+        waiting = []
+        for req in queue:
+            need = footprint_bytes(req.case, req.n, self.precision)
+            if need > self.budget:
+                results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
+                                      now, now, req.n ** 3, 0, "refused"))
+                continue
+            fut = staging.get(req.rid)
+            if fut is not None and not fut.done():
+                waiting.append(req)
+                continue
+            key = (req.case, req.n, steps_per_graph(req.steps))
+            b = buckets.get(key)
+            if b is None:
+                cap = min(self.capacity_for(req.n), int((self.budget - self.used) // need))
+                if cap < 1:
+                    waiting.append(req)
+                    continue
+                b = self.bucket_factory(key, self.precision, self.mg_tol, self.device, cap,
+                                        priority=prio[req.rid])
+                buckets[key] = b
+                self.buckets_made += 1
+                self.used += b.bytes
+                self.peak_used = max(self.peak_used, self.used)
+            slot = b.free_slot()
+            if slot is None:
+                waiting.append(req)
+                continue
+            fut = staging.pop(req.rid, None)
+            b.admit(slot, req, self.clock() - t0, staged=fut.result() if fut is not None else None)
+        queue = waiting
+        self.max_active = max(self.max_active, sum(len(b.resident()) for b in buckets.values()))
+        # launches: every bucket, or the `window` with the least remaining work
+        busy = False
+        order = list(buckets.values())
+        if self.window is not None:
+            order = sorted(order, key=remaining_work)[:self.window]
+        for b in order:
+            if b.poll() < self.inflight:
+                busy |= b.launch()
+        # completion
+        for key in list(buckets):
+            b = buckets[key]
+            for sl in b.slots:
+                if sl.finished():
+                    req = sl.req
+                    status, vcycles, fields = b.outcome(sl, keep_states)
+                    done = self.clock() - t0
+                    results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
+                                          sl.admitted, done, req.n ** 3, vcycles, status))
+                    if keep_states and fields is not None:
+                        states[req.rid] = fields
+                    b.release(sl)
+            if not b.resident() and not any((r.case, r.n, steps_per_graph(r.steps)) == key for r in queue):
+                self.launches += b.launches
+                b.close()
+                self.used -= b.bytes
+                del buckets[key]
+        if not busy:
+            if buckets or staging:
+                time.sleep(2e-4)
+            elif not queue and nxt < len(pending):
+                time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
+        return nxt, queue
 
     def stream_priorities(self, requests, levels=None):
         """{rid: stream priority}: the distinct work values (n^3 x steps) of the requests,

@@ -63,7 +63,7 @@ class FakeBucket:
     def resident(self):
         return [sl for sl in self.slots if sl.req is not None]
 
-    def admit(self, slot, req, now):
+    def admit(self, slot, req, now, staged=None):
         slot.req, slot.launched, slot.admitted, slot.pending = req, 0, now, 0
         FakeBucket.live += 1
         FakeBucket.peak = max(FakeBucket.peak, FakeBucket.live)
