@@ -182,10 +182,19 @@ int nyles_model_set_mg_krylov(NylesModel* m, int on);
  * 1, mixed precision only: the k-th projection of a step starts from the solution of
  * the k-th projection of the previous step (one float-pair solution per projection of
  * the time scheme). The stages of a step project divergences of different tendency
- * combinations, so the same stage one step earlier is the nearer start; the solution
- * is the same to the solve's tolerance, in fewer V-cycles. No counterpart in the
- * reference. NYLES_UNSUPPORTED for an FP64 model (its parity keeps the reference's). */
-int nyles_model_set_mg_warm_start(NylesModel* m, int per_stage);
+ * combinations, so the same stage one step earlier is the nearer start. 2, mixed
+ * precision only: as 1, from the linear extrapolation 2 x(n-1) - x(n-2) of the same
+ * stage's last two solutions (once it has two). 3: the quadratic extrapolation
+ * 3 x(n-1) - 3 x(n-2) + x(n-3) once it has three (linear with two); 4: the cubic one
+ * 4 x(n-1) - 6 x(n-2) + 4 x(n-3) - x(n-4) once it has four. The solution is
+ * the same to the solve's tolerance, in fewer V-cycles. No counterpart in the
+ * reference. The mode sizes the workspace (mode m > 0 keeps nstage x (1 + max(0, m-1))
+ * float-pair solutions of the fine level): select it before
+ * nyles_model_workspace_bytes and nyles_model_bind; a bound model accepts only modes
+ * whose arrays its workspace holds (else NYLES_BAD_ARG). Changing the mode forgets the
+ * kept solutions.
+ * NYLES_UNSUPPORTED for an FP64 model (its parity keeps the reference's). */
+int nyles_model_set_mg_warm_start(NylesModel* m, int mode);
 /* LES.forward: one time step, core/model_les.py:147-149 -> core/timescheme.py:113-221.
  * Returns NYLES_BLOWUP when a pressure solve of the step meets a non-finite divergence
  * (a non-finite velocity, or a buoyancy that reached the velocity): the step stops at

@@ -131,6 +131,12 @@ struct MgImpl {
     size_t off_pdf = 0, off_bdf = 0;
     int nsol = 1, cur_sol = 0;
     size_t sol_bytes = 0;
+    // `nhist` (0..3): behind the nsol solutions, nhist x nsol more arrays holding the
+    // solutions before each one, and per solution a count (0..4) of the solves it has
+    // seen; with `extrap` p (1..nhist) a solve starts from the degree-p extrapolation
+    int nhist = 0;
+    int extrap = 0;
+    size_t off_hist = 0;
     // mixed precision, Krylov acceleration (FCG(1) preconditioned by the V-cycle): the
     // search direction and its image under the operator, level-1 floats
     int krylov = 0;
@@ -147,9 +153,11 @@ struct MgImpl {
     Bat bat;                          // batched launches (set while a batched step is captured)
 };
 
-int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol = 1);
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol = 1, int nhist = 0);
 // the float-pair level-1 solution the next mixed-precision solve works on
 float2* mg_pdf(MgImpl* mg);
+// forget the solutions kept for extrapolated warm starts (the next solves start plain)
+int mg_reset_history(MgImpl* mg);
 int mg_solve(MgImpl* mg, cudaStream_t st);
 void* mg_level_ptr(MgImpl* mg, int lev, int var);
 

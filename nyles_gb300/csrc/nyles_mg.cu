@@ -1586,6 +1586,70 @@ __global__ void __launch_bounds__(256) k_fcg_xupdate(float2* __restrict__ xdf, c
     xdf[i] = df_add(xdf[i], df_mul_f(p[i], alpha));
 }
 
+// Extrapolated warm start of a mixed-precision solve. The solution array x(n-1) has
+// MG_HIST history arrays holding x(n-2), x(n-3), ... With `order` p and at least p + 1
+// solves seen (else the highest order they allow), the start becomes the polynomial
+// extrapolation of the last p + 1 solutions to the next step (equal steps; binomial
+// coefficients: 2, -1; 3, -3, 1; 4, -6, 4, -1), formed in double and split into a float
+// pair. The history then shifts by one. Nothing changes when the right-hand side's
+// norm (scalar slot SC_NORMB, set just before) is zero or not finite: the solve then
+// keeps its start (a zero right-hand side) or stops at once (blow-up).
+// k_mg_hist_count, launched after, counts the solve.
+constexpr int MG_HIST = 3;
+struct HistPtrs {
+    float2* h[MG_HIST];   // x(n-2), x(n-3), x(n-4)
+};
+__global__ void __launch_bounds__(256) k_mg_extrapolate(float2* __restrict__ cur, HistPtrs hp, long long n,
+                                                        int order, const double* __restrict__ sc,
+                                                        const int* __restrict__ count, const Bat bat = Bat()) {
+    int bz;
+    long long dlt;
+    if (!batch_enter(bat, bz, dlt)) return;
+    cur = bshift(cur, dlt);
+#pragma unroll
+    for (int k = 0; k < MG_HIST; ++k) hp.h[k] = bshift(hp.h[k], dlt);
+    sc = bshift(sc, dlt);
+    count = bshift(count, dlt);
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nb = sc[SC_NORMB];
+    if (!(nb > 0.0 && nb <= 1.7976931348623157e308)) return;
+    const int p = min(order, *count - 1);   // order the history allows
+    float2 v[MG_HIST + 1];
+    v[0] = cur[i];
+#pragma unroll
+    for (int k = 0; k < MG_HIST; ++k) v[k + 1] = (k < order) ? hp.h[k][i] : make_float2(0.f, 0.f);
+    if (p >= 1) {
+        double x[MG_HIST + 1];
+#pragma unroll
+        for (int k = 0; k <= MG_HIST; ++k) x[k] = (double)v[k].x + (double)v[k].y;
+        double e;
+        if (p == 1) e = 2.0 * x[0] - x[1];
+        else if (p == 2) e = 3.0 * (x[0] - x[1]) + x[2];
+        else e = 4.0 * (x[0] + x[2]) - 6.0 * x[1] - x[3];
+        const float hi = __double2float_rn(e);
+        cur[i] = make_float2(hi, __double2float_rn(e - (double)hi));
+    }
+#pragma unroll
+    for (int k = MG_HIST - 1; k >= 0; --k)
+        if (k < order) hp.h[k][i] = v[k];
+}
+
+// one thread per run: the count of solves seen by the solution array (saturating at
+// MG_HIST + 1)
+__global__ void k_mg_hist_count(int* count, const double* sc, const Bat bat = Bat()) {
+    const int r = threadIdx.x;
+    if (bat.tab) {
+        if (r >= bat.nrun || !bat.tab->active[r]) return;
+        count = bshift(count, bat.tab->delta[r]);
+        sc = bshift(sc, bat.tab->delta[r]);
+    } else if (r > 0) {
+        return;
+    }
+    const double nb = sc[SC_NORMB];
+    if (nb > 0.0 && nb <= 1.7976931348623157e308 && *count < MG_HIST + 1) *count += 1;
+}
+
 // sum of squares of a float-pair array (high parts, squared and summed in double)
 __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_sumsq_df(const MgGeom g, const float2* __restrict__ v,
                                                               double* __restrict__ partial, const Bat bat = Bat()) {
@@ -1767,14 +1831,22 @@ void* mg_level_ptr(MgImpl* mg, int lev, int var) {
     return mg->ws + off;
 }
 
-// mg_setup.f90:225-307 (create_hierarchy) for one rank. The reference leaves the loop
-// only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
-// 3*2^n sizes terminate (the reference does not terminate on them).
 float2* mg_pdf(MgImpl* mg) {
     return reinterpret_cast<float2*>(mg->ws + mg->off_pdf + (size_t)mg->cur_sol * mg->sol_bytes);
 }
+// the solutions before the current one (history arrays, h = 1..MG_HIST) and the
+// current solution's count
+static float2* mg_pdf_old(MgImpl* mg, int h) {
+    return reinterpret_cast<float2*>(mg->ws + mg->off_pdf + (size_t)(h * mg->nsol + mg->cur_sol) * mg->sol_bytes);
+}
+static int* mg_hist_count(MgImpl* mg) { return reinterpret_cast<int*>(mg->ws + mg->off_hist) + mg->cur_sol; }
 
-int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol) {
+// mg_setup.f90:225-307 (create_hierarchy) for one rank. The reference leaves the loop
+// only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
+// 3*2^n sizes terminate (the reference does not terminate on them).
+
+int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol, int nhist) {
+    if (nhist < 0 || nhist > MG_HIST) { set_error("multigrid: history depth out of range"); return NYLES_BAD_ARG; }
     if (nx < 2 || ny < 2 || nz < 1) { set_error("multigrid: grid too small"); return NYLES_BAD_ARG; }
     if (topology < 1 || topology > 6) { set_error("multigrid: bad topology"); return NYLES_BAD_ARG; }
     mg->precision = precision;
@@ -1815,7 +1887,10 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int
         mg->nsol = nsol < 1 ? 1 : nsol;
         mg->cur_sol = 0;
         mg->sol_bytes = (mg->lev[0].vol * sizeof(float2) + 255) & ~(size_t)255;
-        mg->off_pdf = take(mg->sol_bytes * mg->nsol);
+        mg->nhist = nhist;
+        mg->extrap = 0;
+        mg->off_pdf = take(mg->sol_bytes * mg->nsol * (1 + nhist));
+        if (nhist) mg->off_hist = take(mg->nsol * sizeof(int));
         mg->off_bdf = take(mg->lev[0].vol * sizeof(float2));
         mg->off_fp = take(mg->lev[0].vol * sizeof(float));
         mg->off_fq = take(mg->lev[0].vol * sizeof(float));
@@ -2158,6 +2233,20 @@ static int blowup(MgImpl* mg, int nite, double res, const char* what) {
     return NYLES_BLOWUP;
 }
 
+// extrapolated start of the next mixed solve (after its right-hand side norm)
+static void enqueue_extrapolate(MgImpl* mg, cudaStream_t st) {
+    if (!mg->extrap || mg->extrap > mg->nhist) return;
+    const long long n = mg->lev[0].vol;
+    const unsigned eb = (unsigned)((n + 255) / 256);
+    double* sc = scalars(mg);
+    note_launch(2);
+    HistPtrs hp;
+    for (int k = 0; k < MG_HIST; ++k) hp.h[k] = k < mg->nhist ? mg_pdf_old(mg, k + 1) : nullptr;
+    k_mg_extrapolate<<<bgrid(mg, dim3(eb, 1, 1)), 256, 0, st>>>(mg_pdf(mg), hp, n, mg->extrap, sc,
+                                                                 mg_hist_count(mg), mg->bat);
+    k_mg_hist_count<<<1, mg->bat.tab ? NYLES_MAX_BATCH : 1, 0, st>>>(mg_hist_count(mg), sc, mg->bat);
+}
+
 // solvers.f90:8-33: stop when sum(r^2)/sum(b^2) < tol or after maxite V-cycles
 int mg_solve(MgImpl* mg, cudaStream_t st) {
     if (!mg->ws) { set_error("multigrid: workspace not bound"); return NYLES_BAD_ARG; }
@@ -2191,6 +2280,7 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
         }
     } else {
         enqueue_normb_df(mg, st);
+        enqueue_extrapolate(mg, st);
         if ((rc = read_slot(mg, SC_NORMB, &normb, st))) return rc;
         if (!finite_norm(normb)) return blowup(mg, 0, normb, "right-hand side");
         if (normb > 0.0) {
@@ -2267,6 +2357,7 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         enqueue_resid_sweep(mg, st);
     } else {
         enqueue_normb_df(mg, st);
+        enqueue_extrapolate(mg, st);
         enqueue_resid_df(mg, st);
     }
     const unsigned nctl = mg->bat.tab ? NYLES_MAX_BATCH : 1;   // one thread per run
@@ -2324,8 +2415,14 @@ int mg_read_device_stats(MgImpl* mg, cudaStream_t st, MgDeviceStats* out) {
     return NYLES_OK;
 }
 
+int mg_reset_history(MgImpl* mg) {
+    if (!mg->nhist || !mg->ws) return NYLES_OK;
+    return cuda_status(cudaMemset(mg->ws + mg->off_hist, 0, mg->nsol * sizeof(int)), "multigrid history reset");
+}
+
 int mg_zero_scalars(MgImpl* mg) {
     cudaError_t e = cudaMemset(scalars(mg), 0, 16 * sizeof(double));
+    if (e == cudaSuccess && mg->nhist) e = cudaMemset(mg->ws + mg->off_hist, 0, mg->nsol * sizeof(int));
     return cuda_status(e, "multigrid scalars reset");
 }
 

@@ -157,6 +157,8 @@ struct NylesModel {
     Geom g;
     int scheme = NYLES_SCHEME_RK3_SSP;
     int precision = NYLES_FP64;
+    int topo = NYLES_MG_CLOSED;
+    int nstage = 3;                      // projections per time step (RK3: 3, LFAM3: 2, EF: 1)
     int nprog = 4;
     bool lf_first = true;
     void* fields[NYLES_F_T0 + NYLES_MAX_TR] = {};
@@ -330,6 +332,22 @@ int nyles_mg_solve(NylesMg* mg, NylesMgStats* stats, void* stream) {
 }
 
 // ------------------------------------------------------------------ model
+// Workspace layout: the multigrid (its level arrays; `nsol` float-pair solutions with
+// `nhist` earlier solutions each in mixed precision), then partial sums and scalars.
+// The warm start of nyles_model_set_mg_warm_start sets nsol and nhist before binding.
+static int model_layout(NylesModel* m, int nsol, int nhist) {
+    const NylesDesc* d = &m->d;
+    int rc = mg_init(&m->mg, d->nx, d->ny, d->nz, m->topo, m->precision, nsol, nhist);
+    if (rc) return rc;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
+    m->mg_off = take(m->mg.bytes);
+    m->off_partial = take(m->npartial * sizeof(double));
+    m->off_scalar = take(16 * sizeof(double));
+    m->bytes = off;
+    return NYLES_OK;
+}
+
 int nyles_model_create(const NylesDesc* d, int scheme, int precision, NylesModel** out) {
     if (!out) { set_error("null output"); return NYLES_BAD_ARG; }
     *out = nullptr;
@@ -357,17 +375,10 @@ int nyles_model_create(const NylesDesc* d, int scheme, int precision, NylesModel
         set_error("z-periodic geometry needs x and y periodic (perio_xyz)");
         return NYLES_UNSUPPORTED;
     }
-    // mixed precision: one float-pair solution per projection of a step (RK3: 3, LFAM3:
-    // 2, EF: 1), the per-stage warm starts of nyles_model_set_mg_warm_start
-    const int nstage = scheme == NYLES_SCHEME_RK3_SSP ? 3 : (scheme == NYLES_SCHEME_LFAM3 ? 2 : 1);
-    rc = mg_init(&m->mg, d->nx, d->ny, d->nz, topo, precision, precision == NYLES_MIXED ? nstage : 1);
+    m->topo = topo;
+    m->nstage = scheme == NYLES_SCHEME_RK3_SSP ? 3 : (scheme == NYLES_SCHEME_LFAM3 ? 2 : 1);
+    rc = model_layout(m, 1, 0);
     if (rc) { delete m; return rc; }
-    size_t off = 0;
-    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; };
-    m->mg_off = take(m->mg.bytes);
-    m->off_partial = take(m->npartial * sizeof(double));
-    m->off_scalar = take(16 * sizeof(double));
-    m->bytes = off;
     *out = m;
     return NYLES_OK;
 }
@@ -411,17 +422,28 @@ int nyles_model_set_mg_krylov(NylesModel* m, int on) {
     return set_krylov(&m->mg, on);
 }
 
-int nyles_model_set_mg_warm_start(NylesModel* m, int per_stage) {
+int nyles_model_set_mg_warm_start(NylesModel* m, int mode) {
     if (!m) { set_error("null model"); return NYLES_BAD_ARG; }
+    if (mode < 0 || mode > 4) { set_error("warm start mode must be 0..4"); return NYLES_BAD_ARG; }
     if (m->gexec) { set_error("release the captured graph before changing the warm start"); return NYLES_BAD_ARG; }
-    if (per_stage && m->precision != NYLES_MIXED) {
+    if (mode && m->precision != NYLES_MIXED) {
         set_error("per-stage warm starts are provided for the mixed-precision solve only (the FP64 solve keeps "
                   "the reference's warm start)");
         return NYLES_UNSUPPORTED;
     }
-    m->warm_per_stage = per_stage ? 1 : 0;
+    const int nsol = mode ? m->nstage : 1, nhist = mode >= 2 ? mode - 1 : 0;
+    if (!m->bound) {   // size the workspace for this warm start
+        int rc = model_layout(m, nsol, nhist);
+        if (rc) return rc;
+    } else if (nsol > m->mg.nsol || nhist > m->mg.nhist) {
+        set_error("the bound workspace holds the arrays of a smaller warm start: select this one before "
+                  "nyles_model_workspace_bytes and nyles_model_bind");
+        return NYLES_BAD_ARG;
+    }
+    m->warm_per_stage = mode ? 1 : 0;
+    m->mg.extrap = nhist;
     m->mg.cur_sol = 0;
-    return NYLES_OK;
+    return mg_reset_history(&m->mg);
 }
 
 int nyles_model_reset_scheme(NylesModel* m) {

@@ -390,6 +390,255 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY, RhsMinBlocks<T>::n) k_rhs_march
     }
 }
 
+// ---------------------------------------------------------------- right-hand side, 32-bit offsets
+// k_rhs_march<T, true, 1, false> (buoyancy advection, WENO vortex force, Bernoulli,
+// viscosity) for arrays of fewer than 2^31 cells: the same operations in the same order
+// (values equal up to where the compiler fuses multiply-adds), with fewer instructions
+// per cell:
+//  - 32-bit offsets; the six values around a face are loaded at offsets shared by every
+//    field read along that direction (x: constant offsets from one pointer; y and z:
+//    c + k sy and c + k sz formed once per cell);
+//  - the upwind side is chosen among the six loaded values, so every reconstruction is
+//    one weno5 on registers (no data-dependent addresses);
+//  - the advecting velocity averaged at the face behind the cell, (UU0 of vf_flux),
+//    comes from the neighbouring lane along x and from the previous cell of the column
+//    along z instead of two more loads;
+//  - within three cells of an array end, where flux1d_at takes a closure branch, the
+//    reconstruction falls back to flux1d_at.
+
+// u * weno5 of the five values upwind of the face between v[2] and v[3] (flux1d_at's
+// interior branch): v[0..4] for u > 0, v[5..1] otherwise
+template <typename T>
+__device__ __forceinline__ T weno5_upwind(T u, const T (&v)[6]) {
+    const bool pos = u > T(0);
+    const T qa = pos ? v[0] : v[5];
+    const T qb = pos ? v[1] : v[4];
+    const T qc = pos ? v[2] : v[3];
+    const T qd = pos ? v[3] : v[2];
+    const T qe = pos ? v[4] : v[1];
+    return u * weno5(qa, qb, qc, qd, qe);
+}
+
+// tracer flux at index i of a line through c with stride s (flux1d_at of tr_flux);
+// o[k] = c + (k - 3) s
+template <typename T>
+__device__ __forceinline__ T tr_flux32(const T* __restrict__ q, T u, int c, int i, int n, int s, bool fast,
+                                       const int (&o)[7]) {
+    if (fast) {
+        T v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __ldg(q + o[k + 1]);
+        return weno5_upwind(u, v);
+    }
+    const int base = c - i * s;
+    auto Q = [&](int kk) -> T { return __ldg(q + base + kk * s); };
+    return flux1d_at(i, n, u, Q);
+}
+// the same along x (stride 1: constant offsets)
+template <typename T>
+__device__ __forceinline__ T tr_flux32x(const T* __restrict__ q, T u, int c, int i, int n, bool fast) {
+    if (fast) {
+        T v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __ldg(q + c + (k - 2));
+        return weno5_upwind(u, v);
+    }
+    const int base = c - i;
+    auto Q = [&](int kk) -> T { return __ldg(q + base + kk); };
+    return flux1d_at(i, n, u, Q);
+}
+
+// vortex-force reconstruction of vf_flux given u1: q(kk) = W(kk - 1), q(0) = 0
+template <typename T>
+__device__ __forceinline__ T vf_flux32(const T* __restrict__ W, T u1, int c, int i, int n, int s, bool fast,
+                                       const int (&o)[7]) {
+    if (fast) {
+        T v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __ldg(W + o[k]);
+        return weno5_upwind(u1, v);
+    }
+    const int base = c - i * s;
+    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(W + base + (kk - 1) * s); };
+    return flux1d_at(i, n, u1, Q);
+}
+template <typename T>
+__device__ __forceinline__ T vf_flux32x(const T* __restrict__ W, T u1, int c, int i, int n, bool fast) {
+    if (fast) {
+        T v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = __ldg(W + c + (k - 3));
+        return weno5_upwind(u1, v);
+    }
+    const int base = c - i;
+    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(W + base + (kk - 1)); };
+    return flux1d_at(i, n, u1, Q);
+}
+
+// blocks per SM asked of the register allocator: the six-value loads keep more values in
+// flight than k_rhs_march (64 registers in FP32 and 80 in FP64 hold them without spills)
+template <typename T> struct LesMinBlocks { static constexpr int n = 4; };
+template <> struct LesMinBlocks<double> { static constexpr int n = 3; };
+
+template <typename T, bool BAT>
+__global__ void __launch_bounds__(RZ_BX * RZ_BY, LesMinBlocks<T>::n) k_rhs_les(const RhsArgs<T> a0,
+                                                                             const Bat bat = Bat()) {
+    __shared__ T sfy[RZ_BY][RZ_BX];
+    int bz = blockIdx.z;
+    RhsArgs<T> a = a0;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        shift_rhs_args(a, dlt);
+    }
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = a.lo[2] + blockIdx.x * RZ_BX + tx;
+    const int y = a.lo[1] + blockIdx.y * RZ_BY + ty;
+    const int z0 = a.lo[0] + bz * RZ_ZC;
+    const int z1 = min(z0 + RZ_ZC, a.hi[0]) - 1;
+    const int Nz = a.g.N[0], Ny = a.g.N[1], Nx = a.g.N[2];
+    const int sy = (int)a.g.sy, sz = (int)a.g.sz;
+    const bool valid = x < a.hi[2] && y < a.hi[1];
+    const int xs = min(x, a.hi[2] - 1), ys = min(y, a.hi[1] - 1);   // idle lanes shadow a real cell
+    const T* __restrict__ b = a.b;
+    const T* __restrict__ U0 = a.U[0];
+    const T* __restrict__ U1 = a.U[1];
+    const T* __restrict__ U2 = a.U[2];
+    const T* __restrict__ W0 = a.W[0];
+    const T* __restrict__ W1 = a.W[1];
+    const T* __restrict__ W2 = a.W[2];
+    const T* __restrict__ ke = a.ke;
+    // interior reconstructions: tracer 2 <= i <= n - 4, vortex force 3 <= i <= n - 4
+    const bool xt = xs >= 2 && xs <= Nx - 4, xv = xs >= 3 && xs <= Nx - 4;
+    const bool yt = ys >= 2 && ys <= Ny - 4, yv = ys >= 3 && ys <= Ny - 4;
+    const bool ylo = ys < Ny - 1, xlo = xs < Nx - 1;
+    const int cxy = ys * sy + xs;
+    // carried up the column: the tracer flux through the face below the cell and the
+    // two z-fluxes' velocities averaged at that face
+    T fz_prev = T(0), uu_zy = T(0), uu_zx = T(0);
+    if (z0 > 0) {
+        const int c = (z0 - 1) * sz + cxy;
+        int oz[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) oz[k] = c + (k - 3) * sz;
+        const int zm = z0 - 1;
+        fz_prev = tr_flux32(b, __ldg(U2 + c), c, zm, Nz, sz, zm >= 2 && zm <= Nz - 4, oz);
+        if (ylo) uu_zy = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + sy));
+        if (xlo) uu_zx = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + 1));
+    }
+    for (int z = z0; z <= z1; ++z) {
+        const int c = z * sz + cxy;
+        const bool zt = z >= 2 && z <= Nz - 4, zv = z >= 3 && z <= Nz - 4;
+        const bool zlo = z < Nz - 1;
+        // The fluxes are formed direction by direction (z, y, x: one set of offsets
+        // live at a time) and summed afterwards in the order of TracerMarch::step and
+        // vortex_force_cell.
+        T fz, f4 = T(0), f5 = T(0);
+        {
+            int oz[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) oz[k] = c + (k - 3) * sz;
+            fz = tr_flux32(b, __ldg(U2 + c), c, z, Nz, sz, zt, oz);
+            if (ylo) {   // u_j += U^k w_i along k (U^k averaged along j)
+                const T uu1 = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + sy));
+                const T uu0 = z > 0 ? uu_zy : T(0);
+                uu_zy = uu1;
+                f4 = vf_flux32(W0, T(0.5) * (uu0 + uu1), c, z, Nz, sz, zv, oz);
+            }
+            if (xlo) {   // u_i -= U^k w_j along k (U^k averaged along i)
+                const T uu1 = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + 1));
+                const T uu0 = z > 0 ? uu_zx : T(0);
+                uu_zx = uu1;
+                f5 = vf_flux32(W1, T(0.5) * (uu0 + uu1), c, z, Nz, sz, zv, oz);
+            }
+        }
+        T fy, fym, f2 = T(0), f3 = T(0);
+        {
+            int oy[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) oy[k] = c + (k - 3) * sy;
+            fy = tr_flux32(b, __ldg(U1 + c), c, ys, Ny, sy, yt, oy);
+            sfy[ty][tx] = fy;
+            __syncthreads();
+            fym = (ty > 0) ? sfy[ty - 1][tx] : T(0);
+            __syncthreads();
+            if (xlo) {   // u_i += U^j w_k along j (U^j averaged along i)
+                const T uu1 = T(0.5) * (__ldg(U1 + c) + __ldg(U1 + c + 1));
+                const T uu0 = ys > 0 ? T(0.5) * (__ldg(U1 + c - sy) + __ldg(U1 + c - sy + 1)) : T(0);
+                f2 = vf_flux32(W2, T(0.5) * (uu0 + uu1), c, ys, Ny, sy, yv, oy);
+            }
+            if (zlo) {   // u_k -= U^j w_i along j (U^j averaged along k)
+                const T uu1 = T(0.5) * (__ldg(U1 + c) + __ldg(U1 + c + sz));
+                const T uu0 = ys > 0 ? T(0.5) * (__ldg(U1 + c - sy) + __ldg(U1 + c - sy + sz)) : T(0);
+                f3 = vf_flux32(W0, T(0.5) * (uu0 + uu1), c, ys, Ny, sy, yv, oy);
+            }
+        }
+        if (ty == 0 && ys > 0) {   // the face below the block's first row
+            const int cm = c - sy;
+            int om[7];
+#pragma unroll
+            for (int k = 0; k < 7; ++k) om[k] = cm + (k - 3) * sy;
+            fym = tr_flux32(b, __ldg(U1 + cm), cm, ys - 1, Ny, sy, ys - 1 >= 2 && ys - 1 <= Ny - 4, om);
+        }
+        T fx, fxm, f1 = T(0), f6 = T(0);
+        {
+            fx = tr_flux32x(b, __ldg(U0 + c), c, xs, Nx, xt);
+            fxm = __shfl_up_sync(0xffffffffu, fx, 1);
+            if (tx == 0 && xs > 0) fxm = tr_flux32x(b, __ldg(U0 + c - 1), c - 1, xs - 1, Nx,
+                                                     xs - 1 >= 2 && xs - 1 <= Nx - 4);
+            if (ylo) {   // u_j -= U^i w_k along i (U^i averaged along j)
+                const T uu1 = T(0.5) * (__ldg(U0 + c) + __ldg(U0 + c + sy));
+                T uu0 = __shfl_up_sync(0xffffffffu, uu1, 1);
+                if (tx == 0) uu0 = xs > 0 ? T(0.5) * (__ldg(U0 + c - 1) + __ldg(U0 + c - 1 + sy)) : T(0);
+                f1 = vf_flux32x(W2, T(0.5) * (uu0 + uu1), c, xs, Nx, xv);
+            }
+            if (zlo) {   // u_k += U^i w_j along i (U^i averaged along k)
+                const T uu1 = T(0.5) * (__ldg(U0 + c) + __ldg(U0 + c + sz));
+                T uu0 = __shfl_up_sync(0xffffffffu, uu1, 1);
+                if (tx == 0) uu0 = xs > 0 ? T(0.5) * (__ldg(U0 + c - 1) + __ldg(U0 + c - 1 + sz)) : T(0);
+                f6 = vf_flux32x(W1, T(0.5) * (uu0 + uu1), c, xs, Nx, xv);
+            }
+        }
+        // ---- buoyancy advection, summed as TracerMarch::step
+        T db = (xs > 0) ? (T(0) + fxm) - fx : T(0) - fx;
+        db = (ys > 0) ? (db + fym) - fy : db - fy;
+        db = (z > 0) ? (db + fz_prev) - fz : db - fz;
+        fz_prev = fz;
+        // ---- vortex force, summed in the order of vortex_force_cell
+        T dux = T(0), duy = T(0), duz = T(0);
+        if (ylo) duy = duy - f1;
+        if (xlo) dux = dux + f2;
+        if (zlo) duz = duz - f3;
+        if (ylo) duy = duy + f4;
+        if (xlo) dux = dux - f5;
+        if (zlo) duz = duz + f6;
+        // ---- Bernoulli (core/bernoulli.py:14-23)
+        if (xlo) dux = sub_rn(dux, sub_rn(__ldg(ke + c + 1), __ldg(ke + c)));
+        if (ylo) duy = sub_rn(duy, sub_rn(__ldg(ke + c + sy), __ldg(ke + c)));
+        if (zlo) {
+            duz = sub_rn(duz, sub_rn(__ldg(ke + c + sz), __ldg(ke + c)));
+            if (!a.euler) duz = add_rn(duz, mul_rn(a.half_dz, add_rn(__ldg(b + c + sz), __ldg(b + c))));
+        }
+        if (a.terms & TERM_VISC) {
+            const long long cl = c;
+            const int pos[3] = {z, ys, xs};
+            for (int pass = 0; pass < 3; ++pass) {
+                const int d = 2 - pass;
+                const T cf = a.vcoef[pass];
+                dux = dux + cf * lap1d(a.u[0], a.g, cl, pos[d], d);
+                duy = duy + cf * lap1d(a.u[1], a.g, cl, pos[d], d);
+                duz = duz + cf * lap1d(a.u[2], a.g, cl, pos[d], d);
+            }
+        }
+        if (valid) {
+            a.ds[0][c] = db;
+            a.ds[1][c] = dux;
+            a.ds[2][c] = duy;
+            a.ds[3][c] = duz;
+        }
+    }
+}
+
 // advection of one passive tracer (core/tracer.py:59-72) with the same flux sharing
 template <typename T, bool DIFF>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY) k_tracer_march(const Geom g, const T* __restrict__ Ux,
@@ -478,6 +727,26 @@ __global__ void __launch_bounds__(256) k_tracer_linear(const Geom g, const T* __
         if (diff) acc = acc + kc[d] * lap1d(q, g, c, i, d);
     }
     dq[c] = acc;
+}
+
+// k_rhs_les serves FP32 arrays of fewer than 2^31 cells (32-bit offsets, the largest
+// one c + 3 sz + sy + 1 below 2^31); NYLES_GB300_GENERIC_RHS=1 selects k_rhs_march
+// instead (the same operations; values equal to rounding). The FP64 right-hand side
+// keeps k_rhs_march: it is bound by the FP64 pipe, and k_rhs_les (80 registers, 3
+// blocks per SM) ran it in the same time.
+template <typename T, bool BAT>
+static void launch_rhs_les(dim3 grd, dim3 blk, cudaStream_t st, const RhsArgs<T>& a, const Bat& bat) {
+    if constexpr (sizeof(T) == sizeof(float)) k_rhs_les<T, BAT><<<grd, blk, 0, st>>>(a, bat);
+}
+
+template <typename T>
+static bool rhs32_ok(const Geom& g) {
+    if (sizeof(T) != sizeof(float)) return false;
+    static const bool generic = [] {
+        const char* e = getenv("NYLES_GB300_GENERIC_RHS");
+        return e && e[0] == '1';
+    }();
+    return !generic && g.vol + 4 * g.sz + g.sy + 1 < (1ll << 31);
 }
 
 bool make_geom(const NylesDesc* d, Geom* g) {
@@ -582,7 +851,8 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
             return NYLES_UNSUPPORTED;
         }
         const dim3 gb(grd_box.x, grd_box.y, grd_box.z * bat.nrun);
-        k_rhs_march<T, true, 1, false, true><<<gb, blk, 0, st>>>(a, bat);
+        if (rhs32_ok<T>(g)) launch_rhs_les<T, true>(gb, blk, st, a, bat);
+        else k_rhs_march<T, true, 1, false, true><<<gb, blk, 0, st>>>(a, bat);
         note_launch();
         return cuda_status(cudaGetLastError(), "rhs kernel");
     }
@@ -591,6 +861,7 @@ int launch_rhs(const NylesDesc* d, const Geom& g, const StencilPtrs<T>& s, const
         else if (tr) k_rhs_march<T, true, 2, false><<<grd_box, blk, 0, st>>>(a);
         else k_rhs_march<T, false, 2, false><<<grd_box, blk, 0, st>>>(a);
     } else if (tr && vf && bdiff) k_rhs_march<T, true, 1, true><<<grd_box, blk, 0, st>>>(a);
+    else if (tr && vf && rhs32_ok<T>(g)) launch_rhs_les<T, false>(grd_box, blk, st, a, Bat());
     else if (tr && vf) k_rhs_march<T, true, 1, false><<<grd_box, blk, 0, st>>>(a);
     else if (tr && bdiff) k_rhs_march<T, true, 0, true><<<grd_box, blk, 0, st>>>(a);
     else if (tr) k_rhs_march<T, true, 0, false><<<grd_box, blk, 0, st>>>(a);

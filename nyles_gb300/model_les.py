@@ -58,6 +58,41 @@ def make_desc(param, grid, modelname):
 # mixed precision, mg_krylov "auto": FCG at squared residual ratios at or below this
 # (relative residual 1e-8)
 KRYLOV_AUTO_TOL = 1e-16
+# mg_warm_start modes (nyles_model_set_mg_warm_start; each needs the arrays of the ones
+# before it and more) and the one "auto" takes with FCG
+WARM_STARTS = {"last": 0, "stage": 1, "extrapolate": 2, "extrapolate2": 3, "extrapolate3": 4, "auto": None}
+WARM_AUTO = "extrapolate2"
+
+
+def warm_start_mode(warm, precision, krylov_on):
+    """nyles_model_set_mg_warm_start mode of the gpu parameter mg_warm_start"""
+    if warm not in WARM_STARTS:
+        raise ValueError("mg_warm_start must be one of %s" % ", ".join(WARM_STARTS))
+    if warm not in ("auto", "last") and precision == "fp64":
+        raise ValueError("mg_warm_start = '%s' needs the mixed precision (the FP64 solve keeps the "
+                         "reference's warm start)" % warm)
+    if warm == "auto":
+        warm = WARM_AUTO if krylov_on else "last"
+    return WARM_STARTS[warm]
+
+
+def krylov_on(krylov, precision, tol):
+    """whether the mixed solve runs FCG for the gpu parameter mg_krylov at tolerance tol"""
+    if krylov not in ("auto", "on", "off"):
+        raise ValueError("mg_krylov must be 'auto', 'on' or 'off'")
+    if precision == "fp64":
+        if krylov == "on":
+            raise ValueError("mg_krylov = 'on' needs the mixed precision (the FP64 solve keeps the reference's "
+                             "iteration)")
+        return False
+    return krylov == "on" or (krylov == "auto" and float(tol) <= KRYLOV_AUTO_TOL)
+
+
+def creation_warm_mode(gpu, precision):
+    """warm start mode whose arrays a new model's workspace holds: the one its
+    parameters select"""
+    return warm_start_mode(gpu.get("mg_warm_start", "auto"), precision,
+                           krylov_on(gpu.get("mg_krylov", "auto"), precision, gpu.get("mg_tol", 1e-6)))
 
 
 class LES(object):
@@ -102,6 +137,9 @@ class LES(object):
         nat.check(self.lib.nyles_model_create(ctypes.byref(self.desc), nat.SCHEME[param["timestepping"]],
                                               nat.PRECISION[self.precision], ctypes.byref(h)))
         self._h = h
+        # the workspace holds the arrays of the warm start the parameters select
+        self._warm_alloc = creation_warm_mode(gpu, self.precision)
+        nat.check(self.lib.nyles_model_set_mg_warm_start(h, self._warm_alloc))
         nbytes = ctypes.c_size_t()
         nat.check(self.lib.nyles_model_workspace_bytes(h, ctypes.byref(nbytes)))
         if arena is not None:
@@ -183,11 +221,13 @@ class LES(object):
         iteration; "auto" takes FCG when tol <= KRYLOV_AUTO_TOL, where both solvers land
         within the tolerance of the exact solution (at looser tolerances the stationary
         iterates are the ones that track the FP64 solve). `warm_start` ("auto", "stage",
-        "last"; None keeps the current mode) picks the start of each solve: the previous
-        solve's solution (the reference's), or, mixed precision only, the solution of the
-        same stage one step earlier; "auto" takes "stage" exactly when FCG runs, for the
-        same reason. A captured graph holds the solver and its parameters, so it is
-        released first."""
+        "extrapolate", "last"; None keeps the current mode) picks the start of each
+        solve: the previous solve's solution (the reference's), or, mixed precision only,
+        the solution of the same stage one step earlier, or its linear extrapolation from
+        the same stage's last two (three, four: "extrapolate2", "extrapolate3")
+        solutions; "auto" takes WARM_AUTO exactly when FCG runs, for the same reason, and
+        no more than the workspace holds (the mode the model was created with). A
+        captured graph holds the solver and its parameters, so it is released first."""
         if getattr(self, "graph", None) is not None:
             self.release_graph()
         if krylov is not None:
@@ -196,26 +236,22 @@ class LES(object):
             self.mg_krylov = krylov
         mode = getattr(self, "mg_krylov", "auto")
         nat.check(self.lib.nyles_model_set_mg_params(self._h, float(tol), int(maxite), float(omega)))
-        if self.precision == "fp64":
-            if mode == "on":
-                raise ValueError("mg_krylov = 'on' needs the mixed precision (the FP64 solve keeps the reference's "
-                                 "iteration)")
-            use = False
-        else:
-            use = mode == "on" or (mode == "auto" and float(tol) <= KRYLOV_AUTO_TOL)
+        use = krylov_on(mode, self.precision, tol)
         nat.check(self.lib.nyles_model_set_mg_krylov(self._h, 1 if use else 0))
         self.krylov = use
         if warm_start is not None:
-            if warm_start not in ("auto", "stage", "last"):
-                raise ValueError("mg_warm_start must be 'auto', 'stage' or 'last'")
+            warm_start_mode(warm_start, self.precision, use)      # validates
             self.mg_warm_start = warm_start
-        wmode = getattr(self, "mg_warm_start", "auto")
-        if wmode == "stage" and self.precision == "fp64":
-            raise ValueError("mg_warm_start = 'stage' needs the mixed precision (the FP64 solve keeps the "
-                             "reference's warm start)")
-        per_stage = wmode == "stage" or (wmode == "auto" and use)
-        nat.check(self.lib.nyles_model_set_mg_warm_start(self._h, 1 if per_stage else 0))
-        self.warm_per_stage = per_stage
+        wanted = getattr(self, "mg_warm_start", "auto")
+        code = warm_start_mode(wanted, self.precision, use)
+        if wanted == "auto":
+            code = min(code, self._warm_alloc)
+        elif code > self._warm_alloc:
+            raise ValueError("mg_warm_start = '%s' needs arrays this model's workspace does not hold: pass it in "
+                             "the parameters the model is created with" % wanted)
+        nat.check(self.lib.nyles_model_set_mg_warm_start(self._h, code))
+        self.warm_mode = next(k for k, v in WARM_STARTS.items() if v == code)
+        self.warm_per_stage = code > 0
 
     def mg_stats(self):
         s = nat.NylesMgStats()

@@ -65,6 +65,7 @@ def arena_bytes(user_param):
     nat.check(nat.lib().nyles_model_create(ctypes.byref(desc), nat.SCHEME[param["timestepping"]],
                                            nat.PRECISION[prec], ctypes.byref(h)))
     try:
+        nat.check(nat.lib().nyles_model_set_mg_warm_start(h, model_les.creation_warm_mode(param["gpu"], prec)))
         nb = ctypes.c_size_t()
         nat.check(nat.lib().nyles_model_workspace_bytes(h, ctypes.byref(nb)))
     finally:

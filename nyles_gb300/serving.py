@@ -139,12 +139,13 @@ def initial_state(nyl, case, seed):
         st.get(name).view("i")[...] = torch.from_numpy(arr)
 
 
-def footprint_bytes(case, n, precision="mixed"):
+def footprint_bytes(case, n, precision="mixed", mg_tol=1e-6):
     """Device bytes of one run: 14 state fields, 3 x 4 time-scheme registers, and the
     multigrid workspace (x, b, y per level; in mixed precision also the float-pair
-    solutions of level 1, one per RK3 stage, its float-pair rhs and the two float
-    vectors of the Krylov solver), plus 3% and 256 KiB for partial sums, scalars and
-    allocator rounding."""
+    solution of level 1, or at Krylov tolerances one per RK3 stage and two before each
+    for the extrapolated warm start, its float-pair rhs and the two float vectors
+    of the Krylov solver), plus 3% and 256 KiB for partial sums, scalars and allocator
+    rounding."""
     per = CASES[case]["geometry"]
     e = 8 if precision == "fp64" else 4
     dims = [n + (6 if ax in per else 0) for ax in ("z", "y", "x")]
@@ -158,7 +159,9 @@ def footprint_bytes(case, n, precision="mixed"):
         x //= 2
         z //= 2
     if precision == "mixed":
-        mg += (3 + 1) * 8 * n ** 3 + 2 * 4 * n ** 3
+        from .model_les import KRYLOV_AUTO_TOL
+        pairs = 3 * 3 if mg_tol <= KRYLOV_AUTO_TOL else 1
+        mg += (pairs + 1) * 8 * n ** 3 + 2 * 4 * n ** 3
     return int(1.03 * (fields + mg)) + (1 << 18)
 
 
@@ -497,13 +500,13 @@ class ServingEngine:
             nxt += 1
         if pool is not None:
             for req in queue[:self.prep_ahead]:
-                if req.rid not in staging and footprint_bytes(req.case, req.n, self.precision) <= self.budget:
+                if req.rid not in staging and footprint_bytes(req.case, req.n, self.precision, self.mg_tol) <= self.budget:
                     staging[req.rid] = pool.submit(stage_initial_state, req, dtype, case_grid(req.case, req.n))
         # admission, in arrival order; a request whose bucket is full, or whose
         # initial state is still being built, waits without blocking the others
         waiting = []
         for req in queue:
-            need = footprint_bytes(req.case, req.n, self.precision)
+            need = footprint_bytes(req.case, req.n, self.precision, self.mg_tol)
             if need > self.budget:
                 results.append(Result(req.rid, req.case, req.n, req.steps, req.arrival if realtime else 0.0,
                                       now, now, req.n ** 3, 0, "refused"))

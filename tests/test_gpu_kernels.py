@@ -216,3 +216,63 @@ def test_fill_matches_oracle():
     torch.cuda.synchronize()
     o.fill("ke")
     np.testing.assert_array_equal(m.state.ke.view("i").cpu().numpy(), o.field("ke"))
+
+
+_RHS_CODE = (
+    "import sys, numpy as np, torch\n"
+    "sys.path.insert(0, 'tests')\n"
+    "import helpers\n"
+    "from nyles_gb300.nyles import Nyles\n"
+    "out = []\n"
+    "cases = [dict(geometry='closed', n=(16, 8, 12)), dict(geometry='perio_xy', n=(48, 24, 32)),\n"
+    "         dict(geometry='perio_xyz', n=(8, 8, 8)), dict(geometry='perio_x', n=(48, 8, 8)),\n"
+    "         dict(geometry='closed', n=(64, 16, 16), modelname='Euler3d'),\n"
+    "         dict(geometry='closed', n=(8, 8, 8), diff_coef={'u': 2e-3})]\n"
+    "for prec in ('fp64', 'mixed'):\n"
+    "    for k, cfg in enumerate(cases):\n"
+    "        nyl = Nyles(helpers.make_params(precision=prec, **cfg))\n"
+    "        m = nyl.model\n"
+    "        rng = np.random.Generator(np.random.PCG64(70 + k))\n"
+    "        for s in m.state.scalars():\n"
+    "            a = rng.standard_normal(tuple(s.data.shape))\n"
+    "            s.data.copy_(torch.from_numpy(a))\n"
+    "        for last in (False, True):\n"
+    "            ds = m.timescheme.registers[1]\n"
+    "            ds.storage.fill_(123.0)\n"
+    "            m.rhs(m.state, 0.0, ds, last=last)\n"
+    "            torch.cuda.synchronize()\n"
+    "            out += [ds.get(q).view('i').double().cpu().numpy() for q in ('b', 'u_i', 'u_j', 'u_k')]\n"
+    "np.savez(sys.argv[1], *out)\n")
+
+
+def _rhs_outputs(tmp_path, tag, **env_extra):
+    """right-hand sides of seeded random states (every field drawn) on closed and
+    periodic grids, FP64 and FP32, in a fresh process with the given environment"""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(helpers.HERE)
+    env = dict(os.environ, PYTHONPATH=root, **env_extra)
+    fn = str(tmp_path / ("rhs_%s.npz" % tag))
+    r = subprocess.run([sys.executable, "-c", _RHS_CODE, fn], env=env, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    with np.load(fn) as f:
+        return [f["arr_%d" % i] for i in range(len(f.files))]
+
+
+def test_rhs_32bit_offsets_kernel_matches_generic_kernel(tmp_path):
+    """k_rhs_les (32-bit offsets, six-value loads, neighbour-shared velocity averages)
+    against k_rhs_march (NYLES_GB300_GENERIC_RHS=1): the same operations in the same
+    order, near array ends (closure branches) and in the interior. The compiler fuses
+    multiply-adds differently in the two kernels, so values agree to rounding: 1e-5 of
+    the max-norm in FP32. The FP64 right-hand side runs k_rhs_march either way (the
+    FP64 cases must agree bit for bit)."""
+    new = _rhs_outputs(tmp_path, "les")
+    old = _rhs_outputs(tmp_path, "generic", NYLES_GB300_GENERIC_RHS="1")
+    assert len(new) == len(old) == 2 * 6 * 2 * 4
+    half = len(new) // 2          # FP64 cases first, then mixed
+    for k, (a, b) in enumerate(zip(new, old)):
+        if k < half:
+            np.testing.assert_array_equal(a, b, err_msg=str(k))
+        else:
+            assert helpers.relerr(a, b) < 1e-5, k

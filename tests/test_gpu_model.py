@@ -307,23 +307,24 @@ def test_mixed_krylov_graph_matches_eager():
 
 
 @pytest.mark.parametrize("scheme", ["RK3_SSP", "LFAM3"])
-def test_mixed_per_stage_warm_start(scheme):
-    """Each stage's solve warm-started from the same stage one step earlier: the state
-    stays within the mixed bar of the FP64 run and of the reference's warm start, in
-    fewer V-cycles; graph replay equals eager stepping bit for bit; the FP64 model
-    refuses the mode."""
+@pytest.mark.parametrize("warm", ["stage", "extrapolate", "extrapolate3"])
+def test_mixed_per_stage_warm_start(scheme, warm):
+    """Each stage's solve warm-started from the same stage one step earlier (or from the
+    extrapolation of its last two solutions): the state stays within the mixed bar of
+    the FP64 run and of the reference's warm start, in fewer V-cycles; graph replay
+    equals eager stepping bit for bit; the FP64 model refuses the mode."""
     from nyles_gb300 import _native as nat
     from nyles_gb300.nyles import Nyles
     runs = {}
-    for tag, prec, warm, graphs in (("fp64", "fp64", "last", False), ("last", "mixed", "last", False),
-                                    ("stage", "mixed", "stage", False), ("stage_graph", "mixed", "stage", True)):
+    for tag, prec, wm, graphs in (("fp64", "fp64", "last", False), ("last", "mixed", "last", False),
+                                  ("warm", "mixed", warm, False), ("warm_graph", "mixed", warm, True)):
         p = helpers.make_params(geometry="perio_xy", n=(32, 32, 32), dt=1e-3, precision=prec, mg_tol=1e-20,
                                 mg_maxite=40, timestepping=scheme)
         p.gpu["graphs"] = graphs
-        p.gpu["mg_warm_start"] = warm
+        p.gpu["mg_warm_start"] = wm
         nyl = Nyles(p)
         m = nyl.model
-        assert m.warm_per_stage == (warm == "stage")
+        assert m.warm_per_stage == (wm != "last") and m.warm_mode == wm
         for k, v in helpers.seeded_state(nyl, "noise", 9).items():
             m.state.get(k).view("i")[...] = torch.from_numpy(v)
         m.diagnose_var(m.state)
@@ -334,18 +335,43 @@ def test_mixed_per_stage_warm_start(scheme):
         runs[tag] = ({s: m.state.get(s).view("i").double().cpu().numpy() for s in ("b", "u_i", "u_j", "u_k")},
                      m.mg_stats()["vcycles"] - v0)
     for s in runs["fp64"][0]:
-        assert helpers.relerr(runs["stage"][0][s], runs["fp64"][0][s]) < 1e-5, s
-        assert helpers.relerr(runs["stage"][0][s], runs["last"][0][s]) < 1e-5, s
-        np.testing.assert_array_equal(runs["stage_graph"][0][s], runs["stage"][0][s])
-    assert runs["stage"][1] < runs["last"][1], (runs["stage"][1], runs["last"][1])
-    assert runs["stage_graph"][1] == runs["stage"][1]
+        assert helpers.relerr(runs["warm"][0][s], runs["fp64"][0][s]) < 1e-5, s
+        assert helpers.relerr(runs["warm"][0][s], runs["last"][0][s]) < 1e-5, s
+        np.testing.assert_array_equal(runs["warm_graph"][0][s], runs["warm"][0][s])
+    assert runs["warm"][1] < runs["last"][1], (runs["warm"][1], runs["last"][1])
+    assert runs["warm_graph"][1] == runs["warm"][1]
     p = helpers.make_params(geometry="perio_xy", n=(16, 16, 16), precision="fp64")
-    p.gpu["mg_warm_start"] = "stage"
+    p.gpu["mg_warm_start"] = warm
     with pytest.raises(ValueError):
         Nyles(p)
     nyl = Nyles(helpers.make_params(geometry="perio_xy", n=(16, 16, 16), precision="fp64"))
     assert nat.lib().nyles_model_set_mg_warm_start(nyl.model._h, 1) == nat.NYLES_UNSUPPORTED
+    assert nat.lib().nyles_model_set_mg_warm_start(nyl.model._h, 5) == nat.NYLES_BAD_ARG
 
+
+def test_warm_start_arrays_are_sized_at_creation():
+    """The workspace holds the solution arrays of the warm start the parameters select:
+    one float pair for the reference's start (a loose tolerance), 3 x 4 for the
+    extrapolated one; a bound model refuses a warm start whose arrays it does not hold
+    (the C ABI: NYLES_BAD_ARG; Python: ValueError), and "auto" stays within them."""
+    from nyles_gb300 import _native as nat
+    from nyles_gb300.nyles import Nyles, arena_bytes
+    loose = helpers.make_params(geometry="perio_xy", n=(32, 32, 32), precision="mixed", mg_tol=1e-6)
+    tight = helpers.make_params(geometry="perio_xy", n=(32, 32, 32), precision="mixed", mg_tol=1e-20)
+    assert arena_bytes(tight) - arena_bytes(loose) >= 8 * 8 * 32 ** 3
+    nyl = Nyles(loose)
+    m = nyl.model
+    assert m.warm_mode == "last" and not m.krylov
+    assert nat.lib().nyles_model_set_mg_warm_start(m._h, 2) == nat.NYLES_BAD_ARG
+    assert b"workspace" in nat.lib().nyles_last_error()
+    with pytest.raises(ValueError):
+        m.set_mg_params(1e-20, 40, 0.9, warm_start="extrapolate")
+    m.set_mg_params(1e-20, 40, 0.9, warm_start="auto")
+    assert m.krylov and m.warm_mode == "last"
+    nyl = Nyles(tight)
+    assert nyl.model.warm_mode == "extrapolate2"
+    nyl.model.set_mg_params(1e-20, 40, 0.9, warm_start="stage")
+    assert nyl.model.warm_mode == "stage"
 
 _SOLVES_CODE = (
     "import numpy as np, sys\n"

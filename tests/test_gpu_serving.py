@@ -79,12 +79,13 @@ def test_footprint_model_covers_the_allocation(case, n, precision):
 def test_batched_launches_are_fewer_than_per_run_launches():
     """A bucket of 6 runs of 32^3 is projected with one launch and advances with one
     launch per 10 steps: the library's kernel count for the ensemble is about one run's,
-    not six."""
+    not six. (Initial states built inline, so that all six are admitted in the first
+    pass of the loop; with host threads they join as their states are ready.)"""
     from nyles_gb300 import _native as nat
     from nyles_gb300 import serving as S
     reqs = [S.Request(i, "tgv", 32, 20 + i, 30, 0.0) for i in range(6)]
     l0 = nat.lib().nyles_launch_count()
-    eng = S.ServingEngine(precision="mixed")
+    eng = S.ServingEngine(precision="mixed", prep_threads=0)
     results, _ = eng.serve(reqs, realtime=False)
     batched = nat.lib().nyles_launch_count() - l0
     assert eng.launches == 4 and all(r.status == "ok" for r in results)   # one projection, 3 x 10 steps

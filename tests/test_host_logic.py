@@ -99,3 +99,28 @@ def test_grid_coordinates():
     assert xb[0, 0, 0] == 0.125 and xb.shape == (2, 4, 8)
     assert g.x_vel["i"].view("i").numpy()[0, 0, -1] == 2.0     # east wall face
     assert g.z_vor["k"].view("i").numpy()[1, 0, 0] == pytest.approx(0.375)
+
+
+def test_gpu_parameter_choices_cover_the_model_modes():
+    """Every mg_warm_start and mg_krylov value the model understands passes the
+    parameter check, and the warm start the parameters select at creation follows
+    the tolerance (the Krylov solve's extrapolated start, else the reference's)."""
+    from nyles_gb300 import model_les as M
+    for warm in M.WARM_STARTS:
+        P.InextensibleDict.unfreeze()
+        p = P.UserParameters()
+        p.gpu["precision"] = "mixed"
+        p.gpu["mg_warm_start"] = warm
+        p.check()
+    for kry in ("auto", "on", "off"):
+        P.InextensibleDict.unfreeze()
+        p = P.UserParameters()
+        p.gpu["mg_krylov"] = kry
+        p.check()
+    P.InextensibleDict.unfreeze()
+    assert M.creation_warm_mode({"mg_tol": 1e-20}, "mixed") == M.WARM_STARTS[M.WARM_AUTO]
+    assert M.creation_warm_mode({"mg_tol": 1e-6}, "mixed") == 0
+    assert M.creation_warm_mode({"mg_tol": 1e-20}, "fp64") == 0
+    assert M.creation_warm_mode({"mg_tol": 1e-6, "mg_warm_start": "stage"}, "mixed") == 1
+    with pytest.raises(ValueError):
+        M.creation_warm_mode({"mg_warm_start": "stage"}, "fp64")
