@@ -1590,8 +1590,10 @@ __global__ void __launch_bounds__(256) k_fcg_xupdate(float2* __restrict__ xdf, c
 // MG_HIST history arrays holding x(n-2), x(n-3), ... With `order` p and at least p + 1
 // solves seen (else the highest order they allow), the start becomes the polynomial
 // extrapolation of the last p + 1 solutions to the next step (equal steps; binomial
-// coefficients: 2, -1; 3, -3, 1; 4, -6, 4, -1), formed in double and split into a float
-// pair. The history then shifts by one. Nothing changes when the right-hand side's
+// coefficients: 2, -1; 3, -3, 1; 4, -6, 4, -1), formed in float-pair arithmetic (FP64
+// here ran the kernel at a fifth of the copy bandwidth: GB300's FP64 pipe, which also
+// does the float-double conversions, is a small fraction of its FP32 rate). The
+// history then shifts by one. Nothing changes when the right-hand side's
 // norm (scalar slot SC_NORMB, set just before) is zero or not finite: the solve then
 // keeps its start (a zero right-hand side) or stops at once (blow-up).
 // k_mg_hist_count, launched after, counts the solve.
@@ -1620,15 +1622,11 @@ __global__ void __launch_bounds__(256) k_mg_extrapolate(float2* __restrict__ cur
 #pragma unroll
     for (int k = 0; k < MG_HIST; ++k) v[k + 1] = (k < order) ? hp.h[k][i] : make_float2(0.f, 0.f);
     if (p >= 1) {
-        double x[MG_HIST + 1];
-#pragma unroll
-        for (int k = 0; k <= MG_HIST; ++k) x[k] = (double)v[k].x + (double)v[k].y;
-        double e;
-        if (p == 1) e = 2.0 * x[0] - x[1];
-        else if (p == 2) e = 3.0 * (x[0] - x[1]) + x[2];
-        else e = 4.0 * (x[0] + x[2]) - 6.0 * x[1] - x[3];
-        const float hi = __double2float_rn(e);
-        cur[i] = make_float2(hi, __double2float_rn(e - (double)hi));
+        float2 e;
+        if (p == 1) e = df_add(make_float2(2.f * v[0].x, 2.f * v[0].y), df_neg(v[1]));
+        else if (p == 2) e = df_add(df_mul_f(3.f, df_add(v[0], df_neg(v[1]))), v[2]);
+        else e = df_add(df_add(df_mul_f(4.f, df_add(v[0], v[2])), df_mul_f(-6.f, v[1])), df_neg(v[3]));
+        cur[i] = e;
     }
 #pragma unroll
     for (int k = MG_HIST - 1; k >= 0; --k)

@@ -419,6 +419,19 @@ __device__ __forceinline__ T weno5_upwind(T u, const T (&v)[6]) {
     return u * weno5(qa, qb, qc, qd, qe);
 }
 
+// flux1d_at near an array end, out of line: the closures are rare (walls), and inlined
+// at the nine reconstruction sites they would multiply the kernel's code size
+template <typename T>
+__device__ __noinline__ T tr_flux_closure(const T* __restrict__ q, T u, int base, int i, int n, int s) {
+    auto Q = [&](int kk) -> T { return __ldg(q + base + kk * s); };
+    return flux1d_at(i, n, u, Q);
+}
+template <typename T>
+__device__ __noinline__ T vf_flux_closure(const T* __restrict__ W, T u1, int base, int i, int n, int s) {
+    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(W + base + (kk - 1) * s); };
+    return flux1d_at(i, n, u1, Q);
+}
+
 // tracer flux at index i of a line through c with stride s (flux1d_at of tr_flux);
 // o[k] = c + (k - 3) s
 template <typename T>
@@ -430,9 +443,7 @@ __device__ __forceinline__ T tr_flux32(const T* __restrict__ q, T u, int c, int 
         for (int k = 0; k < 6; ++k) v[k] = __ldg(q + o[k + 1]);
         return weno5_upwind(u, v);
     }
-    const int base = c - i * s;
-    auto Q = [&](int kk) -> T { return __ldg(q + base + kk * s); };
-    return flux1d_at(i, n, u, Q);
+    return tr_flux_closure(q, u, c - i * s, i, n, s);
 }
 // the same along x (stride 1: constant offsets)
 template <typename T>
@@ -443,9 +454,7 @@ __device__ __forceinline__ T tr_flux32x(const T* __restrict__ q, T u, int c, int
         for (int k = 0; k < 6; ++k) v[k] = __ldg(q + c + (k - 2));
         return weno5_upwind(u, v);
     }
-    const int base = c - i;
-    auto Q = [&](int kk) -> T { return __ldg(q + base + kk); };
-    return flux1d_at(i, n, u, Q);
+    return tr_flux_closure(q, u, c - i, i, n, 1);
 }
 
 // vortex-force reconstruction of vf_flux given u1: q(kk) = W(kk - 1), q(0) = 0
@@ -458,9 +467,7 @@ __device__ __forceinline__ T vf_flux32(const T* __restrict__ W, T u1, int c, int
         for (int k = 0; k < 6; ++k) v[k] = __ldg(W + o[k]);
         return weno5_upwind(u1, v);
     }
-    const int base = c - i * s;
-    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(W + base + (kk - 1) * s); };
-    return flux1d_at(i, n, u1, Q);
+    return vf_flux_closure(W, u1, c - i * s, i, n, s);
 }
 template <typename T>
 __device__ __forceinline__ T vf_flux32x(const T* __restrict__ W, T u1, int c, int i, int n, bool fast) {
@@ -470,15 +477,12 @@ __device__ __forceinline__ T vf_flux32x(const T* __restrict__ W, T u1, int c, in
         for (int k = 0; k < 6; ++k) v[k] = __ldg(W + c + (k - 3));
         return weno5_upwind(u1, v);
     }
-    const int base = c - i;
-    auto Q = [&](int kk) -> T { return kk == 0 ? T(0) : __ldg(W + base + (kk - 1)); };
-    return flux1d_at(i, n, u1, Q);
+    return vf_flux_closure(W, u1, c - i, i, n, 1);
 }
 
-// blocks per SM asked of the register allocator: the six-value loads keep more values in
-// flight than k_rhs_march (64 registers in FP32 and 80 in FP64 hold them without spills)
-template <typename T> struct LesMinBlocks { static constexpr int n = 4; };
-template <> struct LesMinBlocks<double> { static constexpr int n = 3; };
+// blocks per SM asked of the register allocator: 48 registers hold the kernel without
+// spills once the closure branches are out of line (inlined, they took it to 64)
+template <typename T> struct LesMinBlocks { static constexpr int n = 5; };
 
 template <typename T, bool BAT>
 __global__ void __launch_bounds__(RZ_BX * RZ_BY, LesMinBlocks<T>::n) k_rhs_les(const RhsArgs<T> a0,
@@ -896,78 +900,55 @@ struct UpdArgs {
     long long vol;
     int nprog;
     int kind;
-    double dt;
+    T k1, k2;         // the stage's coefficients, rounded to T on the host (see launch_update)
     T* s[NYLES_MAX_PROG];
     T* a[NYLES_MAX_PROG];
     T* b[NYLES_MAX_PROG];
     T* c[NYLES_MAX_PROG];
 };
 
-// numpy's evaluation order of core/timescheme.py:113-221, one rounding per operation
-template <typename T>
-__global__ void k_update(const UpdArgs<T> p0, const Bat bat = Bat()) {
+// numpy's evaluation order of core/timescheme.py:113-221, one rounding per operation;
+// one prognostic field after the other, a grid-stride loop over its cells
+template <typename T, int KIND>
+__device__ __forceinline__ void update_field(T* __restrict__ s, const T* __restrict__ a, T* __restrict__ b,
+                                             T* __restrict__ c, long long vol, T k1, T k2) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < vol; i += stride) {
+        if (KIND == UPD_EULER) {   // s += dt*ds
+            s[i] = add_rn(s[i], mul_rn(k1, a[i]));
+        } else if (KIND == UPD_RK3_2) {   // s += (dt/4.)*(ds1-3*ds0)
+            const T t2 = sub_rn(b[i], mul_rn(T(3), a[i]));
+            s[i] = add_rn(s[i], mul_rn(k1, t2));
+        } else if (KIND == UPD_RK3_3) {   // s += (dt/12.)*(8*ds2-ds0-ds1)
+            const T t3 = sub_rn(sub_rn(mul_rn(T(8), c[i]), a[i]), b[i]);
+            s[i] = add_rn(s[i], mul_rn(k1, t3));
+        } else if (KIND == UPD_LF_FIRST) {   // sn = s; sb = s; s += dt*ds  (a = ds, b = sb, c = sn)
+            const T v = s[i];
+            c[i] = v;
+            b[i] = v;
+            s[i] = add_rn(v, mul_rn(k1, a[i]));
+        } else if (KIND == UPD_LF_PRED) {   // sn = s; s = sb + 2dt*ds; s = (1/12)*(5s + 8sn - sb); sb = sn
+            const T sn = s[i];
+            const T sb = b[i];
+            const T lf = add_rn(sb, mul_rn(k1, a[i]));
+            const T t4 = sub_rn(add_rn(mul_rn(T(5), lf), mul_rn(T(8), sn)), sb);
+            s[i] = mul_rn(k2, t4);
+            c[i] = sn;
+            b[i] = sn;
+        } else {   // UPD_LF_CORR: s = sn + dt*ds
+            s[i] = add_rn(c[i], mul_rn(k1, a[i]));
+        }
+    }
+}
+
+template <typename T, int KIND>
+__global__ void k_update(const UpdArgs<T> p, const Bat bat = Bat()) {
     int bz;
     long long dlt;
     if (!batch_enter(bat, bz, dlt)) return;
-    UpdArgs<T> p = p0;
-    if (dlt) {
-        for (int q = 0; q < NYLES_MAX_PROG; ++q) {
-            p.s[q] = bshift(p.s[q], dlt);
-            p.a[q] = bshift(p.a[q], dlt);
-            p.b[q] = bshift(p.b[q], dlt);
-            p.c[q] = bshift(p.c[q], dlt);
-        }
-    }
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.vol; i += stride) {
-        for (int q = 0; q < p.nprog; ++q) {
-            T* s = p.s[q];
-            const T dt = T(p.dt);
-            switch (p.kind) {
-                case UPD_EULER: {   // s += dt*ds
-                    T inc = mul_rn(dt, p.a[q][i]);
-                    s[i] = add_rn(s[i], inc);
-                } break;
-                case UPD_RK3_2: {   // s += (dt/4.)*(ds1-3*ds0)
-                    T t1 = mul_rn(T(3), p.a[q][i]);
-                    T t2 = sub_rn(p.b[q][i], t1);
-                    T inc = mul_rn(T(p.dt / 4.0), t2);
-                    s[i] = add_rn(s[i], inc);
-                } break;
-                case UPD_RK3_3: {   // s += (dt/12.)*(8*ds2-ds0-ds1)
-                    T t1 = mul_rn(T(8), p.c[q][i]);
-                    T t2 = sub_rn(t1, p.a[q][i]);
-                    T t3 = sub_rn(t2, p.b[q][i]);
-                    T inc = mul_rn(T(p.dt / 12.0), t3);
-                    s[i] = add_rn(s[i], inc);
-                } break;
-                case UPD_LF_FIRST: {   // sn = s; sb = s; s += dt*ds  (a = ds, b = sb, c = sn)
-                    T v = s[i];
-                    p.c[q][i] = v;
-                    p.b[q][i] = v;
-                    T inc = mul_rn(dt, p.a[q][i]);
-                    s[i] = add_rn(v, inc);
-                } break;
-                case UPD_LF_PRED: {   // sn = s; s = sb + 2dt*ds; s = (1/12)*(5s + 8sn - sb); sb = sn
-                    T sn = s[i];
-                    T sb = p.b[q][i];
-                    T inc = mul_rn(T(2.0 * p.dt), p.a[q][i]);
-                    T lf = add_rn(sb, inc);
-                    T t1 = mul_rn(T(5), lf);
-                    T t2 = mul_rn(T(8), sn);
-                    T t3 = add_rn(t1, t2);
-                    T t4 = sub_rn(t3, sb);
-                    s[i] = mul_rn(T(1.0 / 12.0), t4);
-                    p.c[q][i] = sn;
-                    p.b[q][i] = sn;
-                } break;
-                case UPD_LF_CORR: {   // s = sn + dt*ds
-                    T inc = mul_rn(dt, p.a[q][i]);
-                    s[i] = add_rn(p.c[q][i], inc);
-                } break;
-            }
-        }
-    }
+    for (int q = 0; q < p.nprog; ++q)
+        update_field<T, KIND>(bshift(p.s[q], dlt), bshift(p.a[q], dlt), bshift(p.b[q], dlt), bshift(p.c[q], dlt),
+                              p.vol, p.k1, p.k2);
 }
 
 template <typename T>
@@ -977,13 +958,28 @@ int launch_update(const Geom& g, int nprog, const ProgPtrs<T>& s, const ProgPtrs
     p.vol = g.vol;
     p.nprog = nprog;
     p.kind = kind;
-    p.dt = dt;
+    // the coefficients numpy forms in double (dt/4., dt/12., 2*dt, 1/12.), rounded to T
+    // once here instead of per cell on the device's FP64 pipe
+    p.k1 = T(dt);
+    p.k2 = T(0);
+    if (kind == UPD_RK3_2) p.k1 = T(dt / 4.0);
+    else if (kind == UPD_RK3_3) p.k1 = T(dt / 12.0);
+    else if (kind == UPD_LF_PRED) { p.k1 = T(2.0 * dt); p.k2 = T(1.0 / 12.0); }
     for (int q = 0; q < NYLES_MAX_PROG; ++q) {
         p.s[q] = s.p[q]; p.a[q] = a.p[q]; p.b[q] = b.p[q]; p.c[q] = c.p[q];
     }
     long long blocks = (g.vol + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_update<T><<<dim3((unsigned)blocks, 1, bat.tab ? bat.nrun : 1), 256, 0, st>>>(p, bat);
+    const dim3 grd((unsigned)blocks, 1, bat.tab ? bat.nrun : 1);
+    switch (kind) {
+        case UPD_EULER: k_update<T, UPD_EULER><<<grd, 256, 0, st>>>(p, bat); break;
+        case UPD_RK3_2: k_update<T, UPD_RK3_2><<<grd, 256, 0, st>>>(p, bat); break;
+        case UPD_RK3_3: k_update<T, UPD_RK3_3><<<grd, 256, 0, st>>>(p, bat); break;
+        case UPD_LF_FIRST: k_update<T, UPD_LF_FIRST><<<grd, 256, 0, st>>>(p, bat); break;
+        case UPD_LF_PRED: k_update<T, UPD_LF_PRED><<<grd, 256, 0, st>>>(p, bat); break;
+        case UPD_LF_CORR: k_update<T, UPD_LF_CORR><<<grd, 256, 0, st>>>(p, bat); break;
+        default: set_error("unknown update kind"); return NYLES_BAD_ARG;
+    }
     note_launch();
     return cuda_status(cudaGetLastError(), "update kernel");
 }

@@ -176,6 +176,18 @@ def auto_capacity(n, cap_max=32):
     return max(1, min(cap_max, CELLS_PER_BUCKET // n ** 3))
 
 
+# cell-steps one graph launch of a run covers at least (up to GRAPH_KMAX steps): small
+# grids take longer graphs, so that each launch keeps the device busy for about as long
+# as a 128^3 run's 10 steps and the run does not wait on the host loop between launches
+GRAPH_CELL_STEPS = 10 << 21
+GRAPH_KMAX = 60
+
+
+def graph_steps(n, steps):
+    """steps per graph launch of an n^3 run of `steps` steps"""
+    return steps_per_graph(steps, max(10, min(GRAPH_KMAX, GRAPH_CELL_STEPS // n ** 3)))
+
+
 def steps_per_graph(steps, kmax=10):
     """largest divisor of `steps` not above kmax: graph launches land exactly on `steps`"""
     for k in range(min(kmax, steps), 0, -1):
@@ -221,9 +233,11 @@ class Bucket:
     """The resident runs of one (case, grid, steps per launch) on `capacity` slots of one
     device buffer. Every slot's model is built in an Arena of the same size, so its
     arrays sit at the same offsets: slot r's memory is slot 0's shifted by r x slot_bytes.
-    Batched graphs recorded on slot 0's model (nyles_model_batch_capture), one per
-    batch size (powers of two up to the capacity, recorded when first needed), advance a
-    list of runs: the table of a launch lists the slots' offsets first, so a launch
+    Batched one-step graphs recorded on slot 0's model (nyles_model_batch_capture), one
+    per batch size (powers of two up to the capacity, recorded when first needed), advance
+    a list of runs, each launch replaying the step graph k times (a k-step graph costs
+    more than k times as much host time to record): the table of a launch lists the
+    slots' offsets first, so a launch
     covers only as many slots as it advances, and the runs are processed in the smallest
     batch size that holds them. Each run's pressure solves stop on their own, so its
     result is the same whatever else shares the launch. A new run's slot is zeroed, its
@@ -279,7 +293,7 @@ class Bucket:
         g = self.graphs.get((kind, size))
         if g is None:
             h = ctypes.c_void_p()
-            steps = self.k if kind == "step" else 0
+            steps = 1 if kind == "step" else 0      # one step, launched k times
             self.nat.check(self.lib.nyles_model_batch_capture(self.template._h, self.dt, steps, size,
                                                               ctypes.c_void_p(self.table.data_ptr()),
                                                               ctypes.byref(h)))
@@ -301,7 +315,7 @@ class Bucket:
         slot.req, slot.launched, slot.last_event, slot.projected = req, 0, None, False
         slot.admitted = now
         if staged is None:
-            staged = stage_initial_state(req, self.template.state.b.dtype)
+            staged = stage_initial_state(req, self.template.dtype)
         lo = slot.index * self.slot_bytes
         with torch.cuda.stream(self.stream):
             self.buf[lo:lo + self.slot_bytes].zero_()
@@ -331,7 +345,9 @@ class Bucket:
         ev_tab = torch.cuda.Event()
         ev_tab.record(self.stream)
         self.ring_events[i] = ev_tab
-        self.nat.check(self.lib.nyles_batch_launch(g, self.nat.stream_ptr(self.stream)))
+        sp = self.nat.stream_ptr(self.stream)
+        for _ in range(self.k if kind == "step" else 1):
+            self.nat.check(self.lib.nyles_batch_launch(g, sp))
         self.launches += 1
 
     def launch(self):
@@ -426,9 +442,12 @@ class ServingEngine:
     stream (CUDA priority by the per-run work n^3 x steps, smallest first, with
     priority "work"; equal with "none"), so buckets of every size overlap on the device.
     `capacity` = slots per bucket (at most NYLES_BATCH_RUNS), or "auto": as many runs as
-    CELLS_PER_BUCKET cells hold (auto_capacity); a bucket with no run left and none
-    waiting is released. The initial states of queued requests are built on
-    `prep_threads` host threads while the loop keeps launching. `window` = W launches only the W buckets with the least
+    CELLS_PER_BUCKET cells hold (auto_capacity). A bucket whose runs have all finished
+    stays, idle, with its models and graphs for later requests of the same key; idle
+    buckets give their memory back, least recently used first, when a new bucket needs
+    it, and all are released when serve returns. The initial states of queued requests
+    are built on `prep_threads` host threads while the loop keeps launching. `window` =
+    W launches only the W buckets with the least
     remaining work (cells x steps not yet launched) at each tick, so that small runs
     finish soon after they arrive and the large ones, which set the makespan, fill the
     device afterwards; None launches every bucket. Completion latency = arrival to the
@@ -478,13 +497,16 @@ class ServingEngine:
                 and self.device.type == "cuda" else None)
         dtype = torch.float64 if self.precision == "fp64" else torch.float32
         staging = {}
+        self._idle = {}           # bucket key -> time its last run left (idle buckets)
         t0 = self.clock()
         nxt = 0
         try:
-            while nxt < len(pending) or queue or buckets:
+            while nxt < len(pending) or queue or any(b.resident() for b in buckets.values()):
                 nxt, queue = self._tick(pending, nxt, queue, buckets, results, states, prio, realtime,
                                         keep_states, t0, pool, staging, dtype)
         finally:
+            for key in list(buckets):
+                self._release(buckets, key)
             if pool is not None:
                 pool.shutdown(wait=True, cancel_futures=True)
         if self.device is not None and self.device.type == "cuda":
@@ -515,10 +537,16 @@ class ServingEngine:
             if fut is not None and not fut.done():
                 waiting.append(req)
                 continue
-            key = (req.case, req.n, steps_per_graph(req.steps))
+            key = (req.case, req.n, graph_steps(req.n, req.steps))
             b = buckets.get(key)
             if b is None:
-                cap = min(self.capacity_for(req.n), int((self.budget - self.used) // need))
+                want = self.capacity_for(req.n)
+                # buckets left idle by earlier runs give their memory back, least recently
+                # used first, when a new bucket needs it
+                idle = sorted((k for k in buckets if k in self._idle), key=lambda k: self._idle[k])
+                while idle and self.used + want * need > self.budget:
+                    self._release(buckets, idle.pop(0))
+                cap = min(want, int((self.budget - self.used) // need))
                 if cap < 1:
                     waiting.append(req)
                     continue
@@ -557,17 +585,23 @@ class ServingEngine:
                     if keep_states and fields is not None:
                         states[req.rid] = fields
                     b.release(sl)
-            if not b.resident() and not any((r.case, r.n, steps_per_graph(r.steps)) == key for r in queue):
-                self.launches += b.launches
-                b.close()
-                self.used -= b.bytes
-                del buckets[key]
+            if b.resident():
+                self._idle.pop(key, None)
+            else:
+                self._idle.setdefault(key, self.clock() - t0)
         if not busy:
-            if buckets or staging:
+            if any(b.resident() for b in buckets.values()) or staging:
                 time.sleep(2e-4)
             elif not queue and nxt < len(pending):
                 time.sleep(max(0.0, min(2e-3, pending[nxt].arrival - (self.clock() - t0))))
         return nxt, queue
+
+    def _release(self, buckets, key):
+        b = buckets.pop(key)
+        self._idle.pop(key, None)
+        self.launches += b.launches
+        b.close()
+        self.used -= b.bytes
 
     def stream_priorities(self, requests, levels=None):
         """{rid: stream priority}: the distinct work values (n^3 x steps) of the requests,

@@ -21,7 +21,8 @@ def test_results_identical_alone_and_in_the_mix():
     reqs = [S.Request(0, "lock", 32, 11, 20, 0.0), S.Request(1, "tgv", 16, 12, 20, 0.0),
             S.Request(2, "tgv", 48, 13, 10, 0.0), S.Request(3, "lock", 16, 14, 30, 0.0),
             S.Request(4, "lock", 32, 15, 20, 0.0)]
-    eng = S.ServingEngine(precision="mixed")
+    # initial states built inline: all five are admitted in the loop's first pass
+    eng = S.ServingEngine(precision="mixed", prep_threads=0)
     results, mixed_states = eng.serve(reqs, realtime=False, keep_states=True)
     assert eng.max_active == len(reqs)
     assert eng.buckets_made == 4                       # the two lock 32^3 runs share a bucket
@@ -77,9 +78,9 @@ def test_footprint_model_covers_the_allocation(case, n, precision):
 
 
 def test_batched_launches_are_fewer_than_per_run_launches():
-    """A bucket of 6 runs of 32^3 is projected with one launch and advances with one
-    launch per 10 steps: the library's kernel count for the ensemble is about one run's,
-    not six. (Initial states built inline, so that all six are admitted in the first
+    """A bucket of 6 runs of 32^3 is projected with one launch and advances its 30
+    steps with one more (graph_steps): the library's kernel count for the ensemble is
+    about one run's, not six. (Initial states built inline, so that all six are admitted in the first
     pass of the loop; with host threads they join as their states are ready.)"""
     from nyles_gb300 import _native as nat
     from nyles_gb300 import serving as S
@@ -88,7 +89,7 @@ def test_batched_launches_are_fewer_than_per_run_launches():
     eng = S.ServingEngine(precision="mixed", prep_threads=0)
     results, _ = eng.serve(reqs, realtime=False)
     batched = nat.lib().nyles_launch_count() - l0
-    assert eng.launches == 4 and all(r.status == "ok" for r in results)   # one projection, 3 x 10 steps
+    assert eng.launches == 2 and all(r.status == "ok" for r in results)   # one projection, one of 30 steps
     l0 = nat.lib().nyles_launch_count()
     one = S.ServingEngine(precision="mixed")
     one.serve(reqs[:1], realtime=False)

@@ -20,6 +20,8 @@ def test_footprint_grows_with_size_and_precision():
     assert all(x < y for x, y in zip(f, f[1:]))
     assert S.footprint_bytes("lock", 64, "fp64") > 1.4 * S.footprint_bytes("lock", 64, "mixed")
     assert S.steps_per_graph(300) == 10 and S.steps_per_graph(7) == 7 and S.steps_per_graph(13) == 1
+    assert S.graph_steps(128, 300) == 10 and S.graph_steps(32, 300) == 60 and S.graph_steps(64, 300) == 60
+    assert S.graph_steps(96, 300) == 20 and S.graph_steps(32, 7) == 7
 
 
 class FakeSlot:
@@ -120,7 +122,7 @@ def test_runs_of_a_bucket_share_its_launches():
     eng = S.ServingEngine(device="cpu", bucket_factory=FakeBucket, capacity=16)
     results, _ = eng.serve(reqs, realtime=False)
     assert len(results) == 9 and eng.buckets_made == 2
-    assert eng.launches == 2 * 3           # 30 steps in launches of 10, once per bucket
+    assert eng.launches == 2 * 1           # 30 steps of 32^3 in one launch, once per bucket
     assert eng.max_active == 9
 
 
