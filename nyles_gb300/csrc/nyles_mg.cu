@@ -350,31 +350,40 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // the level's x faces) and z-chunks of V4_ZC cells; needs nx and nz divisible by 4 and
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
-template <int MODE, bool BAT = false>
-__global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
-                                                               const float* __restrict__ b, float* __restrict__ out,
-                                                               float omega, float2* __restrict__ acc,
-                                                               const float* __restrict__ dot,
-                                                               double* __restrict__ partial,
-                                                               double* __restrict__ partial2, const Bat bat = Bat()) {
-    int bz = blockIdx.z;
-    if constexpr (BAT) {
-        long long dlt;
-        if (!batch_enter(bat, bz, dlt)) return;
-        in = bshift(in, dlt);
-        b = bshift(b, dlt);
-        out = bshift(out, dlt);
-        acc = bshift(acc, dlt);
-        dot = bshift(dot, dlt);
-        partial = bshift(partial, dlt);
-        partial2 = bshift(partial2, dlt);
-    }
+
+// Loads of the vector level kernels. LdPlain: ordinary loads (nothing the kernel reads
+// is written during its launch). LdCoherent: loads through L2 (ld.global.cg) for the
+// persistent coarse-level kernel, whose passes read what other blocks wrote in earlier
+// passes of the same launch: the read-only and L1 paths are not coherent within a
+// launch.
+struct LdPlain {
+    static __device__ __forceinline__ float4 f4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+    static __device__ __forceinline__ float2 f2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+    static __device__ __forceinline__ float f1(const float* p) { return *p; }
+};
+struct LdCoherent {
+    static __device__ __forceinline__ float4 f4(const float* p) { return __ldcg(reinterpret_cast<const float4*>(p)); }
+    static __device__ __forceinline__ float2 f2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
+    static __device__ __forceinline__ float f1(const float* p) { return __ldcg(p); }
+};
+template <typename L>
+__device__ __forceinline__ float mg_ldw_l(const float* a, long long c, bool wet) {
+    const float v = L::f1(a + c);
+    return wet ? v : 0.f;
+}
+
+// One block of the vector half-sweep: block (bx, by, bz) of the grid grid_v4(n, ZC);
+// MODE 2 accumulates the block's sums of out*dot and out into sdot and ssum.
+template <int MODE, int ZC, typename L>
+__device__ __forceinline__ void mg_jacobi_v4_blk(const MgGeom& g, const float* __restrict__ in,
+                                                 const float* __restrict__ b, float* __restrict__ out, float omega,
+                                                 float2* __restrict__ acc, const float* __restrict__ dot, int bx,
+                                                 int by, int bz, float& sdot, float& ssum) {
     const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
-    const int xv = blockIdx.x * MG_BX + lane;
-    const int y = blockIdx.y * MG_BY + threadIdx.y;
-    float sdot = 0.f, ssum = 0.f;
+    const int xv = bx * MG_BX + lane;
+    const int y = by * MG_BY + threadIdx.y;
     // idle lanes shadow the last vector of the row (every lane takes part in the
     // shuffles); only active lanes store and sum
     const bool act = xv < nx4 && y < ny;
@@ -392,9 +401,9 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         dgx[e] = (int)(xx > 0 || g.per[2]) + (int)(xx < nx - 1 || g.per[2]) + (int)nyb.wm + (int)nyb.wp;
     }
     const float cff1 = 1.f - omega;
-    const int zb = bz * V4_ZC;
+    const int zb = bz * ZC;
     const long long c00 = (long long)ys * sy + x0;
-    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
+    auto ld4 = [&](const float* a, long long c) { return L::f4(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     auto zrow = [&](int zz) -> float4 {
         if (zz < 0) return g.per[0] ? ld4(in, c00 + (long long)(nz - 1) * sz) : zero4;
@@ -403,7 +412,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
     };
     float4 zm = zrow(zb - 1), zc = zrow(zb);
 #pragma unroll
-    for (int k = 0; k < V4_ZC; ++k) {
+    for (int k = 0; k < ZC; ++k) {
         const int zz = zb + k;
         const float4 zp = zrow(zz + 1);
         const long long c = c00 + (long long)zz * sz;
@@ -413,8 +422,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         const float4 dv = (MODE == 2) ? ld4(dot, c) : zero4;
         const float sl = __shfl_up_sync(0xffffffffu, zc.w, 1);
         const float sr = __shfl_down_sync(0xffffffffu, zc.x, 1);
-        const float left = ownl ? mg_ldw(in, c + ol, wl) : sl;
-        const float right = ownr ? mg_ldw(in, c + orr, wr) : sr;
+        const float left = ownl ? mg_ldw_l<L>(in, c + ol, wl) : sl;
+        const float right = ownr ? mg_ldw_l<L>(in, c + orr, wr) : sr;
         const int dzw = (int)(zz > 0 || g.per[0]) + (int)(zz < nz - 1 || g.per[0]);
         const float xc[4] = {zc.x, zc.y, zc.z, zc.w};
         const float xm[4] = {left, zc.x, zc.y, zc.z}, xp[4] = {zc.y, zc.z, zc.w, right};
@@ -446,6 +455,29 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         zm = zc;
         zc = zp;
     }
+}
+
+template <int MODE, bool BAT = false, int ZC = V4_ZC>
+__global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom g, const float* __restrict__ in,
+                                                               const float* __restrict__ b, float* __restrict__ out,
+                                                               float omega, float2* __restrict__ acc,
+                                                               const float* __restrict__ dot,
+                                                               double* __restrict__ partial,
+                                                               double* __restrict__ partial2, const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        in = bshift(in, dlt);
+        b = bshift(b, dlt);
+        out = bshift(out, dlt);
+        acc = bshift(acc, dlt);
+        dot = bshift(dot, dlt);
+        partial = bshift(partial, dlt);
+        partial2 = bshift(partial2, dlt);
+    }
+    float sdot = 0.f, ssum = 0.f;
+    mg_jacobi_v4_blk<MODE, ZC, LdPlain>(g, in, b, out, omega, acc, dot, blockIdx.x, blockIdx.y, bz, sdot, ssum);
     if (MODE == 2) block_partial2_f(sdot, ssum, partial, partial2, bz);
 }
 
@@ -615,27 +647,18 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
 // twice the coarse one in every direction and fine nx divisible by 4, and keep the
 // per-cell arithmetic of the full-chunk paths above.
 
-// k_mg_restrict: one coarse row pair of cells per thread, MG_RZC coarse planes (needs
-// coarse nz divisible by MG_RZC)
-template <bool BAT = false>
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom gf, const float* __restrict__ xf,
-                                                                 const float* __restrict__ bf, const MgGeom gc,
-                                                                 float* __restrict__ bc, float* __restrict__ yc,
-                                                                 float omega, const Bat bat = Bat()) {
-    int bz = blockIdx.z;
-    if constexpr (BAT) {
-        long long dlt;
-        if (!batch_enter(bat, bz, dlt)) return;
-        xf = bshift(xf, dlt);
-        bf = bshift(bf, dlt);
-        bc = bshift(bc, dlt);
-        yc = bshift(yc, dlt);
-    }
+// k_mg_restrict: one coarse row pair of cells per thread, RZC coarse planes (needs
+// coarse nz divisible by RZC); block (bx, by, bz) of the grid of v4_restrict_grid
+template <int RZC, typename L>
+__device__ __forceinline__ void mg_restrict_v4_blk(const MgGeom& gf, const float* __restrict__ xf,
+                                                   const float* __restrict__ bf, const MgGeom& gc,
+                                                   float* __restrict__ bc, float* __restrict__ yc, float omega, int bx,
+                                                   int by, int bz) {
     const int nx = gf.n[2], ny = gf.n[1], nz = gf.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
-    const int xv = blockIdx.x * MG_BX + lane;
-    const int jc = blockIdx.y * MG_BY + threadIdx.y;   // coarse row
+    const int xv = bx * MG_BX + lane;
+    const int jc = by * MG_BY + threadIdx.y;   // coarse row
     const bool act = xv < nx4 && jc < gc.n[1];
     const int x0 = min(xv, nx4 - 1) * 4, j0 = 2 * min(jc, gc.n[1] - 1);
     const long long sy = nx, sz = (long long)ny * nx;
@@ -649,9 +672,9 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
     const int ylw = (int)yl.wm, yhw = (int)yh.wp;
     const float wxy[2][4] = {{(float)((int)wl + ylw), (float)(1 + ylw), (float)((int)wl + yhw), (float)(1 + yhw)},
                              {(float)(1 + ylw), (float)((int)wr + ylw), (float)(1 + yhw), (float)((int)wr + yhw)}};
-    const int zcb = bz * MG_RZC, k0 = 2 * zcb;
+    const int zcb = bz * RZC, k0 = 2 * zcb;
     const long long c00 = (long long)j0 * sy + x0;
-    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
+    auto ld4 = [&](const float* a, long long c) { return L::f4(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     struct Rows { float4 r0, r1; };
     // rows j0 and j0 + 1 of fine plane k, one plane outside the level at most: periodic
@@ -671,7 +694,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
     };
     Rows below = plane(k0 - 1), cur = plane(k0);
 #pragma unroll
-    for (int zc = 0; zc < MG_RZC; ++zc) {
+    for (int zc = 0; zc < RZC; ++zc) {
         const int kz = k0 + 2 * zc;
         const Rows up = plane(kz + 1), nxt = plane(kz + 2);
         float sbv[2] = {0.f, 0.f}, sxv[2] = {0.f, 0.f}, sov[2] = {0.f, 0.f};
@@ -687,8 +710,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
             const float4 b0 = ld4(bf, c), b1 = ld4(bf, c + sy);
             const float sl0 = __shfl_up_sync(0xffffffffu, P.r0.w, 1), sl1 = __shfl_up_sync(0xffffffffu, P.r1.w, 1);
             const float sr0 = __shfl_down_sync(0xffffffffu, P.r0.x, 1), sr1 = __shfl_down_sync(0xffffffffu, P.r1.x, 1);
-            const float l0 = ownl ? mg_ldw(xf, c + ol, wl) : sl0, l1 = ownl ? mg_ldw(xf, c + sy + ol, wl) : sl1;
-            const float r0 = ownr ? mg_ldw(xf, c + orr, wr) : sr0, r1 = ownr ? mg_ldw(xf, c + sy + orr, wr) : sr1;
+            const float l0 = ownl ? mg_ldw_l<L>(xf, c + ol, wl) : sl0, l1 = ownl ? mg_ldw_l<L>(xf, c + sy + ol, wl) : sl1;
+            const float r0 = ownr ? mg_ldw_l<L>(xf, c + orr, wr) : sr0, r1 = ownr ? mg_ldw_l<L>(xf, c + sy + orr, wr) : sr1;
             const float x0v[4] = {P.r0.x, P.r0.y, P.r0.z, P.r0.w}, x1v[4] = {P.r1.x, P.r1.y, P.r1.z, P.r1.w};
             const float o0[4] = {O.r0.x, O.r0.y, O.r0.z, O.r0.w}, o1[4] = {O.r1.x, O.r1.y, O.r1.z, O.r1.w};
             const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
@@ -724,24 +747,33 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
     }
 }
 
-// k_mg_prolong: one 4-cell fine row segment per thread, V4_ZC fine planes (needs fine
-// nz divisible by V4_ZC)
-template <bool BAT = false>
-__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf, float* __restrict__ xf,
-                                                                const MgGeom gc, const float* __restrict__ xc,
-                                                                const Bat bat = Bat()) {
+template <bool BAT = false, int RZC = MG_RZC>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom gf, const float* __restrict__ xf,
+                                                                 const float* __restrict__ bf, const MgGeom gc,
+                                                                 float* __restrict__ bc, float* __restrict__ yc,
+                                                                 float omega, const Bat bat = Bat()) {
     int bz = blockIdx.z;
     if constexpr (BAT) {
         long long dlt;
         if (!batch_enter(bat, bz, dlt)) return;
         xf = bshift(xf, dlt);
-        xc = bshift(xc, dlt);
+        bf = bshift(bf, dlt);
+        bc = bshift(bc, dlt);
+        yc = bshift(yc, dlt);
     }
+    mg_restrict_v4_blk<RZC, LdPlain>(gf, xf, bf, gc, bc, yc, omega, blockIdx.x, blockIdx.y, bz);
+}
+
+// k_mg_prolong: one 4-cell fine row segment per thread, ZC fine planes (needs fine nz
+// divisible by ZC, ZC even); block (bx, by, bz) of the grid grid_v4(fine n, ZC)
+template <int ZC, typename L>
+__device__ __forceinline__ void mg_prolong_v4_blk(const MgGeom& gf, float* __restrict__ xf, const MgGeom& gc,
+                                                  const float* __restrict__ xc, int bx, int by, int bz) {
     const int nx = gf.n[2], ny = gf.n[1];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
-    const int xv = blockIdx.x * MG_BX + lane;
-    const int y = blockIdx.y * MG_BY + threadIdx.y;
+    const int xv = bx * MG_BX + lane;
+    const int y = by * MG_BY + threadIdx.y;
     const bool act = xv < nx4 && y < ny;
     const int x0 = min(xv, nx4 - 1) * 4, ys = min(y, ny - 1);
     const int ncx = gc.n[2], ic0 = x0 >> 1, jc = ys >> 1;
@@ -754,36 +786,36 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
     const long long col = ic0 > 0 ? -1 : (gc.per[2] ? (long long)(ncx - 1) : 0);
     const long long cor = ic0 + 2 < ncx ? 2 : (gc.per[2] ? (long long)(2 - ncx) : 0);
     const bool ownl = lane == 0 || x0 == 0, ownr = lane == MG_BX - 1 || x0 + 4 >= nx;
-    const int zb = bz * V4_ZC, kc0 = zb >> 1;
-    const MgNb zl = mg_nb(kc0, gc.n[0], gc.per[0], csz), zh = mg_nb(kc0 + V4_ZC / 2 - 1, gc.n[0], gc.per[0], csz);
+    const int zb = bz * ZC, kc0 = zb >> 1;
+    const MgNb zl = mg_nb(kc0, gc.n[0], gc.per[0], csz), zh = mg_nb(kc0 + ZC / 2 - 1, gc.n[0], gc.per[0], csz);
     const long long cc = mg_at(gc, kc0, jc, ic0);
     // in-plane 9-3-3-1 sums of the 4 fine cells from one coarse plane at c (0 when the
     // plane is dry): fine x0 + e takes coarse ic0 + (e >> 1) and its x neighbour on the
     // side of the fine cell
     auto plane = [&](long long c, bool wet, float* out) {
-        const float2 a = wet ? *reinterpret_cast<const float2*>(xc + c) : make_float2(0.f, 0.f);
-        const float2 d = (wet && wy) ? *reinterpret_cast<const float2*>(xc + c + oy) : make_float2(0.f, 0.f);
+        const float2 a = wet ? L::f2(xc + c) : make_float2(0.f, 0.f);
+        const float2 d = (wet && wy) ? L::f2(xc + c + oy) : make_float2(0.f, 0.f);
         const float sal = __shfl_up_sync(0xffffffffu, a.y, 1), sar = __shfl_down_sync(0xffffffffu, a.x, 1);
         const float sdl = __shfl_up_sync(0xffffffffu, d.y, 1), sdr = __shfl_down_sync(0xffffffffu, d.x, 1);
-        const float al = ownl ? mg_ldw(xc, c + col, wet && cwl) : sal;
-        const float ar = ownr ? mg_ldw(xc, c + cor, wet && cwr) : sar;
-        const float dl = ownl ? mg_ldw(xc, c + oy + col, wet && cwl && wy) : sdl;
-        const float dr = ownr ? mg_ldw(xc, c + oy + cor, wet && cwr && wy) : sdr;
+        const float al = ownl ? mg_ldw_l<L>(xc, c + col, wet && cwl) : sal;
+        const float ar = ownr ? mg_ldw_l<L>(xc, c + cor, wet && cwr) : sar;
+        const float dl = ownl ? mg_ldw_l<L>(xc, c + oy + col, wet && cwl && wy) : sdl;
+        const float dr = ownr ? mg_ldw_l<L>(xc, c + oy + cor, wet && cwr && wy) : sdr;
         const float av[4] = {a.x, a.x, a.y, a.y}, bv[4] = {al, a.y, a.x, ar};
         const float dv[4] = {d.x, d.x, d.y, d.y}, ev[4] = {dl, d.y, d.x, dr};
 #pragma unroll
         for (int e = 0; e < 4; ++e) out[e] = ((9.f * av[e] + 3.f * bv[e]) + 3.f * dv[e]) + ev[e];
     };
     const long long sz = (long long)ny * nx, c0 = (long long)zb * sz + (long long)ys * nx + x0;
-    float4 xv4[V4_ZC];   // the fine values, loaded together with the coarse ones
+    float4 xv4[ZC];   // the fine values, loaded together with the coarse ones
 #pragma unroll
-    for (int k = 0; k < V4_ZC; ++k) xv4[k] = *reinterpret_cast<const float4*>(xf + c0 + k * sz);
-    constexpr int NP = V4_ZC / 2 + 2;
+    for (int k = 0; k < ZC; ++k) xv4[k] = L::f4(xf + c0 + k * sz);
+    constexpr int NP = ZC / 2 + 2;
     float P[NP][4];
     plane(cc + zl.om, zl.wm, P[0]);
 #pragma unroll
     for (int q = 1; q < NP - 1; ++q) plane(cc + (q - 1) * csz, true, P[q]);
-    plane(cc + (V4_ZC / 2 - 1) * csz + zh.op, zh.wp, P[NP - 1]);
+    plane(cc + (ZC / 2 - 1) * csz + zh.op, zh.wp, P[NP - 1]);
     // 1/(Wx*Wy*Wz) of each fine cell: its coarse x neighbour is wet except beyond the
     // level's x faces (cells x0 and x0 + 3)
     float pc_wet[4], pc_lo[4], pc_hi[4];
@@ -796,7 +828,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
         pc_hi[e] = mg_pcoef<float>(gf, bxy | ((int)zh.wp << 2));
     }
 #pragma unroll
-    for (int k = 0; k < V4_ZC; ++k) {
+    for (int k = 0; k < ZC; ++k) {
         const int m = (k >> 1) + 1;   // plane of z >> 1 in P
         const float* bpl = P[m];
         const float* opl = P[(k & 1) ? m + 1 : m - 1];
@@ -804,10 +836,149 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
         float v[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const float pc = (k == 0) ? pc_lo[e] : (k == V4_ZC - 1 ? pc_hi[e] : pc_wet[e]);
+            const float pc = (k == 0) ? pc_lo[e] : (k == ZC - 1 ? pc_hi[e] : pc_wet[e]);
             v[e] = xo[e] + pc * (3.f * bpl[e] + opl[e]);
         }
         if (act) *reinterpret_cast<float4*>(xf + c0 + k * sz) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+}
+
+template <bool BAT = false, int ZC = V4_ZC>
+__global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf, float* __restrict__ xf,
+                                                                const MgGeom gc, const float* __restrict__ xc,
+                                                                const Bat bat = Bat()) {
+    int bz = blockIdx.z;
+    if constexpr (BAT) {
+        long long dlt;
+        if (!batch_enter(bat, bz, dlt)) return;
+        xf = bshift(xf, dlt);
+        xc = bshift(xc, dlt);
+    }
+    mg_prolong_v4_blk<ZC, LdPlain>(gf, xf, gc, xc, blockIdx.x, blockIdx.y, bz);
+}
+
+// ---------------------------------------------------------------- coarse levels, persistent
+// Below level 0 every half-sweep, restriction and prolongation is a launch of a few
+// microseconds whatever the level's size: launch latency, not work. k_mg_coarse runs the
+// levels l0..l1-1 of one V-cycle direction in one cooperative launch instead (all blocks
+// resident, 1-D grid): each pass is the vector block function of the per-level kernel
+// applied to the blocks of that kernel's grid in turn, passes are separated by a grid
+// barrier, and every load goes through L2 (LdCoherent), since a pass reads what other
+// blocks wrote in the passes before it. Down (solvers.f90:35-55 from l0 to the bottom):
+// per level the second pre-smoothing half-sweep (y -> x; the first came with b) and the
+// restriction into l + 1 (its b and first half-sweep). Up: per level from l1 - 1 to l0
+// the prolongation of x(l + 1) into x(l) and the two post-smoothing half-sweeps. The
+// arithmetic is the per-level kernels', so the V-cycle is the same to the last bit.
+constexpr int MG_COARSE_MAXLEV = 12;
+constexpr unsigned long long MG_BAR_SPIN_LIMIT = 1ull << 22;   // x 64 ns sleeps: a few tenths of a second
+struct MgCoarse {
+    int l0, l1;                        // levels l0..l1-1 are smoothed; l1 is the bottom
+    MgGeom g[MG_COARSE_MAXLEV];        // levels l0..l1, indexed l - l0
+    float* x[MG_COARSE_MAXLEV];
+    float* b[MG_COARSE_MAXLEV];
+    float* y[MG_COARSE_MAXLEV];
+    float omega;
+    unsigned long long* arrivals;      // barrier arrivals since the workspace was bound
+    unsigned int* err;                 // set when a barrier gave up waiting
+};
+
+// Grid barrier: every block adds one arrival to a 64-bit counter that only grows (one
+// barrier = nblk arrivals, launches do whole barriers), and waits until the count reaches
+// the end of its barrier's group. The wait is bounded: a block that gives up sets *err
+// and goes on; the launch then poisons its output (see k_mg_coarse).
+__device__ __forceinline__ void mg_grid_sync(unsigned long long* arrivals, unsigned int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const unsigned long long nblk = gridDim.x;
+        __threadfence();   // this block's stores of the pass before its arrival
+        const unsigned long long t = atomicAdd(arrivals, 1ull);
+        const unsigned long long target = (t / nblk + 1) * nblk;
+        unsigned long long it = 0, v;
+        while (true) {
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(arrivals) : "memory");
+            if (v >= target) break;
+            if (++it > MG_BAR_SPIN_LIMIT) {
+                atomicExch(err, 1u);
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+// block (bx, by, bz) of virtual block vb of a grid (gx, gy, *)
+__device__ __forceinline__ void mg_vblock(int vb, const dim3& gd, int& bx, int& by, int& bz) {
+    bx = vb % (int)gd.x;
+    const int t = vb / (int)gd.x;
+    by = t % (int)gd.y;
+    bz = t / (int)gd.y;
+}
+
+template <bool DOWN, int ZC>
+__global__ void __launch_bounds__(MG_BX * MG_BY, 2) k_mg_coarse(const MgCoarse a) {
+    constexpr int RZC = ZC >= 4 ? MG_RZC : 1;   // coarse planes per restriction thread
+    constexpr int PZC = ZC >= 4 ? V4_ZC : 2;    // fine planes per prolongation thread
+    const float om = a.omega;
+    float sd = 0.f, ss = 0.f;
+    auto jacobi = [&](int l, const float* in, float* out) {
+        const MgGeom& g = a.g[l - a.l0];
+        const dim3 gd((unsigned)((g.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((g.n[1] + MG_BY - 1) / MG_BY),
+                      (unsigned)(g.n[0] / ZC));
+        const int nvb = (int)(gd.x * gd.y * gd.z);
+        for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+            int bx, by, bz;
+            mg_vblock(vb, gd, bx, by, bz);
+            mg_jacobi_v4_blk<0, ZC, LdCoherent>(g, in, a.b[l - a.l0], out, om, nullptr, nullptr, bx, by, bz, sd, ss);
+        }
+    };
+    if (DOWN) {
+        for (int l = a.l0; l < a.l1; ++l) {
+            const int i = l - a.l0;
+            jacobi(l, a.y[i], a.x[i]);
+            mg_grid_sync(a.arrivals, a.err);
+            const MgGeom& gf = a.g[i];
+            const MgGeom& gc = a.g[i + 1];
+            const dim3 gd((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
+                          (unsigned)(gc.n[0] / RZC));
+            const int nvb = (int)(gd.x * gd.y * gd.z);
+            for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+                int bx, by, bz;
+                mg_vblock(vb, gd, bx, by, bz);
+                mg_restrict_v4_blk<RZC, LdCoherent>(gf, a.x[i], a.b[i], gc, a.b[i + 1], a.y[i + 1], om, bx, by, bz);
+            }
+            if (l + 1 < a.l1) mg_grid_sync(a.arrivals, a.err);
+        }
+    } else {
+        for (int l = a.l1 - 1; l >= a.l0; --l) {
+            const int i = l - a.l0;
+            const MgGeom& gf = a.g[i];
+            const MgGeom& gc = a.g[i + 1];
+            const dim3 gd((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gf.n[1] + MG_BY - 1) / MG_BY),
+                          (unsigned)(gf.n[0] / PZC));
+            const int nvb = (int)(gd.x * gd.y * gd.z);
+            for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
+                int bx, by, bz;
+                mg_vblock(vb, gd, bx, by, bz);
+                mg_prolong_v4_blk<PZC, LdCoherent>(gf, a.x[i], gc, a.x[i + 1], bx, by, bz);
+            }
+            mg_grid_sync(a.arrivals, a.err);
+            jacobi(l, a.x[i], a.y[i]);
+            mg_grid_sync(a.arrivals, a.err);
+            jacobi(l, a.y[i], a.x[i]);
+            if (l > a.l0) mg_grid_sync(a.arrivals, a.err);
+        }
+    }
+    // A barrier that gave up leaves the passes unordered: the level handed on (the
+    // bottom's right-hand side going down, x of level l0 going up) becomes NaN, so the
+    // solve's stop test reports a non-finite residual instead of a wrong answer.
+    if (*(volatile unsigned int*)a.err) {
+        const int i = DOWN ? a.l1 - a.l0 : 0;
+        float* const v = DOWN ? a.b[i] : a.x[i];
+        const long long n = (long long)a.g[i].n[0] * a.g[i].n[1] * a.g[i].n[2];
+        const long long t0 = (long long)blockIdx.x * blockDim.x * blockDim.y + threadIdx.y * blockDim.x + threadIdx.x;
+        for (long long q = t0; q < n; q += (long long)gridDim.x * blockDim.x * blockDim.y) v[q] = __int_as_float(0x7fc00000);
     }
 }
 
@@ -981,14 +1152,16 @@ __device__ __forceinline__ T bottom_prolong(const MgGeom& gf, const MgGeom& gc, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const MgBottom<T> a0, const Bat bat = Bat()) {
+__global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const MgBottom<T> a, const Bat bat = Bat()) {
     extern __shared__ __align__(16) unsigned char mg_smem[];
     int bz;
     long long dlt;
     if (!batch_enter(bat, bz, dlt)) return;
-    MgBottom<T> a = a0;
-    a.xg = bshift(a.xg, dlt);
-    a.bg = bshift(a.bg, dlt);
+    // the arguments stay in parameter space (their level table is indexed at run time:
+    // a copy of the struct would sit in every thread's local memory); only the two
+    // global pointers are shifted to the block's run
+    T* const xg = bshift(a.xg, dlt);
+    const T* const bg = bshift(a.bg, dlt);
     T* sm = reinterpret_cast<T*>(mg_smem);
     const T om = a.omega, cff1 = T(1) - om;
     const int L = a.nlev;
@@ -998,7 +1171,7 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
     // level l0 starts from x = 0: its first half-sweep is y = from_zero(b)
     bottom_cells(a.g[0], [&](int z, int y, int x, const MgNbI& nx, const MgNbI& ny) {
         const int c = (z * a.g[0].n[1] + y) * a.g[0].n[2] + x;
-        const T bv = a.bg[c];
+        const T bv = bg[c];
         Bv(0)[c] = bv;
         Y(0)[c] = mg_jacobi_from_zero(bv, om, bottom_idiag<T>(a.g[0], z, nx, ny));
     });
@@ -1032,7 +1205,7 @@ __global__ void __launch_bounds__(MgBottomThreads<T>::n, 1) k_mg_bottom(const Mg
         bottom_sweep(gf, Y(l), Bv(l), X(l), cff1, om);
     }
     const int v0 = mg_vol(a.g[0]);
-    for (int q = threadIdx.x; q < v0; q += blockDim.x) a.xg[q] = X(0)[q];
+    for (int q = threadIdx.x; q < v0; q += blockDim.x) xg[q] = X(0)[q];
 }
 
 // ---------------------------------------------------------------- reductions
@@ -1772,25 +1945,71 @@ static inline dim3 bgrid(const MgImpl* mg, dim3 g) {
     return g;
 }
 
-// the 4-cell vector kernels apply to a level whose x and z extents allow them
-static inline bool use_v4(const MgImpl* mg, const int n[3]) { return mg->vec4 && n[2] % 4 == 0 && n[0] % V4_ZC == 0; }
-static inline dim3 grid_v4(const int n[3]) {
+// the 4-cell vector kernels apply to a level whose x and z extents allow them; zc = the
+// z cells per thread (V4_ZC on level 0 and for the float-pair and Krylov kernels,
+// lvl_zc below)
+static inline bool use_v4(const MgImpl* mg, const int n[3], int zc = V4_ZC) {
+    return mg->vec4 && n[2] % 4 == 0 && n[0] % zc == 0;
+}
+static inline dim3 grid_v4(const int n[3], int zc = V4_ZC) {
     return dim3((unsigned)((n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((n[1] + MG_BY - 1) / MG_BY),
-                (unsigned)(n[0] / V4_ZC));
+                (unsigned)(n[0] / zc));
+}
+// z cells per thread of the half-sweeps of level l: level 0 reuses each z row from
+// registers over V4_ZC cells; the coarser levels are latency-bound (a few microseconds
+// per launch whatever their size), where more blocks with shorter chains of dependent
+// loads finish sooner
+static inline int lvl_zc(const MgImpl* mg, int l) { return l == 0 ? V4_ZC : mg->czc; }
+// coarse planes per thread of the restriction out of level l, fine planes per thread of
+// the prolongation into level l (even)
+static inline int lvl_rzc(const MgImpl* mg, int l) { return l == 0 ? MG_RZC : (mg->czc >= 4 ? MG_RZC : 1); }
+static inline int lvl_pzc(const MgImpl* mg, int l) { return l == 0 ? V4_ZC : (mg->czc >= 4 ? V4_ZC : 2); }
+static inline dim3 grid_v4_restrict(const MgGeom& gf, const MgGeom& gc, int rzc) {
+    return dim3((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
+                (unsigned)(gc.n[0] / rzc));
 }
 // the vector transfers between levels l and l + 1: exact halving in every direction,
 // fine nx divisible by 4, and the z chunk of each kernel dividing its extent
-static inline bool v4_restrict(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc) {
-    if (!mg->vec4 || gf.n[2] % 4 != 0 || gc.n[0] % MG_RZC != 0) return false;
+static inline bool v4_restrict(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc, int rzc) {
+    if (!mg->vec4 || gf.n[2] % 4 != 0 || gc.n[0] % rzc != 0) return false;
     for (int k = 0; k < 3; ++k)
         if (gf.n[k] != 2 * gc.n[k]) return false;
     return true;
 }
-static inline bool v4_prolong(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc) {
-    if (!mg->vec4 || gf.n[2] % 4 != 0 || gf.n[0] % V4_ZC != 0) return false;
+static inline bool v4_prolong(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc, int pzc) {
+    if (!mg->vec4 || gf.n[2] % 4 != 0 || gf.n[0] % pzc != 0) return false;
     for (int k = 0; k < 3; ++k)
         if (gf.n[k] != 2 * gc.n[k]) return false;
     return true;
+}
+
+// launches of the MODE-0 vector half-sweep and of the vector transfers with a z chunk
+// chosen at run time
+template <bool BAT>
+static void launch_jacobi_v4_0(int zc, dim3 grd, cudaStream_t st, const MgGeom& g, const float* in, const float* b,
+                               float* out, float om, const Bat& bt) {
+    if (zc == 1)
+        k_mg_jacobi_v4<0, BAT, 1><<<grd, kBlk, 0, st>>>(g, in, b, out, om, nullptr, nullptr, nullptr, nullptr, bt);
+    else if (zc == 2)
+        k_mg_jacobi_v4<0, BAT, 2><<<grd, kBlk, 0, st>>>(g, in, b, out, om, nullptr, nullptr, nullptr, nullptr, bt);
+    else
+        k_mg_jacobi_v4<0, BAT, 4><<<grd, kBlk, 0, st>>>(g, in, b, out, om, nullptr, nullptr, nullptr, nullptr, bt);
+}
+template <bool BAT>
+static void launch_restrict_v4(int rzc, dim3 grd, cudaStream_t st, const MgGeom& gf, const float* xf, const float* bf,
+                               const MgGeom& gc, float* bc, float* yc, float om, const Bat& bt) {
+    if (rzc == 1)
+        k_mg_restrict_v4<BAT, 1><<<grd, kBlk, 0, st>>>(gf, xf, bf, gc, bc, yc, om, bt);
+    else
+        k_mg_restrict_v4<BAT, MG_RZC><<<grd, kBlk, 0, st>>>(gf, xf, bf, gc, bc, yc, om, bt);
+}
+template <bool BAT>
+static void launch_prolong_v4(int pzc, dim3 grd, cudaStream_t st, const MgGeom& gf, float* xf, const MgGeom& gc,
+                              const float* xc, const Bat& bt) {
+    if (pzc == 2)
+        k_mg_prolong_v4<BAT, 2><<<grd, kBlk, 0, st>>>(gf, xf, gc, xc, bt);
+    else
+        k_mg_prolong_v4<BAT, V4_ZC><<<grd, kBlk, 0, st>>>(gf, xf, gc, xc, bt);
 }
 
 static inline MgGeom mgg(const MgImpl* mg, int l) {
@@ -1842,6 +2061,37 @@ static int* mg_hist_count(MgImpl* mg) { return reinterpret_cast<int*>(mg->ws + m
 // mg_setup.f90:225-307 (create_hierarchy) for one rank. The reference leaves the loop
 // only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
 // 3*2^n sizes terminate (the reference does not terminate on them).
+
+// k_mg_coarse applies when levels coarse_l0..bottom-1 exist, every level from 1 to the
+// bottom halves the one above in each direction, and their extents suit the vector block
+// functions at the chosen z chunk
+static bool coarse_levels_fit(const MgImpl* mg) {
+    const int B = mg->bottom, L = mg->nlevels;
+    if (B < mg->coarse_l0 + 1 || B >= L || B - mg->coarse_l0 + 1 > MG_COARSE_MAXLEV) return false;
+    const int zc = mg->czc, rzc = zc >= 4 ? MG_RZC : 1, pzc = zc >= 4 ? V4_ZC : 2;
+    for (int l = 1; l <= B; ++l) {
+        const int* n = mg->lev[l].n;
+        const int* p = mg->lev[l - 1].n;
+        if (mg->lev[l].vol == 0) return false;
+        for (int k = 0; k < 3; ++k)
+            if (p[k] != 2 * n[k]) return false;
+        if (l < B && (n[2] % 4 != 0 || n[0] % zc != 0 || n[0] % pzc != 0)) return false;
+        if (l > 1 && n[0] % rzc != 0) return false;
+    }
+    return true;
+}
+template <int ZC>
+static cudaError_t coarse_occupancy_zc(int* occ) {
+    const int nt = MG_BX * MG_BY;
+    int a = 0, b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_mg_coarse<true, ZC>, nt, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_mg_coarse<false, ZC>, nt, 0);
+    *occ = a < b ? a : b;
+    return e;
+}
+static cudaError_t coarse_occupancy(int zc, int* occ) {
+    return zc == 1 ? coarse_occupancy_zc<1>(occ) : (zc == 2 ? coarse_occupancy_zc<2>(occ) : coarse_occupancy_zc<4>(occ));
+}
 
 int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol, int nhist) {
     if (nhist < 0 || nhist > MG_HIST) { set_error("multigrid: history depth out of range"); return NYLES_BAD_ARG; }
@@ -1925,10 +2175,30 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int
     {
         const char* e = getenv("NYLES_GB300_SCALAR_KERNELS");
         mg->vec4 = !(e && e[0] == '1');
+        const char* c = getenv("NYLES_GB300_COARSE_ZC");
+        const int czc = c ? atoi(c) : 1;
+        mg->czc = (czc == 2 || czc == 4) ? czc : 1;
     }
     mg->off_partial = take(mg->npartial * sizeof(double));
     mg->off_partial2 = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
+    mg->off_cbar = take(64);
+    mg->coarse_blocks = 0;
+    {
+        const char* e = getenv("NYLES_GB300_COARSE_PERSISTENT");
+        mg->coarse_l0 = e ? atoi(e) : 0;
+    }
+    if (precision == NYLES_MIXED && mg->vec4 && mg->coarse_l0 >= 1 && coarse_levels_fit(mg)) {
+        {
+            int dev = 0, nsm = 0, coop = 0, occ = 0;
+            cudaError_t ce = cudaGetDevice(&dev);
+            if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+            if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+            if (ce == cudaSuccess) ce = coarse_occupancy(mg->czc, &occ);
+            if (ce != cudaSuccess) return cuda_status(ce, "multigrid coarse-level kernel setup");
+            if (coop && occ > 0) mg->coarse_blocks = nsm * (occ < 2 ? occ : 2);
+        }
+    }
     mg->bytes = off;
     return NYLES_OK;
 }
@@ -1952,13 +2222,14 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
         const Bat& bt = mg->bat;
         float2* pdf = last_mode == 1 ? mg_pdf(mg) : nullptr;
         if constexpr (sizeof(T) == sizeof(float)) {
-            if (use_v4(mg, g.n)) {
-                const dim3 gv = bgrid(mg, grid_v4(g.n));
-                if (!from_y) k_mg_jacobi_v4<0, true><<<gv, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr, bt);
+            const int zc = last_mode == 1 ? V4_ZC : lvl_zc(mg, l);
+            if (use_v4(mg, g.n, zc)) {
+                const dim3 gv = bgrid(mg, grid_v4(g.n, zc));
+                if (!from_y) launch_jacobi_v4_0<true>(zc, gv, st, g, x, b, y, om, bt);
                 if (last_mode == 1)
                     k_mg_jacobi_v4<1, true><<<gv, kBlk, 0, st>>>(g, y, b, x, om, pdf, nullptr, nullptr, nullptr, bt);
                 else
-                    k_mg_jacobi_v4<0, true><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr, bt);
+                    launch_jacobi_v4_0<true>(zc, gv, st, g, y, b, x, om, bt);
                 return;
             }
         }
@@ -1971,9 +2242,10 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
         return;
     }
     if constexpr (sizeof(T) == sizeof(float)) {
-        if (use_v4(mg, g.n)) {
-            const dim3 gv = grid_v4(g.n);
-            if (!from_y) k_mg_jacobi_v4<0><<<gv, kBlk, 0, st>>>(g, x, b, y, om, nullptr, nullptr, nullptr, nullptr);
+        const int zc = last_mode != 0 ? V4_ZC : lvl_zc(mg, l);
+        if (use_v4(mg, g.n, zc)) {
+            const dim3 gv = grid_v4(g.n, zc);
+            if (!from_y) launch_jacobi_v4_0<false>(zc, gv, st, g, x, b, y, om, Bat());
             if (last_mode == 1)
                 k_mg_jacobi_v4<1><<<gv, kBlk, 0, st>>>(g, y, b, x, om, mg_pdf(mg),
                                                       nullptr, nullptr, nullptr);
@@ -1983,7 +2255,7 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
                                                       reinterpret_cast<double*>(mg->ws + mg->off_partial),
                                                       reinterpret_cast<double*>(mg->ws + mg->off_partial2));
             else
-                k_mg_jacobi_v4<0><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr, nullptr, nullptr, nullptr);
+                launch_jacobi_v4_0<false>(zc, gv, st, g, y, b, x, om, Bat());
             return;
         }
     }
@@ -2022,15 +2294,58 @@ static void bottom(MgImpl* mg, cudaStream_t st) {
     k_mg_bottom<T><<<bgrid(mg, dim3(1, 1, 1)), MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a, mg->bat);
 }
 
+// levels coarse_l0..bottom-1 of a mixed V-cycle, one direction, as one cooperative
+// launch of k_mg_coarse (false: the per-level launches are to be used)
+static bool coarse_launch(MgImpl* mg, cudaStream_t st, bool down) {
+    if (!mg->coarse_blocks || mg->bat.tab || mg->precision != NYLES_MIXED) return false;
+    MgCoarse a;
+    a.l0 = mg->coarse_l0;
+    a.l1 = mg->bottom;
+    for (int l = a.l0; l <= a.l1; ++l) {
+        a.g[l - a.l0] = mgg(mg, l);
+        a.x[l - a.l0] = lvp<float>(mg, l, 1);
+        a.b[l - a.l0] = lvp<float>(mg, l, 2);
+        a.y[l - a.l0] = lvp<float>(mg, l, 3);
+    }
+    a.omega = (float)mg->omega;
+    a.arrivals = reinterpret_cast<unsigned long long*>(mg->ws + mg->off_cbar);
+    a.err = reinterpret_cast<unsigned int*>(mg->ws + mg->off_cbar + 8);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)mg->coarse_blocks, 1, 1);
+    cfg.blockDim = kBlk;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ProfScope ps(mg->prof, 8, st);
+    note_launch();
+    const int zc = mg->czc;
+    if (down) {
+        if (zc == 1) cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 1>, a);
+        else if (zc == 2) cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 2>, a);
+        else cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 4>, a);
+    } else {
+        if (zc == 1) cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 1>, a);
+        else if (zc == 2) cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 2>, a);
+        else cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 4>, a);
+    }
+    return true;
+}
+
 // level0_last: mode of the last level-0 half-sweep (see smooth)
 template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
     const int L = mg->nlevels;
     const int B = mg->bottom;   // < L: levels B..L-1 in one block
+    bool persistent = false;    // levels 1..B-1 in k_mg_coarse (mixed precision)
     // The first half-sweep of level 0 was written by the stop-test residual kernel that
     // precedes every V-cycle (k_mg_resid_sweep; mixed: k_mg_resid_df, from a zero
     // correction); every restricted level gets it from the restriction.
     for (int l = 0; l < L - 1 && l < B; ++l) {
+        if (l == mg->coarse_l0 && (persistent = coarse_launch(mg, st, true))) break;
         smooth<T>(mg, l, st, 0, true);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -2038,17 +2353,17 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
             note_launch();
             bool done = false;
             if constexpr (sizeof(T) == sizeof(float)) {
-                if (v4_restrict(mg, gf, gc)) {
-                    const dim3 gv((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
-                                  (unsigned)(gc.n[0] / MG_RZC));
+                const int rzc = lvl_rzc(mg, l);
+                if (v4_restrict(mg, gf, gc, rzc)) {
+                    const dim3 gv = grid_v4_restrict(gf, gc, rzc);
                     if (mg->bat.tab)
-                        k_mg_restrict_v4<true><<<bgrid(mg, gv), kBlk, 0, st>>>(
-                            gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc, lvp<float>(mg, l + 1, 2),
-                            lvp<float>(mg, l + 1, 3), (float)mg->omega, mg->bat);
+                        launch_restrict_v4<true>(rzc, bgrid(mg, gv), st, gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
+                                                 lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3), (float)mg->omega,
+                                                 mg->bat);
                     else
-                        k_mg_restrict_v4<<<gv, kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
-                                                              lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3),
-                                                              (float)mg->omega);
+                        launch_restrict_v4<false>(rzc, gv, st, gf, lvp<float>(mg, l, 1), lvp<float>(mg, l, 2), gc,
+                                                  lvp<float>(mg, l + 1, 2), lvp<float>(mg, l + 1, 3), (float)mg->omega,
+                                                  Bat());
                     done = true;
                 }
             }
@@ -2066,20 +2381,22 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
         bottom<T>(mg, st);
     else
         smooth<T>(mg, L - 1, st, L == 1 ? level0_last : 0, true);
-    for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
+    if (persistent) coarse_launch(mg, st, false);
+    for (int l = persistent ? mg->coarse_l0 - 1 : (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 10, st);
             note_launch();
             bool done = false;
             if constexpr (sizeof(T) == sizeof(float)) {
-                if (v4_prolong(mg, gf, gc)) {
+                const int pzc = lvl_pzc(mg, l);
+                if (v4_prolong(mg, gf, gc, pzc)) {
                     if (mg->bat.tab)
-                        k_mg_prolong_v4<true><<<bgrid(mg, grid_v4(gf.n)), kBlk, 0, st>>>(
-                            gf, lvp<float>(mg, l, 1), gc, lvp<float>(mg, l + 1, 1), mg->bat);
+                        launch_prolong_v4<true>(pzc, bgrid(mg, grid_v4(gf.n, pzc)), st, gf, lvp<float>(mg, l, 1), gc,
+                                                lvp<float>(mg, l + 1, 1), mg->bat);
                     else
-                        k_mg_prolong_v4<<<grid_v4(gf.n), kBlk, 0, st>>>(gf, lvp<float>(mg, l, 1), gc,
-                                                                        lvp<float>(mg, l + 1, 1));
+                        launch_prolong_v4<false>(pzc, grid_v4(gf.n, pzc), st, gf, lvp<float>(mg, l, 1), gc,
+                                                 lvp<float>(mg, l + 1, 1), Bat());
                     done = true;
                 }
             }
@@ -2420,6 +2737,7 @@ int mg_reset_history(MgImpl* mg) {
 
 int mg_zero_scalars(MgImpl* mg) {
     cudaError_t e = cudaMemset(scalars(mg), 0, 16 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(mg->ws + mg->off_cbar, 0, 64);
     if (e == cudaSuccess && mg->nhist) e = cudaMemset(mg->ws + mg->off_hist, 0, mg->nsol * sizeof(int));
     return cuda_status(e, "multigrid scalars reset");
 }

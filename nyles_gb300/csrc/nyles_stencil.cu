@@ -457,6 +457,70 @@ __device__ __forceinline__ T tr_flux32x(const T* __restrict__ q, T u, int c, int
     return tr_flux_closure(q, u, c - i, i, n, 1);
 }
 
+// ---- two FP32 reconstructions at once. Blackwell issues two FP32 lanes' worth of
+// multiply-adds in one paired instruction (__ffma2_rn, __fadd2_rn, __fmul2_rn), and the
+// FP32 right-hand side is bound by instruction issue: the two vortex-force fluxes that
+// share a direction (and so their load offsets) are reconstructed together. The same
+// formula as weno5<float>; the weights' divisions stay per component (hardware
+// reciprocal).
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 weno5_x2(float2 qmm, float2 qm, float2 q0, float2 qp, float2 qpp) {
+    typedef WenoK<float> K;
+    const float2 qi1 = __ffma2_rn(f2s(K::c116()), q0, __ffma2_rn(f2s(-K::c76()), qm, __fmul2_rn(f2s(K::c13()), qmm)));
+    const float2 qi2 = __ffma2_rn(f2s(K::c13()), qp, __ffma2_rn(f2s(K::c56()), q0, __fmul2_rn(f2s(-K::c16()), qm)));
+    const float2 qi3 = __ffma2_rn(f2s(-K::c16()), qpp, __ffma2_rn(f2s(K::c56()), qp, __fmul2_rn(f2s(K::c13()), q0)));
+    const float2 a1 = __fadd2_rn(__ffma2_rn(f2s(-2.f), qm, qmm), q0);
+    const float2 b1 = __ffma2_rn(f2s(3.f), q0, __ffma2_rn(f2s(-4.f), qm, qmm));
+    const float2 a2 = __fadd2_rn(__ffma2_rn(f2s(-2.f), q0, qm), qp);
+    const float2 b2 = __ffma2_rn(f2s(-1.f), qp, qm);
+    const float2 a3 = __fadd2_rn(__ffma2_rn(f2s(-2.f), qp, q0), qpp);
+    const float2 b3 = __fadd2_rn(__ffma2_rn(f2s(-4.f), qp, __fmul2_rn(f2s(3.f), q0)), qpp);
+    auto beta = [&](float2 a, float2 b) {
+        return __ffma2_rn(__fmul2_rn(f2s(K::k1()), a), a, __fmul2_rn(__fmul2_rn(f2s(0.25f), b), b));
+    };
+    const float2 be1 = beta(a1, b1), be2 = beta(a2, b2), be3 = beta(a3, b3);
+    const float2 t = __ffma2_rn(f2s(-1.f), be3, be1);
+    const float2 tau5 = make_float2(fabsf(t.x), fabsf(t.y));
+    const float2 d1 = __fadd2_rn(be1, f2s(K::eps5())), d2 = __fadd2_rn(be2, f2s(K::eps5())),
+                 d3 = __fadd2_rn(be3, f2s(K::eps5()));
+    const float2 r1 = make_float2(__fdividef(tau5.x, d1.x), __fdividef(tau5.y, d1.y));
+    const float2 r2 = make_float2(__fdividef(tau5.x, d2.x), __fdividef(tau5.y, d2.y));
+    const float2 r3 = make_float2(__fdividef(tau5.x, d3.x), __fdividef(tau5.y, d3.y));
+    const float2 w1 = __fadd2_rn(f2s(1.f), r1);
+    const float2 w2 = __fmul2_rn(f2s(6.f), __fadd2_rn(f2s(1.f), r2));
+    const float2 w3 = __fmul2_rn(f2s(3.f), __fadd2_rn(f2s(1.f), r3));
+    const float2 num = __ffma2_rn(w3, qi3, __ffma2_rn(w2, qi2, __fmul2_rn(w1, qi1)));
+    const float2 den = __fadd2_rn(__fadd2_rn(w1, w2), w3);
+    return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+}
+// u * weno5_x2 of the five values upwind of the face, each component on its own side
+__device__ __forceinline__ float2 weno5_upwind_x2(float2 u, const float2 (&v)[6]) {
+    const bool px = u.x > 0.f, py = u.y > 0.f;
+    auto sel = [&](int a, int b) { return make_float2(px ? v[a].x : v[b].x, py ? v[a].y : v[b].y); };
+    return __fmul2_rn(u, weno5_x2(sel(0, 5), sel(1, 4), sel(2, 3), sel(3, 2), sel(4, 1)));
+}
+// vf_flux32 of two vorticity fields along one direction (offsets o shared)
+__device__ __forceinline__ float2 vf_flux32_x2(const float* __restrict__ Wa, const float* __restrict__ Wb, float2 u1,
+                                               int c, int i, int n, int s, bool fast, const int (&o)[7]) {
+    if (fast) {
+        float2 v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = make_float2(__ldg(Wa + o[k]), __ldg(Wb + o[k]));
+        return weno5_upwind_x2(u1, v);
+    }
+    return make_float2(vf_flux_closure(Wa, u1.x, c - i * s, i, n, s), vf_flux_closure(Wb, u1.y, c - i * s, i, n, s));
+}
+__device__ __forceinline__ float2 vf_flux32x_x2(const float* __restrict__ Wa, const float* __restrict__ Wb, float2 u1,
+                                                int c, int i, int n, bool fast) {
+    if (fast) {
+        float2 v[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v[k] = make_float2(__ldg(Wa + c + (k - 3)), __ldg(Wb + c + (k - 3)));
+        return weno5_upwind_x2(u1, v);
+    }
+    return make_float2(vf_flux_closure(Wa, u1.x, c - i, i, n, 1), vf_flux_closure(Wb, u1.y, c - i, i, n, 1));
+}
+
 // vortex-force reconstruction of vf_flux given u1: q(kk) = W(kk - 1), q(0) = 0
 template <typename T>
 __device__ __forceinline__ T vf_flux32(const T* __restrict__ W, T u1, int c, int i, int n, int s, bool fast,
@@ -480,8 +544,9 @@ __device__ __forceinline__ T vf_flux32x(const T* __restrict__ W, T u1, int c, in
     return vf_flux_closure(W, u1, c - i, i, n, 1);
 }
 
-// blocks per SM asked of the register allocator: 48 registers hold the kernel without
-// spills once the closure branches are out of line (inlined, they took it to 64)
+// blocks per SM asked of the register allocator: 48 registers (the closure branches out
+// of line; inlined, they took it to 64). The paired reconstructions spill a few values
+// at 48 and still beat 4 blocks per SM at 64 registers (2.28 vs 2.41 ms per 256^3 step)
 template <typename T> struct LesMinBlocks { static constexpr int n = 5; };
 
 template <typename T, bool BAT>
@@ -543,17 +608,25 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY, LesMinBlocks<T>::n) k_rhs_les(c
 #pragma unroll
             for (int k = 0; k < 7; ++k) oz[k] = c + (k - 3) * sz;
             fz = tr_flux32(b, __ldg(U2 + c), c, z, Nz, sz, zt, oz);
-            if (ylo) {   // u_j += U^k w_i along k (U^k averaged along j)
+            // f4 (ylo): u_j += U^k w_i along k (U^k averaged along j); f5 (xlo): u_i -= U^k
+            // w_j along k (U^k averaged along i); reconstructed as a pair
+            float2 u45 = make_float2(0.f, 0.f);
+            if (ylo) {
                 const T uu1 = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + sy));
                 const T uu0 = z > 0 ? uu_zy : T(0);
                 uu_zy = uu1;
-                f4 = vf_flux32(W0, T(0.5) * (uu0 + uu1), c, z, Nz, sz, zv, oz);
+                u45.x = T(0.5) * (uu0 + uu1);
             }
-            if (xlo) {   // u_i -= U^k w_j along k (U^k averaged along i)
+            if (xlo) {
                 const T uu1 = T(0.5) * (__ldg(U2 + c) + __ldg(U2 + c + 1));
                 const T uu0 = z > 0 ? uu_zx : T(0);
                 uu_zx = uu1;
-                f5 = vf_flux32(W1, T(0.5) * (uu0 + uu1), c, z, Nz, sz, zv, oz);
+                u45.y = T(0.5) * (uu0 + uu1);
+            }
+            if (ylo || xlo) {
+                const float2 f45 = vf_flux32_x2(W0, W1, u45, c, z, Nz, sz, zv, oz);
+                f4 = f45.x;
+                f5 = f45.y;
             }
         }
         T fy, fym, f2 = T(0), f3 = T(0);
@@ -566,15 +639,23 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY, LesMinBlocks<T>::n) k_rhs_les(c
             __syncthreads();
             fym = (ty > 0) ? sfy[ty - 1][tx] : T(0);
             __syncthreads();
-            if (xlo) {   // u_i += U^j w_k along j (U^j averaged along i)
+            // f2 (xlo): u_i += U^j w_k along j (U^j averaged along i); f3 (zlo): u_k -= U^j
+            // w_i along j (U^j averaged along k)
+            float2 u23 = make_float2(0.f, 0.f);
+            if (xlo) {
                 const T uu1 = T(0.5) * (__ldg(U1 + c) + __ldg(U1 + c + 1));
                 const T uu0 = ys > 0 ? T(0.5) * (__ldg(U1 + c - sy) + __ldg(U1 + c - sy + 1)) : T(0);
-                f2 = vf_flux32(W2, T(0.5) * (uu0 + uu1), c, ys, Ny, sy, yv, oy);
+                u23.x = T(0.5) * (uu0 + uu1);
             }
-            if (zlo) {   // u_k -= U^j w_i along j (U^j averaged along k)
+            if (zlo) {
                 const T uu1 = T(0.5) * (__ldg(U1 + c) + __ldg(U1 + c + sz));
                 const T uu0 = ys > 0 ? T(0.5) * (__ldg(U1 + c - sy) + __ldg(U1 + c - sy + sz)) : T(0);
-                f3 = vf_flux32(W0, T(0.5) * (uu0 + uu1), c, ys, Ny, sy, yv, oy);
+                u23.y = T(0.5) * (uu0 + uu1);
+            }
+            if (xlo || zlo) {
+                const float2 f23 = vf_flux32_x2(W2, W0, u23, c, ys, Ny, sy, yv, oy);
+                f2 = f23.x;
+                f3 = f23.y;
             }
         }
         if (ty == 0 && ys > 0) {   // the face below the block's first row
@@ -590,17 +671,25 @@ __global__ void __launch_bounds__(RZ_BX * RZ_BY, LesMinBlocks<T>::n) k_rhs_les(c
             fxm = __shfl_up_sync(0xffffffffu, fx, 1);
             if (tx == 0 && xs > 0) fxm = tr_flux32x(b, __ldg(U0 + c - 1), c - 1, xs - 1, Nx,
                                                      xs - 1 >= 2 && xs - 1 <= Nx - 4);
-            if (ylo) {   // u_j -= U^i w_k along i (U^i averaged along j)
+            // f1 (ylo): u_j -= U^i w_k along i (U^i averaged along j); f6 (zlo): u_k += U^i
+            // w_j along i (U^i averaged along k)
+            float2 u16 = make_float2(0.f, 0.f);
+            if (ylo) {
                 const T uu1 = T(0.5) * (__ldg(U0 + c) + __ldg(U0 + c + sy));
                 T uu0 = __shfl_up_sync(0xffffffffu, uu1, 1);
                 if (tx == 0) uu0 = xs > 0 ? T(0.5) * (__ldg(U0 + c - 1) + __ldg(U0 + c - 1 + sy)) : T(0);
-                f1 = vf_flux32x(W2, T(0.5) * (uu0 + uu1), c, xs, Nx, xv);
+                u16.x = T(0.5) * (uu0 + uu1);
             }
-            if (zlo) {   // u_k += U^i w_j along i (U^i averaged along k)
+            if (zlo) {
                 const T uu1 = T(0.5) * (__ldg(U0 + c) + __ldg(U0 + c + sz));
                 T uu0 = __shfl_up_sync(0xffffffffu, uu1, 1);
                 if (tx == 0) uu0 = xs > 0 ? T(0.5) * (__ldg(U0 + c - 1) + __ldg(U0 + c - 1 + sz)) : T(0);
-                f6 = vf_flux32x(W1, T(0.5) * (uu0 + uu1), c, xs, Nx, xv);
+                u16.y = T(0.5) * (uu0 + uu1);
+            }
+            if (ylo || zlo) {
+                const float2 f16 = vf_flux32x_x2(W2, W1, u16, c, xs, Nx, xv);
+                f1 = f16.x;
+                f6 = f16.y;
             }
         }
         // ---- buoyancy advection, summed as TracerMarch::step

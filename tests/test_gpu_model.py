@@ -393,7 +393,13 @@ _SOLVES_CODE = (
     "print(' '.join(str(o[0]) for o in out))\n")
 
 
-def _mixed_solves(tmp_path, tag, **env_extra):
+# grids whose multigrid has levels between level 0 and the one-block bottom (the bottom
+# takes the coarsest levels that fit in shared memory): 64^3 -> level 1, 128^3 -> 1 and 2
+_COARSE_CASES = ("[('perio_xy', (128, 128, 128)), ('closed', (128, 64, 64)), ('perio_xyz', (64, 64, 64)),"
+                 " ('perio_x', (64, 64, 128))]")
+
+
+def _mixed_solves(tmp_path, tag, code=None, **env_extra):
     """FCG solves and single stationary V-cycles of a seeded right-hand side on every
     topology (and on 3·2^n grids, whose coarser levels leave the vector kernels' shapes
     part-way down), in a fresh process with the given environment (the kernel switches
@@ -405,10 +411,31 @@ def _mixed_solves(tmp_path, tag, **env_extra):
     root = os.path.dirname(helpers.HERE)
     env = dict(os.environ, PYTHONPATH=root, **env_extra)
     fn = str(tmp_path / ("solves_%s.npz" % tag))
-    r = subprocess.run([sys.executable, "-c", _SOLVES_CODE, fn], env=env, capture_output=True, text=True, cwd=root)
+    r = subprocess.run([sys.executable, "-c", code or _SOLVES_CODE, fn], env=env, capture_output=True, text=True,
+                       cwd=root)
     assert r.returncode == 0, r.stderr[-2000:]
     with np.load(fn) as f:
         return [int(v) for v in r.stdout.split()], [f["arr_%d" % i] for i in range(len(f.files))]
+
+
+def test_coarse_level_launches_match_per_level_launches(tmp_path):
+    """The levels below level 0 of the mixed V-cycle with 1, 2 or 4 z cells per thread,
+    one launch per half-sweep, restriction and prolongation or (from level 1 or 2 to the
+    bottom) one persistent cooperative launch per direction (k_mg_coarse), against one
+    launch per pass with 4: the decomposition changes, the arithmetic of every cell does
+    not, so the FCG solves take the same iterations and every solution and one-cycle
+    iterate is equal bit for bit."""
+    code = _SOLVES_CODE.replace("cases = [(t, (64, 32, 32)) for t in ('closed', 'perio_x', 'perio_y', 'perio_xy')]",
+                                "cases = " + _COARSE_CASES)
+    assert code != _SOLVES_CODE
+    ref = _mixed_solves(tmp_path, "levels", code, NYLES_GB300_COARSE_PERSISTENT="0", NYLES_GB300_COARSE_ZC="4")
+    for zc in ("1", "2", "4"):
+        for pers in ("0", "1", "2"):
+            got = _mixed_solves(tmp_path, "c%s%s" % (pers, zc), code, NYLES_GB300_COARSE_PERSISTENT=pers,
+                                NYLES_GB300_COARSE_ZC=zc)
+            assert got[0] == ref[0], (zc, pers, got[0], ref[0])
+            for a, c in zip(got[1], ref[1]):
+                np.testing.assert_array_equal(a, c)
 
 
 def test_vector_kernels_match_scalar_kernels(tmp_path):
