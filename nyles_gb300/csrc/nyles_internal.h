@@ -141,19 +141,15 @@ struct MgImpl {
     // search direction and its image under the operator, level-1 floats
     int krylov = 0;
     size_t off_fp = 0, off_fq = 0;
+    int fcg_k = 0;                    // iteration of the V-cycle being enqueued (-1: read on the device)
     // 4-cell vector kernels where the level-1 extents allow (off with the environment
     // variable NYLES_GB300_SCALAR_KERNELS=1, read when the solver is created)
     bool vec4 = true;
     // z-chunk of the vector kernels below level 0 (cells per thread along z: 1, 2 or 4;
     // NYLES_GB300_COARSE_ZC, read when the solver is created); level 0 keeps 4
     int czc = 1;
-    // levels coarse_l0..bottom-1 of the mixed V-cycle in one cooperative launch per
-    // direction (k_mg_coarse; NYLES_GB300_COARSE_PERSISTENT = coarse_l0, off by default:
-    // per-level launches measured faster): its grid (0: off) and its barrier counter and
-    // error flag in the workspace
-    int coarse_blocks = 0;
-    int coarse_l0 = 0;
-    size_t off_cbar = 0;
+    // the ticket counter of reductions finished by their kernel's last block (MgFin)
+    size_t off_ticket = 0;
     size_t off_partial = 0, off_partial2 = 0, off_scalars = 0;
     int npartial = 0;
     size_t bytes = 0;

@@ -256,6 +256,84 @@ __device__ __forceinline__ void block_partial2_f(float s, float t, double* __res
     }
 }
 
+// ---- the final sum of a reduction folded into the kernel that stores the partials
+// The block that stores its partial last (a ticket from an atomic counter, taken after
+// a fence that orders every block's partial store before its ticket) adds all partials
+// in block order and finishes the reduction itself, instead of a separate one-block
+// launch after the kernel; it resets the counter for the next launch. `ticket` lies in
+// the solver's workspace (zeroed when the workspace is bound; batched launches: each
+// run's own). The sum's order depends on the grid only, so results are deterministic.
+struct MgFin {
+    unsigned int* ticket = nullptr;   // null: the partials are summed by a later launch
+    double* sc = nullptr;             // the solve's scalars (shifted to the run in batched launches)
+    int k = 0;                        // Krylov iteration (-1: read sc[SC_NITE])
+    double vol = 0.0;                 // level-0 cells
+};
+__device__ __forceinline__ bool mg_last_block(unsigned int* ticket, unsigned int nblk) {
+    __shared__ unsigned int s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const unsigned int t = atomicAdd(ticket, 1u);
+        s_last = (t == nblk - 1) ? 1u : 0u;
+        if (s_last) atomicExch(ticket, 0u);
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+// totals of n partials of one or two sums, added in a fixed order by the threads of a
+// MG_BX x MG_BY block (loads through L2: other blocks of the launch stored them); the
+// result is valid in thread (0, 0)
+__device__ __forceinline__ double2 mg_block_total2(const double* pa, const double* pb, int n) {
+    __shared__ double sm[2][MG_BX * MG_BY / 32];
+    const int tid = threadIdx.y * MG_BX + threadIdx.x;
+    double a = 0.0, b = 0.0;
+    for (int i = tid; i < n; i += MG_BX * MG_BY) {
+        a += __ldcg(pa + i);
+        if (pb) b += __ldcg(pb + i);
+    }
+    a = warp_sum(a);
+    b = warp_sum(b);
+    if ((tid & 31) == 0) {
+        sm[0][tid >> 5] = a;
+        sm[1][tid >> 5] = b;
+    }
+    __syncthreads();
+    double2 r = make_double2(0.0, 0.0);
+    if (tid < 32) {
+        double x = (tid < MG_BX * MG_BY / 32) ? sm[0][tid] : 0.0;
+        double y = (tid < MG_BX * MG_BY / 32) ? sm[1][tid] : 0.0;
+        x = warp_sum(x);
+        y = warp_sum(y);
+        r = make_double2(x, y);
+    }
+    return r;
+}
+// beta = -(z.q)/(p.q) of the previous iteration (0 on the first: k = iteration of this
+// solve, or sc[SC_NITE] when k < 0) stored as a float, and the mean of z (float)
+__device__ __forceinline__ void fcg_set_beta(double zq, double zs, double vol, double* sc, int k) {
+    const int it = k >= 0 ? k : (int)sc[SC_NITE];
+    const double pq = sc[SC_PQ];
+    double beta = (it > 0 && pq != 0.0) ? -zq / pq : 0.0;
+    if (!isfinite(beta)) beta = 0.0;
+    double zmean = zs / vol;
+    if (!isfinite(zmean)) zmean = 0.0;
+    sc[SC_ZQ] = zq;
+    reinterpret_cast<float*>(sc + SC_BETA)[0] = (float)beta;
+    reinterpret_cast<float*>(sc + SC_ZMEAN)[0] = (float)zmean;
+}
+// alpha = (p.r)/(p.q) stored as a float pair
+__device__ __forceinline__ void fcg_set_alpha(double pq, double pr, double* sc) {
+    double alpha = pq != 0.0 ? pr / pq : 0.0;
+    if (!isfinite(alpha)) alpha = 0.0;
+    sc[SC_PQ] = pq;
+    sc[SC_PR] = pr;
+    const float hi = (float)alpha;
+    float2* a2 = reinterpret_cast<float2*>(sc + SC_ALPHA);
+    *a2 = make_float2(hi, (float)(alpha - (double)hi));
+}
+
 // one damped-Jacobi half-sweep, out = (1-omega)*in + omega*(sum(in_nb) - b)*idiag
 // (basicoperators.f90:379-398). MODE 0 stores it; MODE 1 adds it to the float-pair
 // solution `acc` instead (mixed precision: the correction of iterative refinement,
@@ -351,20 +429,12 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
 
-// Loads of the vector level kernels. LdPlain: ordinary loads (nothing the kernel reads
-// is written during its launch). LdCoherent: loads through L2 (ld.global.cg) for the
-// persistent coarse-level kernel, whose passes read what other blocks wrote in earlier
-// passes of the same launch: the read-only and L1 paths are not coherent within a
-// launch.
+// Loads of the vector level kernels (a policy type, so that a kernel whose passes read
+// what other blocks of the same launch wrote could route them through L2).
 struct LdPlain {
     static __device__ __forceinline__ float4 f4(const float* p) { return *reinterpret_cast<const float4*>(p); }
     static __device__ __forceinline__ float2 f2(const float* p) { return *reinterpret_cast<const float2*>(p); }
     static __device__ __forceinline__ float f1(const float* p) { return *p; }
-};
-struct LdCoherent {
-    static __device__ __forceinline__ float4 f4(const float* p) { return __ldcg(reinterpret_cast<const float4*>(p)); }
-    static __device__ __forceinline__ float2 f2(const float* p) { return __ldcg(reinterpret_cast<const float2*>(p)); }
-    static __device__ __forceinline__ float f1(const float* p) { return __ldcg(p); }
 };
 template <typename L>
 __device__ __forceinline__ float mg_ldw_l(const float* a, long long c, bool wet) {
@@ -463,7 +533,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
                                                                float omega, float2* __restrict__ acc,
                                                                const float* __restrict__ dot,
                                                                double* __restrict__ partial,
-                                                               double* __restrict__ partial2, const Bat bat = Bat()) {
+                                                               double* __restrict__ partial2, const Bat bat = Bat(),
+                                                               const MgFin fin = MgFin()) {
     int bz = blockIdx.z;
     if constexpr (BAT) {
         long long dlt;
@@ -478,7 +549,17 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
     }
     float sdot = 0.f, ssum = 0.f;
     mg_jacobi_v4_blk<MODE, ZC, LdPlain>(g, in, b, out, omega, acc, dot, blockIdx.x, blockIdx.y, bz, sdot, ssum);
-    if (MODE == 2) block_partial2_f(sdot, ssum, partial, partial2, bz);
+    if constexpr (MODE == 2) {
+        block_partial2_f(sdot, ssum, partial, partial2, bz);
+        // the Krylov solve's beta and mean of z from the totals (k_fcg_final_beta's work)
+        if (!BAT && fin.ticket) {
+            const unsigned int nblk = gridDim.x * gridDim.y * gridDim.z;
+            if (mg_last_block(fin.ticket, nblk)) {
+                const double2 t = mg_block_total2(partial, partial2, (int)nblk);
+                if (threadIdx.x == 0 && threadIdx.y == 0) fcg_set_beta(t.x, t.y, fin.vol, fin.sc, fin.k);
+            }
+        }
+    }
 }
 
 // First half-sweep of a level whose solution is zero: (1-omega)*0 + omega*(0-b)*idiag
@@ -855,131 +936,6 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
         xc = bshift(xc, dlt);
     }
     mg_prolong_v4_blk<ZC, LdPlain>(gf, xf, gc, xc, blockIdx.x, blockIdx.y, bz);
-}
-
-// ---------------------------------------------------------------- coarse levels, persistent
-// Below level 0 every half-sweep, restriction and prolongation is a launch of a few
-// microseconds whatever the level's size: launch latency, not work. k_mg_coarse runs the
-// levels l0..l1-1 of one V-cycle direction in one cooperative launch instead (all blocks
-// resident, 1-D grid): each pass is the vector block function of the per-level kernel
-// applied to the blocks of that kernel's grid in turn, passes are separated by a grid
-// barrier, and every load goes through L2 (LdCoherent), since a pass reads what other
-// blocks wrote in the passes before it. Down (solvers.f90:35-55 from l0 to the bottom):
-// per level the second pre-smoothing half-sweep (y -> x; the first came with b) and the
-// restriction into l + 1 (its b and first half-sweep). Up: per level from l1 - 1 to l0
-// the prolongation of x(l + 1) into x(l) and the two post-smoothing half-sweeps. The
-// arithmetic is the per-level kernels', so the V-cycle is the same to the last bit.
-constexpr int MG_COARSE_MAXLEV = 12;
-constexpr unsigned long long MG_BAR_SPIN_LIMIT = 1ull << 22;   // x 64 ns sleeps: a few tenths of a second
-struct MgCoarse {
-    int l0, l1;                        // levels l0..l1-1 are smoothed; l1 is the bottom
-    MgGeom g[MG_COARSE_MAXLEV];        // levels l0..l1, indexed l - l0
-    float* x[MG_COARSE_MAXLEV];
-    float* b[MG_COARSE_MAXLEV];
-    float* y[MG_COARSE_MAXLEV];
-    float omega;
-    unsigned long long* arrivals;      // barrier arrivals since the workspace was bound
-    unsigned int* err;                 // set when a barrier gave up waiting
-};
-
-// Grid barrier: every block adds one arrival to a 64-bit counter that only grows (one
-// barrier = nblk arrivals, launches do whole barriers), and waits until the count reaches
-// the end of its barrier's group. The wait is bounded: a block that gives up sets *err
-// and goes on; the launch then poisons its output (see k_mg_coarse).
-__device__ __forceinline__ void mg_grid_sync(unsigned long long* arrivals, unsigned int* err) {
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        const unsigned long long nblk = gridDim.x;
-        __threadfence();   // this block's stores of the pass before its arrival
-        const unsigned long long t = atomicAdd(arrivals, 1ull);
-        const unsigned long long target = (t / nblk + 1) * nblk;
-        unsigned long long it = 0, v;
-        while (true) {
-            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(arrivals) : "memory");
-            if (v >= target) break;
-            if (++it > MG_BAR_SPIN_LIMIT) {
-                atomicExch(err, 1u);
-                break;
-            }
-            __nanosleep(64);
-        }
-        __threadfence();
-    }
-    __syncthreads();
-}
-
-// block (bx, by, bz) of virtual block vb of a grid (gx, gy, *)
-__device__ __forceinline__ void mg_vblock(int vb, const dim3& gd, int& bx, int& by, int& bz) {
-    bx = vb % (int)gd.x;
-    const int t = vb / (int)gd.x;
-    by = t % (int)gd.y;
-    bz = t / (int)gd.y;
-}
-
-template <bool DOWN, int ZC>
-__global__ void __launch_bounds__(MG_BX * MG_BY, 2) k_mg_coarse(const MgCoarse a) {
-    constexpr int RZC = ZC >= 4 ? MG_RZC : 1;   // coarse planes per restriction thread
-    constexpr int PZC = ZC >= 4 ? V4_ZC : 2;    // fine planes per prolongation thread
-    const float om = a.omega;
-    float sd = 0.f, ss = 0.f;
-    auto jacobi = [&](int l, const float* in, float* out) {
-        const MgGeom& g = a.g[l - a.l0];
-        const dim3 gd((unsigned)((g.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((g.n[1] + MG_BY - 1) / MG_BY),
-                      (unsigned)(g.n[0] / ZC));
-        const int nvb = (int)(gd.x * gd.y * gd.z);
-        for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-            int bx, by, bz;
-            mg_vblock(vb, gd, bx, by, bz);
-            mg_jacobi_v4_blk<0, ZC, LdCoherent>(g, in, a.b[l - a.l0], out, om, nullptr, nullptr, bx, by, bz, sd, ss);
-        }
-    };
-    if (DOWN) {
-        for (int l = a.l0; l < a.l1; ++l) {
-            const int i = l - a.l0;
-            jacobi(l, a.y[i], a.x[i]);
-            mg_grid_sync(a.arrivals, a.err);
-            const MgGeom& gf = a.g[i];
-            const MgGeom& gc = a.g[i + 1];
-            const dim3 gd((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
-                          (unsigned)(gc.n[0] / RZC));
-            const int nvb = (int)(gd.x * gd.y * gd.z);
-            for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-                int bx, by, bz;
-                mg_vblock(vb, gd, bx, by, bz);
-                mg_restrict_v4_blk<RZC, LdCoherent>(gf, a.x[i], a.b[i], gc, a.b[i + 1], a.y[i + 1], om, bx, by, bz);
-            }
-            if (l + 1 < a.l1) mg_grid_sync(a.arrivals, a.err);
-        }
-    } else {
-        for (int l = a.l1 - 1; l >= a.l0; --l) {
-            const int i = l - a.l0;
-            const MgGeom& gf = a.g[i];
-            const MgGeom& gc = a.g[i + 1];
-            const dim3 gd((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gf.n[1] + MG_BY - 1) / MG_BY),
-                          (unsigned)(gf.n[0] / PZC));
-            const int nvb = (int)(gd.x * gd.y * gd.z);
-            for (int vb = blockIdx.x; vb < nvb; vb += gridDim.x) {
-                int bx, by, bz;
-                mg_vblock(vb, gd, bx, by, bz);
-                mg_prolong_v4_blk<PZC, LdCoherent>(gf, a.x[i], gc, a.x[i + 1], bx, by, bz);
-            }
-            mg_grid_sync(a.arrivals, a.err);
-            jacobi(l, a.x[i], a.y[i]);
-            mg_grid_sync(a.arrivals, a.err);
-            jacobi(l, a.y[i], a.x[i]);
-            if (l > a.l0) mg_grid_sync(a.arrivals, a.err);
-        }
-    }
-    // A barrier that gave up leaves the passes unordered: the level handed on (the
-    // bottom's right-hand side going down, x of level l0 going up) becomes NaN, so the
-    // solve's stop test reports a non-finite residual instead of a wrong answer.
-    if (*(volatile unsigned int*)a.err) {
-        const int i = DOWN ? a.l1 - a.l0 : 0;
-        float* const v = DOWN ? a.b[i] : a.x[i];
-        const long long n = (long long)a.g[i].n[0] * a.g[i].n[1] * a.g[i].n[2];
-        const long long t0 = (long long)blockIdx.x * blockDim.x * blockDim.y + threadIdx.y * blockDim.x + threadIdx.x;
-        for (long long q = t0; q < n; q += (long long)gridDim.x * blockDim.x * blockDim.y) v[q] = __int_as_float(0x7fc00000);
-    }
 }
 
 // ---------------------------------------------------------------- coarse levels in one block
@@ -1428,7 +1384,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
                                                                     float* __restrict__ r32, float* __restrict__ y32,
                                                                     float omega, const double* __restrict__ sc,
                                                                     double* __restrict__ partial,
-                                                                    const Bat bat = Bat()) {
+                                                                    const Bat bat = Bat(), MgFin fin = MgFin()) {
     int bz = blockIdx.z;
     if constexpr (BAT) {
         long long dlt;
@@ -1439,6 +1395,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
         y32 = bshift(y32, dlt);
         sc = bshift(sc, dlt);
         partial = bshift(partial, dlt);
+        fin.ticket = bshift(fin.ticket, dlt);
+        fin.sc = bshift(fin.sc, dlt);
     }
     const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
     const int nx4 = nx >> 2;
@@ -1517,6 +1475,14 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 3) k_mg_resid_df_v4(const MgGeo
         zc = zp;
     }
     block_partial_f(s, sc[SC_INVSCALE2], partial, bz);
+    // sum(r^2) into sc[SC_RR] (k_mg_final's work)
+    if (fin.ticket) {
+        const unsigned int nblk = gridDim.x * gridDim.y * (gridDim.z / (BAT ? bat.nrun : 1));
+        if (mg_last_block(fin.ticket, nblk)) {
+            const double2 t = mg_block_total2(partial, nullptr, (int)nblk);
+            if (threadIdx.x == 0 && threadIdx.y == 0) fin.sc[SC_RR] = t.x;
+        }
+    }
 }
 
 // ---------------------------------------------------------------- Krylov acceleration
@@ -1557,17 +1523,7 @@ __global__ void k_fcg_final_beta(const double* __restrict__ pzq, const double* _
         double zq = in ? sm[0][threadIdx.x] : 0.0, zs = in ? sm[1][threadIdx.x] : 0.0;
         zq = warp_sum(zq);
         zs = warp_sum(zs);
-        if (threadIdx.x == 0) {
-            const int it = k >= 0 ? k : (int)sc[SC_NITE];
-            const double pq = sc[SC_PQ];
-            double beta = (it > 0 && pq != 0.0) ? -zq / pq : 0.0;
-            if (!isfinite(beta)) beta = 0.0;
-            double zmean = zs / vol;
-            if (!isfinite(zmean)) zmean = 0.0;
-            sc[SC_ZQ] = zq;
-            reinterpret_cast<float*>(sc + SC_BETA)[0] = (float)beta;
-            reinterpret_cast<float*>(sc + SC_ZMEAN)[0] = (float)zmean;
-        }
+        if (threadIdx.x == 0) fcg_set_beta(zq, zs, vol, sc, k);
     }
 }
 
@@ -1637,7 +1593,8 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_fcg_direction_v4(const MgG
                                                                     const float* __restrict__ r, float* __restrict__ p,
                                                                     float* __restrict__ q,
                                                                     const double* __restrict__ sc,
-                                                                    double* __restrict__ ppq, double* __restrict__ ppr) {
+                                                                    double* __restrict__ ppq, double* __restrict__ ppr,
+                                                                    const MgFin fin = MgFin()) {
     const int nx = g.n[2], ny = g.n[1], nz = g.n[0];
     const int nx4 = nx >> 2;
     const int lane = threadIdx.x;
@@ -1715,6 +1672,14 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_fcg_direction_v4(const MgG
         zc = zp;
     }
     block_partial2_f(spq, spr, ppq, ppr, blockIdx.z);
+    // alpha from the totals of p.q and p.r (k_fcg_final_alpha's work)
+    if (fin.ticket) {
+        const unsigned int nblk = gridDim.x * gridDim.y * gridDim.z;
+        if (mg_last_block(fin.ticket, nblk)) {
+            const double2 t = mg_block_total2(ppq, ppr, (int)nblk);
+            if (threadIdx.x == 0 && threadIdx.y == 0) fcg_set_alpha(t.x, t.y, fin.sc);
+        }
+    }
 }
 
 // sums of p.q and p.r, then alpha = (p.r)/(p.q) stored as a float pair
@@ -1738,15 +1703,7 @@ __global__ void k_fcg_final_alpha(const double* __restrict__ ppq, const double* 
         double pq = in ? sm[0][threadIdx.x] : 0.0, pr = in ? sm[1][threadIdx.x] : 0.0;
         pq = warp_sum(pq);
         pr = warp_sum(pr);
-        if (threadIdx.x == 0) {
-            double alpha = pq != 0.0 ? pr / pq : 0.0;
-            if (!isfinite(alpha)) alpha = 0.0;
-            sc[SC_PQ] = pq;
-            sc[SC_PR] = pr;
-            const float hi = (float)alpha;
-            float2* a2 = reinterpret_cast<float2*>(sc + SC_ALPHA);
-            *a2 = make_float2(hi, (float)(alpha - (double)hi));
-        }
+        if (threadIdx.x == 0) fcg_set_alpha(pq, pr, sc);
     }
 }
 
@@ -1968,6 +1925,12 @@ static inline dim3 grid_v4_restrict(const MgGeom& gf, const MgGeom& gc, int rzc)
     return dim3((unsigned)((gf.n[2] / 4 + MG_BX - 1) / MG_BX), (unsigned)((gc.n[1] + MG_BY - 1) / MG_BY),
                 (unsigned)(gc.n[0] / rzc));
 }
+// ticket counter of the reductions folded into their kernels (MgFin), in a workspace
+// slot zeroed when the workspace is bound
+static inline unsigned int* fin_ticket(MgImpl* mg) {
+    return reinterpret_cast<unsigned int*>(mg->ws + mg->off_ticket);
+}
+
 // the vector transfers between levels l and l + 1: exact halving in every direction,
 // fine nx divisible by 4, and the z chunk of each kernel dividing its extent
 static inline bool v4_restrict(const MgImpl* mg, const MgGeom& gf, const MgGeom& gc, int rzc) {
@@ -2062,37 +2025,6 @@ static int* mg_hist_count(MgImpl* mg) { return reinterpret_cast<int*>(mg->ws + m
 // only when x == 2 or y == 2; here coarsening also stops before an odd extent, so
 // 3*2^n sizes terminate (the reference does not terminate on them).
 
-// k_mg_coarse applies when levels coarse_l0..bottom-1 exist, every level from 1 to the
-// bottom halves the one above in each direction, and their extents suit the vector block
-// functions at the chosen z chunk
-static bool coarse_levels_fit(const MgImpl* mg) {
-    const int B = mg->bottom, L = mg->nlevels;
-    if (B < mg->coarse_l0 + 1 || B >= L || B - mg->coarse_l0 + 1 > MG_COARSE_MAXLEV) return false;
-    const int zc = mg->czc, rzc = zc >= 4 ? MG_RZC : 1, pzc = zc >= 4 ? V4_ZC : 2;
-    for (int l = 1; l <= B; ++l) {
-        const int* n = mg->lev[l].n;
-        const int* p = mg->lev[l - 1].n;
-        if (mg->lev[l].vol == 0) return false;
-        for (int k = 0; k < 3; ++k)
-            if (p[k] != 2 * n[k]) return false;
-        if (l < B && (n[2] % 4 != 0 || n[0] % zc != 0 || n[0] % pzc != 0)) return false;
-        if (l > 1 && n[0] % rzc != 0) return false;
-    }
-    return true;
-}
-template <int ZC>
-static cudaError_t coarse_occupancy_zc(int* occ) {
-    const int nt = MG_BX * MG_BY;
-    int a = 0, b = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_mg_coarse<true, ZC>, nt, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_mg_coarse<false, ZC>, nt, 0);
-    *occ = a < b ? a : b;
-    return e;
-}
-static cudaError_t coarse_occupancy(int zc, int* occ) {
-    return zc == 1 ? coarse_occupancy_zc<1>(occ) : (zc == 2 ? coarse_occupancy_zc<2>(occ) : coarse_occupancy_zc<4>(occ));
-}
-
 int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int nsol, int nhist) {
     if (nhist < 0 || nhist > MG_HIST) { set_error("multigrid: history depth out of range"); return NYLES_BAD_ARG; }
     if (nx < 2 || ny < 2 || nz < 1) { set_error("multigrid: grid too small"); return NYLES_BAD_ARG; }
@@ -2182,23 +2114,7 @@ int mg_init(MgImpl* mg, int nx, int ny, int nz, int topology, int precision, int
     mg->off_partial = take(mg->npartial * sizeof(double));
     mg->off_partial2 = take(mg->npartial * sizeof(double));
     mg->off_scalars = take(16 * sizeof(double));
-    mg->off_cbar = take(64);
-    mg->coarse_blocks = 0;
-    {
-        const char* e = getenv("NYLES_GB300_COARSE_PERSISTENT");
-        mg->coarse_l0 = e ? atoi(e) : 0;
-    }
-    if (precision == NYLES_MIXED && mg->vec4 && mg->coarse_l0 >= 1 && coarse_levels_fit(mg)) {
-        {
-            int dev = 0, nsm = 0, coop = 0, occ = 0;
-            cudaError_t ce = cudaGetDevice(&dev);
-            if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-            if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-            if (ce == cudaSuccess) ce = coarse_occupancy(mg->czc, &occ);
-            if (ce != cudaSuccess) return cuda_status(ce, "multigrid coarse-level kernel setup");
-            if (coop && occ > 0) mg->coarse_blocks = nsm * (occ < 2 ? occ : 2);
-        }
-    }
+    mg->off_ticket = take(64);
     mg->bytes = off;
     return NYLES_OK;
 }
@@ -2249,11 +2165,18 @@ static void smooth(MgImpl* mg, int l, cudaStream_t st, int last_mode, bool from_
             if (last_mode == 1)
                 k_mg_jacobi_v4<1><<<gv, kBlk, 0, st>>>(g, y, b, x, om, mg_pdf(mg),
                                                       nullptr, nullptr, nullptr);
-            else if (last_mode == 2)
+            else if (last_mode == 2) {   // also beta and the mean of z for the Krylov update
+                MgFin fin;
+                fin.ticket = fin_ticket(mg);
+                fin.sc = reinterpret_cast<double*>(mg->ws + mg->off_scalars);
+                fin.k = mg->fcg_k;
+                fin.vol = (double)mg->lev[0].vol;
                 k_mg_jacobi_v4<2><<<gv, kBlk, 0, st>>>(g, y, b, x, om, nullptr,
                                                       reinterpret_cast<const float*>(mg->ws + mg->off_fq),
                                                       reinterpret_cast<double*>(mg->ws + mg->off_partial),
-                                                      reinterpret_cast<double*>(mg->ws + mg->off_partial2));
+                                                      reinterpret_cast<double*>(mg->ws + mg->off_partial2), Bat(),
+                                                      fin);
+            }
             else
                 launch_jacobi_v4_0<false>(zc, gv, st, g, y, b, x, om, Bat());
             return;
@@ -2294,58 +2217,15 @@ static void bottom(MgImpl* mg, cudaStream_t st) {
     k_mg_bottom<T><<<bgrid(mg, dim3(1, 1, 1)), MgBottomThreads<T>::n, mg->bottom_smem, st>>>(a, mg->bat);
 }
 
-// levels coarse_l0..bottom-1 of a mixed V-cycle, one direction, as one cooperative
-// launch of k_mg_coarse (false: the per-level launches are to be used)
-static bool coarse_launch(MgImpl* mg, cudaStream_t st, bool down) {
-    if (!mg->coarse_blocks || mg->bat.tab || mg->precision != NYLES_MIXED) return false;
-    MgCoarse a;
-    a.l0 = mg->coarse_l0;
-    a.l1 = mg->bottom;
-    for (int l = a.l0; l <= a.l1; ++l) {
-        a.g[l - a.l0] = mgg(mg, l);
-        a.x[l - a.l0] = lvp<float>(mg, l, 1);
-        a.b[l - a.l0] = lvp<float>(mg, l, 2);
-        a.y[l - a.l0] = lvp<float>(mg, l, 3);
-    }
-    a.omega = (float)mg->omega;
-    a.arrivals = reinterpret_cast<unsigned long long*>(mg->ws + mg->off_cbar);
-    a.err = reinterpret_cast<unsigned int*>(mg->ws + mg->off_cbar + 8);
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)mg->coarse_blocks, 1, 1);
-    cfg.blockDim = kBlk;
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    ProfScope ps(mg->prof, 8, st);
-    note_launch();
-    const int zc = mg->czc;
-    if (down) {
-        if (zc == 1) cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 1>, a);
-        else if (zc == 2) cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 2>, a);
-        else cudaLaunchKernelEx(&cfg, k_mg_coarse<true, 4>, a);
-    } else {
-        if (zc == 1) cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 1>, a);
-        else if (zc == 2) cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 2>, a);
-        else cudaLaunchKernelEx(&cfg, k_mg_coarse<false, 4>, a);
-    }
-    return true;
-}
-
 // level0_last: mode of the last level-0 half-sweep (see smooth)
 template <typename T>
 static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
     const int L = mg->nlevels;
     const int B = mg->bottom;   // < L: levels B..L-1 in one block
-    bool persistent = false;    // levels 1..B-1 in k_mg_coarse (mixed precision)
     // The first half-sweep of level 0 was written by the stop-test residual kernel that
     // precedes every V-cycle (k_mg_resid_sweep; mixed: k_mg_resid_df, from a zero
     // correction); every restricted level gets it from the restriction.
     for (int l = 0; l < L - 1 && l < B; ++l) {
-        if (l == mg->coarse_l0 && (persistent = coarse_launch(mg, st, true))) break;
         smooth<T>(mg, l, st, 0, true);
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
@@ -2381,8 +2261,7 @@ static void vcycle(MgImpl* mg, cudaStream_t st, int level0_last) {
         bottom<T>(mg, st);
     else
         smooth<T>(mg, L - 1, st, L == 1 ? level0_last : 0, true);
-    if (persistent) coarse_launch(mg, st, false);
-    for (int l = persistent ? mg->coarse_l0 - 1 : (B < L ? B - 1 : L - 2); l >= 0; --l) {
+    for (int l = (B < L ? B - 1 : L - 2); l >= 0; --l) {
         if (!empty(mg, l + 1)) {
             MgGeom gf = mgg(mg, l), gc = mgg(mg, l + 1);
             ProfScope ps(mg->prof, 10, st);
@@ -2454,24 +2333,28 @@ static void enqueue_resid_df(MgImpl* mg, cudaStream_t st) {
     const bool v4 = use_v4(mg, g.n);
     const dim3 grd = v4 ? grid_v4(g.n) : grid_zc(g.n, MG_DFZC);
     ProfScope ps(mg->prof, 11, st);
-    note_launch(2);
+    note_launch(v4 ? 1 : 2);
     const float2* pdf = mg_pdf(mg);
     const float2* bdf = reinterpret_cast<const float2*>(mg->ws + mg->off_bdf);
+    MgFin fin;   // the vector kernel also adds the partials into sc[SC_RR]
+    fin.ticket = fin_ticket(mg);
+    fin.sc = sc;
     if (mg->bat.tab) {
         if (v4)
             k_mg_resid_df_v4<true><<<bgrid(mg, grd), kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
-                                                                    (float)mg->omega, sc, part, mg->bat);
+                                                                    (float)mg->omega, sc, part, mg->bat, fin);
         else
             k_mg_resid_df<true><<<bgrid(mg, grd), kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
                                                                  (float)mg->omega, sc, part, mg->bat);
     } else if (v4) {
         k_mg_resid_df_v4<<<grd, kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3),
-                                               (float)mg->omega, sc, part);
+                                               (float)mg->omega, sc, part, Bat(), fin);
     } else {
         k_mg_resid_df<<<grd, kBlk, 0, st>>>(g, pdf, bdf, lvp<float>(mg, 0, 2), lvp<float>(mg, 0, 3), (float)mg->omega,
                                             sc, part);
     }
-    k_mg_final<<<bgrid(mg, dim3(1, 1, 1)), 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR, mg->bat);
+    if (!v4)
+        k_mg_final<<<bgrid(mg, dim3(1, 1, 1)), 1024, 0, st>>>(part, (int)(grd.x * grd.y * grd.z), sc + SC_RR, mg->bat);
 }
 
 // FP64: enqueue the stop-test sum(r^2) into sc[SC_RR] together with the next V-cycle's
@@ -2506,18 +2389,22 @@ static void enqueue_fcg_update(MgImpl* mg, cudaStream_t st, int k) {
     const int nb = (int)(grd.x * grd.y * grd.z);
     const unsigned eb = (unsigned)((n + 255) / 256);
     ProfScope ps(mg->prof, 11, st);
-    note_launch(4);
-    // the partial sums of z.q and z were written by the V-cycle's last level-0 half-sweep
-    const dim3 gj = use_v4(mg, g.n) ? grid_v4(g.n) : grd;   // grid of the level-0 half-sweep that summed z.q
-    k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, (int)(gj.x * gj.y * gj.z), (double)n, sc, k);
     if (use_v4(mg, g.n)) {
-        const dim3 gv = grid_v4(g.n);
-        k_fcg_direction_v4<<<gv, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
-        k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, (int)(gv.x * gv.y * gv.z), sc);
+        // beta came with the V-cycle's last level-0 half-sweep (k_mg_jacobi_v4<2>); the
+        // direction kernel also sets alpha
+        note_launch(1);
+        MgFin fin;
+        fin.ticket = fin_ticket(mg);
+        fin.sc = sc;
+        k_fcg_direction_v4<<<grid_v4(g.n), kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2, fin);
     } else {
+        // the partial sums of z.q and z were written by the V-cycle's last level-0 half-sweep
+        note_launch(3);
+        k_fcg_final_beta<<<1, 1024, 0, st>>>(part, part2, nb, (double)n, sc, k);
         k_fcg_direction<<<grd, kBlk, 0, st>>>(g, z, r, P, Q, sc, part, part2);
         k_fcg_final_alpha<<<1, 1024, 0, st>>>(part, part2, nb, sc);
     }
+    note_launch(1);
     k_fcg_xupdate<<<eb, 256, 0, st>>>(mg_pdf(mg), P, n, sc);
 }
 
@@ -2607,6 +2494,7 @@ int mg_solve(MgImpl* mg, cudaStream_t st) {
         while (true) {
             if (res < mg->tol) break;
             if (mg->krylov) {              // z = V(r) preconditions an FCG(1) update of p
+                mg->fcg_k = nite;
                 vcycle<float>(mg, st, 2);
                 enqueue_fcg_update(mg, st, nite);
             } else {
@@ -2698,6 +2586,7 @@ int mg_solve_graph(MgImpl* mg, GraphBuilder& gb) {
         vcycle<double>(mg, st, 0);
         enqueue_resid_sweep(mg, st);
     } else if (mg->krylov) {
+        mg->fcg_k = -1;
         vcycle<float>(mg, st, 2);
         enqueue_fcg_update(mg, st, -1);
         enqueue_resid_df(mg, st);
@@ -2737,7 +2626,7 @@ int mg_reset_history(MgImpl* mg) {
 
 int mg_zero_scalars(MgImpl* mg) {
     cudaError_t e = cudaMemset(scalars(mg), 0, 16 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemset(mg->ws + mg->off_cbar, 0, 64);
+    if (e == cudaSuccess) e = cudaMemset(mg->ws + mg->off_ticket, 0, 64);
     if (e == cudaSuccess && mg->nhist) e = cudaMemset(mg->ws + mg->off_hist, 0, mg->nsol * sizeof(int));
     return cuda_status(e, "multigrid scalars reset");
 }
