@@ -234,8 +234,8 @@ def mg_levels(n):
 RHS_FP64_OPS_PER_CELL = 936
 RHS_FP64_INSTR_PER_CELL = 699
 # DRAM bytes (read + write) per interior cell of one launch: ncu, FP64 at 128^3
-# (159.0 + 43.7 MB), mixed at 256^3 (607.6 + 255.1 MB)
-RHS_DRAM_BYTES_PER_CELL = {8: 202.72e6 / 128 ** 3, 4: 862.71e6 / 256 ** 3}
+# (159.0 + 43.7 MB), mixed (k_rhs_les) at 256^3 (614.8 + 257.5 MB)
+RHS_DRAM_BYTES_PER_CELL = {8: 202.72e6 / 128 ** 3, 4: 872.35e6 / 256 ** 3}
 # DRAM bytes of one level-0 Jacobi half-sweep launch at 256^3, mixed (ncu, vector form:
 # 134.3 + 40.9 MB; algorithmic 201.3 MB, the rest of the output still in L2 at the end)
 JACOBI_F32_L0_DRAM_BYTES_256 = 175.2e6

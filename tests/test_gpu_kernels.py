@@ -33,6 +33,8 @@ def test_flux1d_f64_matches_oracle(n):
     u[:, ::3] = np.abs(u[:, ::3])
     q = rng.standard_normal((nlines, n)) * np.exp(rng.uniform(-8, 2, size=(nlines, 1)))
     q[::7] = 1.25    # constant lines: tau5 = 0 path
+    # tiny lines: tau5 below the normal float range (REAL(4) rounding to float subnormals)
+    q[3::7] *= np.exp(rng.uniform(-60, -40, size=(len(q[3::7]), 1)))
     ud, qd = torch.from_numpy(u).cuda(), torch.from_numpy(q).cuda()
     fd = torch.zeros_like(ud)
     nat.check(nat.lib().nyles_flux1d_f64(ctypes.c_void_p(ud.data_ptr()), ctypes.c_void_p(qd.data_ptr()),
