@@ -1208,6 +1208,14 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div(const Geom g, const T* __
 // multigrid right-hand side as (hi, lo); the model's div field gets hi + lo rounded.
 // One column per thread, as k_div.
 
+// (a - b) * (s.hi + s.lo) as a float pair: the difference of two floats is exact as a
+// pair (TwoSum), then one pair product (both within ~2^-48 of the exact value)
+__device__ __forceinline__ float2 ddiff_mul(float a, float b, float2 s) {
+    float d, e;
+    two_sum(a, -b, d, e);
+    return df_mul(make_float2(d, e), s);
+}
+
 __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const float* __restrict__ ux,
                                                           const float* __restrict__ uy, const float* __restrict__ uz,
                                                           float2 idx2, float2 idy2, float2 idz2,
@@ -1232,14 +1240,9 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_div_df(const Geom g, const fl
     for (int z = z0; z < z1; ++z) {
         const int zz = g.wrap(0, z);
         const long long c = (long long)zz * g.sz + cxy;
-        float2 acc = df_mul_f(ux[c], idx2);
-        if (xx != 0) acc = df_add(acc, df_neg(df_mul_f(ux[c - 1], idx2)));
-        float2 t = df_mul_f(uy[c], idy2);
-        if (yy != 0) t = df_add(t, df_neg(df_mul_f(uy[c - g.sy], idy2)));
-        acc = df_add(acc, t);
-        t = df_mul_f(uz[c], idz2);
-        if (zz != 0) t = df_add(t, df_neg(df_mul_f(uz[c - g.sz], idz2)));
-        acc = df_add(acc, t);
+        float2 acc = ddiff_mul(ux[c], xx != 0 ? ux[c - 1] : 0.f, idx2);
+        acc = df_add(acc, ddiff_mul(uy[c], yy != 0 ? uy[c - g.sy] : 0.f, idy2));
+        acc = df_add(acc, ddiff_mul(uz[c], zz != 0 ? uz[c - g.sz] : 0.f, idz2));
         div[g.at(z, y, x)] = df_value(acc);
         if (own_xy && zz == z) {
             const int iz = zz - (g.per[0] ? g.nh : 0);
@@ -1354,6 +1357,12 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a
     const int x = blockIdx.x * PJ_BX + threadIdx.x;
     const int y = blockIdx.y * PJ_BY + threadIdx.y;
     if (x >= g.N[2] || y >= g.N[1]) return;
+    // distinct arrays: the loads of the next cell need not wait for this cell's stores
+    const float2* __restrict__ X = a.x;
+    float* __restrict__ P = a.p;
+    float* __restrict__ U0 = a.u[0];
+    float* __restrict__ U1 = a.u[1];
+    float* __restrict__ U2 = a.u[2];
     const int z0 = bz * PJ_ZC, z1 = min(z0 + PJ_ZC, g.N[0]);
     const int oz = g.per[0] ? g.nh : 0, oy = g.per[1] ? g.nh : 0, ox = g.per[2] ? g.nh : 0;
     const int yy = g.wrap(1, y), xx = g.wrap(2, x);
@@ -1368,15 +1377,15 @@ __global__ void __launch_bounds__(PJ_BX * PJ_BY) k_correct_df(const CorrDfArgs a
         const long long c = g.at(z, y, x);
         const int zz = g.wrap(0, z);
         const long long iz = (long long)(zz - oz) * sxy;
-        const float2 p0 = a.x[iz + ixy];
-        a.p[c] = df_value(df_mul(p0, a.dx2));
+        const float2 p0 = X[iz + ixy];
+        P[c] = df_value(df_mul(p0, a.dx2));
         if (!own_xy || zz != z) continue;   // halo: filled later
         const float2 np0 = df_neg(p0);
-        if (hx) a.u[0][c] = __fsub_rn(a.u[0][c], df_value(df_mul(df_add(a.x[iz + ixy_x], np0), a.dx2)));
-        if (hy) a.u[1][c] = __fsub_rn(a.u[1][c], df_value(df_mul(df_add(a.x[iz + ixy_y], np0), a.dx2)));
+        if (hx) U0[c] = __fsub_rn(U0[c], df_value(df_mul(df_add(X[iz + ixy_x], np0), a.dx2)));
+        if (hy) U1[c] = __fsub_rn(U1[c], df_value(df_mul(df_add(X[iz + ixy_y], np0), a.dx2)));
         if (z < g.N[0] - 1) {
             const long long iz1 = (long long)(g.wrap(0, z + 1) - oz) * sxy;
-            a.u[2][c] = __fsub_rn(a.u[2][c], df_value(df_mul(df_add(a.x[iz1 + ixy], np0), a.dx2)));
+            U2[c] = __fsub_rn(U2[c], df_value(df_mul(df_add(X[iz1 + ixy], np0), a.dx2)));
         }
     }
 }
