@@ -429,8 +429,10 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
 
-// Loads of the vector level kernels (a policy type, so that a kernel whose passes read
-// what other blocks of the same launch wrote could route them through L2).
+// Loads of the vector level kernels, a policy type of the block functions below: plain
+// loads, valid because nothing a launch reads is written during it. A kernel running
+// several passes in one launch would route its loads through L2 (ld.global.cg) instead,
+// the read-only and L1 paths not being coherent within a launch.
 struct LdPlain {
     static __device__ __forceinline__ float4 f4(const float* p) { return *reinterpret_cast<const float4*>(p); }
     static __device__ __forceinline__ float2 f2(const float* p) { return *reinterpret_cast<const float2*>(p); }
