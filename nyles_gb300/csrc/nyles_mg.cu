@@ -429,24 +429,15 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_jacobi(const MgGeom g, con
 // V4_ZC. Same per-cell arithmetic and modes as k_mg_jacobi.
 constexpr int V4_ZC = 4;
 
-// Loads of the vector level kernels, a policy type of the block functions below: plain
-// loads, valid because nothing a launch reads is written during it. A kernel running
-// several passes in one launch would route its loads through L2 (ld.global.cg) instead,
-// the read-only and L1 paths not being coherent within a launch.
-struct LdPlain {
-    static __device__ __forceinline__ float4 f4(const float* p) { return *reinterpret_cast<const float4*>(p); }
-    static __device__ __forceinline__ float2 f2(const float* p) { return *reinterpret_cast<const float2*>(p); }
-    static __device__ __forceinline__ float f1(const float* p) { return *p; }
-};
-template <typename L>
-__device__ __forceinline__ float mg_ldw_l(const float* a, long long c, bool wet) {
-    const float v = L::f1(a + c);
+// value at c, or 0 across a closed wall (mg_ldw for the float vector kernels)
+__device__ __forceinline__ float mg_ldw_f(const float* __restrict__ a, long long c, bool wet) {
+    const float v = a[c];
     return wet ? v : 0.f;
 }
 
 // One block of the vector half-sweep: block (bx, by, bz) of the grid grid_v4(n, ZC);
 // MODE 2 accumulates the block's sums of out*dot and out into sdot and ssum.
-template <int MODE, int ZC, typename L>
+template <int MODE, int ZC>
 __device__ __forceinline__ void mg_jacobi_v4_blk(const MgGeom& g, const float* __restrict__ in,
                                                  const float* __restrict__ b, float* __restrict__ out, float omega,
                                                  float2* __restrict__ acc, const float* __restrict__ dot, int bx,
@@ -475,7 +466,7 @@ __device__ __forceinline__ void mg_jacobi_v4_blk(const MgGeom& g, const float* _
     const float cff1 = 1.f - omega;
     const int zb = bz * ZC;
     const long long c00 = (long long)ys * sy + x0;
-    auto ld4 = [&](const float* a, long long c) { return L::f4(a + c); };
+    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     auto zrow = [&](int zz) -> float4 {
         if (zz < 0) return g.per[0] ? ld4(in, c00 + (long long)(nz - 1) * sz) : zero4;
@@ -494,8 +485,8 @@ __device__ __forceinline__ void mg_jacobi_v4_blk(const MgGeom& g, const float* _
         const float4 dv = (MODE == 2) ? ld4(dot, c) : zero4;
         const float sl = __shfl_up_sync(0xffffffffu, zc.w, 1);
         const float sr = __shfl_down_sync(0xffffffffu, zc.x, 1);
-        const float left = ownl ? mg_ldw_l<L>(in, c + ol, wl) : sl;
-        const float right = ownr ? mg_ldw_l<L>(in, c + orr, wr) : sr;
+        const float left = ownl ? mg_ldw_f(in, c + ol, wl) : sl;
+        const float right = ownr ? mg_ldw_f(in, c + orr, wr) : sr;
         const int dzw = (int)(zz > 0 || g.per[0]) + (int)(zz < nz - 1 || g.per[0]);
         const float xc[4] = {zc.x, zc.y, zc.z, zc.w};
         const float xm[4] = {left, zc.x, zc.y, zc.z}, xp[4] = {zc.y, zc.z, zc.w, right};
@@ -550,7 +541,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY, 5) k_mg_jacobi_v4(const MgGeom 
         partial2 = bshift(partial2, dlt);
     }
     float sdot = 0.f, ssum = 0.f;
-    mg_jacobi_v4_blk<MODE, ZC, LdPlain>(g, in, b, out, omega, acc, dot, blockIdx.x, blockIdx.y, bz, sdot, ssum);
+    mg_jacobi_v4_blk<MODE, ZC>(g, in, b, out, omega, acc, dot, blockIdx.x, blockIdx.y, bz, sdot, ssum);
     if constexpr (MODE == 2) {
         block_partial2_f(sdot, ssum, partial, partial2, bz);
         // the Krylov solve's beta and mean of z from the totals (k_fcg_final_beta's work)
@@ -732,7 +723,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
 
 // k_mg_restrict: one coarse row pair of cells per thread, RZC coarse planes (needs
 // coarse nz divisible by RZC); block (bx, by, bz) of the grid of v4_restrict_grid
-template <int RZC, typename L>
+template <int RZC>
 __device__ __forceinline__ void mg_restrict_v4_blk(const MgGeom& gf, const float* __restrict__ xf,
                                                    const float* __restrict__ bf, const MgGeom& gc,
                                                    float* __restrict__ bc, float* __restrict__ yc, float omega, int bx,
@@ -757,7 +748,7 @@ __device__ __forceinline__ void mg_restrict_v4_blk(const MgGeom& gf, const float
                              {(float)(1 + ylw), (float)((int)wr + ylw), (float)(1 + yhw), (float)((int)wr + yhw)}};
     const int zcb = bz * RZC, k0 = 2 * zcb;
     const long long c00 = (long long)j0 * sy + x0;
-    auto ld4 = [&](const float* a, long long c) { return L::f4(a + c); };
+    auto ld4 = [&](const float* a, long long c) { return *reinterpret_cast<const float4*>(a + c); };
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     struct Rows { float4 r0, r1; };
     // rows j0 and j0 + 1 of fine plane k, one plane outside the level at most: periodic
@@ -793,8 +784,8 @@ __device__ __forceinline__ void mg_restrict_v4_blk(const MgGeom& gf, const float
             const float4 b0 = ld4(bf, c), b1 = ld4(bf, c + sy);
             const float sl0 = __shfl_up_sync(0xffffffffu, P.r0.w, 1), sl1 = __shfl_up_sync(0xffffffffu, P.r1.w, 1);
             const float sr0 = __shfl_down_sync(0xffffffffu, P.r0.x, 1), sr1 = __shfl_down_sync(0xffffffffu, P.r1.x, 1);
-            const float l0 = ownl ? mg_ldw_l<L>(xf, c + ol, wl) : sl0, l1 = ownl ? mg_ldw_l<L>(xf, c + sy + ol, wl) : sl1;
-            const float r0 = ownr ? mg_ldw_l<L>(xf, c + orr, wr) : sr0, r1 = ownr ? mg_ldw_l<L>(xf, c + sy + orr, wr) : sr1;
+            const float l0 = ownl ? mg_ldw_f(xf, c + ol, wl) : sl0, l1 = ownl ? mg_ldw_f(xf, c + sy + ol, wl) : sl1;
+            const float r0 = ownr ? mg_ldw_f(xf, c + orr, wr) : sr0, r1 = ownr ? mg_ldw_f(xf, c + sy + orr, wr) : sr1;
             const float x0v[4] = {P.r0.x, P.r0.y, P.r0.z, P.r0.w}, x1v[4] = {P.r1.x, P.r1.y, P.r1.z, P.r1.w};
             const float o0[4] = {O.r0.x, O.r0.y, O.r0.z, O.r0.w}, o1[4] = {O.r1.x, O.r1.y, O.r1.z, O.r1.w};
             const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
@@ -844,12 +835,12 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_restrict_v4(const MgGeom g
         bc = bshift(bc, dlt);
         yc = bshift(yc, dlt);
     }
-    mg_restrict_v4_blk<RZC, LdPlain>(gf, xf, bf, gc, bc, yc, omega, blockIdx.x, blockIdx.y, bz);
+    mg_restrict_v4_blk<RZC>(gf, xf, bf, gc, bc, yc, omega, blockIdx.x, blockIdx.y, bz);
 }
 
 // k_mg_prolong: one 4-cell fine row segment per thread, ZC fine planes (needs fine nz
 // divisible by ZC, ZC even); block (bx, by, bz) of the grid grid_v4(fine n, ZC)
-template <int ZC, typename L>
+template <int ZC>
 __device__ __forceinline__ void mg_prolong_v4_blk(const MgGeom& gf, float* __restrict__ xf, const MgGeom& gc,
                                                   const float* __restrict__ xc, int bx, int by, int bz) {
     const int nx = gf.n[2], ny = gf.n[1];
@@ -876,14 +867,14 @@ __device__ __forceinline__ void mg_prolong_v4_blk(const MgGeom& gf, float* __res
     // plane is dry): fine x0 + e takes coarse ic0 + (e >> 1) and its x neighbour on the
     // side of the fine cell
     auto plane = [&](long long c, bool wet, float* out) {
-        const float2 a = wet ? L::f2(xc + c) : make_float2(0.f, 0.f);
-        const float2 d = (wet && wy) ? L::f2(xc + c + oy) : make_float2(0.f, 0.f);
+        const float2 a = wet ? *reinterpret_cast<const float2*>(xc + c) : make_float2(0.f, 0.f);
+        const float2 d = (wet && wy) ? *reinterpret_cast<const float2*>(xc + c + oy) : make_float2(0.f, 0.f);
         const float sal = __shfl_up_sync(0xffffffffu, a.y, 1), sar = __shfl_down_sync(0xffffffffu, a.x, 1);
         const float sdl = __shfl_up_sync(0xffffffffu, d.y, 1), sdr = __shfl_down_sync(0xffffffffu, d.x, 1);
-        const float al = ownl ? mg_ldw_l<L>(xc, c + col, wet && cwl) : sal;
-        const float ar = ownr ? mg_ldw_l<L>(xc, c + cor, wet && cwr) : sar;
-        const float dl = ownl ? mg_ldw_l<L>(xc, c + oy + col, wet && cwl && wy) : sdl;
-        const float dr = ownr ? mg_ldw_l<L>(xc, c + oy + cor, wet && cwr && wy) : sdr;
+        const float al = ownl ? mg_ldw_f(xc, c + col, wet && cwl) : sal;
+        const float ar = ownr ? mg_ldw_f(xc, c + cor, wet && cwr) : sar;
+        const float dl = ownl ? mg_ldw_f(xc, c + oy + col, wet && cwl && wy) : sdl;
+        const float dr = ownr ? mg_ldw_f(xc, c + oy + cor, wet && cwr && wy) : sdr;
         const float av[4] = {a.x, a.x, a.y, a.y}, bv[4] = {al, a.y, a.x, ar};
         const float dv[4] = {d.x, d.x, d.y, d.y}, ev[4] = {dl, d.y, d.x, dr};
 #pragma unroll
@@ -892,7 +883,7 @@ __device__ __forceinline__ void mg_prolong_v4_blk(const MgGeom& gf, float* __res
     const long long sz = (long long)ny * nx, c0 = (long long)zb * sz + (long long)ys * nx + x0;
     float4 xv4[ZC];   // the fine values, loaded together with the coarse ones
 #pragma unroll
-    for (int k = 0; k < ZC; ++k) xv4[k] = L::f4(xf + c0 + k * sz);
+    for (int k = 0; k < ZC; ++k) xv4[k] = *reinterpret_cast<const float4*>(xf + c0 + k * sz);
     constexpr int NP = ZC / 2 + 2;
     float P[NP][4];
     plane(cc + zl.om, zl.wm, P[0]);
@@ -937,7 +928,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong_v4(const MgGeom gf
         xf = bshift(xf, dlt);
         xc = bshift(xc, dlt);
     }
-    mg_prolong_v4_blk<ZC, LdPlain>(gf, xf, gc, xc, blockIdx.x, blockIdx.y, bz);
+    mg_prolong_v4_blk<ZC>(gf, xf, gc, xc, blockIdx.x, blockIdx.y, bz);
 }
 
 // ---------------------------------------------------------------- coarse levels in one block
