@@ -215,6 +215,15 @@ CASES = [
          rotating=True, coriolis=2.0, diff_coef={"u": 1e-3}),
     dict(name="perioxy_linear_lfam3", geometry="perio_xy", modelname="linear", timestepping="LFAM3",
          n=(8, 8, 8), L=(1.0, 1.0, 1.0), n_tracers=0, auto_dt=False, dt=1e-2, steps=3, init="shear"),
+    # anisotropic grids (dx = 2 dy = 2 dz; dx = dz = dy / 2): three steps, before the
+    # projection's over-correction grows large, pin p = x*dx**2 and the anisotropic metric
+    dict(name="closed_les_rk3_aniso", geometry="closed", modelname="LES", timestepping="RK3_SSP",
+         n=(16, 8, 8), L=(4.0, 1.0, 1.0), n_tracers=0, auto_dt=False, dt=2e-3, steps=3, init="lock"),
+    dict(name="perioxy_les_rk3_2tracers_aniso", geometry="perio_xy", modelname="LES", timestepping="RK3_SSP",
+         n=(16, 8, 16), L=(1.0, 1.0, 1.0), n_tracers=2, auto_dt=True, cfl=0.8, dt_max=0.05, steps=3, init="shear"),
+    # 16^3: a multigrid of four levels (16, 8, 4, 2)
+    dict(name="perioxy_les_lfam3_16", geometry="perio_xy", modelname="LES", timestepping="LFAM3",
+         n=(16, 16, 16), L=(1.0, 1.0, 1.0), n_tracers=1, auto_dt=True, cfl=0.8, dt_max=0.05, steps=3, init="shear"),
 ]
 
 
@@ -361,10 +370,14 @@ def params_cases(refparams):
     return res
 
 
-def main():
+def main(only=()):
+    """Every case (or the named ones) and the parameter cases; a case's seed is fixed by
+    its position in CASES."""
     refparams, refnyles, mgmod = _import_reference()
     os.makedirs(HERE, exist_ok=True)
     for k, case in enumerate(CASES):
+        if only and case["name"] not in only:
+            continue
         out = run_case(refparams, refnyles, mgmod, case, seed=100 + k)
         np.savez_compressed(os.path.join(HERE, case["name"] + ".npz"), **out)
         print("wrote", case["name"], "nites", out["nites_last"], "dts", out["dts"])
@@ -376,5 +389,5 @@ def main():
 if __name__ == "__main__":
     REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NYLES_REFERENCE_CORE")
     if not REF or not os.path.isfile(os.path.join(REF, "nyles.py")):
-        sys.exit("usage: make_golden.py <reference core/ directory> (or set NYLES_REFERENCE_CORE)")
-    main()
+        sys.exit("usage: make_golden.py <reference core/ directory> [case names] (or set NYLES_REFERENCE_CORE)")
+    main(tuple(sys.argv[2:]))
