@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(MG_BX * MG_BY) k_mg_prolong(const MgGeom gf, T
 // per-cell arithmetic of the full-chunk paths above.
 
 // k_mg_restrict: one coarse row pair of cells per thread, RZC coarse planes (needs
-// coarse nz divisible by RZC); block (bx, by, bz) of the grid of v4_restrict_grid
+// coarse nz divisible by RZC); block (bx, by, bz) of the grid grid_v4_restrict(fine, coarse, RZC)
 template <int RZC>
 __device__ __forceinline__ void mg_restrict_v4_blk(const MgGeom& gf, const float* __restrict__ xf,
                                                    const float* __restrict__ bf, const MgGeom& gc,
