@@ -1,6 +1,6 @@
 """Layout of the C ABI's structs as the C compiler sees them, against the ctypes
-mirrors: the package's (nyles_gb300/_native.py) and the one INTEGRATION.md tells a
-reference maintainer to paste. A struct that gains a field in include/nyles_gb300.h
+mirrors: the package's (nyles_gb300/_native.py) and the one the integration guide at the
+repository root tells a reference maintainer to paste. A struct that gains a field in include/nyles_gb300.h
 without its mirrors fails here (no GPU needed: gcc compiles a probe of the header)."""
 import ctypes
 import os
@@ -51,8 +51,8 @@ def _c_layout(tmp_path, name, fields):
 
 
 def _integration_desc_class():
-    """The NylesDesc class of INTEGRATION.md section 3.1, executed as written (the CDLL
-    line is left out: this check needs no library)."""
+    """The NylesDesc class of the integration guide's section 3.1, executed as written
+    (the CDLL line is left out: this check needs no library)."""
     text = open(os.path.join(REPO, "INTEGRATION.md")).read()
     block = re.search(r"### 3\.1.*?```python\n(.*?)```", text, flags=re.S).group(1)
     cls = re.search(r"(class NylesDesc\(ctypes\.Structure\):.*?\])\n", block, flags=re.S).group(1)
