@@ -1,8 +1,8 @@
 """The vortex-force binding that the integration guide at the repository root (its
 section 3.1) gives a reference maintainer to paste into core/vortex_force.py, executed
-as written: its NylesDesc filled field by field from the
-package's descriptor, its vortex_force() called on a small state, and the tendencies
-compared with the oracle (the FP64 kernel bar, 1e-13)."""
+as written: its NylesDesc filled field by field from the package's descriptor, its
+vortex_force() called on a small state, and the tendencies compared with the oracle
+(the FP64 kernel bar, 1e-13)."""
 import os
 import re
 
