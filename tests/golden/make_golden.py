@@ -224,6 +224,12 @@ CASES = [
     # 16^3: a multigrid of four levels (16, 8, 4, 2)
     dict(name="perioxy_les_lfam3_16", geometry="perio_xy", modelname="LES", timestepping="LFAM3",
          n=(16, 16, 16), L=(1.0, 1.0, 1.0), n_tracers=1, auto_dt=True, cfl=0.8, dt_max=0.05, steps=3, init="shear"),
+    # Euler3d between walls (its projection precedes the halo fill) with a tracer; Euler
+    # forward LES with a tracer in the triply periodic box
+    dict(name="closed_euler_rk3_tracer", geometry="closed", modelname="Euler3d", timestepping="RK3_SSP",
+         n=(16, 8, 8), L=(2.0, 1.0, 1.0), n_tracers=1, auto_dt=True, cfl=0.8, dt_max=0.05, steps=3, init="shear"),
+    dict(name="perioxyz_les_ef_tracer", geometry="perio_xyz", modelname="LES", timestepping="EF",
+         n=(8, 8, 8), L=(6.283185307179586,) * 3, n_tracers=1, auto_dt=False, dt=2e-2, steps=3, init="tgv"),
 ]
 
 
