@@ -269,11 +269,12 @@ struct MgFin {
     int k = 0;                        // Krylov iteration (-1: read sc[SC_NITE])
     double vol = 0.0;                 // level-0 cells
 };
+// Thread (0, 0) stored the block's partial (block_partial*): it alone fences that store
+// before taking the ticket (a fence in every thread stalled every block on its way out).
 __device__ __forceinline__ bool mg_last_block(unsigned int* ticket, unsigned int nblk) {
     __shared__ unsigned int s_last;
-    __threadfence();
-    __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
         const unsigned int t = atomicAdd(ticket, 1u);
         s_last = (t == nblk - 1) ? 1u : 0u;
         if (s_last) atomicExch(ticket, 0u);
