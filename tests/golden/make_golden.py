@@ -230,6 +230,10 @@ CASES = [
          n=(16, 8, 8), L=(2.0, 1.0, 1.0), n_tracers=1, auto_dt=True, cfl=0.8, dt_max=0.05, steps=3, init="shear"),
     dict(name="perioxyz_les_ef_tracer", geometry="perio_xyz", modelname="LES", timestepping="EF",
          n=(8, 8, 8), L=(6.283185307179586,) * 3, n_tracers=1, auto_dt=False, dt=2e-2, steps=3, init="tgv"),
+    # the linear model between walls, with viscosity
+    dict(name="closed_linear_rk3_visc", geometry="closed", modelname="linear", timestepping="RK3_SSP",
+         n=(16, 8, 8), L=(2.0, 1.0, 1.0), n_tracers=0, auto_dt=False, dt=2e-3, steps=3, init="lock",
+         diff_coef={"u": 1e-3}),
 ]
 
 
